@@ -1,0 +1,237 @@
+"""ctypes driver for a library that exports the preqx C ABI of ``include/hxgpu.h``.
+
+It makes the calls the Fortran driver makes (``src/share/prim_driver_mod.F90:1042-1105``
+for initialisation, ``src/prim_main.F90:297-317`` for the time loop), with numpy arrays
+in the Fortran layouts, so the same code drives the CUDA library (``libhxgpu.so``) and
+the CPU oracle.  Python is only the test/benchmark harness here: every array crosses
+the boundary as a plain pointer.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+
+import numpy as np
+
+NP, NLEV = 4, 72
+
+_c_int_p = C.POINTER(C.c_int)
+_c_dbl_p = C.POINTER(C.c_double)
+
+
+def _pp(a: np.ndarray):
+    """Pointer-to-pointer argument (Fortran passes type(c_ptr) by reference)."""
+    assert a.flags.c_contiguous and a.dtype == np.float64
+    return C.byref(C.c_void_p(a.ctypes.data))
+
+
+def _i(v: int):
+    return C.byref(C.c_int(int(v)))
+
+
+def _d(v: float):
+    return C.byref(C.c_double(float(v)))
+
+
+def _b(v: bool):
+    return C.byref(C.c_bool(bool(v)))
+
+
+@dataclass
+class SimParams:
+    """Namelist values ``init_simulation_params_c`` receives."""
+    remap_alg: int = 1
+    limiter_option: int = 8
+    rsplit: int = 1
+    qsplit: int = 1
+    time_step_type: int = 5
+    energy_fixer: int = 0
+    qsize: int = 4
+    state_frequency: int = 1_000_000
+    nu: float = 1e16
+    nu_p: float = -1.0
+    nu_q: float = -1.0
+    nu_s: float = -1.0
+    nu_div: float = -1.0
+    nu_top: float = 2.5e5
+    hypervis_order: int = 2
+    hypervis_subcycle: int = 3
+    hypervis_scaling: float = 0.0
+    ftype: int = -1
+    prescribed_wind: bool = False
+    moisture: bool = False
+    disable_diagnostics: bool = True
+    use_cpstar: bool = False
+    use_semi_lagrangian_transport: bool = False
+
+    def resolved(self) -> "SimParams":
+        """Negative nu_s/nu_q/nu_p/nu_div default to nu (namelist_mod.F90:970-972)."""
+        p = SimParams(**self.__dict__)
+        for k in ("nu_s", "nu_q", "nu_p", "nu_div"):
+            if getattr(p, k) < 0:
+                setattr(p, k, p.nu)
+        return p
+
+
+class HxLibrary:
+    """A loaded preqx library plus the arrays it was initialised with."""
+
+    def __init__(self, path: str):
+        self.path = path
+        self.lib = C.CDLL(path)
+        L = self.lib
+        L.hx_last_error.restype = C.c_int
+        L.hx_last_error.argtypes = [C.c_char_p, C.c_int]
+        L.hx_set_precision.argtypes = [C.c_int]
+        L.hx_get_field.argtypes = [C.c_char_p, C.c_int, C.c_void_p]
+        L.hx_set_field.argtypes = [C.c_char_p, C.c_int, C.c_void_p]
+        L.hx_run_caar_stage.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.c_double]
+        L.hx_run_rk5.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double]
+        L.hx_run_hypervis.argtypes = [C.c_int, C.c_double, C.c_double]
+        L.hx_run_euler_step.argtypes = [C.c_int, C.c_int, C.c_double, C.c_double, C.c_int]
+        L.hx_run_tracers_rk2.argtypes = [C.c_double]
+        L.hx_run_remap.argtypes = [C.c_int, C.c_int, C.c_double]
+        L.hx_run_prim_step.argtypes = [C.c_double]
+        L.hx_run_dss.argtypes = [C.c_char_p, C.c_int, C.c_int]
+        L.hx_launch_count.restype = C.c_longlong
+        L.hx_kernel_stats.argtypes = [C.c_char_p, C.c_int, C.POINTER(C.c_longlong),
+                                      C.POINTER(C.c_double), C.c_int]
+        self.nelem = 0
+        self.qsize = 0
+
+    # -- status ----------------------------------------------------------------------
+    def last_error(self):
+        buf = C.create_string_buffer(512)
+        code = self.lib.hx_last_error(buf, 512)
+        return code, buf.value.decode(errors="replace")
+
+    def check(self, what: str = ""):
+        code, msg = self.last_error()
+        if code:
+            raise RuntimeError(f"{what}: error {code}: {msg}")
+
+    # -- initialisation (prim_init1 / prim_init2 order) --------------------------------
+    def init(self, mesh, hv, params: SimParams, state: dict, precision: int = 0,
+             abort_on_error: bool = False, time_levels=(1, 2, 3)):
+        L = self.lib
+        p = params.resolved()
+        L.hx_set_abort_on_error(0 if not abort_on_error else 1)
+        L.initialize_hommexx_session()
+        self.check("initialize_hommexx_session")
+        L.reset_cxx_comm(_i(0))
+        L.init_connectivity(_i(mesh.nelem))
+        for t in mesh.f90_connections():
+            L.add_connection(*[_i(x) for x in t])
+        L.finalize_connectivity()
+        self._keep = {}
+        dvv = np.ascontiguousarray(mesh.dvv, dtype=np.float64)
+        self._keep["dvv"] = dvv
+        L.init_derivative_c(_pp(dvv))
+        L.init_simulation_params_c(
+            _i(p.remap_alg), _i(p.limiter_option), _i(p.rsplit), _i(p.qsplit),
+            _i(p.time_step_type), _i(p.energy_fixer), _i(p.qsize), _i(p.state_frequency),
+            _d(p.nu), _d(p.nu_p), _d(p.nu_q), _d(p.nu_s), _d(p.nu_div), _d(p.nu_top),
+            _i(p.hypervis_order), _i(p.hypervis_subcycle), _d(p.hypervis_scaling),
+            _i(p.ftype), _b(p.prescribed_wind), _b(p.moisture), _b(p.disable_diagnostics),
+            _b(p.use_cpstar), _b(p.use_semi_lagrangian_transport))
+        self.check("init_simulation_params_c")
+        if L.hx_set_precision(int(precision)) != 0:
+            self.check("hx_set_precision")
+        arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (
+            mesh.D, mesh.Dinv, mesh.fcor, mesh.mp, mesh.spheremp, mesh.rspheremp,
+            mesh.metdet, mesh.metinv, mesh.phis, mesh.tensorvisc, mesh.vec_sph2cart)]
+        self._keep["metric"] = arrs
+        L.init_elements_2d_c(_i(mesh.nelem), *[_pp(a) for a in arrs],
+                             _b(p.hypervis_scaling == 0.0))
+        self.check("init_elements_2d_c")
+        self.nelem = mesh.nelem
+        self.qsize = p.qsize
+        self.set_state(state)
+        hyam = np.ascontiguousarray(hv.hyam)
+        hyai = np.ascontiguousarray(hv.hyai)
+        hybm = np.ascontiguousarray(hv.hybm)
+        hybi = np.ascontiguousarray(hv.hybi)
+        self._keep["hv"] = (hyam, hyai, hybm, hybi)
+        L.init_hvcoord_c(_d(hv.ps0), _pp(hyam), _pp(hyai), _pp(hybm), _pp(hybi))
+        L.init_boundary_exchanges_c()
+        self.check("init_boundary_exchanges_c")
+        nm1, n0, np1 = time_levels
+        L.init_time_level_c(_i(nm1), _i(n0), _i(np1), _i(0), _i(0))
+        self.tl = [nm1 - 1, n0 - 1, np1 - 1, 0]
+        return self
+
+    def set_state(self, state: dict):
+        arrs = [np.ascontiguousarray(state[k], dtype=np.float64)
+                for k in ("v", "T", "dp3d", "Qdp", "ps_v")]
+        self.lib.init_elements_states_c(*[_pp(a) for a in arrs])
+        self.check("init_elements_states_c")
+
+    # -- time stepping -----------------------------------------------------------------
+    def run_subcycle(self, dt: float, last_step: int = 1 << 30):
+        nstep, nm1, n0, np1 = (C.c_int(self.tl[3]), C.c_int(self.tl[0]),
+                               C.c_int(self.tl[1]), C.c_int(self.tl[2]))
+        self.lib.prim_run_subcycle_c(_d(dt), C.byref(nstep), C.byref(nm1), C.byref(n0),
+                                     C.byref(np1), _i(last_step))
+        self.check("prim_run_subcycle_c")
+        self.tl = [nm1.value, n0.value, np1.value, nstep.value]
+        return self.tl
+
+    def push_results(self, out: dict | None = None):
+        E, Q = self.nelem, self.qsize
+        if out is None:
+            out = dict(
+                v=np.empty((E, 3, NLEV, 2, NP, NP)), T=np.empty((E, 3, NLEV, NP, NP)),
+                dp3d=np.empty((E, 3, NLEV, NP, NP)), Qdp=np.empty((E, 2, Q, NLEV, NP, NP)),
+                Q=np.empty((E, Q, NLEV, NP, NP)), ps_v=np.empty((E, 3, NP, NP)),
+                omega_p=np.empty((E, NLEV, NP, NP)))
+        self.lib.cxx_push_results_to_f90(*[_pp(out[k]) for k in
+                                           ("v", "T", "dp3d", "Qdp", "Q", "ps_v", "omega_p")])
+        self.check("cxx_push_results_to_f90")
+        return out
+
+    # -- field access and per-phase entry points ---------------------------------------
+    _SHAPES = {"v": (2, NLEV * 0 + NLEV), "vn0": (2, NLEV)}
+
+    def field_shape(self, name: str):
+        E, Q = self.nelem, self.qsize
+        if name in ("v", "vn0"):
+            return (E, NLEV, 2, NP, NP)
+        if name in ("Qdp", "Q"):
+            return (E, Q, NLEV, NP, NP)
+        if name == "ps_v":
+            return (E, NP, NP)
+        return (E, NLEV, NP, NP)
+
+    def get(self, name: str, tl: int = 0) -> np.ndarray:
+        out = np.empty(self.field_shape(name))
+        rc = self.lib.hx_get_field(name.encode(), int(tl), out.ctypes.data)
+        if rc:
+            raise RuntimeError(f"hx_get_field({name}) -> {rc}")
+        return out
+
+    def set(self, name: str, tl: int, arr: np.ndarray):
+        a = np.ascontiguousarray(arr, dtype=np.float64).reshape(self.field_shape(name))
+        rc = self.lib.hx_set_field(name.encode(), int(tl), a.ctypes.data)
+        if rc:
+            raise RuntimeError(f"hx_set_field({name}) -> {rc}")
+
+    def call(self, fn: str, *args):
+        rc = getattr(self.lib, fn)(*args)
+        if rc:
+            code, msg = self.last_error()
+            raise RuntimeError(f"{fn}{args} -> {rc}: {msg}")
+        return rc
+
+    def kernel_stats(self, maxn: int = 64):
+        names = C.create_string_buffer(64 * maxn)
+        la = (C.c_longlong * maxn)()
+        ms = (C.c_double * maxn)()
+        n = self.lib.hx_kernel_stats(names, 64, la, ms, maxn)
+        out = []
+        for i in range(min(n, maxn)):
+            nm = names.raw[64 * i: 64 * (i + 1)].split(b"\0", 1)[0].decode()
+            out.append((nm, int(la[i]), float(ms[i])))
+        return out
+
+    def finalize(self):
+        self.lib.finalize_hommexx_session()

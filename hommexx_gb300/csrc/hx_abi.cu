@@ -1,0 +1,873 @@
+// hx_abi.cu — host runtime and C ABI of libhxgpu.so (declared in include/hxgpu.h).
+//
+// One process, one GPU, one CUDA stream.  The whole cubed-sphere mesh is resident in
+// HBM in the Fortran layout the ABI receives, so init/push are plain copies (plus an
+// on-device FP64<->FP32 conversion in the mixed form).  The orchestration below
+// restates, call for call, the reference's host glue:
+//   prim_run_subcycle_c  src/share/cxx/prim_driver.cpp:31-156
+//   prim_step            src/share/cxx/prim_step.cpp:20-103
+//   u3_5stage_timestep   src/share/cxx/prim_advance_exp.cpp:113-161
+//   prim_advec_tracers_remap_RK2  src/share/cxx/prim_advec_tracers_remap.cpp:32-90
+//   TimeLevel            src/share/cxx/TimeLevel.hpp:37-67
+// There is no MPI: every connection is local, and DSS is a gather over a table built
+// once from the add_connection calls (src/share/cxx/mpi/Connectivity.cpp:77-170).
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <string>
+#include <type_traits>
+#include <vector>
+
+#include "../../include/hxgpu.h"
+#include "hx_kernels.cuh"
+
+namespace hx {
+namespace {
+
+struct Params {
+  int remap_alg = 1, limiter_option = 8, rsplit = 1, qsplit = 1, time_step_type = 5, qsize = 0;
+  int state_frequency = 1, hypervis_order = 2, hypervis_subcycle = 1, ftype = -1;
+  double nu = 0, nu_p = 0, nu_q = 0, nu_s = 0, nu_div = 0, nu_top = 0, hypervis_scaling = 0;
+  double nu_ratio1 = 1, nu_ratio2 = 1;
+  bool moist = false, set = false;
+};
+
+struct TimeLevel {
+  int nm1 = 0, n0 = 1, np1 = 2, nstep = 0, nstep0 = 0, n0_qdp = 0, np1_qdp = 1;
+  void update_dynamics_levels() {
+    const int tmp = np1;
+    np1 = nm1;
+    nm1 = n0;
+    n0 = tmp;
+    ++nstep;
+  }
+  void update_tracers_levels(int qsplit) {
+    const int i_temp = nstep / qsplit;
+    if (i_temp % 2 == 0) { n0_qdp = 0; np1_qdp = 1; }
+    else { n0_qdp = 1; np1_qdp = 0; }
+  }
+};
+
+struct Failure {
+  int code;
+  std::string msg;
+};
+
+[[noreturn]] void fail(int code, const std::string& msg) { throw Failure{code, msg}; }
+
+void ck(cudaError_t e, const char* what) {
+  if (e != cudaSuccess) fail(HX_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+template <typename T>
+T* dalloc(size_t n) {
+  void* p = nullptr;
+  if (n == 0) n = 1;
+  ck(cudaMalloc(&p, n * sizeof(T)), "cudaMalloc");
+  ck(cudaMemset(p, 0, n * sizeof(T)), "cudaMemset");
+  return static_cast<T*>(p);
+}
+
+// ---- kernel timing ---------------------------------------------------------------------
+struct Timing {
+  bool on = false;
+  long long launches = 0;
+  std::vector<cudaEvent_t> pool;
+  size_t used = 0;
+  std::vector<std::pair<const char*, size_t>> pending;  // name, index of start event
+  std::map<std::string, std::pair<long long, double>> stats;
+};
+Timing g_tim;
+cudaStream_t g_stream = nullptr;
+
+void flush_timing() {
+  if (g_tim.pending.empty()) return;
+  cudaStreamSynchronize(g_stream);
+  for (auto& pr : g_tim.pending) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, g_tim.pool[pr.second], g_tim.pool[pr.second + 1]);
+    auto& s = g_tim.stats[pr.first];
+    s.first += 1;
+    s.second += ms;
+  }
+  g_tim.pending.clear();
+  g_tim.used = 0;
+}
+
+void hook_before(const char* name, cudaStream_t s) {
+  ++g_tim.launches;
+  if (!g_tim.on) return;
+  if (g_tim.used + 2 > g_tim.pool.size()) flush_timing();
+  cudaEventRecord(g_tim.pool[g_tim.used], s);
+  g_tim.pending.push_back({name, g_tim.used});
+  g_tim.used += 2;
+}
+void hook_after(const char*, cudaStream_t s) {
+  if (g_tim.on) cudaEventRecord(g_tim.pool[g_tim.used - 1], s);
+}
+
+// ---- the resident model -----------------------------------------------------------------
+struct Backend {
+  virtual ~Backend() {}
+  virtual void alloc() = 0;
+  virtual void upload_metric(const double* const* arrs, bool consthv) = 0;
+  virtual void set_states(const double* v, const double* T, const double* dp, const double* qdp,
+                          const double* ps_v) = 0;
+  virtual void push(double* v, double* T, double* dp, double* qdp, double* Q, double* ps_v,
+                    double* omega_p) = 0;
+  virtual void run_subcycle(double dt) = 0;
+  virtual void caar_stage(int nm1, int n0, int np1, double dt, double w, int n0_qdp, int combine,
+                          int n0orig) = 0;
+  virtual void rk5(int nm1, int n0, int np1, int n0_qdp, double dt, double w) = 0;
+  virtual void hypervis(int np1, double dt, double w) = 0;
+  virtual void euler_step(int np1_qdp, int n0_qdp, double dt, double rhs, int dssopt, int tavg) = 0;
+  virtual void tracers_rk2(double dt) = 0;
+  virtual void precompute_divdp() = 0;
+  virtual int remap(int np1, int np1_qdp, double dt) = 0;
+  virtual void prim_step(double dt) = 0;
+  virtual int field(const std::string& name, int tl, double* host, bool get) = 0;
+  virtual int dss_field(const std::string& name, int tl, bool rsmp) = 0;
+};
+
+struct Session;
+Session* g_s = nullptr;
+
+struct Session {
+  Params prm;
+  TimeLevel tl;
+  int E = 0, Q = 0;
+  int precision = 0;
+  bool consthv = true;
+  double dvv[16] = {};
+  double ps0 = 0, hyai[NLEV + 1] = {}, hybi[NLEV + 1] = {};
+  bool have_hv = false;
+  std::vector<int> conn;  // [E][8][2]
+  std::unique_ptr<Backend> be;
+  int last_err = 0;
+  std::string last_msg;
+  bool abort_on_error = true;
+  ~Session() {}
+};
+
+Session& S() {
+  if (!g_s) g_s = new Session();
+  return *g_s;
+}
+
+// DSS tables from the connections, in the reference accumulation order
+// (ConnectivityHelpers.hpp:129-205, BoundaryExchange.cpp:505-538).
+const int PTS_FWD[8][4] = {{0, 1, 2, 3}, {12, 13, 14, 15}, {0, 4, 8, 12}, {3, 7, 11, 15},
+                           {0, -1, -1, -1}, {3, -1, -1, -1}, {12, -1, -1, -1}, {15, -1, -1, -1}};
+const int PTS_BWD[8][4] = {{3, 2, 1, 0}, {15, 14, 13, 12}, {12, 8, 4, 0}, {15, 11, 7, 3},
+                           {0, -1, -1, -1}, {3, -1, -1, -1}, {12, -1, -1, -1}, {15, -1, -1, -1}};
+const int DIRECTION[4][4] = {{1, 0, 0, 1}, {0, 1, 1, 0}, {0, 1, 1, 0}, {1, 0, 0, 1}};
+
+void build_tables(const std::vector<int>& conn, int E, std::vector<int>& cnt, std::vector<int>& src,
+                  std::vector<int>& nbr) {
+  cnt.assign((size_t)E * 16, 0);
+  src.assign((size_t)E * 16 * MAXSRC, 0);
+  nbr.assign((size_t)E * 8, -1);
+  auto add = [&](int e, int p, int se, int sp) {
+    int& n = cnt[(size_t)e * 16 + p];
+    if (n >= MAXSRC) fail(13, "more than three DSS contributions at one point");
+    src[((size_t)e * 16 + p) * MAXSRC + n] = se * 16 + sp;
+    ++n;
+  };
+  for (int e = 0; e < E; ++e) {
+    for (int s = 0; s < 8; ++s) nbr[(size_t)e * 8 + s] = conn[((size_t)e * 8 + s) * 2];
+    for (int k = 0; k < NP; ++k)
+      for (int slot = 0; slot < 4; ++slot) {
+        const int r = conn[((size_t)e * 8 + slot) * 2], rs = conn[((size_t)e * 8 + slot) * 2 + 1];
+        if (r < 0) continue;
+        if (r >= E || rs < 0 || rs > 3) fail(13, "invalid edge connection");
+        const int dir = DIRECTION[rs][slot];
+        add(e, PTS_FWD[slot][k], r, dir == 0 ? PTS_FWD[rs][k] : PTS_BWD[rs][k]);
+      }
+    for (int slot = 4; slot < 8; ++slot) {
+      const int r = conn[((size_t)e * 8 + slot) * 2], rs = conn[((size_t)e * 8 + slot) * 2 + 1];
+      if (r < 0) continue;
+      if (r >= E || rs < 4 || rs > 7) fail(13, "invalid corner connection");
+      add(e, PTS_FWD[slot][0], r, PTS_FWD[rs][0]);
+    }
+  }
+}
+
+template <typename R>
+__global__ void k_d2r(const double* __restrict__ a, R* b, size_t n) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) b[i] = (R)a[i];
+}
+template <typename R>
+__global__ void k_r2d(const R* __restrict__ a, double* b, size_t n) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) b[i] = (double)a[i];
+}
+
+template <typename R>
+struct BackendT : Backend {
+  Session& s;
+  explicit BackendT(Session& ss) : s(ss) {}
+  int E = 0, Q = 0;
+  // metric
+  R *D = 0, *Dinv = 0, *metinv = 0, *metdet = 0, *spheremp = 0, *rspheremp = 0, *mp = 0, *fcor = 0,
+    *phis = 0, *tensorvisc = 0, *vec_sph2cart = 0;
+  // state
+  R *v = 0, *T = 0, *dp = 0;
+  double *ps_v = 0, *qdp = 0, *Qc = 0;
+  R *phi = 0, *omega_p = 0, *eta = 0, *derived_dp = 0, *divdp = 0, *divdp_proj = 0, *dpdiss_ave = 0,
+    *dpdiss_bih = 0, *vn0 = 0;
+  // scratch
+  R *caar_out = 0, *bufA = 0, *bufB = 0, *vstar = 0, *dpdissk = 0, *fscr = 0, *qtens = 0, *qscr = 0;
+  double *qlim = 0, *qlim_tmp = 0, *dp0 = 0, *staging = 0;
+  R* gen_scr = 0;
+  int *tab_cnt = 0, *tab_src = 0, *nbr = 0, *invalid = 0;
+  int* h_invalid = nullptr;
+  size_t staging_n = 0;
+
+  ~BackendT() override {
+    void* ptrs[] = {D, Dinv, metinv, metdet, spheremp, rspheremp, mp, fcor, phis, tensorvisc, vec_sph2cart,
+                    v, T, dp, ps_v, qdp, Qc, phi, omega_p, eta, derived_dp, divdp, divdp_proj, dpdiss_ave,
+                    dpdiss_bih, vn0, caar_out, bufA, bufB, vstar, dpdissk, fscr, qtens, qscr, qlim, qlim_tmp,
+                    dp0, staging, gen_scr, tab_cnt, tab_src, nbr, invalid};
+    for (void* p : ptrs)
+      if (p) cudaFree(p);
+    if (h_invalid) cudaFreeHost(h_invalid);
+  }
+
+  size_t N3() const { return (size_t)E * NLEV * 16; }
+
+  void alloc() override {
+    E = s.E;
+    Q = s.Q;
+    const size_t n3 = N3();
+    D = dalloc<R>((size_t)E * 64); Dinv = dalloc<R>((size_t)E * 64); metinv = dalloc<R>((size_t)E * 64);
+    tensorvisc = dalloc<R>((size_t)E * 64); vec_sph2cart = dalloc<R>((size_t)E * 96);
+    metdet = dalloc<R>((size_t)E * 16); spheremp = dalloc<R>((size_t)E * 16);
+    rspheremp = dalloc<R>((size_t)E * 16); mp = dalloc<R>((size_t)E * 16);
+    fcor = dalloc<R>((size_t)E * 16); phis = dalloc<R>((size_t)E * 16);
+    v = dalloc<R>(n3 * NTL * 2); T = dalloc<R>(n3 * NTL); dp = dalloc<R>(n3 * NTL);
+    ps_v = dalloc<double>((size_t)E * NTL * 16);
+    qdp = dalloc<double>(n3 * QTL * Q); Qc = dalloc<double>(n3 * Q);
+    phi = dalloc<R>(n3); omega_p = dalloc<R>(n3); eta = dalloc<R>(n3); derived_dp = dalloc<R>(n3);
+    divdp = dalloc<R>(n3); divdp_proj = dalloc<R>(n3); dpdiss_ave = dalloc<R>(n3); dpdiss_bih = dalloc<R>(n3);
+    vn0 = dalloc<R>(2 * n3);
+    caar_out = dalloc<R>(4 * n3); bufA = dalloc<R>(4 * n3); bufB = dalloc<R>(4 * n3);
+    vstar = dalloc<R>(2 * n3); dpdissk = dalloc<R>(n3); fscr = dalloc<R>(n3);
+    qtens = dalloc<R>(n3 * Q); qscr = dalloc<R>(n3 * Q);
+    qlim = dalloc<double>((size_t)E * Q * 2 * NLEV); qlim_tmp = dalloc<double>((size_t)E * Q * 2 * NLEV);
+    dp0 = dalloc<double>(NLEV);
+    gen_scr = dalloc<R>(n3 * (Q > 2 ? Q : 2));
+    invalid = dalloc<int>(1);
+    ck(cudaMallocHost(&h_invalid, sizeof(int)), "cudaMallocHost");
+    if (std::is_same<R, float>::value) {
+      staging_n = n3 * (NTL * 2 > QTL * Q ? NTL * 2 : QTL * Q);
+      staging = dalloc<double>(staging_n);
+    }
+  }
+
+  void to_dev(R* dst, const double* host, size_t n) {
+    if (std::is_same<R, double>::value) {
+      ck(cudaMemcpyAsync(dst, host, n * sizeof(double), cudaMemcpyHostToDevice, g_stream), "H2D");
+    } else {
+      if (n > staging_n) fail(HX_ERR_STATE, "staging buffer too small");
+      ck(cudaMemcpyAsync(staging, host, n * sizeof(double), cudaMemcpyHostToDevice, g_stream), "H2D");
+      k_d2r<R><<<(unsigned)((n + 255) / 256), 256, 0, g_stream>>>(staging, dst, n);
+      ck(cudaGetLastError(), "convert");
+    }
+  }
+  void to_host(double* host, const R* src, size_t n) {
+    if (std::is_same<R, double>::value) {
+      ck(cudaMemcpyAsync(host, src, n * sizeof(double), cudaMemcpyDeviceToHost, g_stream), "D2H");
+    } else {
+      if (n > staging_n) fail(HX_ERR_STATE, "staging buffer too small");
+      k_r2d<R><<<(unsigned)((n + 255) / 256), 256, 0, g_stream>>>(src, staging, n);
+      ck(cudaGetLastError(), "convert");
+      ck(cudaMemcpyAsync(host, staging, n * sizeof(double), cudaMemcpyDeviceToHost, g_stream), "D2H");
+    }
+  }
+
+  void upload_metric(const double* const* a, bool consthv) override {
+    to_dev(D, a[0], (size_t)E * 64);
+    to_dev(Dinv, a[1], (size_t)E * 64);
+    to_dev(fcor, a[2], (size_t)E * 16);
+    to_dev(mp, a[3], (size_t)E * 16);
+    to_dev(spheremp, a[4], (size_t)E * 16);
+    to_dev(rspheremp, a[5], (size_t)E * 16);
+    to_dev(metdet, a[6], (size_t)E * 16);
+    to_dev(metinv, a[7], (size_t)E * 64);
+    to_dev(phis, a[8], (size_t)E * 16);
+    if (!consthv) {
+      to_dev(tensorvisc, a[9], (size_t)E * 64);
+      to_dev(vec_sph2cart, a[10], (size_t)E * 96);
+    }
+    ck(cudaStreamSynchronize(g_stream), "upload_metric");
+  }
+
+  void set_states(const double* hv, const double* hT, const double* hdp, const double* hq,
+                  const double* hps) override {
+    const size_t n3 = N3();
+    to_dev(v, hv, n3 * NTL * 2);
+    to_dev(T, hT, n3 * NTL);
+    to_dev(dp, hdp, n3 * NTL);
+    if (Q > 0) ck(cudaMemcpyAsync(qdp, hq, n3 * QTL * Q * sizeof(double), cudaMemcpyHostToDevice, g_stream), "H2D qdp");
+    ck(cudaMemcpyAsync(ps_v, hps, (size_t)E * NTL * 16 * sizeof(double), cudaMemcpyHostToDevice, g_stream), "H2D ps");
+  }
+
+  void push(double* hv, double* hT, double* hdp, double* hq, double* hQ, double* hps, double* homega) override {
+    const size_t n3 = N3();
+    to_host(hv, v, n3 * NTL * 2);
+    to_host(hT, T, n3 * NTL);
+    to_host(hdp, dp, n3 * NTL);
+    if (Q > 0) {
+      ck(cudaMemcpyAsync(hq, qdp, n3 * QTL * Q * sizeof(double), cudaMemcpyDeviceToHost, g_stream), "D2H qdp");
+      ck(cudaMemcpyAsync(hQ, Qc, n3 * Q * sizeof(double), cudaMemcpyDeviceToHost, g_stream), "D2H Q");
+    }
+    ck(cudaMemcpyAsync(hps, ps_v, (size_t)E * NTL * 16 * sizeof(double), cudaMemcpyDeviceToHost, g_stream), "D2H ps");
+    to_host(homega, omega_p, n3);
+    ck(cudaStreamSynchronize(g_stream), "push");
+  }
+
+  MetricP<R> metric() const {
+    MetricP<R> m;
+    m.D = D; m.Dinv = Dinv; m.metinv = metinv; m.metdet = metdet; m.spheremp = spheremp;
+    m.rspheremp = rspheremp; m.mp = mp; m.fcor = fcor; m.phis = phis;
+    m.tensorvisc = tensorvisc; m.vec_sph2cart = vec_sph2cart;
+    return m;
+  }
+  DssTable table() const { return DssTable{tab_cnt, tab_src}; }
+
+  void set_tables(const std::vector<int>& cnt, const std::vector<int>& src, const std::vector<int>& nb) {
+    if (!tab_cnt) {
+      tab_cnt = dalloc<int>(cnt.size());
+      tab_src = dalloc<int>(src.size());
+      nbr = dalloc<int>(nb.size());
+    }
+    ck(cudaMemcpy(tab_cnt, cnt.data(), cnt.size() * sizeof(int), cudaMemcpyHostToDevice), "tables");
+    ck(cudaMemcpy(tab_src, src.data(), src.size() * sizeof(int), cudaMemcpyHostToDevice), "tables");
+    ck(cudaMemcpy(nbr, nb.data(), nb.size() * sizeof(int), cudaMemcpyHostToDevice), "tables");
+    double h[NLEV];
+    for (int l = 0; l < NLEV; ++l) {
+      const double ad = s.hyai[l + 1] - s.hyai[l], bd = s.hybi[l + 1] - s.hybi[l];
+      h[l] = ad * s.ps0 + bd * s.ps0;  // HybridVCoord::compute_deltas "BFB way"
+    }
+    ck(cudaMemcpy(dp0, h, sizeof(h), cudaMemcpyHostToDevice), "dp0");
+  }
+
+  void post(const char* what) { ck(cudaGetLastError(), what); }
+
+  // CaarFunctor::run + BoundaryExchange(rspheremp)
+  void caar_stage(int nm1, int n0, int np1, double dt, double w, int n0_qdp, int combine, int n0orig) override {
+    CaarArgs<R> a;
+    a.m = metric();
+    a.v = v; a.T = T; a.dp = dp; a.vn0 = vn0; a.omega_p = omega_p; a.phi = phi;
+    a.qdp = qdp; a.qsize = Q; a.n0_qdp = n0_qdp;
+    a.out = caar_out; a.nm1 = nm1; a.n0 = n0;
+    a.dt = dt; a.eta_ave_w = w; a.p_top = s.hyai[0] * s.ps0;
+    a.rk_combine = combine; a.n0orig = n0orig;
+    launch_caar<R>(a, E, g_stream);
+    post("caar");
+    launch_dss_state<R>(E, caar_out, v, T, dp, np1, rspheremp, table(), g_stream);
+    post("dss_caar");
+  }
+
+  void rk5(int nm1, int n0, int np1, int n0_qdp, double dt, double w) override {
+    caar_stage(n0, n0, nm1, dt / 5.0, w / 4.0, n0_qdp, 0, n0);
+    caar_stage(n0, nm1, np1, dt / 5.0, 0.0, n0_qdp, 0, n0);
+    caar_stage(n0, np1, np1, dt / 3.0, 0.0, n0_qdp, 0, n0);
+    caar_stage(n0, np1, np1, 2.0 * dt / 3.0, 0.0, n0_qdp, 0, n0);
+    // nm1 = (5 nm1 - n0)/4 fused into the last stage
+    caar_stage(nm1, np1, np1, 3.0 * dt / 4.0, 3.0 * w / 4.0, n0_qdp, 1, n0);
+  }
+
+  void hypervis(int np1, double dt, double w) override {
+    HvArgs<R> a;
+    a.m = metric();
+    a.dss = table();
+    a.v = v; a.T = T; a.dp = dp; a.dpdiss_ave = dpdiss_ave; a.dpdiss_bih = dpdiss_bih;
+    a.bufA = bufA; a.bufB = bufB;
+    a.np1 = np1; a.hsub = s.prm.hypervis_subcycle; a.consthv = s.consthv ? 1 : 0;
+    a.dt = dt / s.prm.hypervis_subcycle; a.eta_ave_w = w;
+    a.nu = s.prm.nu; a.nu_s = s.prm.nu_s; a.nu_p = s.prm.nu_p; a.nu_top = s.prm.nu_top;
+    a.nu_ratio1 = s.prm.nu_ratio1; a.nu_ratio2 = s.prm.nu_ratio2;
+    launch_hv<R>(a, E, g_stream);
+    post("hypervis");
+  }
+
+  EulerArgs<R> euler_args() {
+    EulerArgs<R> a;
+    a.m = metric();
+    a.dss = table();
+    a.derived_dp = derived_dp; a.divdp = divdp; a.divdp_proj = divdp_proj; a.vn0 = vn0;
+    a.dpdiss_ave = dpdiss_ave; a.dpdiss_bih = dpdiss_bih; a.f_dss = divdp_proj;
+    a.vstar = vstar; a.dpdissk = dpdissk; a.fscr = fscr; a.qdp = qdp; a.qtens = qtens; a.qscr = qscr;
+    a.qlim = qlim; a.qlim_tmp = qlim_tmp; a.dp0 = dp0; a.conn = nbr;
+    a.Q = Q; a.n0_qdp = 0; a.np1_qdp = 1; a.limiter_option = s.prm.limiter_option;
+    a.consthv = s.consthv ? 1 : 0;
+    a.dt = 0; a.rhs_multiplier = 0; a.rhs_viss = 0; a.nu_p = s.prm.nu_p; a.nu_q = s.prm.nu_q;
+    return a;
+  }
+
+  void precompute_divdp() override {
+    EulerArgs<R> a = euler_args();
+    launch_precompute_divdp<R>(a, E, g_stream);
+    post("precompute_divdp");
+  }
+
+  // EulerStepFunctorImpl::euler_step; dssopt 0 = ETA, 1 = OMEGA, 2 = DIV_VDP_AVE
+  void euler_step(int np1_qdp, int n0_qdp, double dt, double rhs, int dssopt, int tavg) override {
+    EulerArgs<R> a = euler_args();
+    a.np1_qdp = np1_qdp; a.n0_qdp = n0_qdp; a.dt = dt; a.rhs_multiplier = rhs;
+    a.f_dss = dssopt == 0 ? eta : dssopt == 1 ? omega_p : divdp_proj;
+    launch_euler_step<R>(a, E, tavg, g_stream);
+    post("euler_step");
+  }
+
+  void tracers_rk2(double dt) override {
+    s.tl.update_tracers_levels(s.prm.qsplit);
+    precompute_divdp();
+    euler_step(s.tl.np1_qdp, s.tl.n0_qdp, dt / 2.0, 0.0, 2, 0);
+    euler_step(s.tl.np1_qdp, s.tl.np1_qdp, dt / 2.0, 1.0, 0, 0);
+    // the last stage's DSS applies qdp_time_avg (EulerStepFunctorImpl.hpp:379-403)
+    euler_step(s.tl.np1_qdp, s.tl.np1_qdp, dt / 2.0, 2.0, 1, 1);
+  }
+
+  void launch_remap(int np1, int np1_qdp) {
+    RemapArgs<R> a;
+    a.v = v; a.T = T; a.dp = dp; a.qdp = qdp; a.ps_v = ps_v;
+    a.np1 = np1; a.n0_qdp = np1_qdp; a.Q = Q; a.remap_alg = s.prm.remap_alg; a.nelem = E;
+    a.ps0 = s.ps0; a.hyai0 = s.hyai[0]; a.invalid = invalid;
+    ck(cudaMemsetAsync(invalid, 0, sizeof(int), g_stream), "memset");
+    hx::launch_remap<R>(a, g_stream);
+    post("remap");
+  }
+  int remap_status() {
+    ck(cudaMemcpyAsync(h_invalid, invalid, sizeof(int), cudaMemcpyDeviceToHost, g_stream), "flag");
+    ck(cudaStreamSynchronize(g_stream), "remap sync");
+    return *h_invalid ? 101 : 0;
+  }
+  int remap(int np1, int np1_qdp, double) override {
+    launch_remap(np1, np1_qdp);
+    return remap_status();
+  }
+
+  void prim_step(double dt) override {
+    const Params& p = s.prm;
+    launch_prim_step_init<R>(E, eta, vn0, omega_p, dpdiss_ave, dpdiss_bih, derived_dp, dp, s.tl.n0,
+                             p.nu_p > 0 ? 1 : 0, g_stream);
+    post("prim_step_init");
+    for (int n = 0; n < p.qsplit; ++n) {
+      if (n > 0) s.tl.update_dynamics_levels();
+      int n0_qdp = -1;
+      if (p.moist) {
+        s.tl.update_tracers_levels(p.qsplit);
+        n0_qdp = s.tl.n0_qdp;
+      }
+      const double w = 1.0 / p.qsplit;
+      rk5(s.tl.nm1, s.tl.n0, s.tl.np1, n0_qdp, dt, w);
+      hypervis(s.tl.np1, dt, w);
+    }
+    if (p.qsize > 0) tracers_rk2(dt * p.qsplit);
+  }
+
+  void run_subcycle(double dt) override {
+    const Params& p = s.prm;
+    s.tl.update_tracers_levels(p.qsplit);
+    launch_dp_from_ps<R>(E, dp, ps_v, s.tl.n0, s.ps0, g_stream);
+    post("dp3d_from_ps");
+    prim_step(dt);
+    for (int r = 1; r < p.rsplit; ++r) {
+      s.tl.update_dynamics_levels();
+      prim_step(dt);
+    }
+    s.tl.update_tracers_levels(p.qsplit);
+    launch_remap(s.tl.np1, s.tl.np1_qdp);
+    launch_update_q<R>(E, Q, qdp, Qc, ps_v, s.tl.np1, s.tl.np1_qdp, s.ps0, g_stream);
+    post("update_q");
+    const int st = remap_status();
+    s.tl.update_dynamics_levels();
+    if (st) fail(101, "Negative (or nan) layer thickness detected, aborting!");
+  }
+
+  // Field access in the Fortran layout of one time level.
+  int field(const std::string& n, int tl, double* host, bool get) override {
+    const size_t n3 = N3();
+    auto xfer_R = [&](R* base, long long es, int ncomp) {
+      // base + e*es holds ncomp*[72][16]... contiguous per element: [72][ncomp][16]
+      const size_t per = (size_t)NLEV * 16 * ncomp;
+      for (int e = 0; e < E; ++e) {
+        if (get) to_host(host + (size_t)e * per, base + (size_t)e * es, per);
+        else to_dev(base + (size_t)e * es, host + (size_t)e * per, per);
+      }
+    };
+    auto xfer_D = [&](double* base, long long es, size_t per) {
+      for (int e = 0; e < E; ++e) {
+        if (get) ck(cudaMemcpyAsync(host + (size_t)e * per, base + (size_t)e * es, per * 8, cudaMemcpyDeviceToHost, g_stream), "D2H");
+        else ck(cudaMemcpyAsync(base + (size_t)e * es, host + (size_t)e * per, per * 8, cudaMemcpyHostToDevice, g_stream), "H2D");
+      }
+    };
+    if (n == "v") xfer_R(v + (size_t)tl * NLEV * 32, (long long)NTL * NLEV * 32, 2);
+    else if (n == "T") xfer_R(T + (size_t)tl * NLEV * 16, (long long)NTL * NLEV * 16, 1);
+    else if (n == "dp3d") xfer_R(dp + (size_t)tl * NLEV * 16, (long long)NTL * NLEV * 16, 1);
+    else if (n == "vn0") xfer_R(vn0, (long long)NLEV * 32, 2);
+    else if (n == "omega_p") xfer_R(omega_p, NLEV * 16, 1);
+    else if (n == "phi") xfer_R(phi, NLEV * 16, 1);
+    else if (n == "eta_dot_dpdn") xfer_R(eta, NLEV * 16, 1);
+    else if (n == "derived_dp") xfer_R(derived_dp, NLEV * 16, 1);
+    else if (n == "divdp") xfer_R(divdp, NLEV * 16, 1);
+    else if (n == "divdp_proj") xfer_R(divdp_proj, NLEV * 16, 1);
+    else if (n == "dpdiss_ave") xfer_R(dpdiss_ave, NLEV * 16, 1);
+    else if (n == "dpdiss_biharmonic") xfer_R(dpdiss_bih, NLEV * 16, 1);
+    else if (n == "ps_v") xfer_D(ps_v + (size_t)tl * 16, NTL * 16, 16);
+    else if (n == "Qdp") xfer_D(qdp + (size_t)tl * Q * NLEV * 16, (long long)QTL * Q * NLEV * 16, (size_t)Q * NLEV * 16);
+    else if (n == "Q") xfer_D(Qc, (long long)Q * NLEV * 16, (size_t)Q * NLEV * 16);
+    else return HX_ERR_STATE;
+    (void)n3;
+    ck(cudaStreamSynchronize(g_stream), "field");
+    return 0;
+  }
+
+  int dss_field(const std::string& n, int tl, bool rs) override {
+    const R* r = rs ? rspheremp : nullptr;
+    if (n == "v") launch_dss_inplace<R>(E, 2, v + (size_t)tl * NLEV * 32, 16, (long long)NTL * NLEV * 32, 32, gen_scr, r, table(), g_stream);
+    else if (n == "T") launch_dss_inplace<R>(E, 1, T + (size_t)tl * NLEV * 16, 0, (long long)NTL * NLEV * 16, 16, gen_scr, r, table(), g_stream);
+    else if (n == "dp3d") launch_dss_inplace<R>(E, 1, dp + (size_t)tl * NLEV * 16, 0, (long long)NTL * NLEV * 16, 16, gen_scr, r, table(), g_stream);
+    else if (n == "omega_p") launch_dss_inplace<R>(E, 1, omega_p, 0, NLEV * 16, 16, gen_scr, r, table(), g_stream);
+    else if (n == "Qdp") {
+      // FP64 tracer mass through the double path
+      double* scr = reinterpret_cast<double*>(qscr);
+      if (sizeof(R) != sizeof(double)) scr = staging;
+      const double* rd = nullptr;
+      std::vector<double> h;
+      if (rs) {
+        // rspheremp in double
+        static double* rsd = nullptr;
+        if (!rsd) rsd = dalloc<double>((size_t)E * 16);
+        k_r2d<R><<<(E * 16 + 255) / 256, 256, 0, g_stream>>>(rspheremp, rsd, (size_t)E * 16);
+        rd = rsd;
+      }
+      launch_dss_inplace_d(E, Q, qdp + (size_t)tl * Q * NLEV * 16, NLEV * 16, (long long)QTL * Q * NLEV * 16, 16, scr, rd, table(), g_stream);
+    } else return HX_ERR_STATE;
+    post("dss_field");
+    ck(cudaStreamSynchronize(g_stream), "dss_field");
+    return 0;
+  }
+};
+
+
+void record(int code, const std::string& msg) {
+  Session& s = S();
+  s.last_err = code;
+  s.last_msg = msg;
+  if (s.abort_on_error) {
+    std::fprintf(stderr, "%s\nExiting...\n", msg.c_str());
+    std::exit(code);
+  }
+}
+
+template <typename F>
+int run(F&& f) {
+  Session& s = S();
+  s.last_err = 0;
+  s.last_msg.clear();
+  try {
+    f();
+  } catch (const Failure& x) {
+    record(x.code, x.msg);
+    return x.code;
+  }
+  return 0;
+}
+
+Backend& B() {
+  Session& s = S();
+  if (!s.be) fail(HX_ERR_STATE, "library not initialised (call init_elements_2d_c first)");
+  return *s.be;
+}
+
+}  // namespace
+}  // namespace hx
+
+using namespace hx;
+
+extern "C" {
+
+void initialize_hommexx_session(void) {
+  run([] {
+    Session& s = S();
+    (void)s;
+    if (!g_stream) {
+      int n = 0;
+      ck(cudaGetDeviceCount(&n), "cudaGetDeviceCount");
+      if (n < 1) fail(HX_ERR_CUDA, "no CUDA device");
+      ck(cudaSetDevice(0), "cudaSetDevice");
+      ck(cudaStreamCreateWithFlags(&g_stream, cudaStreamNonBlocking), "cudaStreamCreate");
+      g_tim.pool.resize(8192);
+      for (auto& e : g_tim.pool) ck(cudaEventCreate(&e), "cudaEventCreate");
+      set_kernel_hook(hook_before, hook_after);
+    }
+  });
+}
+
+void finalize_hommexx_session(void) {
+  run([] {
+    if (g_stream) cudaStreamSynchronize(g_stream);
+    delete g_s;
+    g_s = nullptr;
+    g_tim.stats.clear();
+    g_tim.pending.clear();
+    g_tim.used = 0;
+    g_tim.launches = 0;
+  });
+}
+
+void reset_cxx_comm(const int*) {}
+
+void init_connectivity(const int* n) {
+  run([&] {
+    Session& s = S();
+    s.conn.assign((size_t)(*n) * 16, -1);
+  });
+}
+
+void add_connection(const int* fl, const int* fg, const int* fp, const int* fpid, const int* sl,
+                    const int* sg, const int* sp, const int* spid) {
+  run([&] {
+    Session& s = S();
+    if (*fl <= 0 || *fg <= 0 || *fp <= 0 || *fpid <= 0 || *sl <= 0 || *sg <= 0 || *sp <= 0 || *spid <= 0)
+      fail(13, "ERROR! We were assuming F90 indices started at 1, but it appears there is an exception.");
+    auto convert = [](int fpos) { return fpos <= 4 ? (((fpos - 1) + 2) % 4) : (fpos - 1); };
+    const int e = *fl - 1, slot = convert(*fp);
+    if ((size_t)e * 16 >= s.conn.size() || slot < 0 || slot > 7) fail(13, "add_connection: element or position out of range");
+    s.conn[((size_t)e * 8 + slot) * 2] = *sl - 1;
+    s.conn[((size_t)e * 8 + slot) * 2 + 1] = convert(*sp);
+  });
+}
+
+void finalize_connectivity(void) {}
+
+void init_derivative_c(const double* const* dvv) {
+  run([&] { std::memcpy(S().dvv, *dvv, sizeof(double) * 16); });
+}
+
+void init_simulation_params_c(const int* remap_alg, const int* limiter_option, const int* rsplit, const int* qsplit,
+                              const int* time_step_type, const int*, const int* qsize,
+                              const int* state_frequency, const double* nu, const double* nu_p,
+                              const double* nu_q, const double* nu_s, const double* nu_div,
+                              const double* nu_top, const int* hypervis_order, const int* hypervis_subcycle,
+                              const double* hypervis_scaling, const int* ftype, const bool* prescribed_wind,
+                              const bool* moisture, const bool*, const bool*,
+                              const bool* use_semi_lagrangian_transport) {
+  run([&] {
+    auto bad = [](const char* opt) {
+      fail(11, std::string("Error in init_simulation_params_c: unsupported value for input parameter '") + opt + "'.");
+    };
+    // option checks of cxx_f90_interface.cpp:43-52
+    if (*remap_alg != 1 && *remap_alg != 2) bad("vert_remap_q_alg");
+    if (*prescribed_wind) bad("prescribed_wind");
+    if (*hypervis_order != 2) bad("hypervis_order");
+    if (*use_semi_lagrangian_transport) bad("use_semi_lagrangian_transport");
+    if (*time_step_type != 5) bad("time_step_type");
+    if (*limiter_option != 8 && *limiter_option != 9) bad("limiter_option");
+    if (*ftype != -1 && *ftype != 0 && *ftype != 2) bad("ftype");
+    if (!(*nu_p > 0)) bad("nu_p");
+    if (!(*nu > 0)) bad("nu");
+    if (!(*nu_div > 0)) bad("nu_div");
+    if (*ftype != -1) fail(12, "CAM forcing (ftype 0/2) is not part of this build");
+    if (*rsplit == 0) fail(12, "rsplit=0 (vertically Eulerian step) is not part of this build");
+    if (*qsplit < 1 || *hypervis_subcycle < 1 || *qsize < 0) fail(13, "invalid qsplit/hypervis_subcycle/qsize");
+    Params& p = S().prm;
+    p.remap_alg = *remap_alg; p.limiter_option = *limiter_option; p.rsplit = *rsplit; p.qsplit = *qsplit;
+    p.time_step_type = *time_step_type; p.qsize = *qsize; p.state_frequency = *state_frequency;
+    p.nu = *nu; p.nu_p = *nu_p; p.nu_q = *nu_q; p.nu_s = *nu_s; p.nu_div = *nu_div; p.nu_top = *nu_top;
+    p.hypervis_order = *hypervis_order; p.hypervis_subcycle = *hypervis_subcycle;
+    p.hypervis_scaling = *hypervis_scaling; p.ftype = *ftype; p.moist = *moisture;
+    if (p.nu != p.nu_div) {
+      const double ratio = p.nu_div / p.nu;
+      if (p.hypervis_scaling != 0.0) { p.nu_ratio1 = ratio * ratio; p.nu_ratio2 = 1.0; }
+      else { p.nu_ratio1 = ratio; p.nu_ratio2 = ratio; }
+    } else {
+      p.nu_ratio1 = 1.0; p.nu_ratio2 = 1.0;
+    }
+    p.set = true;
+  });
+}
+
+void init_hvcoord_c(const double* ps0, const double* const*, const double* const* hyai, const double* const*,
+                    const double* const* hybi) {
+  run([&] {
+    Session& s = S();
+    s.ps0 = *ps0;
+    std::memcpy(s.hyai, *hyai, sizeof(double) * (NLEV + 1));
+    std::memcpy(s.hybi, *hybi, sizeof(double) * (NLEV + 1));
+    s.have_hv = true;
+  });
+}
+
+void init_elements_2d_c(const int* nelemd, const double* const* D, const double* const* Dinv,
+                        const double* const* fcor, const double* const* mp, const double* const* spheremp,
+                        const double* const* rspheremp, const double* const* metdet, const double* const* metinv,
+                        const double* const* phis, const double* const* tensorvisc,
+                        const double* const* vec_sph2cart, const bool* consthv) {
+  run([&] {
+    Session& s = S();
+    if (!s.prm.set) fail(HX_ERR_STATE, "init_simulation_params_c must come before init_elements_2d_c");
+    if (!g_stream) initialize_hommexx_session();
+    if (!g_stream) fail(HX_ERR_CUDA, "no CUDA stream");
+    s.E = *nelemd;
+    s.Q = s.prm.qsize;
+    s.consthv = *consthv;
+    if (s.precision == 0) s.be.reset(new BackendT<double>(s));
+    else s.be.reset(new BackendT<float>(s));
+    s.be->alloc();
+    const double* arrs[11] = {*D, *Dinv, *fcor, *mp, *spheremp, *rspheremp, *metdet, *metinv, *phis,
+                              *tensorvisc, *vec_sph2cart};
+    s.be->upload_metric(arrs, s.consthv);
+  });
+}
+
+void init_elements_states_c(const double* const* v, const double* const* T, const double* const* dp3d,
+                            const double* const* Qdp, const double* const* ps_v) {
+  run([&] {
+    B().set_states(*v, *T, *dp3d, *Qdp, *ps_v);
+    ck(cudaStreamSynchronize(g_stream), "init_elements_states_c");
+  });
+}
+
+void init_diagnostics_c(double* const*, double* const*, double* const*, double* const*, double* const*,
+                        double* const*, double* const*, double* const*) {}
+
+void init_boundary_exchanges_c(void) {
+  run([] {
+    Session& s = S();
+    if (!s.have_hv) fail(HX_ERR_STATE, "init_hvcoord_c must come before init_boundary_exchanges_c");
+    if (s.conn.size() != (size_t)s.E * 16) fail(HX_ERR_STATE, "connectivity does not match nelemd");
+    std::vector<int> cnt, src, nb;
+    build_tables(s.conn, s.E, cnt, src, nb);
+    upload_constants(s.dvv, s.hyai, s.hybi, s.ps0, g_stream);
+    if (s.precision == 0) static_cast<BackendT<double>&>(B()).set_tables(cnt, src, nb);
+    else static_cast<BackendT<float>&>(B()).set_tables(cnt, src, nb);
+  });
+}
+
+void init_time_level_c(const int* nm1, const int* n0, const int* np1, const int* nstep, const int* nstep0) {
+  run([&] {
+    TimeLevel& t = S().tl;
+    t.nm1 = *nm1 - 1; t.n0 = *n0 - 1; t.np1 = *np1 - 1; t.nstep = *nstep; t.nstep0 = *nstep0;
+  });
+}
+
+void prim_run_subcycle_c(const double* dt, int* nstep, int* nm1, int* n0, int* np1, const int*) {
+  run([&] {
+    B().run_subcycle(*dt);
+    const TimeLevel& t = S().tl;
+    *nstep = t.nstep; *nm1 = t.nm1; *n0 = t.n0; *np1 = t.np1;
+  });
+}
+
+void cxx_push_results_to_f90(double* const* v, double* const* T, double* const* dp3d, double* const* Qdp,
+                             double* const* Q, double* const* ps_v, double* const* omega_p) {
+  run([&] { B().push(*v, *T, *dp3d, *Qdp, *Q, *ps_v, *omega_p); });
+}
+
+int hx_last_error(char* buf, int buflen) {
+  Session& s = S();
+  if (buf && buflen > 0) {
+    std::strncpy(buf, s.last_msg.c_str(), buflen - 1);
+    buf[buflen - 1] = 0;
+  }
+  return s.last_err;
+}
+
+void hx_set_abort_on_error(int a) { S().abort_on_error = a != 0; }
+
+int hx_set_precision(int mode) {
+  return run([&] {
+    if (mode != 0 && mode != 1) fail(11, "hx_set_precision: mode must be 0 (FP64) or 1 (mixed)");
+    if (S().be) fail(HX_ERR_STATE, "hx_set_precision must come before init_elements_2d_c");
+    S().precision = mode;
+  });
+}
+
+int hx_get_field(const char* name, int tl, double* out) {
+  int rc = 0;
+  int st = run([&] { rc = B().field(name, tl, out, true); });
+  return st ? st : rc;
+}
+int hx_set_field(const char* name, int tl, const double* in) {
+  int rc = 0;
+  int st = run([&] { rc = B().field(name, tl, const_cast<double*>(in), false); });
+  return st ? st : rc;
+}
+
+int hx_run_caar_stage(int nm1, int n0, int np1, double dt, double w) {
+  return run([&] { B().caar_stage(nm1, n0, np1, dt, w, -1, 0, n0); ck(cudaStreamSynchronize(g_stream), "sync"); });
+}
+int hx_run_rk5(int nm1, int n0, int np1, int n0_qdp, double dt, double w) {
+  return run([&] { B().rk5(nm1, n0, np1, n0_qdp, dt, w); ck(cudaStreamSynchronize(g_stream), "sync"); });
+}
+int hx_run_hypervis(int np1, double dt, double w) {
+  return run([&] { B().hypervis(np1, dt, w); ck(cudaStreamSynchronize(g_stream), "sync"); });
+}
+int hx_run_euler_step(int np1_qdp, int n0_qdp, double dt, double rhs, int dssopt) {
+  return run([&] {
+    if (dssopt < 0 || dssopt > 2) fail(11, "dss_opt must be 0, 1 or 2");
+    B().euler_step(np1_qdp, n0_qdp, dt, rhs, dssopt, 0);
+    ck(cudaStreamSynchronize(g_stream), "sync");
+  });
+}
+int hx_run_tracers_rk2(double dt) {
+  return run([&] { B().tracers_rk2(dt); ck(cudaStreamSynchronize(g_stream), "sync"); });
+}
+int hx_run_remap(int np1, int np1_qdp, double dt) {
+  int st = 0;
+  int rc = run([&] { st = B().remap(np1, np1_qdp, dt); });
+  return rc ? rc : st;
+}
+int hx_run_prim_step(double dt) {
+  return run([&] { B().prim_step(dt); ck(cudaStreamSynchronize(g_stream), "sync"); });
+}
+int hx_run_dss(const char* name, int tl, int rsmp) {
+  int rc = 0;
+  int st = run([&] { rc = B().dss_field(name, tl, rsmp != 0); });
+  return st ? st : rc;
+}
+
+int hx_num_elems(void) { return S().E; }
+int hx_qsize(void) { return S().Q; }
+
+int hx_enable_timing(int on) {
+  return run([&] {
+    if (!on) flush_timing();
+    g_tim.on = on != 0;
+  });
+}
+
+int hx_kernel_stats(char* names, int name_len, long long* launches, double* total_ms, int maxn) {
+  flush_timing();
+  int i = 0;
+  for (auto& kv : g_tim.stats) {
+    if (i < maxn) {
+      if (names && name_len > 0) {
+        std::strncpy(names + (size_t)i * name_len, kv.first.c_str(), name_len - 1);
+        names[(size_t)i * name_len + name_len - 1] = 0;
+      }
+      if (launches) launches[i] = kv.second.first;
+      if (total_ms) total_ms[i] = kv.second.second;
+    }
+    ++i;
+  }
+  return i;
+}
+
+long long hx_launch_count(void) { return g_tim.launches; }
+
+int hx_synchronize(void) {
+  return run([] { if (g_stream) ck(cudaStreamSynchronize(g_stream), "cudaStreamSynchronize"); });
+}
+
+}  // extern "C"

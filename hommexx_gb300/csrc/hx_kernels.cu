@@ -1,0 +1,1297 @@
+// hx_kernels.cu — hand-written sm_103a kernels of the preqx dycore step.
+//
+// Thread mapping of the element kernels: one CTA per element (or per element x
+// tracer), 16*LG threads; thread (p = tid % 16, lg = tid / 16) owns GLL point p on
+// levels lg, lg+LG, ...  The 16 points of a level sit in one half-warp, so the 4x4
+// derivative contractions of the sphere operators are register shuffles within the
+// half-warp (no shared memory, no barriers).  Vertical scans go through shared memory
+// ([lev][17] rows) and run as segmented warp scans in double.  DSS is a gather over a
+// precomputed table (whole mesh resident, no buffers, no MPI): each output point adds
+// its neighbours' values in the reference's fixed order, in double.
+//
+// Reference routines restated here (all under src/share/cxx/):
+//   SphereOperators.hpp:291-862, CaarFunctorImpl.hpp:97-889, CaarFunctor.cpp:96-116,
+//   HyperviscosityFunctorImpl.{hpp:72-257,cpp:56-112}, EulerStepFunctorImpl.hpp:118-884,
+//   RemapFunctor.hpp:299-463, PpmRemap.hpp:174-689, BoundaryExchange.cpp:285-849,
+//   prim_driver.cpp:90-206, prim_step.cpp:42-66, prim_advance_exp.cpp:138-156.
+#include <cstdio>
+
+#include "hx_kernels.cuh"
+
+namespace hx {
+
+namespace {
+
+constexpr unsigned FULL = 0xffffffffu;
+constexpr int SROW = 17;  // padded shared-memory row of 16 points
+
+__constant__ double c_dvv[16];
+__constant__ float c_dvvf[16];
+__constant__ double c_hyai[NLEV + 1];
+__constant__ double c_hybi[NLEV + 1];
+__constant__ double c_ai_delta[NLEV];
+__constant__ double c_bi_delta[NLEV];
+
+template <typename R> __device__ __forceinline__ R dvv_at(int a, int b);
+template <> __device__ __forceinline__ double dvv_at<double>(int a, int b) { return c_dvv[a * 4 + b]; }
+template <> __device__ __forceinline__ float dvv_at<float>(int a, int b) { return c_dvvf[a * 4 + b]; }
+
+template <typename R> __device__ __forceinline__ R sh16(R v, int src) {
+  return __shfl_sync(FULL, v, src, 16);
+}
+
+template <typename R> __device__ __forceinline__ R rre() { return R(kRrearth); }
+
+// Per-thread GLL point data: index, dvv rows/columns for the four contractions.
+template <typename R>
+struct Pt {
+  int p, i, j;
+  R dx[4], dy[4], tx[4], ty[4];
+  __device__ __forceinline__ void init(int p_) {
+    p = p_;
+    i = p >> 2;
+    j = p & 3;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      dx[k] = dvv_at<R>(j, k);
+      dy[k] = dvv_at<R>(i, k);
+      tx[k] = dvv_at<R>(k, j);
+      ty[k] = dvv_at<R>(k, i);
+    }
+  }
+  // sum_k dvv[j][k] s(i,k)  — derivative along jgp (x1)
+  __device__ __forceinline__ R ddx(R s) const {
+    R a = 0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) a += dx[k] * sh16(s, 4 * i + k);
+    return a;
+  }
+  // sum_k dvv[i][k] s(k,j)  — derivative along igp (x2)
+  __device__ __forceinline__ R ddy(R s) const {
+    R a = 0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) a += dy[k] * sh16(s, 4 * k + j);
+    return a;
+  }
+  // sum_k w(i,k) dvv[k][j]  — weak-form row contraction
+  __device__ __forceinline__ R wrow(R w) const {
+    R a = 0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) a += sh16(w, 4 * i + k) * tx[k];
+    return a;
+  }
+  // sum_k w(k,j) dvv[k][i]  — weak-form column contraction
+  __device__ __forceinline__ R wcol(R w) const {
+    R a = 0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) a += sh16(w, 4 * k + j) * ty[k];
+    return a;
+  }
+};
+
+// Metric of one GLL point of one element.
+template <typename R>
+struct PM {
+  R di00, di01, di10, di11, d00, d01, d10, d11, md, fdiv, sp, mp, a00, a01, a10, a11, rsp;
+  __device__ __forceinline__ void load(const MetricP<R>& m, int e, int p) {
+    const R* Di = m.Dinv + (size_t)e * 64;
+    const R* D = m.D + (size_t)e * 64;
+    const R* Mi = m.metinv + (size_t)e * 64;
+    di00 = Di[p]; di01 = Di[16 + p]; di10 = Di[32 + p]; di11 = Di[48 + p];
+    d00 = D[p]; d01 = D[16 + p]; d10 = D[32 + p]; d11 = D[48 + p];
+    md = m.metdet[(size_t)e * 16 + p];
+    fdiv = R(1.0) / md * rre<R>();
+    sp = m.spheremp[(size_t)e * 16 + p];
+    rsp = m.rspheremp[(size_t)e * 16 + p];
+    mp = m.mp[(size_t)e * 16 + p];
+    a00 = Mi[p] * md; a01 = Mi[16 + p] * md; a10 = Mi[32 + p] * md; a11 = Mi[48 + p] * md;
+  }
+};
+
+// ---- sphere operators on one point-level (SphereOperators.hpp) ------------------------
+template <typename R>
+__device__ __forceinline__ void gradient_sphere(const Pt<R>& t, const PM<R>& m, R s, R& g0, R& g1) {
+  const R v0 = t.ddx(s) * rre<R>();
+  const R v1 = t.ddy(s) * rre<R>();
+  g0 = m.di00 * v0 + m.di01 * v1;
+  g1 = m.di10 * v0 + m.di11 * v1;
+}
+
+template <typename R>
+__device__ __forceinline__ R divergence_sphere(const Pt<R>& t, const PM<R>& m, R v0, R v1) {
+  const R gv0 = (m.di00 * v0 + m.di10 * v1) * m.md;
+  const R gv1 = (m.di01 * v0 + m.di11 * v1) * m.md;
+  return (t.ddx(gv0) + t.ddy(gv1)) * m.fdiv;
+}
+
+template <typename R>
+__device__ __forceinline__ R vorticity_sphere(const Pt<R>& t, const PM<R>& m, R v0, R v1) {
+  const R c0 = m.d00 * v0 + m.d01 * v1;
+  const R c1 = m.d10 * v0 + m.d11 * v1;
+  return (t.ddx(c1) - t.ddy(c0)) * m.fdiv;
+}
+
+// divergence_sphere_wk of the vector (g0, g1)
+template <typename R>
+__device__ __forceinline__ R divergence_sphere_wk(const Pt<R>& t, const PM<R>& m, R g0, R g1) {
+  const R w0 = m.sp * (m.di00 * g0 + m.di10 * g1);
+  const R w1 = m.sp * (m.di01 * g0 + m.di11 * g1);
+  return -(t.wrow(w0) + t.wcol(w1)) * rre<R>();
+}
+
+template <typename R>
+__device__ __forceinline__ R laplace_simple(const Pt<R>& t, const PM<R>& m, R s) {
+  R g0, g1;
+  gradient_sphere(t, m, s, g0, g1);
+  return divergence_sphere_wk(t, m, g0, g1);
+}
+
+template <typename R>
+__device__ __forceinline__ R laplace_tensor(const Pt<R>& t, const PM<R>& m, const R* tv, R s) {
+  R g0, g1;
+  gradient_sphere(t, m, s, g0, g1);
+  const R t0 = tv[0] * g0 + tv[2] * g1;
+  const R t1 = tv[1] * g0 + tv[3] * g1;
+  return divergence_sphere_wk(t, m, t0, t1);
+}
+
+// vlaplace_sphere_wk_contra (SphereOperators.hpp:816-862)
+template <typename R>
+__device__ __forceinline__ void vlaplace_contra(const Pt<R>& t, const PM<R>& m, R nu_ratio, R v0, R v1,
+                                                R& l0, R& l1) {
+  R div = divergence_sphere(t, m, v0, v1);
+  if (nu_ratio > R(0) && nu_ratio != R(1)) div *= nu_ratio;
+  // grad_sphere_wk_testcov(div)
+  const R w = m.mp * div;
+  const R X = t.wrow(w), Y = t.wcol(w);
+  const R b0 = -(m.a00 * X + m.a01 * Y);
+  const R b1 = -(m.a10 * X + m.a11 * Y);
+  R g0 = (m.d00 * b0 + m.d10 * b1) * rre<R>();
+  R g1 = (m.d01 * b0 + m.d11 * b1) * rre<R>();
+  // curl_sphere_wk_testcov_update(-1, 1, vort, g)
+  const R vort = vorticity_sphere(t, m, v0, v1);
+  const R wv = m.mp * vort;
+  const R sb0 = -t.wcol(wv), sb1 = t.wrow(wv);
+  g0 = g0 - (m.d00 * sb0 + m.d10 * sb1) * rre<R>();
+  g1 = g1 - (m.d01 * sb0 + m.d11 * sb1) * rre<R>();
+  const R f = R(2) * m.sp * rre<R>() * rre<R>();
+  l0 = f * v0 + g0;
+  l1 = f * v1 + g1;
+}
+
+// vlaplace_sphere_wk_cartesian (SphereOperators.hpp:750-814); tv = tensorVisc[0..3],
+// s2c = vec_sph2cart[2][3] of this point.
+template <typename R>
+__device__ __forceinline__ void vlaplace_cartesian(const Pt<R>& t, const PM<R>& m, const R* tv, const R* s2c,
+                                                   R v0, R v1, R& l0, R& l1) {
+  R lc[3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) lc[c] = laplace_tensor(t, m, tv, s2c[c] * v0 + s2c[3 + c] * v1);
+  const R f = R(2) * m.sp * rre<R>() * rre<R>();
+  l0 = s2c[0] * lc[0] + s2c[1] * lc[1] + s2c[2] * lc[2] + f * v0;
+  l1 = s2c[3] * lc[0] + s2c[4] * lc[1] + s2c[5] * lc[2] + f * v1;
+}
+
+// DSS gather of one point-level: own value plus the table's sources, in order, in double.
+template <typename T>
+__device__ __forceinline__ double dss_gather(const T* base, long long es, int ls, int e, int l, int p,
+                                             const DssTable& tab) {
+  const int ep = e * 16 + p;
+  double acc = (double)base[(size_t)e * es + (size_t)l * ls + p];
+  const int n = tab.cnt[ep];
+  for (int k = 0; k < n; ++k) {
+    const int s = tab.src[ep * MAXSRC + k];
+    acc += (double)base[(size_t)(s >> 4) * es + (size_t)l * ls + (s & 15)];
+  }
+  return acc;
+}
+
+// ---- segmented column scans (128 threads: 16 columns x 8 segments of 9 levels) ------
+// Exclusive prefix of the per-segment totals within an 8-lane group.
+__device__ __forceinline__ double seg_excl_prefix(double tot, int seg) {
+  double incl = tot;
+#pragma unroll
+  for (int off = 1; off < 8; off <<= 1) {
+    const double y = __shfl_up_sync(FULL, incl, off, 8);
+    if (seg >= off) incl += y;
+  }
+  double ex = __shfl_up_sync(FULL, incl, 1, 8);
+  return seg == 0 ? 0.0 : ex;
+}
+// Exclusive suffix (sum of later segments).
+__device__ __forceinline__ double seg_excl_suffix(double tot, int seg) {
+  double incl = tot;
+#pragma unroll
+  for (int off = 1; off < 8; off <<= 1) {
+    const double y = __shfl_down_sync(FULL, incl, off, 8);
+    if (seg + off < 8) incl += y;
+  }
+  double ex = __shfl_down_sync(FULL, incl, 1, 8);
+  return seg == 7 ? 0.0 : ex;
+}
+
+// ======================================================================================
+// Caar RK stage (CaarFunctorImpl::operator(), rsplit > 0), one CTA per element.
+// Writes the pre-DSS v, T, dp3d of time level np1 to a.out; updates vn0, omega_p, phi.
+// ======================================================================================
+template <typename R, int LG>
+__global__ void __launch_bounds__(LG * 16) k_caar(CaarArgs<R> a) {
+  constexpr int NL = NLEV / LG;
+  extern __shared__ double sm[];
+  double* s_dp = sm;                    // dp3d(n0), later phi
+  double* s_tv = sm + NLEV * SROW;      // T_v
+  double* s_div = sm + 2 * NLEV * SROW; // div(v dp)
+  double* s_p = sm + 3 * NLEV * SROW;   // pressure
+  double* s_om = sm + 4 * NLEV * SROW;  // sum_{j<k} div_vdp_j
+  const int e = blockIdx.x, tid = threadIdx.x, p = tid & 15, lg = tid >> 4;
+  Pt<R> t;
+  t.init(p);
+  PM<R> m;
+  m.load(a.m, e, p);
+  const R eta = R(a.eta_ave_w);
+  const size_t vN0 = ((size_t)e * NTL + a.n0) * NLEV * 32;
+  const size_t sN0 = ((size_t)e * NTL + a.n0) * NLEV * 16;
+  // ---- phase A: v dp, vn0, div(v dp), T_v ----
+#pragma unroll 1
+  for (int k = 0; k < NL; ++k) {
+    const int l = lg + LG * k;
+    const R u = a.v[vN0 + l * 32 + p], w = a.v[vN0 + l * 32 + 16 + p];
+    const R tt = a.T[sN0 + l * 16 + p], d = a.dp[sN0 + l * 16 + p];
+    const R vd0 = u * d, vd1 = w * d;
+    const size_t iv = ((size_t)e * NLEV + l) * 32 + p;
+    a.vn0[iv] += eta * vd0;
+    a.vn0[iv + 16] += eta * vd1;
+    const R div = divergence_sphere(t, m, vd0, vd1);
+    R tv = tt;
+    if (a.n0_qdp >= 0) {
+      R Qt = R(a.qdp[((((size_t)e * QTL + a.n0_qdp) * a.qsize) * NLEV + l) * 16 + p]) / d;
+      Qt *= R(kRwaterVapor / kRgas - 1.0);
+      Qt += R(1);
+      tv = tt * Qt;
+    }
+    s_dp[l * SROW + p] = (double)d;
+    s_tv[l * SROW + p] = (double)tv;
+    s_div[l * SROW + p] = (double)div;
+  }
+  __syncthreads();
+  // ---- phase B: pressure, geopotential, omega integral (double) ----
+  if (tid < 128) {
+    const int col = tid >> 3, seg = tid & 7, l0 = seg * 9;
+    // pressure: p_k = p_{k-1} + (dp_{k-1} + dp_k)/2, p_{-1} = hyai0 ps0, dp_{-1} = 0
+    double prev = seg == 0 ? 0.0 : s_dp[(l0 - 1) * SROW + col];
+    double tot = 0.0;
+#pragma unroll
+    for (int k = 0; k < 9; ++k) {
+      const double d = s_dp[(l0 + k) * SROW + col];
+      tot += 0.5 * (prev + d);
+      prev = d;
+    }
+    double pr = a.p_top + seg_excl_prefix(tot, seg);
+    prev = seg == 0 ? 0.0 : s_dp[(l0 - 1) * SROW + col];
+    double r[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) {
+      const double d = s_dp[(l0 + k) * SROW + col];
+      pr = pr + 0.5 * (prev + d);
+      prev = d;
+      s_p[(l0 + k) * SROW + col] = pr;
+      r[k] = kRgas * s_tv[(l0 + k) * SROW + col] * (d * 0.5 / pr);
+    }
+    // geopotential: phi_k = phis + 2 sum_{j>k} r_j + r_k
+    double rt = 0.0;
+#pragma unroll
+    for (int k = 0; k < 9; ++k) rt += r[k];
+    double integ = seg_excl_suffix(rt, seg);
+    const double phis = (double)a.m.phis[(size_t)e * 16 + col];
+    R* phig = a.phi + (size_t)e * NLEV * 16;
+#pragma unroll
+    for (int k = 8; k >= 0; --k) {
+      const double ph = phis + 2.0 * integ + r[k];
+      integ = integ + r[k];
+      s_dp[(l0 + k) * SROW + col] = ph;  // dp no longer needed: holds phi now
+      phig[(l0 + k) * 16 + col] = (R)ph;
+    }
+    // omega integral: exclusive prefix of div_vdp
+    double dt_ = 0.0;
+#pragma unroll
+    for (int k = 0; k < 9; ++k) dt_ += s_div[(l0 + k) * SROW + col];
+    double acc = seg_excl_prefix(dt_, seg);
+#pragma unroll
+    for (int k = 0; k < 9; ++k) {
+      s_om[(l0 + k) * SROW + col] = acc;
+      acc = acc + s_div[(l0 + k) * SROW + col];
+    }
+  }
+  __syncthreads();
+  // ---- phase C: omega_p, T, v, dp3d at np1 ----
+  const R dt = R(a.dt);
+  const R fcor = a.m.fcor[(size_t)e * 16 + p];
+  const size_t vM = ((size_t)e * NTL + a.nm1) * NLEV * 32;
+  const size_t sM = ((size_t)e * NTL + a.nm1) * NLEV * 16;
+  const size_t vO = ((size_t)e * NTL + a.n0orig) * NLEV * 32;
+  const size_t sO = ((size_t)e * NTL + a.n0orig) * NLEV * 16;
+  R* out = a.out + (size_t)e * NLEV * 64;
+#pragma unroll 1
+  for (int k = 0; k < NL; ++k) {
+    const int l = lg + LG * k;
+    const R pr = (R)s_p[l * SROW + p];
+    R gp0, gp1;
+    gradient_sphere(t, m, pr, gp0, gp1);
+    const R u = a.v[vN0 + l * 32 + p], w = a.v[vN0 + l * 32 + 16 + p];
+    const R tt = a.T[sN0 + l * 16 + p];
+    const R div = (R)s_div[l * SROW + p];
+    const R vgp = u * gp0 + w * gp1;
+    const R omega = (vgp - ((R)s_om[l * SROW + p] + R(0.5) * div)) / pr;
+    a.omega_p[((size_t)e * NLEV + l) * 16 + p] += eta * omega;
+    // time level "nm1" (RK combine of stage 5 fused here)
+    R tm = a.T[sM + l * 16 + p], dm = a.dp[sM + l * 16 + p];
+    R vm0 = a.v[vM + l * 32 + p], vm1 = a.v[vM + l * 32 + 16 + p];
+    if (a.rk_combine) {
+      tm = (R(5) * tm - a.T[sO + l * 16 + p]) / R(4);
+      dm = (R(5) * dm - a.dp[sO + l * 16 + p]) / R(4);
+      vm0 = (R(5) * vm0 - a.v[vO + l * 32 + p]) / R(4);
+      vm1 = (R(5) * vm1 - a.v[vO + l * 32 + 16 + p]) / R(4);
+      a.T[sM + l * 16 + p] = tm;
+      a.dp[sM + l * 16 + p] = dm;
+      a.v[vM + l * 32 + p] = vm0;
+      a.v[vM + l * 32 + 16 + p] = vm1;
+    }
+    // temperature (compute_temperature_np1)
+    R gt0, gt1;
+    gradient_sphere(t, m, tt, gt0, gt1);
+    const R tv = (R)s_tv[l * SROW + p];
+    const R vgt = u * gt0 + w * gt1;
+    const R ttens = -vgt + R(kKappa) * tv * omega;
+    const R tnew = m.sp * (ttens * dt + tm);
+    // velocity (compute_velocity_np1 with compute_energy_grad)
+    const R rr = R(kRgas) * (tv / pr);
+    R eg0 = rr * gp0, eg1 = rr * gp1;
+    const R ephi = R(0.5) * (u * u + w * w) + (R)s_dp[l * SROW + p];
+    R ge0, ge1;
+    gradient_sphere(t, m, ephi, ge0, ge1);
+    eg0 += ge0;
+    eg1 += ge1;
+    const R vort = vorticity_sphere(t, m, u, w) + fcor;
+    eg0 = -eg0 + w * vort;
+    eg1 = -eg1 - u * vort;
+    const R vn0_ = m.sp * (eg0 * dt + vm0);
+    const R vn1_ = m.sp * (eg1 * dt + vm1);
+    // dp3d (compute_dp3d_np1, eta_dot_dpdn = 0 for rsplit > 0)
+    const R dnew = m.sp * (dm - div * dt);
+    out[l * 64 + p] = vn0_;
+    out[l * 64 + 16 + p] = vn1_;
+    out[l * 64 + 32 + p] = tnew;
+    out[l * 64 + 48 + p] = dnew;
+  }
+}
+
+// DSS of the Caar output into the state of time level np1, times rspheremp
+// (BoundaryExchange::exchange(rspheremp) on v, T, dp3d: CaarFunctor.cpp:114).
+template <typename R>
+__global__ void k_dss_state(int E, const R* __restrict__ src, R* v, R* T, R* dp, int np1,
+                            const R* __restrict__ rsmp, DssTable tab) {
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= E * NLEV * 16) return;
+  const int e = idx / (NLEV * 16), l = (idx / 16) % NLEV, p = idx & 15;
+  const double r = (double)rsmp[e * 16 + p];
+  const double a0 = dss_gather(src, NLEV * 64, 64, e, l, p, tab) * r;
+  const double a1 = dss_gather(src + 16, NLEV * 64, 64, e, l, p, tab) * r;
+  const double a2 = dss_gather(src + 32, NLEV * 64, 64, e, l, p, tab) * r;
+  const double a3 = dss_gather(src + 48, NLEV * 64, 64, e, l, p, tab) * r;
+  const size_t vb = (((size_t)e * NTL + np1) * NLEV + l) * 32 + p;
+  const size_t sb = (((size_t)e * NTL + np1) * NLEV + l) * 16 + p;
+  v[vb] = (R)a0;
+  v[vb + 16] = (R)a1;
+  T[sb] = (R)a2;
+  dp[sb] = (R)a3;
+}
+
+// ======================================================================================
+// Hyperviscosity (HyperviscosityFunctorImpl): three kernels per subcycle.
+// ======================================================================================
+// TagFirstLaplaceHV: laplacians of the np1 state -> bufA (pre-DSS).
+template <typename R, int LG>
+__global__ void __launch_bounds__(LG * 16) k_hv_lap1(HvArgs<R> a) {
+  constexpr int NL = NLEV / LG;
+  const int e = blockIdx.x, tid = threadIdx.x, p = tid & 15, lg = tid >> 4;
+  Pt<R> t;
+  t.init(p);
+  PM<R> m;
+  m.load(a.m, e, p);
+  const size_t vb = ((size_t)e * NTL + a.np1) * NLEV * 32;
+  const size_t sb = ((size_t)e * NTL + a.np1) * NLEV * 16;
+  R* out = a.bufA + (size_t)e * NLEV * 64;
+  const R nr = R(a.nu_ratio1);
+#pragma unroll 1
+  for (int k = 0; k < NL; ++k) {
+    const int l = lg + LG * k;
+    const R lt = laplace_simple(t, m, a.T[sb + l * 16 + p]);
+    const R ld = laplace_simple(t, m, a.dp[sb + l * 16 + p]);
+    R l0, l1;
+    vlaplace_contra(t, m, nr, a.v[vb + l * 32 + p], a.v[vb + l * 32 + 16 + p], l0, l1);
+    out[l * 64 + p] = l0;
+    out[l * 64 + 16 + p] = l1;
+    out[l * 64 + 32 + p] = lt;
+    out[l * 64 + 48 + p] = ld;
+  }
+}
+
+// DSS(rspheremp) of bufA, second laplacian, TagHyperPreExchange -> bufB (pre-DSS).
+template <typename R, int LG>
+__global__ void __launch_bounds__(LG * 16) k_hv_lap2(HvArgs<R> a) {
+  constexpr int NL = NLEV / LG;
+  const int e = blockIdx.x, tid = threadIdx.x, p = tid & 15, lg = tid >> 4;
+  Pt<R> t;
+  t.init(p);
+  PM<R> m;
+  m.load(a.m, e, p);
+  R tv[4], s2c[6];
+  if (!a.consthv) {
+#pragma unroll
+    for (int c = 0; c < 4; ++c) tv[c] = a.m.tensorvisc[(size_t)e * 64 + c * 16 + p];
+#pragma unroll
+    for (int c = 0; c < 6; ++c) s2c[c] = a.m.vec_sph2cart[(size_t)e * 96 + c * 16 + p];
+  }
+  const size_t vb = ((size_t)e * NTL + a.np1) * NLEV * 32;
+  const size_t sb = ((size_t)e * NTL + a.np1) * NLEV * 16;
+  R* out = a.bufB + (size_t)e * NLEV * 64;
+  const double rs = (double)m.rsp;
+  const R eta_h = R(a.eta_ave_w);
+  const R hs = R(a.hsub);
+  const R dt = R(a.dt);
+#pragma unroll 1
+  for (int k = 0; k < NL; ++k) {
+    const int l = lg + LG * k;
+    const R v0 = (R)(dss_gather(a.bufA, NLEV * 64, 64, e, l, p, a.dss) * rs);
+    const R v1 = (R)(dss_gather(a.bufA + 16, NLEV * 64, 64, e, l, p, a.dss) * rs);
+    const R t1 = (R)(dss_gather(a.bufA + 32, NLEV * 64, 64, e, l, p, a.dss) * rs);
+    const R d1 = (R)(dss_gather(a.bufA + 48, NLEV * 64, 64, e, l, p, a.dss) * rs);
+    R lt, ld, l0, l1;
+    if (a.consthv) {
+      lt = laplace_simple(t, m, t1);
+      ld = laplace_simple(t, m, d1);
+      vlaplace_contra(t, m, R(a.nu_ratio2), v0, v1, l0, l1);
+    } else {
+      lt = laplace_tensor(t, m, tv, t1);
+      ld = laplace_tensor(t, m, tv, d1);
+      vlaplace_cartesian(t, m, tv, s2c, v0, v1, l0, l1);
+    }
+    const size_t i3 = ((size_t)e * NLEV + l) * 16 + p;
+    const R dpn = a.dp[sb + l * 16 + p];
+    a.dpdiss_ave[i3] += eta_h * dpn / hs;
+    a.dpdiss_bih[i3] += eta_h * ld / hs;
+    R vt0 = l0 * R(-a.nu), vt1 = l1 * R(-a.nu);
+    R ttn = lt * R(-a.nu_s), dpt = ld * R(-a.nu_p);
+    if (a.nu_top > 0 && __any_sync(FULL, l < 3)) {
+      // nu_top sponge on the top three levels, applied to the np1 state
+      const R un = a.v[vb + l * 32 + p], wn = a.v[vb + l * 32 + 16 + p];
+      R lv0, lv1;
+      vlaplace_contra(t, m, R(1), un, wn, lv0, lv1);
+      const R ltt = laplace_simple(t, m, a.T[sb + l * 16 + p]);
+      const R ldd = laplace_simple(t, m, dpn);
+      if (l < 3) {
+        const R sc = R((l == 0 ? 4.0 : l == 1 ? 2.0 : 1.0) * a.nu_top);
+        vt0 += sc * lv0;
+        vt1 += sc * lv1;
+        ttn += sc * ltt;
+        dpt += sc * ldd;
+      }
+    }
+    dpt = dpt * dt + dpn * m.sp;
+    out[l * 64 + p] = vt0;
+    out[l * 64 + 16 + p] = vt1;
+    out[l * 64 + 32 + p] = ttn;
+    out[l * 64 + 48 + p] = dpt;
+  }
+}
+
+// DSS of bufB and TagUpdateStates.
+template <typename R>
+__global__ void k_hv_update(HvArgs<R> a, int E) {
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= E * NLEV * 16) return;
+  const int e = idx / (NLEV * 16), l = (idx / 16) % NLEV, p = idx & 15;
+  const R rs = a.m.rspheremp[e * 16 + p];
+  const R dt = R(a.dt);
+  R vt0 = (R)dss_gather(a.bufB, NLEV * 64, 64, e, l, p, a.dss);
+  R vt1 = (R)dss_gather(a.bufB + 16, NLEV * 64, 64, e, l, p, a.dss);
+  R tt = (R)dss_gather(a.bufB + 32, NLEV * 64, 64, e, l, p, a.dss);
+  const R dpt = (R)dss_gather(a.bufB + 48, NLEV * 64, 64, e, l, p, a.dss);
+  const size_t vb = (((size_t)e * NTL + a.np1) * NLEV + l) * 32 + p;
+  const size_t sb = (((size_t)e * NTL + a.np1) * NLEV + l) * 16 + p;
+  vt0 = dt * vt0 * rs;
+  vt1 = dt * vt1 * rs;
+  const R v0 = a.v[vb] + vt0, v1 = a.v[vb + 16] + vt1;
+  a.v[vb] = v0;
+  a.v[vb + 16] = v1;
+  tt = dt * tt * rs;
+  const R heating = vt0 * v0 + vt1 * v1;
+  a.T[sb] = a.T[sb] + tt - heating / R(kCp);
+  a.dp[sb] = dpt * rs;
+}
+
+// ======================================================================================
+// Small element-wise kernels
+// ======================================================================================
+template <typename R>
+__global__ void k_prim_step_init(int E, R* eta, R* vn0, R* omega_p, R* dpa, R* dpb, R* derived_dp,
+                                 const R* dp, int n0, int zero_diss) {
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= E * NLEV * 16) return;
+  const int e = idx / (NLEV * 16), r = idx % (NLEV * 16), l = r / 16, p = r & 15;
+  eta[idx] = 0;
+  omega_p[idx] = 0;
+  vn0[((size_t)e * NLEV + l) * 32 + p] = 0;
+  vn0[((size_t)e * NLEV + l) * 32 + 16 + p] = 0;
+  if (zero_diss) {
+    dpa[idx] = 0;
+    dpb[idx] = 0;
+  }
+  derived_dp[idx] = dp[((size_t)e * NTL + n0) * NLEV * 16 + r];
+}
+
+template <typename R>
+__global__ void k_dp_from_ps(int E, R* dp, const double* ps_v, int n0, double ps0) {
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= E * NLEV * 16) return;
+  const int e = idx / (NLEV * 16), r = idx % (NLEV * 16), l = r / 16, p = r & 15;
+  dp[((size_t)e * NTL + n0) * NLEV * 16 + r] =
+      (R)(c_ai_delta[l] * ps0 + c_bi_delta[l] * ps_v[((size_t)e * NTL + n0) * 16 + p]);
+}
+
+template <typename R>
+__global__ void k_update_q(int E, int Q, const double* qdp, double* Qc, const double* ps_v, int np1,
+                           int np1_qdp, double ps0) {
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (long long)E * Q * NLEV * 16) return;
+  const int p = idx & 15;
+  const int l = (idx / 16) % NLEV;
+  const int q = (idx / (16 * NLEV)) % Q;
+  const int e = idx / (16LL * NLEV * Q);
+  const double dp = c_ai_delta[l] * ps0 + c_bi_delta[l] * ps_v[((size_t)e * NTL + np1) * 16 + p];
+  Qc[idx] = qdp[((((size_t)e * QTL + np1_qdp) * Q + q) * NLEV + l) * 16 + p] / dp;
+}
+
+// ======================================================================================
+// Tracers (EulerStepFunctorImpl)
+// ======================================================================================
+// PrecomputeDivDp: divdp = div(vn0), divdp_proj = divdp.
+template <typename R, int LG>
+__global__ void __launch_bounds__(LG * 16) k_precompute_divdp(EulerArgs<R> a) {
+  constexpr int NL = NLEV / LG;
+  const int e = blockIdx.x, tid = threadIdx.x, p = tid & 15, lg = tid >> 4;
+  Pt<R> t;
+  t.init(p);
+  PM<R> m;
+  m.load(a.m, e, p);
+#pragma unroll 1
+  for (int k = 0; k < NL; ++k) {
+    const int l = lg + LG * k;
+    const size_t iv = ((size_t)e * NLEV + l) * 32 + p;
+    const R d = divergence_sphere(t, m, a.vn0[iv], a.vn0[iv + 16]);
+    const size_t i3 = ((size_t)e * NLEV + l) * 16 + p;
+    a.divdp[i3] = d;
+    a.divdp_proj[i3] = d;
+  }
+}
+
+// compute_dp + compute_qmin_qmax for one (element, tracer): qlim out, Q into qtens when
+// the biharmonic needs it.  Reads qlim (rhs_multiplier == 1) or writes qlim_out.
+template <typename R, int LG>
+__global__ void __launch_bounds__(LG * 16) k_qminmax(EulerArgs<R> a, double* qlim_out, int store_q) {
+  constexpr int NL = NLEV / LG;
+  const int eq = blockIdx.x, e = eq / a.Q, q = eq % a.Q;
+  const int tid = threadIdx.x, p = tid & 15, lg = tid >> 4;
+  const R rhsdt = R(a.rhs_multiplier * a.dt);
+#pragma unroll 1
+  for (int k = 0; k < NL; ++k) {
+    const int l = lg + LG * k;
+    const size_t i3 = ((size_t)e * NLEV + l) * 16 + p;
+    const R dpt = a.derived_dp[i3] - rhsdt * a.divdp_proj[i3];
+    const double qv = a.qdp[((((size_t)e * QTL + a.n0_qdp) * a.Q + q) * NLEV + l) * 16 + p];
+    const R val = R(qv) / dpt;
+    if (store_q) a.qtens[(((size_t)e * a.Q + q) * NLEV + l) * 16 + p] = val;
+    double mn = (double)val, mx = (double)val;
+#pragma unroll
+    for (int off = 8; off >= 1; off >>= 1) {
+      mn = fmin(mn, __shfl_xor_sync(FULL, mn, off, 16));
+      mx = fmax(mx, __shfl_xor_sync(FULL, mx, off, 16));
+    }
+    if (p == 0) {
+      double* ql = qlim_out + ((size_t)e * a.Q + q) * 2 * NLEV;
+      if (a.rhs_multiplier == 1.0) {
+        const double* qo = a.qlim + ((size_t)e * a.Q + q) * 2 * NLEV;
+        mn = fmin(qo[l], mn);
+        mx = fmax(qo[NLEV + l], mx);
+      }
+      ql[l] = mn;
+      ql[NLEV + l] = mx;
+    }
+  }
+}
+
+// Neighbour min/max (exchange_min_max): qlim = minmax(own, all connected neighbours).
+__global__ void k_minmax_nbr(int E, int Q, const double* __restrict__ pre, double* qlim,
+                             const int* __restrict__ conn) {
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= E * Q * NLEV) return;
+  const int l = idx % NLEV, q = (idx / NLEV) % Q, e = idx / (NLEV * Q);
+  double mn = pre[((size_t)e * Q + q) * 2 * NLEV + l];
+  double mx = pre[((size_t)e * Q + q) * 2 * NLEV + NLEV + l];
+  for (int s = 0; s < 8; ++s) {
+    const int r = conn[e * 8 + s];
+    if (r < 0) continue;
+    mn = fmin(mn, pre[((size_t)r * Q + q) * 2 * NLEV + l]);
+    mx = fmax(mx, pre[((size_t)r * Q + q) * 2 * NLEV + NLEV + l]);
+  }
+  qlim[((size_t)e * Q + q) * 2 * NLEV + l] = mn;
+  qlim[((size_t)e * Q + q) * 2 * NLEV + NLEV + l] = mx;
+}
+
+// BIHPre: qtens (Q) [* dpdiss_ave / dp0] -> laplace -> qscr (pre-DSS).
+template <typename R, int LG>
+__global__ void __launch_bounds__(LG * 16) k_bih_pre(EulerArgs<R> a) {
+  constexpr int NL = NLEV / LG;
+  const int eq = blockIdx.x, e = eq / a.Q, q = eq % a.Q;
+  const int tid = threadIdx.x, p = tid & 15, lg = tid >> 4;
+  Pt<R> t;
+  t.init(p);
+  PM<R> m;
+  m.load(a.m, e, p);
+  const size_t qb = ((size_t)e * a.Q + q) * NLEV * 16;
+#pragma unroll 1
+  for (int k = 0; k < NL; ++k) {
+    const int l = lg + LG * k;
+    R s = a.qtens[qb + l * 16 + p];
+    if (a.nu_p > 0) s = s * a.dpdiss_ave[((size_t)e * NLEV + l) * 16 + p] / R(a.dp0[l]);
+    a.qscr[qb + l * 16 + p] = laplace_simple(t, m, s);
+  }
+}
+
+// DSS(rspheremp) of qscr, BIHPostConstHV/TensorHV laplace, rhsviss_adjustment -> qtens.
+template <typename R, int LG>
+__global__ void __launch_bounds__(LG * 16) k_bih_post(EulerArgs<R> a) {
+  constexpr int NL = NLEV / LG;
+  const int eq = blockIdx.x, e = eq / a.Q, q = eq % a.Q;
+  const int tid = threadIdx.x, p = tid & 15, lg = tid >> 4;
+  Pt<R> t;
+  t.init(p);
+  PM<R> m;
+  m.load(a.m, e, p);
+  R tv[4];
+  if (!a.consthv) {
+#pragma unroll
+    for (int c = 0; c < 4; ++c) tv[c] = a.m.tensorvisc[(size_t)e * 64 + c * 16 + p];
+  }
+  const size_t qb = ((size_t)e * a.Q + q) * NLEV * 16;
+  const R* fbase = a.qscr + (size_t)q * NLEV * 16;
+  const R fac = R(-a.rhs_viss * a.dt * a.nu_q);
+  const double rs = (double)m.rsp;
+#pragma unroll 1
+  for (int k = 0; k < NL; ++k) {
+    const int l = lg + LG * k;
+    const R s = (R)(dss_gather(fbase, (long long)a.Q * NLEV * 16, 16, e, l, p, a.dss) * rs);
+    const R lap = a.consthv ? laplace_simple(t, m, s) : laplace_tensor(t, m, tv, s);
+    a.qtens[qb + l * 16 + p] = (fac * R(a.dp0[l]) * lap / m.sp);
+  }
+}
+
+// AALSetupPhase (compute_2d_advection_step): vstar, dpdissk, f_dss * spheremp -> fscr.
+template <typename R>
+__global__ void k_aal_setup(EulerArgs<R> a, int E) {
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= E * NLEV * 16) return;
+  const int e = idx / (NLEV * 16), l = (idx / 16) % NLEV, p = idx & 15;
+  const R rhsdt = R(a.rhs_multiplier * a.dt);
+  const R dpt = a.derived_dp[idx] - rhsdt * a.divdp_proj[idx];
+  const size_t iv = ((size_t)e * NLEV + l) * 32 + p;
+  a.vstar[iv] = a.vn0[iv] / dpt;
+  a.vstar[iv + 16] = a.vn0[iv + 16] / dpt;
+  R dk = dpt - R(a.dt) * a.divdp[idx];
+  if (a.nu_p > 0 && a.rhs_viss != 0.0)
+    dk += R(-a.rhs_viss * a.dt * a.nu_q) * a.dpdiss_bih[idx] / a.m.spheremp[e * 16 + p];
+  a.dpdissk[idx] = dk;
+  a.fscr[idx] = a.f_dss[idx] * a.m.spheremp[e * 16 + p];
+}
+
+// The quasi-monotone limiters of with_limiter_shell (EulerStepFunctorImpl.hpp:693-884)
+// on one level of 16 points, one thread, sums in point order.
+template <typename R>
+__device__ void limiter_level(int option, R* x, const R* c, double& minp_io, double& maxp_io) {
+  R s0 = 0, s1 = 0;
+#pragma unroll
+  for (int k = 0; k < 16; ++k) {
+    s0 += x[k] * c[k];
+    s1 += c[k];
+  }
+  if (s1 <= R(0)) return;
+  R minp = (R)minp_io, maxp = (R)maxp_io;
+  if (minp < R(0)) { minp = R(0); minp_io = 0.0; }
+  if (s0 < minp * s1) { minp = s0 / s1; minp_io = (double)minp; }
+  if (s0 > maxp * s1) { maxp = s0 / s1; maxp_io = (double)maxp; }
+  const R mass = s0;
+  if (option == 8) {
+    const R tol = R(5e-14);
+    for (int iter = 0; iter < 15; ++iter) {
+      R addmass = 0;
+#pragma unroll
+      for (int k = 0; k < 16; ++k) {
+        R delta = 0;
+        if (x[k] > maxp) { delta = x[k] - maxp; x[k] = maxp; }
+        else if (x[k] < minp) { delta = x[k] - minp; x[k] = minp; }
+        addmass += delta * c[k];
+      }
+      if (fabs(addmass) <= tol * fabs(mass)) break;
+      R wsum = 0;
+      if (addmass > R(0)) {
+#pragma unroll
+        for (int k = 0; k < 16; ++k) if (x[k] < maxp) wsum += c[k];
+        if (wsum == R(0)) break;
+        const R adw = addmass / wsum;
+#pragma unroll
+        for (int k = 0; k < 16; ++k) x[k] += (x[k] < maxp) ? adw : R(0);
+      } else {
+#pragma unroll
+        for (int k = 0; k < 16; ++k) if (x[k] > minp) wsum += c[k];
+        if (wsum == R(0)) break;
+        const R adw = addmass / wsum;
+#pragma unroll
+        for (int k = 0; k < 16; ++k) x[k] += (x[k] > minp) ? adw : R(0);
+      }
+    }
+  } else {
+    R addmass = 0;
+#pragma unroll
+    for (int k = 0; k < 16; ++k) {
+      R delta = 0;
+      if (x[k] > maxp) { delta = x[k] - maxp; x[k] = maxp; }
+      else if (x[k] < minp) { delta = x[k] - minp; x[k] = minp; }
+      addmass += delta * c[k];
+    }
+    if (addmass == R(0)) return;
+    R fac = 0;
+    if (addmass > R(0)) {
+#pragma unroll
+      for (int k = 0; k < 16; ++k) fac += c[k] * (maxp - x[k]);
+      if (fac > R(0)) {
+        fac = addmass / fac;
+#pragma unroll
+        for (int k = 0; k < 16; ++k) x[k] += fac * (maxp - x[k]);
+      }
+    } else {
+#pragma unroll
+      for (int k = 0; k < 16; ++k) fac += c[k] * (x[k] - minp);
+      if (fac > R(0)) {
+        fac = addmass / fac;
+#pragma unroll
+        for (int k = 0; k < 16; ++k) x[k] += fac * (x[k] - minp);
+      }
+    }
+  }
+}
+
+// AALTracerPhase: qtens = Qdp - dt div(vstar Qdp) [+ qtens_biharmonic], limiter,
+// spheremp -> qscr (pre-DSS).  One CTA per (element, tracer).
+template <typename R, int LG>
+__global__ void __launch_bounds__(LG * 16) k_aal_tracer(EulerArgs<R> a) {
+  constexpr int NL = NLEV / LG;
+  __shared__ R s_q[NLEV * SROW];
+  __shared__ R s_dm[NLEV * SROW];
+  __shared__ R s_sp[16];
+  const int eq = blockIdx.x, e = eq / a.Q, q = eq % a.Q;
+  const int tid = threadIdx.x, p = tid & 15, lg = tid >> 4;
+  Pt<R> t;
+  t.init(p);
+  PM<R> m;
+  m.load(a.m, e, p);
+  if (tid < 16) s_sp[tid] = m.sp;
+  const size_t qn0 = (((size_t)e * QTL + a.n0_qdp) * a.Q + q) * NLEV * 16;
+  const size_t qb = ((size_t)e * a.Q + q) * NLEV * 16;
+  const bool add_hv = a.rhs_viss != 0.0;
+  const R mdt = R(-a.dt);
+#pragma unroll 1
+  for (int k = 0; k < NL; ++k) {
+    const int l = lg + LG * k;
+    const R qd = (R)a.qdp[qn0 + l * 16 + p];
+    const size_t iv = ((size_t)e * NLEV + l) * 32 + p;
+    const R g0 = a.vstar[iv] * qd, g1 = a.vstar[iv + 16] * qd;
+    const R dv = divergence_sphere(t, m, g0, g1);
+    const R q0 = add_hv ? a.qtens[qb + l * 16 + p] : R(0);
+    s_q[l * SROW + p] = (qd + mdt * dv + q0);
+    s_dm[l * SROW + p] = a.dpdissk[((size_t)e * NLEV + l) * 16 + p];
+  }
+  __syncthreads();
+  for (int l = tid; l < NLEV; l += blockDim.x) {
+    R x[16], c[16];
+    R s1 = 0;
+#pragma unroll
+    for (int k = 0; k < 16; ++k) {
+      const R dpm = s_dm[l * SROW + k];
+      c[k] = s_sp[k] * dpm;
+      x[k] = s_q[l * SROW + k] / dpm;
+      s1 += c[k];
+    }
+    if (s1 > R(0)) {
+      double* ql = a.qlim + ((size_t)e * a.Q + q) * 2 * NLEV;
+      double mn = ql[l], mx = ql[NLEV + l];
+      limiter_level<R>(a.limiter_option, x, c, mn, mx);
+      ql[l] = mn;
+      ql[NLEV + l] = mx;
+#pragma unroll
+      for (int k = 0; k < 16; ++k) s_q[l * SROW + k] = x[k] * s_dm[l * SROW + k];
+    }
+  }
+  __syncthreads();
+#pragma unroll 1
+  for (int k = 0; k < NL; ++k) {
+    const int l = lg + LG * k;
+    a.qscr[qb + l * 16 + p] = m.sp * s_q[l * SROW + p];
+  }
+}
+
+// DSS(rspheremp) of the tracer scratch into Qdp(np1); with time_avg the last RK2 stage
+// also applies qdp_time_avg: Qdp(np1) = (Qdp(n0) + 2 Qdp(np1)) / 3.
+template <typename R>
+__global__ void k_dss_tracers(EulerArgs<R> a, int E, int time_avg) {
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (long long)E * a.Q * NLEV * 16) return;
+  const int p = idx & 15, l = (idx / 16) % NLEV, q = (idx / (16 * NLEV)) % a.Q;
+  const int e = idx / (16LL * NLEV * a.Q);
+  const double rs = (double)a.m.rspheremp[e * 16 + p];
+  const double v = dss_gather(a.qscr + (size_t)q * NLEV * 16, (long long)a.Q * NLEV * 16, 16, e, l, p, a.dss) * rs;
+  const size_t d = ((((size_t)e * QTL + a.np1_qdp) * a.Q + q) * NLEV + l) * 16 + p;
+  if (time_avg) {
+    const size_t s0 = ((((size_t)e * QTL + a.n0_qdp) * a.Q + q) * NLEV + l) * 16 + p;
+    a.qdp[d] = (a.qdp[s0] + 2.0 * v) / 3.0;
+  } else {
+    a.qdp[d] = v;
+  }
+}
+
+template <typename R>
+__global__ void k_dss_field(int E, const R* __restrict__ src, R* dst, const R* __restrict__ rsmp,
+                            DssTable tab) {
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= E * NLEV * 16) return;
+  const int e = idx / (NLEV * 16), l = (idx / 16) % NLEV, p = idx & 15;
+  double v = dss_gather(src, NLEV * 16, 16, e, l, p, tab);
+  if (rsmp) v *= (double)rsmp[e * 16 + p];
+  dst[idx] = (R)v;
+}
+
+// Generic in-place DSS through a scratch copy.
+template <typename R>
+__global__ void k_copy_fields(int E, int nf, const R* base, long long fs, long long es, int ls, R* scr) {
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (long long)E * nf * NLEV * 16) return;
+  const int p = idx & 15, l = (idx / 16) % NLEV, f = (idx / (16 * NLEV)) % nf;
+  const int e = idx / (16LL * NLEV * nf);
+  scr[idx] = base[(size_t)f * fs + (size_t)e * es + (size_t)l * ls + p];
+}
+template <typename R>
+__global__ void k_dss_from_copy(int E, int nf, R* base, long long fs, long long es, int ls, const R* scr,
+                                const R* rsmp, DssTable tab) {
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (long long)E * nf * NLEV * 16) return;
+  const int p = idx & 15, l = (idx / 16) % NLEV, f = (idx / (16 * NLEV)) % nf;
+  const int e = idx / (16LL * NLEV * nf);
+  double v = dss_gather(scr + (size_t)f * NLEV * 16, (long long)nf * NLEV * 16, 16, e, l, p, tab);
+  if (rsmp) v *= (double)rsmp[e * 16 + p];
+  base[(size_t)f * fs + (size_t)e * es + (size_t)l * ls + p] = (R)v;
+}
+
+// ======================================================================================
+// PPM vertical remap (RemapFunctor + PpmVertRemap, rsplit > 0), one CTA per column.
+// ======================================================================================
+constexpr int RT = 64;  // threads per column CTA
+
+// Warp-0 inclusive scan of n <= 96 values in place (lanes own 3 consecutive values).
+__device__ void warp_scan_incl(double* x, int n) {
+  const int lane = threadIdx.x & 31;
+  double v[3], run = 0.0;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const int i = lane * 3 + k;
+    v[k] = i < n ? x[i] : 0.0;
+    run += v[k];
+  }
+  double incl = run;
+#pragma unroll
+  for (int off = 1; off < 32; off <<= 1) {
+    const double y = __shfl_up_sync(FULL, incl, off);
+    if (lane >= off) incl += y;
+  }
+  double ex = __shfl_up_sync(FULL, incl, 1);
+  if (lane == 0) ex = 0.0;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const int i = lane * 3 + k;
+    ex += v[k];
+    if (i < n) x[i] = ex;
+  }
+}
+
+template <typename R>
+__global__ void __launch_bounds__(RT) k_remap(RemapArgs<R> a) {
+  __shared__ double src[NLEV], tgt[NLEV], pio[NLEV + 2], pin[NLEV + 1], Dp[NLEV + 4], z2[NLEV];
+  __shared__ int kid[NLEV];
+  __shared__ double g[10][NLEV + 2];
+  __shared__ double Ap[NLEV + 4], mass[NLEV + 2], dma[NLEV + 2], ai[NLEV + 1], coef[3][NLEV], col[NLEV];
+  __shared__ double ps_s;
+  const int cidx = blockIdx.x, e = cidx >> 4, p = cidx & 15, tid = threadIdx.x;
+  double* D = Dp + 2;
+  double* A = Ap + 2;
+  const size_t sb = ((size_t)e * NTL + a.np1) * NLEV * 16 + p;
+  for (int l = tid; l < NLEV; l += RT) src[l] = (double)a.dp[sb + (size_t)l * 16];
+  __syncthreads();
+  if (tid == 0) {  // compute_ps_v, sequential as in the reference
+    double ps = 0.0;
+    for (int l = 0; l < NLEV; ++l) ps += src[l];
+    ps += a.hyai0 * a.ps0;
+    ps_s = ps;
+    a.ps_v[((size_t)e * NTL + a.np1) * 16 + p] = ps;
+  }
+  __syncthreads();
+  const double ps = ps_s;
+  for (int l = tid; l < NLEV; l += RT) {
+    tgt[l] = (c_hyai[l + 1] - c_hyai[l]) * a.ps0 + (c_hybi[l + 1] - c_hybi[l]) * ps;
+    const double s = src[l];
+    if (isnan(s) || s < 0.0) atomicExch(a.invalid, 1);
+    D[l] = s;
+    pio[l + 1] = s;   // inclusive-scan input shifted by one
+    pin[l + 1] = tgt[l];
+  }
+  __syncthreads();
+  if (tid < 32) {
+    warp_scan_incl(pio + 1, NLEV);
+    warp_scan_incl(pin + 1, NLEV);
+  }
+  __syncthreads();
+  if (tid == 0) {
+    pio[0] = 0.0;
+    pin[0] = 0.0;
+    pio[NLEV + 1] = pio[NLEV] + 1.0;
+    pin[NLEV] = pio[NLEV];
+    D[-1] = D[0];
+    D[-2] = D[1];
+    D[NLEV] = D[NLEV - 1];
+    D[NLEV + 1] = D[NLEV - 2];
+  }
+  __syncthreads();
+  for (int k = tid; k < NLEV; k += RT) {  // compute_integral_bounds
+    int kk = k + 1;
+    while (kk < NLEV + 2 && pio[kk - 1] <= pin[k + 1]) kk++;
+    kk--;
+    if (kk == NLEV + 1) kk = NLEV;
+    if (kk < 1) {  // only reachable with a non-monotone (invalid) source grid
+      kk = 1;
+      atomicExch(a.invalid, 1);
+    }
+    kid[k] = kk - 1;
+    z2[k] = (pin[k + 1] - (pio[kk - 1] + pio[kk]) * 0.5) / D[kk - 1];
+  }
+  for (int j = tid; j < NLEV + 2; j += RT) {  // compute_grids
+    g[0][j] = D[j - 1] / (D[j - 2] + D[j - 1] + D[j]);
+    g[1][j] = (2.0 * D[j - 2] + D[j - 1]) / (D[j - 1] + D[j]);
+    g[2][j] = (D[j - 1] + 2.0 * D[j]) / (D[j - 2] + D[j - 1]);
+    if (j < NLEV + 1) {
+      g[3][j] = D[j - 1] / (D[j - 1] + D[j]);
+      g[4][j] = 1.0 / (D[j - 2] + D[j - 1] + D[j] + D[j + 1]);
+      g[5][j] = (2.0 * D[j - 1] * D[j]) / (D[j - 1] + D[j]);
+      g[6][j] = (D[j - 2] + D[j - 1]) / (2.0 * D[j - 1] + D[j]);
+      g[7][j] = (D[j + 1] + D[j]) / (2.0 * D[j] + D[j - 1]);
+      g[8][j] = D[j - 1] * (D[j - 2] + D[j - 1]) / (2.0 * D[j - 1] + D[j]);
+      g[9][j] = D[j] * (D[j] + D[j + 1]) / (D[j - 1] + 2.0 * D[j]);
+    }
+  }
+  __syncthreads();
+  const int nvar = 3 + a.Q;
+  for (int var = 0; var < nvar; ++var) {
+    // load the field (states in extrinsic form v dp, T dp); mass[1 + m] is scanned into
+    // the mass below interface m: mass[1] = 0, mass[m + 1] = sum_{j<m} x_j
+    for (int l = tid; l < NLEV; l += RT) {
+      double x;
+      if (var < 2) x = (double)a.v[((size_t)e * NTL + a.np1) * NLEV * 32 + (size_t)l * 32 + var * 16 + p] * src[l];
+      else if (var == 2) x = (double)a.T[sb + (size_t)l * 16] * src[l];
+      else x = a.qdp[((((size_t)e * QTL + a.n0_qdp) * a.Q + (var - 3)) * NLEV + l) * 16 + p];
+      col[l] = x;
+      A[l] = x / D[l];
+      if (l < NLEV - 1) mass[l + 2] = x;
+    }
+    if (tid == 0) {
+      mass[0] = 0.0;
+      mass[1] = 0.0;
+    }
+    __syncthreads();
+    if (tid < 32) warp_scan_incl(mass + 1, NLEV);
+    if (tid == 32) {
+      if (a.remap_alg == 3) {
+        A[-1] = A[-2] = A[0];
+        A[NLEV] = A[NLEV + 1] = A[NLEV - 1];
+      } else {
+        A[-1] = A[0];
+        A[-2] = A[1];
+        A[NLEV] = A[NLEV - 1];
+        A[NLEV + 1] = A[NLEV - 2];
+      }
+    }
+    __syncthreads();
+    for (int j = tid; j < NLEV + 2; j += RT) {
+      if ((A[j] - A[j - 1]) * (A[j - 1] - A[j - 2]) > 0.0) {
+        const double da = g[0][j] * (g[1][j] * (A[j] - A[j - 1]) + g[2][j] * (A[j - 1] - A[j - 2]));
+        dma[j] = fmin(fmin(fabs(da), 2.0 * fabs(A[j - 1] - A[j - 2])), 2.0 * fabs(A[j] - A[j - 1])) *
+                 copysign(1.0, da);
+      } else {
+        dma[j] = 0.0;
+      }
+    }
+    if (tid == 0) mass[NLEV + 1] = mass[NLEV] + col[NLEV - 1];
+    __syncthreads();
+    for (int j = tid; j < NLEV + 1; j += RT) {
+      ai[j] = A[j - 1] + g[3][j] * (A[j] - A[j - 1]) +
+              g[4][j] * (g[5][j] * (g[6][j] - g[7][j]) * (A[j] - A[j - 1]) - g[8][j] * dma[j + 1] +
+                         g[9][j] * dma[j]);
+    }
+    __syncthreads();
+    for (int jp = tid; jp < NLEV; jp += RT) {
+      const int j = jp + 1;
+      double al = ai[j - 1], ar = ai[j];
+      const double cm = A[j - 1];
+      if ((ar - cm) * (cm - al) <= 0.) { al = cm; ar = cm; }
+      if ((ar - al) * (cm - (al + ar) / 2.0) > (ar - al) * (ar - al) / 6.0) al = 3.0 * cm - 2.0 * ar;
+      if ((ar - al) * (cm - (al + ar) / 2.0) < -(ar - al) * (ar - al) / 6.0) ar = 3.0 * cm - 2.0 * al;
+      coef[0][jp] = 1.5 * cm - (al + ar) / 4.0;
+      coef[1][jp] = ar - al;
+      coef[2][jp] = 3.0 * (-2.0 * cm + (al + ar));
+      if (a.remap_alg == 2 && (jp < 2 || jp >= NLEV - 2)) {  // PpmFixedParabola
+        coef[0][jp] = A[jp];
+        coef[1][jp] = 0.0;
+        coef[2][jp] = 0.0;
+      }
+    }
+    __syncthreads();
+    for (int k = tid; k < NLEV; k += RT) {  // compute_remap, GPU form
+      double m1 = 0.0;
+      if (k > 0) {
+        const int kk = kid[k - 1];
+        const double x2 = z2[k - 1], x1 = -0.5;
+        const double in = (coef[0][kk] * (x2 - x1) + coef[1][kk] * (x2 * x2 - x1 * x1) / 2.0) +
+                          coef[2][kk] * (x2 * x2 * x2 - x1 * x1 * x1) / 3.0;
+        m1 = mass[kk + 1] + in * D[kk];
+      }
+      const int kk = kid[k];
+      const double x2 = z2[k], x1 = -0.5;
+      const double in = (coef[0][kk] * (x2 - x1) + coef[1][kk] * (x2 * x2 - x1 * x1) / 2.0) +
+                        coef[2][kk] * (x2 * x2 * x2 - x1 * x1 * x1) / 3.0;
+      const double m2 = mass[kk + 1] + in * D[kk];
+      const double out = m2 - m1;
+      if (var < 2) a.v[((size_t)e * NTL + a.np1) * NLEV * 32 + (size_t)k * 32 + var * 16 + p] = (R)(out / tgt[k]);
+      else if (var == 2) a.T[sb + (size_t)k * 16] = (R)(out / tgt[k]);
+      else a.qdp[((((size_t)e * QTL + a.n0_qdp) * a.Q + (var - 3)) * NLEV + k) * 16 + p] = out;
+    }
+    __syncthreads();
+  }
+}
+
+// ---- launch bookkeeping --------------------------------------------------------------
+const char* g_last = "";
+void (*g_before)(const char*, cudaStream_t) = nullptr;
+void (*g_after)(const char*, cudaStream_t) = nullptr;
+
+struct KScope {
+  const char* n;
+  cudaStream_t s;
+  KScope(const char* name, cudaStream_t st) : n(name), s(st) {
+    g_last = name;
+    if (g_before) g_before(name, st);
+  }
+  ~KScope() {
+    if (g_after) g_after(n, s);
+  }
+};
+
+inline int nblk(long long n, int b) { return (int)((n + b - 1) / b); }
+
+template <typename R> constexpr int LG_CAAR() { return 8; }
+template <typename R> constexpr int LG_HV() { return 8; }
+template <typename R> constexpr int LG_TR() { return 8; }
+
+}  // namespace
+
+const char* last_kernel_name() { return g_last; }
+void set_kernel_hook(void (*b)(const char*, cudaStream_t), void (*a)(const char*, cudaStream_t)) {
+  g_before = b;
+  g_after = a;
+}
+
+void upload_constants(const double* dvv16, const double* hyai, const double* hybi, double ps0,
+                      cudaStream_t s) {
+  float f[16];
+  for (int i = 0; i < 16; ++i) f[i] = (float)dvv16[i];
+  double ad[NLEV], bd[NLEV];
+  for (int l = 0; l < NLEV; ++l) {
+    ad[l] = hyai[l + 1] - hyai[l];
+    bd[l] = hybi[l + 1] - hybi[l];
+  }
+  (void)ps0;
+  cudaMemcpyToSymbolAsync(c_dvv, dvv16, sizeof(double) * 16, 0, cudaMemcpyHostToDevice, s);
+  cudaMemcpyToSymbolAsync(c_dvvf, f, sizeof(float) * 16, 0, cudaMemcpyHostToDevice, s);
+  cudaMemcpyToSymbolAsync(c_hyai, hyai, sizeof(double) * (NLEV + 1), 0, cudaMemcpyHostToDevice, s);
+  cudaMemcpyToSymbolAsync(c_hybi, hybi, sizeof(double) * (NLEV + 1), 0, cudaMemcpyHostToDevice, s);
+  cudaMemcpyToSymbolAsync(c_ai_delta, ad, sizeof(double) * NLEV, 0, cudaMemcpyHostToDevice, s);
+  cudaMemcpyToSymbolAsync(c_bi_delta, bd, sizeof(double) * NLEV, 0, cudaMemcpyHostToDevice, s);
+  cudaStreamSynchronize(s);
+}
+
+template <typename R>
+void launch_prim_step_init(int E, R* eta, R* vn0, R* omega_p, R* dpa, R* dpb, R* derived_dp, const R* dp,
+                           int n0, int zero_diss, cudaStream_t s) {
+  KScope k("prim_step_init", s);
+  k_prim_step_init<R><<<nblk((long long)E * NLEV * 16, 256), 256, 0, s>>>(E, eta, vn0, omega_p, dpa, dpb,
+                                                                          derived_dp, dp, n0, zero_diss);
+}
+
+template <typename R>
+void launch_dp_from_ps(int E, R* dp, const double* ps_v, int n0, double ps0, cudaStream_t s) {
+  KScope k("dp3d_from_ps", s);
+  k_dp_from_ps<R><<<nblk((long long)E * NLEV * 16, 256), 256, 0, s>>>(E, dp, ps_v, n0, ps0);
+}
+
+template <typename R>
+void launch_caar(const CaarArgs<R>& a, int E, cudaStream_t s) {
+  constexpr int LG = LG_CAAR<R>();
+  const size_t smem = 5 * NLEV * SROW * sizeof(double);
+  static bool init = false;
+  if (!init) {
+    cudaFuncSetAttribute(k_caar<R, LG>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    init = true;
+  }
+  KScope k("caar_stage", s);
+  k_caar<R, LG><<<E, LG * 16, smem, s>>>(a);
+}
+
+template <typename R>
+void launch_dss_state(int E, const R* src, R* v, R* T, R* dp, int np1, const R* rsmp, DssTable t,
+                      cudaStream_t s) {
+  KScope k("dss_caar", s);
+  k_dss_state<R><<<nblk((long long)E * NLEV * 16, 256), 256, 0, s>>>(E, src, v, T, dp, np1, rsmp, t);
+}
+
+template <typename R>
+void launch_hv(const HvArgs<R>& a, int E, cudaStream_t s) {
+  constexpr int LG = LG_HV<R>();
+  for (int c = 0; c < a.hsub; ++c) {
+    {
+      KScope k("hv_laplace1", s);
+      k_hv_lap1<R, LG><<<E, LG * 16, 0, s>>>(a);
+    }
+    {
+      KScope k("hv_laplace2", s);
+      k_hv_lap2<R, LG><<<E, LG * 16, 0, s>>>(a);
+    }
+    {
+      KScope k("hv_dss_update", s);
+      k_hv_update<R><<<nblk((long long)E * NLEV * 16, 256), 256, 0, s>>>(a, E);
+    }
+  }
+}
+
+template <typename R>
+void launch_precompute_divdp(const EulerArgs<R>& a, int E, cudaStream_t s) {
+  constexpr int LG = LG_TR<R>();
+  KScope k("precompute_divdp", s);
+  k_precompute_divdp<R, LG><<<E, LG * 16, 0, s>>>(a);
+}
+
+template <typename R>
+void launch_euler_step(EulerArgs<R>& a, int E, int time_avg, cudaStream_t s) {
+  constexpr int LG = LG_TR<R>();
+  const int EQ = E * a.Q;
+  a.rhs_viss = 0.0;
+  if (a.Q > 0) {
+    const bool nbr = (a.rhs_multiplier == 0.0 || a.rhs_multiplier == 2.0);
+    {
+      KScope k("euler_qminmax", s);
+      k_qminmax<R, LG><<<EQ, LG * 16, 0, s>>>(a, nbr ? a.qlim_tmp : a.qlim, a.rhs_multiplier == 2.0);
+    }
+    if (a.rhs_multiplier == 2.0) {
+      a.rhs_viss = 3.0;
+      {
+        KScope k("euler_bih_pre", s);
+        k_bih_pre<R, LG><<<EQ, LG * 16, 0, s>>>(a);
+      }
+      {
+        KScope k("euler_bih_post", s);
+        k_bih_post<R, LG><<<EQ, LG * 16, 0, s>>>(a);
+      }
+    }
+    if (nbr) {
+      KScope k("euler_minmax_nbr", s);
+      k_minmax_nbr<<<nblk((long long)E * a.Q * NLEV, 256), 256, 0, s>>>(E, a.Q, a.qlim_tmp, a.qlim, a.conn);
+    }
+  }
+  {
+    KScope k("euler_aal_setup", s);
+    k_aal_setup<R><<<nblk((long long)E * NLEV * 16, 256), 256, 0, s>>>(a, E);
+  }
+  if (a.Q > 0) {
+    {
+      KScope k("euler_aal_tracer", s);
+      k_aal_tracer<R, LG><<<EQ, LG * 16, 0, s>>>(a);
+    }
+    {
+      KScope k("euler_dss_qdp", s);
+      k_dss_tracers<R><<<nblk((long long)E * a.Q * NLEV * 16, 256), 256, 0, s>>>(a, E, time_avg);
+    }
+  }
+  {
+    KScope k("euler_dss_fvar", s);
+    k_dss_field<R><<<nblk((long long)E * NLEV * 16, 256), 256, 0, s>>>(E, a.fscr, a.f_dss, a.m.rspheremp, a.dss);
+  }
+}
+
+template <typename R>
+void launch_remap(const RemapArgs<R>& a, cudaStream_t s) {
+  KScope k("ppm_remap", s);
+  k_remap<R><<<a.nelem * 16, RT, 0, s>>>(a);
+}
+
+template <typename R>
+void launch_update_q(int E, int Q, const double* qdp, double* Qc, const double* ps_v, int np1, int np1_qdp,
+                     double ps0, cudaStream_t s) {
+  if (Q == 0) return;
+  KScope k("update_q", s);
+  k_update_q<R><<<nblk((long long)E * Q * NLEV * 16, 256), 256, 0, s>>>(E, Q, qdp, Qc, ps_v, np1, np1_qdp, ps0);
+}
+
+template <typename R>
+void launch_dss_inplace(int E, int nf, R* base, long long fs, long long es, int ls, R* scr, const R* rsmp,
+                        DssTable t, cudaStream_t s) {
+  KScope k("dss_generic", s);
+  const long long n = (long long)E * nf * NLEV * 16;
+  k_copy_fields<R><<<nblk(n, 256), 256, 0, s>>>(E, nf, base, fs, es, ls, scr);
+  k_dss_from_copy<R><<<nblk(n, 256), 256, 0, s>>>(E, nf, base, fs, es, ls, scr, rsmp, t);
+}
+
+void launch_dss_inplace_d(int E, int nf, double* base, long long fs, long long es, int ls, double* scr,
+                          const double* rsmp, DssTable t, cudaStream_t s) {
+  launch_dss_inplace<double>(E, nf, base, fs, es, ls, scr, rsmp, t, s);
+}
+
+#define HX_INST(R)                                                                                      \
+  template void launch_prim_step_init<R>(int, R*, R*, R*, R*, R*, R*, const R*, int, int, cudaStream_t); \
+  template void launch_dp_from_ps<R>(int, R*, const double*, int, double, cudaStream_t);                \
+  template void launch_caar<R>(const CaarArgs<R>&, int, cudaStream_t);                                  \
+  template void launch_dss_state<R>(int, const R*, R*, R*, R*, int, const R*, DssTable, cudaStream_t);  \
+  template void launch_hv<R>(const HvArgs<R>&, int, cudaStream_t);                                      \
+  template void launch_precompute_divdp<R>(const EulerArgs<R>&, int, cudaStream_t);                     \
+  template void launch_euler_step<R>(EulerArgs<R>&, int, int, cudaStream_t);                            \
+  template void launch_remap<R>(const RemapArgs<R>&, cudaStream_t);                                     \
+  template void launch_update_q<R>(int, int, const double*, double*, const double*, int, int, double,   \
+                                   cudaStream_t);                                                       \
+  template void launch_dss_inplace<R>(int, int, R*, long long, long long, int, R*, const R*, DssTable,  \
+                                      cudaStream_t);
+HX_INST(double)
+HX_INST(float)
+
+}  // namespace hx

@@ -1,0 +1,175 @@
+/*
+ * hxgpu.h — C ABI of the GB300 preqx dycore step (libhxgpu.so).
+ *
+ * The first block keeps the symbol names and by-reference argument conventions of the
+ * HOMMEXX C++ entry points that the Fortran driver binds with ISO_C_BINDING, so that
+ * linking libhxgpu.so in place of the reference's C++ library is a drop-in for the
+ * preqx step.  Fortran passes every argument by reference: scalars arrive as pointers,
+ * and `type(c_ptr)` arrays arrive as a pointer to the c_ptr (the reference's
+ * `CF90Ptr&` / `F90Ptr&`, here `const double* const*` / `double* const*`).
+ * Arrays are in Fortran column-major layout, e.g. state T is (np,np,nlev,3,nelemd).
+ *
+ * On a bad option or a negative layer thickness the reference aborts the process with
+ * codes 11/12/13/101 (src/share/cxx/ErrorDefs.hpp:51-57).  These symbols do the same by
+ * default; after hx_set_abort_on_error(0) they record the error instead, and
+ * hx_last_error() returns it.
+ *
+ * The second block (hx_*) has no counterpart in the reference: status reporting,
+ * precision selection, per-phase entry points used by the parity tests, field
+ * access and timing.
+ */
+#ifndef HXGPU_H
+#define HXGPU_H
+
+#ifdef __cplusplus
+#include <cstddef>
+extern "C" {
+#else
+#include <stdbool.h>
+#include <stddef.h>
+#endif
+
+/* ---- Reference entry points ------------------------------------------------------ */
+
+/* src/share/cxx/Hommexx_Session.cpp:35 — selects the GPU, creates the stream. */
+void initialize_hommexx_session(void);
+/* src/share/cxx/Hommexx_Session.cpp:75 — frees all device memory. */
+void finalize_hommexx_session(void);
+
+/* src/share/cxx/mpi/mpi_cxx_f90_interface.cpp:20 — single GPU, whole mesh resident:
+ * the communicator is recorded and otherwise unused. */
+void reset_cxx_comm(const int* f_comm);
+/* src/share/cxx/mpi/mpi_cxx_f90_interface.cpp:27-60 — 1-based ids, F90 positions
+ * W=1 E=2 S=3 N=4 SW=5 SE=6 NW=7 NE=8. */
+void init_connectivity(const int* num_local_elems);
+void add_connection(const int* first_elem_lid, const int* first_elem_gid,
+                    const int* first_elem_pos, const int* first_elem_pid,
+                    const int* second_elem_lid, const int* second_elem_gid,
+                    const int* second_elem_pos, const int* second_elem_pid);
+void finalize_connectivity(void);
+
+/* src/share/cxx/cxx_f90_interface.cpp:207 — dvv(np,np). */
+void init_derivative_c(const double* const* dvv);
+
+/* src/share/cxx/cxx_f90_interface.cpp:33-117 — same option checks. */
+void init_simulation_params_c(const int* remap_alg, const int* limiter_option,
+                              const int* rsplit, const int* qsplit,
+                              const int* time_step_type, const int* energy_fixer,
+                              const int* qsize, const int* state_frequency,
+                              const double* nu, const double* nu_p, const double* nu_q,
+                              const double* nu_s, const double* nu_div, const double* nu_top,
+                              const int* hypervis_order, const int* hypervis_subcycle,
+                              const double* hypervis_scaling, const int* ftype,
+                              const bool* prescribed_wind, const bool* moisture,
+                              const bool* disable_diagnostics, const bool* use_cpstar,
+                              const bool* use_semi_lagrangian_transport);
+
+/* src/share/cxx/cxx_f90_interface.cpp:119-124 — hyam/hybm(nlev), hyai/hybi(nlev+1). */
+void init_hvcoord_c(const double* ps0, const double* const* hybrid_am,
+                    const double* const* hybrid_ai, const double* const* hybrid_bm,
+                    const double* const* hybrid_bi);
+
+/* src/share/cxx/cxx_f90_interface.cpp:224-233 — D/Dinv/metinv (np,np,2,2,nelemd),
+ * 2-D fields (np,np,nelemd), tensorvisc (np,np,2,2,nelemd),
+ * vec_sph2cart (np,np,3,2,nelemd). */
+void init_elements_2d_c(const int* nelemd, const double* const* D,
+                        const double* const* Dinv, const double* const* fcor,
+                        const double* const* mp, const double* const* spheremp,
+                        const double* const* rspheremp, const double* const* metdet,
+                        const double* const* metinv, const double* const* phis,
+                        const double* const* tensorvisc, const double* const* vec_sph2cart,
+                        const bool* consthv);
+
+/* src/share/cxx/cxx_f90_interface.cpp:235-251 — v (np,np,2,nlev,3,nelemd),
+ * T/dp3d (np,np,nlev,3,nelemd), Qdp (np,np,nlev,qsize_d,2,nelemd),
+ * ps_v (np,np,3,nelemd).  Host -> device copies. */
+void init_elements_states_c(const double* const* v, const double* const* T,
+                            const double* const* dp3d, const double* const* Qdp,
+                            const double* const* ps_v);
+
+/* src/share/cxx/cxx_f90_interface.cpp:253-262 — diagnostics are off on the timed
+ * step; the pointers are recorded only. */
+void init_diagnostics_c(double* const* q, double* const* qvar, double* const* qmass,
+                        double* const* q1mass, double* const* iener,
+                        double* const* iener_wet, double* const* kener,
+                        double* const* pener);
+
+/* src/share/cxx/cxx_f90_interface.cpp:264-280 — builds the DSS gather tables. */
+void init_boundary_exchanges_c(void);
+
+/* src/share/cxx/cxx_f90_interface.cpp:213-222 — 1-based in, stored 0-based. */
+void init_time_level_c(const int* nm1, const int* n0, const int* np1,
+                       const int* nstep, const int* nstep0);
+
+/* src/share/cxx/prim_driver.cpp:31-156 — one remap interval; time levels return
+ * 0-based as in the reference. */
+void prim_run_subcycle_c(const double* dt, int* nstep, int* nm1, int* n0, int* np1,
+                         const int* last_time_step);
+
+/* src/share/cxx/cxx_f90_interface.cpp:126-154 — device -> host copies; Q and omega_p
+ * are (np,np,nlev,qsize_d,nelemd) and (np,np,nlev,nelemd). */
+void cxx_push_results_to_f90(double* const* v, double* const* T, double* const* dp3d,
+                             double* const* Qdp, double* const* Q, double* const* ps_v,
+                             double* const* omega_p);
+
+/* ---- Additions (no counterpart in the reference) ------------------------------------ */
+
+/* Status of the last call: 0 on success, else the reference's error code
+ * (11, 12, 13, 101) or HX_ERR_CUDA; the message is copied into buf. */
+#define HX_ERR_CUDA 200
+#define HX_ERR_STATE 201
+int hx_last_error(char* buf, int buflen);
+/* 1 (default) = exit the process with the reference's code on error; 0 = record. */
+void hx_set_abort_on_error(int abort_on_error);
+
+/* 0 = FP64 plain form (default); 1 = mixed form: sphere operators, caar,
+ * hyperviscosity and tracer advection in FP32; pressure/geopotential scans, DSS
+ * accumulation and PPM remap integrals in FP64.  Call before init_elements_2d_c. */
+int hx_set_precision(int mode);
+
+/* Field access in the Fortran layout of one time level, e.g. "T" is
+ * (np,np,nlev,nelemd) for time level tl (0-based).  Names: v T dp3d ps_v Qdp Q
+ * omega_p phi vn0 eta_dot_dpdn derived_dp divdp divdp_proj dpdiss_ave
+ * dpdiss_biharmonic.  tl is ignored for fields without time levels. */
+int hx_get_field(const char* name, int tl, double* out);
+int hx_set_field(const char* name, int tl, const double* in);
+
+/* Per-phase entry points (0-based time levels), each one reference routine:
+ *  CaarFunctor::run + DSS (src/share/cxx/CaarFunctor.cpp:96-116),
+ *  u3_5stage_timestep (src/share/cxx/prim_advance_exp.cpp:113-161),
+ *  HyperviscosityFunctorImpl::run (src/share/cxx/HyperviscosityFunctorImpl.cpp:56-84),
+ *  EulerStepFunctorImpl::euler_step (src/share/cxx/EulerStepFunctorImpl.hpp:514-561)
+ *    with dss_opt 0 = ETA, 1 = OMEGA, 2 = DIV_VDP_AVE,
+ *  prim_advec_tracers_remap_RK2 (src/share/cxx/prim_advec_tracers_remap.cpp:32-90),
+ *  RemapFunctor::run_remap (src/share/cxx/RemapFunctor.hpp:299-331),
+ *  prim_step (src/share/cxx/prim_step.cpp:20-103). */
+int hx_run_caar_stage(int nm1, int n0, int np1, double dt, double eta_ave_w);
+int hx_run_rk5(int nm1, int n0, int np1, int n0_qdp, double dt, double eta_ave_w);
+int hx_run_hypervis(int np1, double dt, double eta_ave_w);
+int hx_run_euler_step(int np1_qdp, int n0_qdp, double dt, double rhs_multiplier,
+                      int dss_opt);
+int hx_run_tracers_rk2(double dt);
+int hx_run_remap(int np1, int np1_qdp, double dt);
+int hx_run_prim_step(double dt);
+/* DSS of one registered field at time level tl, optionally scaled by rspheremp. */
+int hx_run_dss(const char* name, int tl, int apply_rspheremp);
+
+/* Sizes the library was initialised with. */
+int hx_num_elems(void);
+int hx_qsize(void);
+
+/* Device kernel timing: when enabled, every launch is bracketed by CUDA events and
+ * its time accumulated per kernel name; hx_kernel_stats fills up to max entries of
+ * (name, launches, total ms) and returns the number of kernels seen. */
+int hx_enable_timing(int on);
+int hx_kernel_stats(char* names, int name_len, long long* launches, double* total_ms,
+                    int max);
+/* Number of kernels this library launched since initialisation. */
+long long hx_launch_count(void);
+/* Block the host until all device work of the session has finished. */
+int hx_synchronize(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* HXGPU_H */

@@ -1,0 +1,1622 @@
+// hx_oracle.cpp — CPU oracle for the preqx dycore step.  TEST INFRASTRUCTURE ONLY.
+//
+// This file is the checker the GPU library is compared against.  It is a plain C++17
+// (+OpenMP over elements) restatement, loop for loop, of the reference HOMMEXX C++
+// functors, in FP64, compiled without FMA contraction so the result does not depend on
+// the host CPU.  Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg
+// load it; nothing in the product links or calls it.
+//
+// Parity status: the reference cannot be built here (its hot path needs Kokkos, which
+// is not vendored — cmake/Trilinos.cmake:103-108 — and its Fortran twins need gfortran
+// and MPI) and it ships no golden vectors, so this restatement is pinned by the
+// reference's own property tests (limiter bounds/mass/1-norm, preqx_ut.cpp:1330-1527),
+// analytic operator identities and conservation checks, not by reference outputs.
+//
+// It exports the same C symbols as libhxgpu.so (include/hxgpu.h), so one driver can
+// run either library.  Internal arrays use the reference device layout, level index
+// fastest: v [E][3][2][16][72], T/dp3d [E][3][16][72], Qdp [E][2][Q][16][72]
+// (src/share/cxx/Elements.hpp:44-67, Tracers.hpp:26-30); the Fortran arrays are
+// transposed on init/push as in src/share/cxx/utilities/SyncUtils.hpp.
+//
+// Point index p = igp*4 + jgp with the reference C++ names (igp = Fortran j,
+// jgp = Fortran i).
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <limits>
+#include <string>
+#include <vector>
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#include "hxgpu.h"
+
+namespace {
+
+constexpr int NP = 4;
+constexpr int NP2 = 16;
+constexpr int NLEV = 72;
+constexpr int NTL = 3;
+constexpr int QTL = 2;
+
+// src/share/cxx/PhysicalConstants.hpp:17-22
+constexpr double Rwater_vapor = 461.5;
+constexpr double Rgas = 287.04;
+constexpr double cp = 1005.0;
+constexpr double kappa = Rgas / cp;
+constexpr double rrearth = 1.0 / 6.376e6;
+
+struct Params {
+  int remap_alg = 1, limiter_option = 8, rsplit = 1, qsplit = 1, time_step_type = 5;
+  int qsize = 0, state_frequency = 1, hypervis_order = 2, hypervis_subcycle = 1, ftype = -1;
+  double nu = 0, nu_p = 0, nu_q = 0, nu_s = 0, nu_div = 0, nu_top = 0, hypervis_scaling = 0;
+  double nu_ratio1 = 1, nu_ratio2 = 1;
+  bool moist = false, disable_diagnostics = true, set = false;
+};
+
+struct TimeLevel {
+  int nm1 = 0, n0 = 1, np1 = 2, nstep = 0, nstep0 = 0, n0_qdp = 0, np1_qdp = 1;
+  void update_dynamics_levels() {  // LEAPFROG, TimeLevel.hpp:37-52
+    int tmp = np1;
+    np1 = nm1;
+    nm1 = n0;
+    n0 = tmp;
+    ++nstep;
+  }
+  void update_tracers_levels(int qsplit) {  // TimeLevel.hpp:58-67
+    int i_temp = nstep / qsplit;
+    if (i_temp % 2 == 0) { n0_qdp = 0; np1_qdp = 1; }
+    else { n0_qdp = 1; np1_qdp = 0; }
+  }
+};
+
+struct Ctx {
+  Params prm;
+  TimeLevel tl;
+  int E = 0, Q = 0;
+  bool consthv = true;
+  double dvv[NP][NP] = {};
+  // hybrid coordinate
+  double ps0 = 0, hyai[NLEV + 1] = {}, hybi[NLEV + 1] = {}, ai_delta[NLEV] = {},
+         bi_delta[NLEV] = {}, dp0[NLEV] = {}, hyai0 = 0;
+  // metric, C++ index order == Fortran memory
+  std::vector<double> D, Dinv, metinv, tensorvisc, vec_sph2cart;
+  std::vector<double> fcor, mp, spheremp, rspheremp, metdet, phis;
+  // state
+  std::vector<double> v, t, dp3d, ps_v, qdp, Qc;
+  std::vector<double> phi, omega_p, eta_dot_dpdn, derived_dp, divdp, divdp_proj,
+      dpdiss_ave, dpdiss_bih, vn0;
+  // buffers
+  std::vector<double> vtens, ttens, dptens, qtens_bih, qlim, vstar, dpdissk, dp_buf;
+  // connectivity: conn[e][slot] = {remote elem, remote slot}
+  std::vector<int> conn;
+  std::vector<int> g_src_e, g_src_p, g_cnt;  // gather table [E][16][3], [E][16]
+  bool conn_final = false, tables = false;
+  int last_err = 0;
+  std::string last_msg;
+  bool abort_on_error = true;
+  int valid_remap = 1;
+};
+
+Ctx* g = nullptr;
+Ctx& C() {
+  if (!g) g = new Ctx();
+  return *g;
+}
+
+void set_error(int code, const std::string& msg) {
+  Ctx& c = C();
+  c.last_err = code;
+  c.last_msg = msg;
+  if (c.abort_on_error) {
+    std::fprintf(stderr, "%s\nExiting...\n", msg.c_str());
+    std::exit(code);
+  }
+}
+
+inline size_t IV(int e, int tl, int comp, int p, int k) {
+  return ((((size_t)e * NTL + tl) * 2 + comp) * NP2 + p) * NLEV + k;
+}
+inline size_t IS(int e, int tl, int p, int k) {  // T, dp3d
+  return (((size_t)e * NTL + tl) * NP2 + p) * NLEV + k;
+}
+inline size_t IQ(int e, int qtl, int q, int p, int k, int Q) {
+  return ((((size_t)e * QTL + qtl) * Q + q) * NP2 + p) * NLEV + k;
+}
+inline size_t I3(int e, int p, int k) { return ((size_t)e * NP2 + p) * NLEV + k; }
+inline size_t I3V(int e, int comp, int p, int k) {
+  return (((size_t)e * 2 + comp) * NP2 + p) * NLEV + k;
+}
+
+// ----------------------------------------------------------------------------------
+// Sphere operators (src/share/cxx/SphereOperators.hpp:291-862), multi-level form.
+// Fields are [16][NLEV] (point, level); vectors [2][16][NLEV].  Operators act on the
+// first nl levels.
+// ----------------------------------------------------------------------------------
+struct EM {  // metric of one element
+  const double *D, *Dinv, *metinv, *metdet, *spheremp, *mp, *tensor, *sph2cart;
+  const double (*dvv)[NP];
+  double d(int a, int b, int p) const { return D[(a * 2 + b) * NP2 + p]; }
+  double di(int a, int b, int p) const { return Dinv[(a * 2 + b) * NP2 + p]; }
+  double mi(int a, int b, int p) const { return metinv[(a * 2 + b) * NP2 + p]; }
+  double tv(int a, int b, int p) const { return tensor[(a * 2 + b) * NP2 + p]; }
+  double s2c(int a, int b, int p) const { return sph2cart[(a * 3 + b) * NP2 + p]; }
+};
+
+inline int P(int i, int j) { return i * NP + j; }
+#define F(arr, p, k) (arr)[(p) * NLEV + (k)]
+#define FV(arr, c, p, k) (arr)[((c) * NP2 + (p)) * NLEV + (k)]
+
+// SphereOperators.hpp:291-319
+void gradient_sphere(const EM& m, const double* s, double* g, int nl) {
+  for (int igp = 0; igp < NP; ++igp)
+    for (int jgp = 0; jgp < NP; ++jgp)
+      for (int l = 0; l < nl; ++l) {
+        double v0 = 0, v1 = 0;
+        for (int k = 0; k < NP; ++k) {
+          v0 += m.dvv[jgp][k] * F(s, P(igp, k), l);
+          v1 += m.dvv[igp][k] * F(s, P(k, jgp), l);
+        }
+        v0 *= rrearth;
+        v1 *= rrearth;
+        const int p = P(igp, jgp);
+        FV(g, 0, p, l) = m.di(0, 0, p) * v0 + m.di(0, 1, p) * v1;
+        FV(g, 1, p, l) = m.di(1, 0, p) * v0 + m.di(1, 1, p) * v1;
+      }
+}
+
+// SphereOperators.hpp:321-348
+void gradient_sphere_update(const EM& m, const double* s, double* g, int nl) {
+  for (int igp = 0; igp < NP; ++igp)
+    for (int jgp = 0; jgp < NP; ++jgp)
+      for (int l = 0; l < nl; ++l) {
+        double dsdx = 0, dsdy = 0;
+        for (int k = 0; k < NP; ++k) {
+          dsdx += m.dvv[jgp][k] * F(s, P(igp, k), l);
+          dsdy += m.dvv[igp][k] * F(s, P(k, jgp), l);
+        }
+        dsdx *= rrearth;
+        dsdy *= rrearth;
+        const int p = P(igp, jgp);
+        FV(g, 0, p, l) += m.di(0, 0, p) * dsdx + m.di(0, 1, p) * dsdy;
+        FV(g, 1, p, l) += m.di(1, 0, p) * dsdx + m.di(1, 1, p) * dsdy;
+      }
+}
+
+// SphereOperators.hpp:350-392
+void divergence_sphere(const EM& m, const double* v, double* div, int nl) {
+  std::vector<double> gv(2 * NP2 * NLEV);
+  for (int p = 0; p < NP2; ++p)
+    for (int l = 0; l < nl; ++l) {
+      const double v0 = FV(v, 0, p, l), v1 = FV(v, 1, p, l);
+      FV(gv.data(), 0, p, l) = (m.di(0, 0, p) * v0 + m.di(1, 0, p) * v1) * m.metdet[p];
+      FV(gv.data(), 1, p, l) = (m.di(0, 1, p) * v0 + m.di(1, 1, p) * v1) * m.metdet[p];
+    }
+  for (int igp = 0; igp < NP; ++igp)
+    for (int jgp = 0; jgp < NP; ++jgp)
+      for (int l = 0; l < nl; ++l) {
+        double dudx = 0, dvdy = 0;
+        for (int k = 0; k < NP; ++k) {
+          dudx += m.dvv[jgp][k] * FV(gv.data(), 0, P(igp, k), l);
+          dvdy += m.dvv[igp][k] * FV(gv.data(), 1, P(k, jgp), l);
+        }
+        const int p = P(igp, jgp);
+        F(div, p, l) = (dudx + dvdy) * (1.0 / m.metdet[p] * rrearth);
+      }
+}
+
+// SphereOperators.hpp:394-444: qtens = qdp + alpha*div(vstar*qdp) [+ qtens]
+void divergence_sphere_update(const EM& m, double alpha, bool add_hv, const double* vstar,
+                              const double* qdp, double* qtens, int nl) {
+  std::vector<double> gv(2 * NP2 * NLEV);
+  for (int p = 0; p < NP2; ++p)
+    for (int l = 0; l < nl; ++l) {
+      const double q = F(qdp, p, l);
+      const double v0 = FV(vstar, 0, p, l) * q;
+      const double v1 = FV(vstar, 1, p, l) * q;
+      FV(gv.data(), 0, p, l) = (m.di(0, 0, p) * v0 + m.di(1, 0, p) * v1) * m.metdet[p];
+      FV(gv.data(), 1, p, l) = (m.di(0, 1, p) * v0 + m.di(1, 1, p) * v1) * m.metdet[p];
+    }
+  for (int igp = 0; igp < NP; ++igp)
+    for (int jgp = 0; jgp < NP; ++jgp)
+      for (int l = 0; l < nl; ++l) {
+        double dudx = 0, dvdy = 0;
+        for (int k = 0; k < NP; ++k) {
+          dudx += m.dvv[jgp][k] * FV(gv.data(), 0, P(igp, k), l);
+          dvdy += m.dvv[igp][k] * FV(gv.data(), 1, P(k, jgp), l);
+        }
+        const int p = P(igp, jgp);
+        const double q0 = add_hv ? F(qtens, p, l) : 0.0;
+        F(qtens, p, l) =
+            (F(qdp, p, l) + alpha * ((dudx + dvdy) * (1.0 / m.metdet[p] * rrearth)) + q0);
+      }
+}
+
+// SphereOperators.hpp:492-533
+void vorticity_sphere(const EM& m, const double* v, double* vort, int nl) {
+  std::vector<double> vc(2 * NP2 * NLEV);
+  for (int p = 0; p < NP2; ++p)
+    for (int l = 0; l < nl; ++l) {
+      const double v0 = FV(v, 0, p, l), v1 = FV(v, 1, p, l);
+      FV(vc.data(), 0, p, l) = m.d(0, 0, p) * v0 + m.d(0, 1, p) * v1;
+      FV(vc.data(), 1, p, l) = m.d(1, 0, p) * v0 + m.d(1, 1, p) * v1;
+    }
+  for (int igp = 0; igp < NP; ++igp)
+    for (int jgp = 0; jgp < NP; ++jgp)
+      for (int l = 0; l < nl; ++l) {
+        double dudy = 0, dvdx = 0;
+        for (int k = 0; k < NP; ++k) {
+          dvdx += m.dvv[jgp][k] * FV(vc.data(), 1, P(igp, k), l);
+          dudy += m.dvv[igp][k] * FV(vc.data(), 0, P(k, jgp), l);
+        }
+        const int p = P(igp, jgp);
+        F(vort, p, l) = (dvdx - dudy) * (1.0 / m.metdet[p] * rrearth);
+      }
+}
+
+// SphereOperators.hpp:536-583 (the input vector is overwritten, as in the reference)
+void divergence_sphere_wk(const EM& m, double* v, double* div, int nl) {
+  for (int p = 0; p < NP2; ++p)
+    for (int l = 0; l < nl; ++l) {
+      const double v0 = FV(v, 0, p, l), v1 = FV(v, 1, p, l);
+      FV(v, 0, p, l) = m.di(0, 0, p) * v0 + m.di(1, 0, p) * v1;
+      FV(v, 1, p, l) = m.di(0, 1, p) * v0 + m.di(1, 1, p) * v1;
+    }
+  for (int ngp = 0; ngp < NP; ++ngp)
+    for (int mgp = 0; mgp < NP; ++mgp)
+      for (int l = 0; l < nl; ++l) {
+        double dd = 0;
+        for (int jgp = 0; jgp < NP; ++jgp) {
+          dd -= (m.spheremp[P(ngp, jgp)] * FV(v, 0, P(ngp, jgp), l) * m.dvv[jgp][mgp] +
+                 m.spheremp[P(jgp, mgp)] * FV(v, 1, P(jgp, mgp), l) * m.dvv[jgp][ngp]) *
+                rrearth;
+        }
+        F(div, P(ngp, mgp), l) = dd;
+      }
+}
+
+// SphereOperators.hpp:585-597
+void laplace_simple(const EM& m, const double* field, double* lap, int nl) {
+  std::vector<double> gs(2 * NP2 * NLEV);
+  gradient_sphere(m, field, gs.data(), nl);
+  divergence_sphere_wk(m, gs.data(), lap, nl);
+}
+
+// SphereOperators.hpp:599-635
+void laplace_tensor(const EM& m, const double* field, double* lap, int nl) {
+  std::vector<double> gs(2 * NP2 * NLEV), sb(2 * NP2 * NLEV);
+  gradient_sphere(m, field, gs.data(), nl);
+  for (int p = 0; p < NP2; ++p)
+    for (int l = 0; l < nl; ++l) {
+      const double g0 = FV(gs.data(), 0, p, l), g1 = FV(gs.data(), 1, p, l);
+      FV(sb.data(), 0, p, l) = m.tv(0, 0, p) * g0 + m.tv(1, 0, p) * g1;
+      FV(sb.data(), 1, p, l) = m.tv(0, 1, p) * g0 + m.tv(1, 1, p) * g1;
+    }
+  divergence_sphere_wk(m, sb.data(), lap, nl);
+}
+
+// SphereOperators.hpp:680-710: curls = beta*curls + alpha*curl(scalar)
+void curl_sphere_wk_testcov_update(const EM& m, double alpha, double beta,
+                                   const double* scalar, double* curls, int nl) {
+  for (int ngp = 0; ngp < NP; ++ngp)
+    for (int mgp = 0; mgp < NP; ++mgp)
+      for (int l = 0; l < nl; ++l) {
+        double sb0 = 0, sb1 = 0;
+        for (int j = 0; j < NP; ++j) {
+          sb0 -= m.mp[P(j, mgp)] * F(scalar, P(j, mgp), l) * m.dvv[j][ngp];
+          sb1 += m.mp[P(ngp, j)] * F(scalar, P(ngp, j), l) * m.dvv[j][mgp];
+        }
+        const int p = P(ngp, mgp);
+        FV(curls, 0, p, l) = beta * FV(curls, 0, p, l) +
+                             alpha * (m.d(0, 0, p) * sb0 + m.d(1, 0, p) * sb1) * rrearth;
+        FV(curls, 1, p, l) = beta * FV(curls, 1, p, l) +
+                             alpha * (m.d(0, 1, p) * sb0 + m.d(1, 1, p) * sb1) * rrearth;
+      }
+}
+
+// SphereOperators.hpp:712-748
+void grad_sphere_wk_testcov(const EM& m, const double* scalar, double* grads, int nl) {
+  for (int ngp = 0; ngp < NP; ++ngp)
+    for (int mgp = 0; mgp < NP; ++mgp)
+      for (int l = 0; l < nl; ++l) {
+        double b0 = 0, b1 = 0;
+        const int p = P(ngp, mgp);
+        for (int j = 0; j < NP; ++j) {
+          const double mpnj = m.mp[P(ngp, j)];
+          const double mpjm = m.mp[P(j, mgp)];
+          const double md = m.metdet[p];
+          const double snj = F(scalar, P(ngp, j), l);
+          const double sjm = F(scalar, P(j, mgp), l);
+          const double djm = m.dvv[j][mgp];
+          const double djn = m.dvv[j][ngp];
+          b0 -= (mpnj * m.mi(0, 0, p) * md * snj * djm + mpjm * m.mi(0, 1, p) * md * sjm * djn);
+          b1 -= (mpnj * m.mi(1, 0, p) * md * snj * djm + mpjm * m.mi(1, 1, p) * md * sjm * djn);
+        }
+        FV(grads, 0, p, l) = (m.d(0, 0, p) * b0 + m.d(1, 0, p) * b1) * rrearth;
+        FV(grads, 1, p, l) = (m.d(0, 1, p) * b0 + m.d(1, 1, p) * b1) * rrearth;
+      }
+}
+
+// SphereOperators.hpp:816-862 (input and output may alias)
+void vlaplace_sphere_wk_contra(const EM& m, double nu_ratio, const double* vec, double* lap,
+                               int nl) {
+  std::vector<double> div(NP2 * NLEV), gcc(2 * NP2 * NLEV);
+  divergence_sphere(m, vec, div.data(), nl);
+  if (nu_ratio > 0 && nu_ratio != 1.0)
+    for (int p = 0; p < NP2; ++p)
+      for (int l = 0; l < nl; ++l) F(div.data(), p, l) *= nu_ratio;
+  grad_sphere_wk_testcov(m, div.data(), gcc.data(), nl);
+  std::vector<double>& vort = div;
+  vorticity_sphere(m, vec, vort.data(), nl);
+  curl_sphere_wk_testcov_update(m, -1.0, 1.0, vort.data(), gcc.data(), nl);
+  const double re2 = rrearth * rrearth;
+  for (int p = 0; p < NP2; ++p)
+    for (int l = 0; l < nl; ++l) {
+      const double f = 2.0 * m.spheremp[p];
+      const double a0 = f * FV(vec, 0, p, l) * re2 + FV(gcc.data(), 0, p, l);
+      const double a1 = f * FV(vec, 1, p, l) * re2 + FV(gcc.data(), 1, p, l);
+      FV(lap, 0, p, l) = a0;
+      FV(lap, 1, p, l) = a1;
+    }
+}
+
+// SphereOperators.hpp:750-814 (input and output may alias)
+void vlaplace_sphere_wk_cartesian(const EM& m, const double* vec, double* lap, int nl) {
+  std::vector<double> l0(NP2 * NLEV), l1(NP2 * NLEV), l2(NP2 * NLEV), vin(2 * NP2 * NLEV);
+  std::copy(vec, vec + 2 * NP2 * NLEV, vin.begin());
+  for (int p = 0; p < NP2; ++p)
+    for (int l = 0; l < nl; ++l) {
+      const double v0 = FV(vin.data(), 0, p, l), v1 = FV(vin.data(), 1, p, l);
+      F(l0.data(), p, l) = m.s2c(0, 0, p) * v0 + m.s2c(1, 0, p) * v1;
+      F(l1.data(), p, l) = m.s2c(0, 1, p) * v0 + m.s2c(1, 1, p) * v1;
+      F(l2.data(), p, l) = m.s2c(0, 2, p) * v0 + m.s2c(1, 2, p) * v1;
+    }
+  laplace_tensor(m, l0.data(), l0.data(), nl);
+  laplace_tensor(m, l1.data(), l1.data(), nl);
+  laplace_tensor(m, l2.data(), l2.data(), nl);
+  for (int p = 0; p < NP2; ++p)
+    for (int l = 0; l < nl; ++l) {
+      FV(lap, 0, p, l) = m.s2c(0, 0, p) * F(l0.data(), p, l) + m.s2c(0, 1, p) * F(l1.data(), p, l) +
+                         m.s2c(0, 2, p) * F(l2.data(), p, l) +
+                         2.0 * m.spheremp[p] * FV(vin.data(), 0, p, l) * (rrearth) * (rrearth);
+      FV(lap, 1, p, l) = m.s2c(1, 0, p) * F(l0.data(), p, l) + m.s2c(1, 1, p) * F(l1.data(), p, l) +
+                         m.s2c(1, 2, p) * F(l2.data(), p, l) +
+                         2.0 * m.spheremp[p] * FV(vin.data(), 1, p, l) * (rrearth) * (rrearth);
+    }
+}
+
+EM metric(int e) {
+  Ctx& c = C();
+  EM m;
+  m.D = &c.D[(size_t)e * 64];
+  m.Dinv = &c.Dinv[(size_t)e * 64];
+  m.metinv = &c.metinv[(size_t)e * 64];
+  m.metdet = &c.metdet[(size_t)e * 16];
+  m.spheremp = &c.spheremp[(size_t)e * 16];
+  m.mp = &c.mp[(size_t)e * 16];
+  m.tensor = c.tensorvisc.empty() ? nullptr : &c.tensorvisc[(size_t)e * 64];
+  m.sph2cart = c.vec_sph2cart.empty() ? nullptr : &c.vec_sph2cart[(size_t)e * 96];
+  m.dvv = c.dvv;
+  return m;
+}
+
+// ----------------------------------------------------------------------------------
+// DSS (src/share/cxx/mpi/BoundaryExchange.cpp:285-618, ConnectivityHelpers.hpp)
+// ----------------------------------------------------------------------------------
+const int PTS_FWD[8][4] = {{0, 1, 2, 3}, {12, 13, 14, 15}, {0, 4, 8, 12}, {3, 7, 11, 15},
+                           {0, -1, -1, -1}, {3, -1, -1, -1}, {12, -1, -1, -1}, {15, -1, -1, -1}};
+const int PTS_BWD[8][4] = {{3, 2, 1, 0}, {15, 14, 13, 12}, {12, 8, 4, 0}, {15, 11, 7, 3},
+                           {0, -1, -1, -1}, {3, -1, -1, -1}, {12, -1, -1, -1}, {15, -1, -1, -1}};
+// 0 = forward, 1 = backward (ConnectivityHelpers.hpp:129-139)
+const int DIRECTION[4][4] = {{1, 0, 0, 1}, {0, 1, 1, 0}, {0, 1, 1, 0}, {1, 0, 0, 1}};
+
+void build_tables() {
+  Ctx& c = C();
+  const int E = c.E;
+  c.g_src_e.assign((size_t)E * 16 * 3, 0);
+  c.g_src_p.assign((size_t)E * 16 * 3, 0);
+  c.g_cnt.assign((size_t)E * 16, 0);
+  auto add = [&](int e, int p, int se, int sp) {
+    int& n = c.g_cnt[(size_t)e * 16 + p];
+    c.g_src_e[((size_t)e * 16 + p) * 3 + n] = se;
+    c.g_src_p[((size_t)e * 16 + p) * 3 + n] = sp;
+    ++n;
+  };
+  for (int e = 0; e < E; ++e) {
+    for (int k = 0; k < NP; ++k)
+      for (int slot = 0; slot < 4; ++slot) {  // S, N, W, E
+        const int r = c.conn[(e * 8 + slot) * 2], rs = c.conn[(e * 8 + slot) * 2 + 1];
+        if (r < 0) continue;
+        const int dir = DIRECTION[rs][slot];
+        add(e, PTS_FWD[slot][k], r, dir == 0 ? PTS_FWD[rs][k] : PTS_BWD[rs][k]);
+      }
+    for (int slot = 4; slot < 8; ++slot) {  // SW, SE, NW, NE
+      const int r = c.conn[(e * 8 + slot) * 2], rs = c.conn[(e * 8 + slot) * 2 + 1];
+      if (r < 0) continue;
+      add(e, PTS_FWD[slot][0], r, PTS_FWD[rs][0]);
+    }
+  }
+  c.tables = true;
+}
+
+// One registered 3-D field: element block of [16][NLEV] at base + e*estride.
+struct FieldRef {
+  double* base;
+  size_t estride;
+};
+
+// BoundaryExchange::exchange: pack all (pre-exchange values), unpack in the fixed order,
+// then optionally multiply by rspheremp.
+void dss(const std::vector<FieldRef>& fields, bool rsmp) {
+  Ctx& c = C();
+  const int E = c.E;
+  for (const FieldRef& f : fields) {
+    std::vector<double> pre((size_t)E * NP2 * NLEV);
+#pragma omp parallel for
+    for (int e = 0; e < E; ++e)
+      std::memcpy(&pre[(size_t)e * NP2 * NLEV], f.base + (size_t)e * f.estride,
+                  sizeof(double) * NP2 * NLEV);
+#pragma omp parallel for
+    for (int e = 0; e < E; ++e) {
+      double* dst = f.base + (size_t)e * f.estride;
+      for (int p = 0; p < NP2; ++p) {
+        const int n = c.g_cnt[(size_t)e * 16 + p];
+        for (int s = 0; s < n; ++s) {
+          const int se = c.g_src_e[((size_t)e * 16 + p) * 3 + s];
+          const int sp = c.g_src_p[((size_t)e * 16 + p) * 3 + s];
+          const double* src = &pre[((size_t)se * NP2 + sp) * NLEV];
+          for (int l = 0; l < NLEV; ++l) dst[p * NLEV + l] += src[l];
+        }
+      }
+      if (rsmp)
+        for (int p = 0; p < NP2; ++p) {
+          const double r = c.rspheremp[(size_t)e * 16 + p];
+          for (int l = 0; l < NLEV; ++l) dst[p * NLEV + l] *= r;
+        }
+    }
+  }
+}
+
+// BoundaryExchange.cpp:620-849 on qlim [E][Q][2][NLEV]
+void dss_minmax() {
+  Ctx& c = C();
+  const int E = c.E, Q = c.Q;
+  std::vector<double> pre(c.qlim);
+#pragma omp parallel for
+  for (int e = 0; e < E; ++e)
+    for (int q = 0; q < Q; ++q)
+      for (int l = 0; l < NLEV; ++l)
+        for (int slot = 0; slot < 8; ++slot) {
+          const int r = c.conn[(e * 8 + slot) * 2];
+          if (r < 0) continue;
+          double& mx = c.qlim[(((size_t)e * Q + q) * 2 + 1) * NLEV + l];
+          double& mn = c.qlim[(((size_t)e * Q + q) * 2 + 0) * NLEV + l];
+          mx = std::max(mx, pre[(((size_t)r * Q + q) * 2 + 1) * NLEV + l]);
+          mn = std::min(mn, pre[(((size_t)r * Q + q) * 2 + 0) * NLEV + l]);
+        }
+}
+
+// ----------------------------------------------------------------------------------
+// Caar (src/share/cxx/CaarFunctorImpl.hpp), rsplit > 0 path, one element.
+// ----------------------------------------------------------------------------------
+void caar_element(int e, int nm1, int n0, int np1, double dt, double eta_ave_w, int n0_qdp) {
+  Ctx& c = C();
+  const EM m = metric(e);
+  const size_t N3 = NP2 * NLEV;
+  std::vector<double> tv(N3), vdp(2 * N3), div_vdp(N3), pressure(N3), gradp(2 * N3),
+      omega(N3), gradt(2 * N3), eg(2 * N3), ephi(N3), vort(N3);
+  const double* V0 = &c.v[IV(e, n0, 0, 0, 0)];
+  const double* T0 = &c.t[IS(e, n0, 0, 0)];
+  const double* DP0 = &c.dp3d[IS(e, n0, 0, 0)];
+  // compute_temperature_div_vdp: CaarFunctorImpl.hpp:330-409
+  for (int p = 0; p < NP2; ++p)
+    for (int l = 0; l < NLEV; ++l) {
+      if (n0_qdp < 0) {
+        F(tv.data(), p, l) = F(T0, p, l);
+      } else {
+        double Qt = c.qdp[IQ(e, n0_qdp, 0, p, l, c.Q)] / F(DP0, p, l);
+        Qt *= (Rwater_vapor / Rgas - 1.0);
+        Qt += 1.0;
+        F(tv.data(), p, l) = F(T0, p, l) * Qt;
+      }
+    }
+  for (int p = 0; p < NP2; ++p)
+    for (int l = 0; l < NLEV; ++l) {
+      FV(vdp.data(), 0, p, l) = FV(V0, 0, p, l) * F(DP0, p, l);
+      FV(vdp.data(), 1, p, l) = FV(V0, 1, p, l) * F(DP0, p, l);
+      c.vn0[I3V(e, 0, p, l)] += eta_ave_w * FV(vdp.data(), 0, p, l);
+      c.vn0[I3V(e, 1, p, l)] += eta_ave_w * FV(vdp.data(), 1, p, l);
+    }
+  divergence_sphere(m, vdp.data(), div_vdp.data(), NLEV);
+  // compute_pressure (serial form, CaarFunctorImpl.hpp:618-647)
+  for (int p = 0; p < NP2; ++p) {
+    double dp_prev = 0;
+    double p_prev = c.hyai0 * c.ps0;
+    for (int l = 0; l < NLEV; ++l) {
+      F(pressure.data(), p, l) = p_prev + 0.5 * (dp_prev + F(DP0, p, l));
+      p_prev = F(pressure.data(), p, l);
+      dp_prev = F(DP0, p, l);
+    }
+  }
+  // preq_hydrostatic (serial form, :686-730)
+  double* PHI = &c.phi[I3(e, 0, 0)];
+  for (int p = 0; p < NP2; ++p) {
+    const double phis = c.phis[(size_t)e * 16 + p];
+    double integration = 0;
+    for (int l = NLEV - 1; l >= 0; --l) {
+      const double r = Rgas * F(tv.data(), p, l) * (F(DP0, p, l) * 0.5 / F(pressure.data(), p, l));
+      F(PHI, p, l) = phis + 2.0 * integration + r;
+      integration = integration + r;
+    }
+  }
+  // preq_omega_ps (serial form, :848-889)
+  gradient_sphere(m, pressure.data(), gradp.data(), NLEV);
+  for (int p = 0; p < NP2; ++p) {
+    double integration = 0;
+    for (int l = 0; l < NLEV; ++l) {
+      const double vgrad_p = FV(V0, 0, p, l) * FV(gradp.data(), 0, p, l) +
+                             FV(V0, 1, p, l) * FV(gradp.data(), 1, p, l);
+      const double dv = F(div_vdp.data(), p, l);
+      F(omega.data(), p, l) = (vgrad_p - (integration + 0.5 * dv)) / F(pressure.data(), p, l);
+      integration = integration + dv;
+    }
+  }
+  // compute_phase_3 (:136-148): omega_p, T, v, dp3d
+  for (int p = 0; p < NP2; ++p)
+    for (int l = 0; l < NLEV; ++l) c.omega_p[I3(e, p, l)] += eta_ave_w * F(omega.data(), p, l);
+  // compute_temperature_np1 (:424-460)
+  gradient_sphere(m, T0, gradt.data(), NLEV);
+  std::vector<double> t_new(N3), v_new(2 * N3), dp_new(N3);
+  const double* Tm = &c.t[IS(e, nm1, 0, 0)];
+  for (int p = 0; p < NP2; ++p)
+    for (int l = 0; l < NLEV; ++l) {
+      const double vgrad_t = FV(V0, 0, p, l) * FV(gradt.data(), 0, p, l) +
+                             FV(V0, 1, p, l) * FV(gradt.data(), 1, p, l);
+      const double ttens = (0.0 - vgrad_t) + kappa * F(tv.data(), p, l) * F(omega.data(), p, l);
+      double temp_np1 = ttens * dt + F(Tm, p, l);
+      temp_np1 *= c.spheremp[(size_t)e * 16 + p];
+      F(t_new.data(), p, l) = temp_np1;
+    }
+  // compute_velocity_np1 (:183-232) with compute_energy_grad (:97-132)
+  for (int p = 0; p < NP2; ++p)
+    for (int l = 0; l < NLEV; ++l) {
+      const double r = Rgas * (F(tv.data(), p, l) / F(pressure.data(), p, l));
+      FV(eg.data(), 0, p, l) = r * FV(gradp.data(), 0, p, l);
+      FV(eg.data(), 1, p, l) = r * FV(gradp.data(), 1, p, l);
+      const double ke = 0.5 * (FV(V0, 0, p, l) * FV(V0, 0, p, l) + FV(V0, 1, p, l) * FV(V0, 1, p, l));
+      F(ephi.data(), p, l) = ke + F(PHI, p, l);
+    }
+  gradient_sphere_update(m, ephi.data(), eg.data(), NLEV);
+  vorticity_sphere(m, V0, vort.data(), NLEV);
+  const double* Vm = &c.v[IV(e, nm1, 0, 0, 0)];
+  for (int p = 0; p < NP2; ++p)
+    for (int l = 0; l < NLEV; ++l) {
+      F(vort.data(), p, l) += c.fcor[(size_t)e * 16 + p];
+      double e0 = FV(eg.data(), 0, p, l), e1 = FV(eg.data(), 1, p, l);
+      const double vo = F(vort.data(), p, l);
+      e0 *= -1;
+      e0 += 0.0 + FV(V0, 1, p, l) * vo;
+      e1 *= -1;
+      e1 += 0.0 - FV(V0, 0, p, l) * vo;
+      e0 *= dt;
+      e0 += FV(Vm, 0, p, l);
+      e1 *= dt;
+      e1 += FV(Vm, 1, p, l);
+      const double smp = c.spheremp[(size_t)e * 16 + p];
+      FV(v_new.data(), 0, p, l) = smp * e0;
+      FV(v_new.data(), 1, p, l) = smp * e1;
+    }
+  // compute_dp3d_np1 (:462-493), eta_dot_dpdn buffer is zero when rsplit > 0
+  const double* DPm = &c.dp3d[IS(e, nm1, 0, 0)];
+  for (int p = 0; p < NP2; ++p)
+    for (int l = 0; l < NLEV; ++l) {
+      double tmp = 0.0;
+      tmp += F(div_vdp.data(), p, l);
+      tmp -= 0.0;
+      tmp = F(DPm, p, l) - tmp * dt;
+      F(dp_new.data(), p, l) = c.spheremp[(size_t)e * 16 + p] * tmp;
+    }
+  std::memcpy(&c.t[IS(e, np1, 0, 0)], t_new.data(), sizeof(double) * N3);
+  std::memcpy(&c.v[IV(e, np1, 0, 0, 0)], v_new.data(), sizeof(double) * 2 * N3);
+  std::memcpy(&c.dp3d[IS(e, np1, 0, 0)], dp_new.data(), sizeof(double) * N3);
+}
+
+void caar_run(int nm1, int n0, int np1, double dt, double eta_ave_w, int n0_qdp) {
+  Ctx& c = C();
+#pragma omp parallel for schedule(static)
+  for (int e = 0; e < c.E; ++e) caar_element(e, nm1, n0, np1, dt, eta_ave_w, n0_qdp);
+  // BoundaryExchange registered in CaarFunctorImpl.hpp:68-79: v(2), T, dp3d
+  const size_t sv = (size_t)NTL * 2 * NP2 * NLEV, ss = (size_t)NTL * NP2 * NLEV;
+  dss({{&c.v[IV(0, np1, 0, 0, 0)], sv}, {&c.v[IV(0, np1, 1, 0, 0)], sv},
+       {&c.t[IS(0, np1, 0, 0)], ss}, {&c.dp3d[IS(0, np1, 0, 0)], ss}},
+      true);
+}
+
+// prim_advance_exp.cpp:113-161
+void u3_5stage(int nm1, int n0, int np1, int n0_qdp, double dt, double w) {
+  Ctx& c = C();
+  caar_run(n0, n0, nm1, dt / 5.0, w / 4.0, n0_qdp);
+  caar_run(n0, nm1, np1, dt / 5.0, 0.0, n0_qdp);
+  caar_run(n0, np1, np1, dt / 3.0, 0.0, n0_qdp);
+  caar_run(n0, np1, np1, 2.0 * dt / 3.0, 0.0, n0_qdp);
+#pragma omp parallel for
+  for (int e = 0; e < c.E; ++e)
+    for (int p = 0; p < NP2; ++p)
+      for (int l = 0; l < NLEV; ++l) {
+        double& t = c.t[IS(e, nm1, p, l)];
+        t = (5.0 * t - c.t[IS(e, n0, p, l)]) / 4.0;
+        double& v0 = c.v[IV(e, nm1, 0, p, l)];
+        v0 = (5.0 * v0 - c.v[IV(e, n0, 0, p, l)]) / 4.0;
+        double& v1 = c.v[IV(e, nm1, 1, p, l)];
+        v1 = (5.0 * v1 - c.v[IV(e, n0, 1, p, l)]) / 4.0;
+        double& d = c.dp3d[IS(e, nm1, p, l)];
+        d = (5.0 * d - c.dp3d[IS(e, n0, p, l)]) / 4.0;
+      }
+  caar_run(nm1, np1, np1, 3.0 * dt / 4.0, 3.0 * w / 4.0, n0_qdp);
+}
+
+// ----------------------------------------------------------------------------------
+// Hyperviscosity (src/share/cxx/HyperviscosityFunctorImpl.{hpp,cpp})
+// ----------------------------------------------------------------------------------
+void hypervis_run(int np1, double dt_in, double eta_ave_w) {
+  Ctx& c = C();
+  const Params& pr = c.prm;
+  const int hsub = pr.hypervis_subcycle;
+  const double dt = dt_in / hsub;
+  const size_t N3 = NP2 * NLEV;
+  double nu_scale_top[3] = {4.0 * pr.nu_top, 2.0 * pr.nu_top, 1.0 * pr.nu_top};
+  for (int icycle = 0; icycle < hsub; ++icycle) {
+    // TagFirstLaplaceHV
+#pragma omp parallel for
+    for (int e = 0; e < c.E; ++e) {
+      const EM m = metric(e);
+      laplace_simple(m, &c.t[IS(e, np1, 0, 0)], &c.ttens[I3(e, 0, 0)], NLEV);
+      laplace_simple(m, &c.dp3d[IS(e, np1, 0, 0)], &c.dptens[I3(e, 0, 0)], NLEV);
+      vlaplace_sphere_wk_contra(m, pr.nu_ratio1, &c.v[IV(e, np1, 0, 0, 0)],
+                                &c.vtens[I3V(e, 0, 0, 0)], NLEV);
+    }
+    const std::vector<FieldRef> tens = {{&c.vtens[I3V(0, 0, 0, 0)], 2 * N3},
+                                        {&c.vtens[I3V(0, 1, 0, 0)], 2 * N3},
+                                        {&c.ttens[0], N3},
+                                        {&c.dptens[0], N3}};
+    dss(tens, true);
+    // TagSecondLaplaceConstHV / TensorHV
+#pragma omp parallel for
+    for (int e = 0; e < c.E; ++e) {
+      const EM m = metric(e);
+      if (c.consthv) {
+        laplace_simple(m, &c.ttens[I3(e, 0, 0)], &c.ttens[I3(e, 0, 0)], NLEV);
+        laplace_simple(m, &c.dptens[I3(e, 0, 0)], &c.dptens[I3(e, 0, 0)], NLEV);
+        vlaplace_sphere_wk_contra(m, pr.nu_ratio2, &c.vtens[I3V(e, 0, 0, 0)],
+                                  &c.vtens[I3V(e, 0, 0, 0)], NLEV);
+      } else {
+        laplace_tensor(m, &c.ttens[I3(e, 0, 0)], &c.ttens[I3(e, 0, 0)], NLEV);
+        laplace_tensor(m, &c.dptens[I3(e, 0, 0)], &c.dptens[I3(e, 0, 0)], NLEV);
+        vlaplace_sphere_wk_cartesian(m, &c.vtens[I3V(e, 0, 0, 0)], &c.vtens[I3V(e, 0, 0, 0)],
+                                     NLEV);
+      }
+    }
+    // TagHyperPreExchange (HyperviscosityFunctorImpl.hpp:161-257)
+#pragma omp parallel for
+    for (int e = 0; e < c.E; ++e) {
+      const EM m = metric(e);
+      for (int p = 0; p < NP2; ++p)
+        for (int l = 0; l < NLEV; ++l) {
+          c.dpdiss_ave[I3(e, p, l)] += eta_ave_w * c.dp3d[IS(e, np1, p, l)] / hsub;
+          c.dpdiss_bih[I3(e, p, l)] += eta_ave_w * c.dptens[I3(e, p, l)] / hsub;
+        }
+      std::vector<double> lap_v(2 * N3), lap_t(N3), lap_dp(N3);
+      if (pr.nu_top > 0) {
+        vlaplace_sphere_wk_contra(m, 1.0, &c.v[IV(e, np1, 0, 0, 0)], lap_v.data(), 3);
+        laplace_simple(m, &c.t[IS(e, np1, 0, 0)], lap_t.data(), 3);
+        laplace_simple(m, &c.dp3d[IS(e, np1, 0, 0)], lap_dp.data(), 3);
+      }
+      for (int p = 0; p < NP2; ++p) {
+        for (int l = 0; l < NLEV; ++l) {
+          c.vtens[I3V(e, 0, p, l)] *= -pr.nu;
+          c.vtens[I3V(e, 1, p, l)] *= -pr.nu;
+          c.ttens[I3(e, p, l)] *= -pr.nu_s;
+          c.dptens[I3(e, p, l)] *= -pr.nu_p;
+        }
+        if (pr.nu_top > 0)
+          for (int l = 0; l < 3; ++l) {
+            c.vtens[I3V(e, 0, p, l)] += nu_scale_top[l] * FV(lap_v.data(), 0, p, l);
+            c.vtens[I3V(e, 1, p, l)] += nu_scale_top[l] * FV(lap_v.data(), 1, p, l);
+            c.ttens[I3(e, p, l)] += nu_scale_top[l] * F(lap_t.data(), p, l);
+            c.dptens[I3(e, p, l)] += nu_scale_top[l] * F(lap_dp.data(), p, l);
+          }
+        for (int l = 0; l < NLEV; ++l) {
+          c.dptens[I3(e, p, l)] *= dt;
+          c.dptens[I3(e, p, l)] += c.dp3d[IS(e, np1, p, l)] * m.spheremp[p];
+        }
+      }
+    }
+    dss(tens, false);
+    // TagUpdateStates (HyperviscosityFunctorImpl.hpp:134-158)
+#pragma omp parallel for
+    for (int e = 0; e < c.E; ++e)
+      for (int p = 0; p < NP2; ++p) {
+        const double rsmp = c.rspheremp[(size_t)e * 16 + p];
+        for (int l = 0; l < NLEV; ++l) {
+          double& vt0 = c.vtens[I3V(e, 0, p, l)];
+          double& vt1 = c.vtens[I3V(e, 1, p, l)];
+          vt0 = (dt * vt0 * rsmp);
+          vt1 = (dt * vt1 * rsmp);
+          double& v0 = c.v[IV(e, np1, 0, p, l)];
+          double& v1 = c.v[IV(e, np1, 1, p, l)];
+          v0 += vt0;
+          v1 += vt1;
+          double& tt = c.ttens[I3(e, p, l)];
+          tt = (dt * tt * rsmp);
+          const double heating = vt0 * v0 + vt1 * v1;
+          double& t = c.t[IS(e, np1, p, l)];
+          t = t + tt - heating / cp;
+          c.dp3d[IS(e, np1, p, l)] = (c.dptens[I3(e, p, l)] * rsmp);
+        }
+      }
+  }
+}
+
+// ----------------------------------------------------------------------------------
+// Euler step (src/share/cxx/EulerStepFunctorImpl.hpp)
+// ----------------------------------------------------------------------------------
+
+// with_limiter_shell + Limit functors (EulerStepFunctorImpl.hpp:693-884); team form,
+// reductions in k order.  x, c are [16]; returns with x limited.
+void limiter_level(int option, double* x, const double* cw, double& minp_io, double& maxp_io) {
+  double s0 = 0, s1 = 0;
+  for (int k = 0; k < NP2; ++k) {
+    s0 += x[k] * cw[k];
+    s1 += cw[k];
+  }
+  if (s1 <= 0) return;
+  double minp = minp_io, maxp = maxp_io;
+  if (minp < 0) minp = minp_io = 0;
+  if (s0 < minp * s1) minp = minp_io = s0 / s1;
+  if (s0 > maxp * s1) maxp = maxp_io = s0 / s1;
+  const double mass = s0;
+  if (option == 8) {
+    const int maxiter = NP2 - 1;
+    const double tol_limiter = 5e-14;
+    for (int iter = 0; iter < maxiter; ++iter) {
+      double addmass = 0;
+      for (int k = 0; k < NP2; ++k) {
+        double delta = 0;
+        if (x[k] > maxp) {
+          delta = x[k] - maxp;
+          x[k] = maxp;
+        } else if (x[k] < minp) {
+          delta = x[k] - minp;
+          x[k] = minp;
+        }
+        addmass += delta * cw[k];
+      }
+      if (std::abs(addmass) <= tol_limiter * std::abs(mass)) break;
+      if (addmass > 0) {
+        double weightssum = 0;
+        for (int k = 0; k < NP2; ++k)
+          if (x[k] < maxp) weightssum += cw[k];
+        if (weightssum == 0) break;  // see the serial limiter's f != 0 guard
+        const double adw = addmass / weightssum;
+        for (int k = 0; k < NP2; ++k) x[k] += (x[k] < maxp) ? adw : 0;
+      } else {
+        double weightssum = 0;
+        for (int k = 0; k < NP2; ++k)
+          if (x[k] > minp) weightssum += cw[k];
+        if (weightssum == 0) break;
+        const double adw = addmass / weightssum;
+        for (int k = 0; k < NP2; ++k) x[k] += (x[k] > minp) ? adw : 0;
+      }
+    }
+  } else {  // option 9, clip and assured sum
+    double addmass = 0;
+    for (int k = 0; k < NP2; ++k) {
+      double delta = 0;
+      if (x[k] > maxp) {
+        delta = x[k] - maxp;
+        x[k] = maxp;
+      } else if (x[k] < minp) {
+        delta = x[k] - minp;
+        x[k] = minp;
+      }
+      addmass += delta * cw[k];
+    }
+    if (addmass == 0) return;
+    if (addmass > 0) {
+      double fac = 0;
+      for (int k = 0; k < NP2; ++k) fac += cw[k] * (maxp - x[k]);
+      if (fac > 0) {
+        fac = addmass / fac;
+        for (int k = 0; k < NP2; ++k) x[k] += fac * (maxp - x[k]);
+      }
+    } else {
+      double fac = 0;
+      for (int k = 0; k < NP2; ++k) fac += cw[k] * (x[k] - minp);
+      if (fac > 0) {
+        fac = addmass / fac;
+        for (int k = 0; k < NP2; ++k) x[k] += fac * (x[k] - minp);
+      }
+    }
+  }
+}
+
+void euler_step(int np1_qdp, int n0_qdp, double dt, double rhs_multiplier, int dssopt) {
+  Ctx& c = C();
+  const Params& pr = c.prm;
+  const int E = c.E, Q = c.Q;
+  double rhs_viss = 0.0;
+  const size_t N3 = NP2 * NLEV;
+  // compute_dp (EulerStepFunctorImpl.hpp:405-435): buffer "pressure" holds dp
+#pragma omp parallel for
+  for (int e = 0; e < E; ++e)
+    for (int p = 0; p < NP2; ++p)
+      for (int l = 0; l < NLEV; ++l)
+        c.dp_buf[I3(e, p, l)] =
+            c.derived_dp[I3(e, p, l)] - (rhs_multiplier * dt) * c.divdp_proj[I3(e, p, l)];
+  // compute_qmin_qmax (:437-482)
+#pragma omp parallel for collapse(2)
+  for (int e = 0; e < E; ++e)
+    for (int q = 0; q < Q; ++q) {
+      double* qb = &c.qtens_bih[((size_t)e * Q + q) * N3];
+      double* ql = &c.qlim[((size_t)e * Q + q) * 2 * NLEV];
+      for (int l = 0; l < NLEV; ++l) {
+        if (rhs_multiplier != 1.0) {
+          const double v = c.qdp[IQ(e, n0_qdp, q, 0, l, Q)] / c.dp_buf[I3(e, 0, l)];
+          qb[l] = v;
+          ql[l] = v;
+          ql[NLEV + l] = v;
+        }
+        for (int p = 0; p < NP2; ++p) {
+          const double v = c.qdp[IQ(e, n0_qdp, q, p, l, Q)] / c.dp_buf[I3(e, p, l)];
+          qb[p * NLEV + l] = v;
+          ql[l] = std::min(ql[l], v);
+          ql[NLEV + l] = std::max(ql[NLEV + l], v);
+        }
+      }
+    }
+  if (rhs_multiplier == 0.0) {
+    dss_minmax();
+  } else if (rhs_multiplier == 2.0) {
+    // minmax_and_biharmonic (:493-499); min/max of the pre-biharmonic qlim
+    rhs_viss = 3.0;
+    // compute_biharmonic_pre (BIHPreNup / BIHPreNoNup)
+#pragma omp parallel for collapse(2)
+    for (int e = 0; e < E; ++e)
+      for (int q = 0; q < Q; ++q) {
+        const EM m = metric(e);
+        double* qb = &c.qtens_bih[((size_t)e * Q + q) * N3];
+        if (pr.nu_p > 0)
+          for (int p = 0; p < NP2; ++p)
+            for (int l = 0; l < NLEV; ++l)
+              qb[p * NLEV + l] = qb[p * NLEV + l] * c.dpdiss_ave[I3(e, p, l)] / c.dp0[l];
+        laplace_simple(m, qb, qb, NLEV);
+      }
+    std::vector<FieldRef> f;
+    for (int q = 0; q < Q; ++q) f.push_back({&c.qtens_bih[(size_t)q * N3], (size_t)Q * N3});
+    dss(f, true);
+    // compute_biharmonic_post (BIHPostConstHV / TensorHV + rhsviss_adjustment)
+    const double fac = -rhs_viss * dt * pr.nu_q;
+#pragma omp parallel for collapse(2)
+    for (int e = 0; e < E; ++e)
+      for (int q = 0; q < Q; ++q) {
+        const EM m = metric(e);
+        double* qb = &c.qtens_bih[((size_t)e * Q + q) * N3];
+        if (c.consthv) laplace_simple(m, qb, qb, NLEV);
+        else laplace_tensor(m, qb, qb, NLEV);
+        for (int p = 0; p < NP2; ++p)
+          for (int l = 0; l < NLEV; ++l)
+            qb[p * NLEV + l] = (fac * c.dp0[l] * qb[p * NLEV + l] / m.spheremp[p]);
+      }
+    dss_minmax();
+  }
+  // advect_and_limit: AALSetupPhase (compute_2d_advection_step, :585-631)
+  const bool add_ps_diss = pr.nu_p > 0 && rhs_viss != 0.0;
+  const double diss_fac = add_ps_diss ? -rhs_viss * dt * pr.nu_q : 0;
+  std::vector<double>& f_dss = dssopt == 0 ? c.eta_dot_dpdn : dssopt == 1 ? c.omega_p : c.divdp_proj;
+#pragma omp parallel for
+  for (int e = 0; e < E; ++e)
+    for (int p = 0; p < NP2; ++p)
+      for (int l = 0; l < NLEV; ++l) {
+        const double dp = c.dp_buf[I3(e, p, l)];
+        c.vstar[I3V(e, 0, p, l)] = c.vn0[I3V(e, 0, p, l)] / dp;
+        c.vstar[I3V(e, 1, p, l)] = c.vn0[I3V(e, 1, p, l)] / dp;
+        c.dpdissk[I3(e, p, l)] = dp - dt * c.divdp[I3(e, p, l)];
+        if (add_ps_diss)
+          c.dpdissk[I3(e, p, l)] +=
+              diss_fac * c.dpdiss_bih[I3(e, p, l)] / c.spheremp[(size_t)e * 16 + p];
+        f_dss[I3(e, p, l)] *= c.spheremp[(size_t)e * 16 + p];
+      }
+  // AALTracerPhase: compute_qtens, limiter, apply_spheremp (:563-582, 633-687)
+#pragma omp parallel for collapse(2)
+  for (int e = 0; e < E; ++e)
+    for (int q = 0; q < Q; ++q) {
+      const EM m = metric(e);
+      double* qt = &c.qtens_bih[((size_t)e * Q + q) * N3];
+      divergence_sphere_update(m, -dt, rhs_viss != 0.0, &c.vstar[I3V(e, 0, 0, 0)],
+                               &c.qdp[IQ(e, n0_qdp, q, 0, 0, Q)], qt, NLEV);
+      if (pr.limiter_option == 8 || pr.limiter_option == 9) {
+        double* ql = &c.qlim[((size_t)e * Q + q) * 2 * NLEV];
+        for (int l = 0; l < NLEV; ++l) {
+          double x[NP2], cw[NP2];
+          for (int k = 0; k < NP2; ++k) {
+            const double dpm = c.dpdissk[I3(e, k, l)];
+            cw[k] = m.spheremp[k] * dpm;
+            x[k] = qt[k * NLEV + l] / dpm;
+          }
+          double s1 = 0;
+          for (int k = 0; k < NP2; ++k) s1 += cw[k];
+          if (s1 <= 0) continue;
+          limiter_level(pr.limiter_option, x, cw, ql[l], ql[NLEV + l]);
+          for (int k = 0; k < NP2; ++k) qt[k * NLEV + l] = x[k] * c.dpdissk[I3(e, k, l)];
+        }
+      }
+      for (int p = 0; p < NP2; ++p)
+        for (int l = 0; l < NLEV; ++l)
+          c.qdp[IQ(e, np1_qdp, q, p, l, Q)] = m.spheremp[p] * qt[p * NLEV + l];
+    }
+  // exchange_qdp_dss_var (:501-504): Qdp(np1) and the DSS-option field, rspheremp
+  std::vector<FieldRef> f;
+  for (int q = 0; q < Q; ++q) f.push_back({&c.qdp[IQ(0, np1_qdp, q, 0, 0, Q)], (size_t)QTL * Q * N3});
+  f.push_back({f_dss.data(), N3});
+  dss(f, true);
+}
+
+void precompute_divdp() {  // EulerStepFunctorImpl.hpp:348-377
+  Ctx& c = C();
+#pragma omp parallel for
+  for (int e = 0; e < c.E; ++e) {
+    const EM m = metric(e);
+    divergence_sphere(m, &c.vn0[I3V(e, 0, 0, 0)], &c.divdp[I3(e, 0, 0)], NLEV);
+    std::memcpy(&c.divdp_proj[I3(e, 0, 0)], &c.divdp[I3(e, 0, 0)], sizeof(double) * NP2 * NLEV);
+  }
+}
+
+void qdp_time_avg(int n0_qdp, int np1_qdp) {  // EulerStepFunctorImpl.hpp:379-403
+  Ctx& c = C();
+  const double rkstage = 3.0;
+#pragma omp parallel for collapse(2)
+  for (int e = 0; e < c.E; ++e)
+    for (int q = 0; q < c.Q; ++q)
+      for (int p = 0; p < NP2; ++p)
+        for (int l = 0; l < NLEV; ++l) {
+          double& a = c.qdp[IQ(e, np1_qdp, q, p, l, c.Q)];
+          a = (c.qdp[IQ(e, n0_qdp, q, p, l, c.Q)] + (rkstage - 1) * a) / rkstage;
+        }
+}
+
+void tracers_rk2(double dt) {  // prim_advec_tracers_remap.cpp:32-90
+  Ctx& c = C();
+  c.tl.update_tracers_levels(c.prm.qsplit);
+  precompute_divdp();
+  euler_step(c.tl.np1_qdp, c.tl.n0_qdp, dt / 2.0, 0.0, 2);
+  euler_step(c.tl.np1_qdp, c.tl.np1_qdp, dt / 2.0, 1.0, 0);
+  euler_step(c.tl.np1_qdp, c.tl.np1_qdp, dt / 2.0, 2.0, 1);
+  qdp_time_avg(c.tl.n0_qdp, c.tl.np1_qdp);
+}
+
+// ----------------------------------------------------------------------------------
+// PPM vertical remap (src/share/cxx/RemapFunctor.hpp, PpmRemap.hpp); rsplit > 0.
+// Padded arrays use A(m) = a[m + 2] for m in [-2, NLEV+1].
+// ----------------------------------------------------------------------------------
+struct ColumnGrid {
+  double pio[NLEV + 2], pin[NLEV + 1], dpo[NLEV + 4], z2[NLEV];
+  int kid[NLEV];
+  double g[10][NLEV + 2];
+};
+
+void ppm_grids(const double* src, const double* tgt, ColumnGrid& G) {
+  // compute_partitions (PpmRemap.hpp:488-575)
+  double acc = 0;
+  for (int k = 0; k < NLEV; ++k) {
+    G.pio[k] = acc;
+    acc += src[k];
+  }
+  acc = 0;
+  for (int k = 0; k < NLEV; ++k) {
+    G.pin[k] = acc;
+    acc += tgt[k];
+  }
+  G.pio[NLEV] = G.pio[NLEV - 1] + src[NLEV - 1];
+  G.pin[NLEV] = G.pin[NLEV - 1] + tgt[NLEV - 1];
+  G.pio[NLEV + 1] = G.pio[NLEV] + 1.0;
+  G.pin[NLEV] = G.pio[NLEV];
+  double* D = G.dpo + 2;
+  for (int k = 0; k < NLEV; ++k) D[k] = src[k];
+  for (int k = 0; k < 2; ++k) {
+    D[-1 - k] = D[k];
+    D[NLEV + k] = D[NLEV - 1 - k];
+  }
+  // compute_integral_bounds (:577-648)
+  for (int k = 0; k < NLEV; ++k) {
+    int kk = k + 1;
+    while (kk < NLEV + 2 && G.pio[kk - 1] <= G.pin[k + 1]) kk++;
+    kk--;
+    if (kk == NLEV + 1) kk = NLEV;
+    if (kk < 1) kk = 1;  // invalid (non-monotone) source grid; flagged by the caller
+    G.kid[k] = kk - 1;
+    G.z2[k] = (G.pin[k + 1] - (G.pio[kk - 1] + G.pio[kk]) * 0.5) / D[kk - 1];
+  }
+  // compute_grids (:355-413); dx(j + 1 + off) = D(j - 1)
+  for (int j = 0; j < NLEV + 2; ++j) {
+    G.g[0][j] = D[j - 1] / (D[j - 2] + D[j - 1] + D[j]);
+    G.g[1][j] = (2.0 * D[j - 2] + D[j - 1]) / (D[j - 1] + D[j]);
+    G.g[2][j] = (D[j - 1] + 2.0 * D[j]) / (D[j - 2] + D[j - 1]);
+  }
+  for (int j = 0; j < NLEV + 1; ++j) {
+    G.g[3][j] = D[j - 1] / (D[j - 1] + D[j]);
+    G.g[4][j] = 1.0 / (D[j - 2] + D[j - 1] + D[j] + D[j + 1]);
+    G.g[5][j] = (2.0 * D[j - 1] * D[j]) / (D[j - 1] + D[j]);
+    G.g[6][j] = (D[j - 2] + D[j - 1]) / (2.0 * D[j - 1] + D[j]);
+    G.g[7][j] = (D[j + 1] + D[j]) / (2.0 * D[j] + D[j - 1]);
+    G.g[8][j] = D[j - 1] * (D[j - 2] + D[j - 1]) / (2.0 * D[j - 1] + D[j]);
+    G.g[9][j] = D[j] * (D[j] + D[j + 1]) / (D[j - 1] + 2.0 * D[j]);
+  }
+}
+
+inline double integrate_parabola(double sq, double lin, double cst, double x1, double x2) {
+  return (cst * (x2 - x1) + lin * (x2 * x2 - x1 * x1) / 2.0) + sq * (x2 * x2 * x2 - x1 * x1 * x1) / 3.0;
+}
+
+// compute_remap_phase + compute_ppm + compute_remap (PpmRemap.hpp:202-483)
+void ppm_remap_column(const ColumnGrid& G, int remap_alg, double* q /* [NLEV] */) {
+  const double* D = G.dpo + 2;
+  double a_[NLEV + 4];
+  double* A = a_ + 2;
+  double mass[NLEV + 2];
+  double dma[NLEV + 2], ai[NLEV + 1], coef[3][NLEV];
+  for (int k = 0; k < NLEV; ++k) A[k] = q[k] / D[k];
+  if (remap_alg == 3) {
+    for (int k = 0; k < 2; ++k) {
+      A[-1 - k] = A[0];
+      A[NLEV + k] = A[NLEV - 1];
+    }
+  } else {
+    for (int k = 0; k < 2; ++k) {
+      A[-1 - k] = A[k];
+      A[NLEV + k] = A[NLEV - 1 - k];
+    }
+  }
+  double acc = 0;
+  for (int k = 0; k < NLEV; ++k) {
+    mass[k + 1] = acc;
+    acc += q[k];
+  }
+  mass[0] = 0.0;
+  mass[NLEV + 1] = mass[NLEV] + q[NLEV - 1];
+  for (int j = 0; j < NLEV + 2; ++j) {
+    if ((A[j] - A[j - 1]) * (A[j - 1] - A[j - 2]) > 0.0) {
+      const double da = G.g[0][j] * (G.g[1][j] * (A[j] - A[j - 1]) + G.g[2][j] * (A[j - 1] - A[j - 2]));
+      dma[j] = std::min(std::min(std::fabs(da), 2.0 * std::fabs(A[j - 1] - A[j - 2])),
+                        2.0 * std::fabs(A[j] - A[j - 1])) *
+               std::copysign(1.0, da);
+    } else {
+      dma[j] = 0.0;
+    }
+  }
+  for (int j = 0; j < NLEV + 1; ++j) {
+    ai[j] = A[j - 1] + G.g[3][j] * (A[j] - A[j - 1]) +
+            G.g[4][j] * (G.g[5][j] * (G.g[6][j] - G.g[7][j]) * (A[j] - A[j - 1]) -
+                         G.g[8][j] * dma[j + 1] + G.g[9][j] * dma[j]);
+  }
+  for (int jp = 0; jp < NLEV; ++jp) {
+    const int j = jp + 1;
+    double al = ai[j - 1], ar = ai[j];
+    const double cm = A[j - 1];
+    if ((ar - cm) * (cm - al) <= 0.) {
+      al = cm;
+      ar = cm;
+    }
+    if ((ar - al) * (cm - (al + ar) / 2.0) > (ar - al) * (ar - al) / 6.0) al = 3.0 * cm - 2.0 * ar;
+    if ((ar - al) * (cm - (al + ar) / 2.0) < -(ar - al) * (ar - al) / 6.0) ar = 3.0 * cm - 2.0 * al;
+    coef[0][jp] = 1.5 * cm - (al + ar) / 4.0;
+    coef[1][jp] = ar - al;
+    coef[2][jp] = 3.0 * (-2.0 * cm + (al + ar));
+  }
+  if (remap_alg == 2) {  // PpmFixedParabola::apply_ppm_boundary
+    coef[0][0] = A[0];
+    coef[0][1] = A[1];
+    coef[0][NLEV - 2] = A[NLEV - 2];
+    coef[0][NLEV - 1] = A[NLEV - 1];
+    coef[1][0] = coef[1][1] = coef[2][0] = coef[2][1] = 0.0;
+    coef[1][NLEV - 2] = coef[1][NLEV - 1] = coef[2][NLEV - 2] = coef[2][NLEV - 1] = 0.0;
+  }
+  // compute_remap, GPU form (each level recomputes the lower interface mass)
+  auto cmass = [&](int kk, double x2) {
+    const double integral = integrate_parabola(coef[2][kk], coef[1][kk], coef[0][kk], -0.5, x2);
+    return mass[kk + 1] + integral * D[kk];
+  };
+  double out[NLEV];
+  for (int k = 0; k < NLEV; ++k) {
+    const double m1 = k > 0 ? cmass(G.kid[k - 1], G.z2[k - 1]) : 0.0;
+    const double m2 = cmass(G.kid[k], G.z2[k]);
+    out[k] = m2 - m1;
+  }
+  for (int k = 0; k < NLEV; ++k) q[k] = out[k];
+}
+
+void remap_run(int np1, int n0_qdp, double dt) {  // RemapFunctor::run_remap, rsplit > 0
+  Ctx& c = C();
+  (void)dt;
+  const int E = c.E, Q = c.Q;
+  int valid = 1;
+#pragma omp parallel for reduction(& : valid)
+  for (int e = 0; e < E; ++e) {
+    for (int p = 0; p < NP2; ++p) {
+      double src[NLEV], tgt[NLEV];
+      // compute_ps_v
+      double ps = 0.0;
+      for (int l = 0; l < NLEV; ++l) ps += c.dp3d[IS(e, np1, p, l)];
+      ps += c.hyai0 * c.ps0;
+      c.ps_v[((size_t)e * NTL + np1) * NP2 + p] = ps;
+      for (int l = 0; l < NLEV; ++l) {
+        tgt[l] = (c.hyai[l + 1] - c.hyai[l]) * c.ps0 + (c.hybi[l + 1] - c.hybi[l]) * ps;
+        src[l] = c.dp3d[IS(e, np1, p, l)];
+        if (std::isnan(src[l]) || src[l] < 0.0) valid = 0;
+      }
+      ColumnGrid G;
+      ppm_grids(src, tgt, G);
+      double col[NLEV];
+      for (int var = 0; var < 3; ++var) {
+        double* base = var < 2 ? &c.v[IV(e, np1, var, p, 0)] : &c.t[IS(e, np1, p, 0)];
+        for (int l = 0; l < NLEV; ++l) col[l] = base[l] * src[l];
+        ppm_remap_column(G, c.prm.remap_alg, col);
+        for (int l = 0; l < NLEV; ++l) base[l] = col[l] / tgt[l];
+      }
+      for (int q = 0; q < Q; ++q) {
+        double* base = &c.qdp[IQ(e, n0_qdp, q, p, 0, Q)];
+        for (int l = 0; l < NLEV; ++l) col[l] = base[l];
+        ppm_remap_column(G, c.prm.remap_alg, col);
+        for (int l = 0; l < NLEV; ++l) base[l] = col[l];
+      }
+    }
+  }
+  c.valid_remap = valid;
+}
+
+// prim_step.cpp:20-103
+void prim_step(double dt) {
+  Ctx& c = C();
+  const Params& pr = c.prm;
+#pragma omp parallel for
+  for (int e = 0; e < c.E; ++e)
+    for (int p = 0; p < NP2; ++p)
+      for (int l = 0; l < NLEV; ++l) {
+        c.eta_dot_dpdn[I3(e, p, l)] = 0;
+        c.vn0[I3V(e, 0, p, l)] = 0;
+        c.vn0[I3V(e, 1, p, l)] = 0;
+        c.omega_p[I3(e, p, l)] = 0;
+        if (pr.nu_p > 0) {
+          c.dpdiss_ave[I3(e, p, l)] = 0;
+          c.dpdiss_bih[I3(e, p, l)] = 0;
+        }
+        c.derived_dp[I3(e, p, l)] = c.dp3d[IS(e, c.tl.n0, p, l)];
+      }
+  for (int n = 0; n < pr.qsplit; ++n) {
+    if (n > 0) c.tl.update_dynamics_levels();
+    int n0_qdp = -1;
+    if (pr.moist) {
+      c.tl.update_tracers_levels(pr.qsplit);
+      n0_qdp = c.tl.n0_qdp;
+    }
+    const double w = 1.0 / pr.qsplit;
+    u3_5stage(c.tl.nm1, c.tl.n0, c.tl.np1, n0_qdp, dt, w);
+    hypervis_run(c.tl.np1, dt, w);
+  }
+  if (pr.qsize > 0) tracers_rk2(dt * pr.qsplit);
+}
+
+void prim_run_subcycle(double dt, int& nstep, int& nm1, int& n0, int& np1) {  // prim_driver.cpp:31-156
+  Ctx& c = C();
+  const Params& pr = c.prm;
+  const double dt_q = dt * pr.qsplit;
+  double dt_remap = dt_q;
+  if (pr.rsplit > 0) dt_remap = dt_q * pr.rsplit;
+  c.tl.update_tracers_levels(pr.qsplit);
+  // dp3d from ps_v
+  const int tn0 = c.tl.n0;
+#pragma omp parallel for
+  for (int e = 0; e < c.E; ++e)
+    for (int p = 0; p < NP2; ++p)
+      for (int l = 0; l < NLEV; ++l)
+        c.dp3d[IS(e, tn0, p, l)] =
+            c.ai_delta[l] * c.ps0 + c.bi_delta[l] * c.ps_v[((size_t)e * NTL + tn0) * NP2 + p];
+  prim_step(dt);
+  for (int r = 1; r < pr.rsplit; ++r) {
+    c.tl.update_dynamics_levels();
+    prim_step(dt);
+  }
+  c.tl.update_tracers_levels(pr.qsplit);
+  remap_run(c.tl.np1, c.tl.np1_qdp, dt_remap);
+  if (!c.valid_remap) {
+    set_error(101, "Negative (or nan) layer thickness detected, aborting!");
+    return;
+  }
+  // update_q (prim_driver.cpp:171-206)
+  const int tnp1 = c.tl.np1, np1_qdp = c.tl.np1_qdp;
+#pragma omp parallel for collapse(2)
+  for (int e = 0; e < c.E; ++e)
+    for (int q = 0; q < c.Q; ++q)
+      for (int p = 0; p < NP2; ++p)
+        for (int l = 0; l < NLEV; ++l) {
+          const double dp = c.ai_delta[l] * c.ps0 + c.bi_delta[l] * c.ps_v[((size_t)e * NTL + tnp1) * NP2 + p];
+          c.Qc[(((size_t)e * c.Q + q) * NP2 + p) * NLEV + l] = c.qdp[IQ(e, np1_qdp, q, p, l, c.Q)] / dp;
+        }
+  c.tl.update_dynamics_levels();
+  nstep = c.tl.nstep;
+  nm1 = c.tl.nm1;
+  n0 = c.tl.n0;
+  np1 = c.tl.np1;
+}
+
+// Fortran <-> internal transposes (SyncUtils.hpp).  Fortran per-element/time-level
+// blocks are [lev][comp][16]; internal blocks are [comp][16][lev].
+void pull_block(const double* f, double* in, int ncomp) {
+  for (int l = 0; l < NLEV; ++l)
+    for (int cc = 0; cc < ncomp; ++cc)
+      for (int p = 0; p < NP2; ++p) in[(cc * NP2 + p) * NLEV + l] = f[(l * ncomp + cc) * NP2 + p];
+}
+void push_block(const double* in, double* f, int ncomp) {
+  for (int l = 0; l < NLEV; ++l)
+    for (int cc = 0; cc < ncomp; ++cc)
+      for (int p = 0; p < NP2; ++p) f[(l * ncomp + cc) * NP2 + p] = in[(cc * NP2 + p) * NLEV + l];
+}
+
+}  // namespace
+
+// ====================================================================================
+// Exported C ABI (same names as libhxgpu.so; see include/hxgpu.h)
+// ====================================================================================
+extern "C" {
+
+void initialize_hommexx_session(void) { C(); }
+void finalize_hommexx_session(void) {
+  delete g;
+  g = nullptr;
+}
+void reset_cxx_comm(const int*) {}
+
+void init_connectivity(const int* n) {
+  Ctx& c = C();
+  c.conn.assign((size_t)(*n) * 16, -1);
+  c.conn_final = false;
+}
+
+void add_connection(const int* fl, const int*, const int* fp, const int*, const int* sl,
+                    const int*, const int* sp, const int*) {
+  Ctx& c = C();
+  auto convert = [](int fpos) { return fpos <= 4 ? (((fpos - 1) + 2) % 4) : (fpos - 1); };
+  const int e = *fl - 1, s = convert(*fp);
+  c.conn[(e * 8 + s) * 2] = *sl - 1;
+  c.conn[(e * 8 + s) * 2 + 1] = convert(*sp);
+}
+void finalize_connectivity(void) { C().conn_final = true; }
+
+void init_derivative_c(const double* const* dvv) {
+  Ctx& c = C();
+  for (int i = 0; i < NP; ++i)
+    for (int j = 0; j < NP; ++j) c.dvv[i][j] = (*dvv)[i * NP + j];
+}
+
+void init_simulation_params_c(const int* remap_alg, const int* limiter_option, const int* rsplit,
+                              const int* qsplit, const int* time_step_type, const int*,
+                              const int* qsize, const int* state_frequency, const double* nu,
+                              const double* nu_p, const double* nu_q, const double* nu_s,
+                              const double* nu_div, const double* nu_top,
+                              const int* hypervis_order, const int* hypervis_subcycle,
+                              const double* hypervis_scaling, const int* ftype,
+                              const bool* prescribed_wind, const bool* moisture,
+                              const bool* disable_diagnostics, const bool*,
+                              const bool* use_semi_lagrangian_transport) {
+  Ctx& c = C();
+  c.last_err = 0;
+  auto bad = [&](const char* opt) {
+    set_error(11, std::string("Error in init_simulation_params_c: unsupported value for input parameter '") + opt + "'.");
+  };
+  if (*remap_alg != 1 && *remap_alg != 2) return bad("vert_remap_q_alg");
+  if (*prescribed_wind) return bad("prescribed_wind");
+  if (*hypervis_order != 2) return bad("hypervis_order");
+  if (*use_semi_lagrangian_transport) return bad("use_semi_lagrangian_transport");
+  if (*time_step_type != 5) return bad("time_step_type");
+  if (*limiter_option != 8 && *limiter_option != 9) return bad("limiter_option");
+  if (*ftype != -1 && *ftype != 0 && *ftype != 2) return bad("ftype");
+  if (!(*nu_p > 0)) return bad("nu_p");
+  if (!(*nu > 0)) return bad("nu");
+  if (!(*nu_div > 0)) return bad("nu_div");
+  if (*ftype != -1) {
+    set_error(12, "CAM forcing (ftype 0/2) is not part of this build.");
+    return;
+  }
+  if (*rsplit == 0) {
+    set_error(12, "rsplit=0 (vertically Eulerian) is not part of this build.");
+    return;
+  }
+  Params& p = c.prm;
+  p.remap_alg = *remap_alg;
+  p.limiter_option = *limiter_option;
+  p.rsplit = *rsplit;
+  p.qsplit = *qsplit;
+  p.time_step_type = *time_step_type;
+  p.qsize = *qsize;
+  p.state_frequency = *state_frequency;
+  p.nu = *nu;
+  p.nu_p = *nu_p;
+  p.nu_q = *nu_q;
+  p.nu_s = *nu_s;
+  p.nu_div = *nu_div;
+  p.nu_top = *nu_top;
+  p.hypervis_order = *hypervis_order;
+  p.hypervis_subcycle = *hypervis_subcycle;
+  p.hypervis_scaling = *hypervis_scaling;
+  p.ftype = *ftype;
+  p.moist = *moisture;
+  p.disable_diagnostics = *disable_diagnostics;
+  if (p.nu != p.nu_div) {
+    const double ratio = p.nu_div / p.nu;
+    if (p.hypervis_scaling != 0.0) {
+      p.nu_ratio1 = ratio * ratio;
+      p.nu_ratio2 = 1.0;
+    } else {
+      p.nu_ratio1 = ratio;
+      p.nu_ratio2 = ratio;
+    }
+  } else {
+    p.nu_ratio1 = 1.0;
+    p.nu_ratio2 = 1.0;
+  }
+  p.set = true;
+}
+
+void init_hvcoord_c(const double* ps0, const double* const*, const double* const* hyai,
+                    const double* const*, const double* const* hybi) {
+  Ctx& c = C();
+  c.ps0 = *ps0;
+  for (int k = 0; k <= NLEV; ++k) {
+    c.hyai[k] = (*hyai)[k];
+    c.hybi[k] = (*hybi)[k];
+  }
+  c.hyai0 = c.hyai[0];
+  for (int l = 0; l < NLEV; ++l) {  // HybridVCoord::compute_deltas
+    c.ai_delta[l] = c.hyai[l + 1] - c.hyai[l];
+    c.bi_delta[l] = c.hybi[l + 1] - c.hybi[l];
+    c.dp0[l] = c.ai_delta[l] * c.ps0 + c.bi_delta[l] * c.ps0;
+  }
+}
+
+void init_elements_2d_c(const int* nelemd, const double* const* D, const double* const* Dinv,
+                        const double* const* fcor, const double* const* mp,
+                        const double* const* spheremp, const double* const* rspheremp,
+                        const double* const* metdet, const double* const* metinv,
+                        const double* const* phis, const double* const* tensorvisc,
+                        const double* const* vec_sph2cart, const bool* consthv) {
+  Ctx& c = C();
+  const int E = *nelemd;
+  c.E = E;
+  c.Q = c.prm.qsize;
+  c.consthv = *consthv;
+  auto cp = [](std::vector<double>& dst, const double* src, size_t n) { dst.assign(src, src + n); };
+  cp(c.D, *D, (size_t)E * 64);
+  cp(c.Dinv, *Dinv, (size_t)E * 64);
+  cp(c.metinv, *metinv, (size_t)E * 64);
+  cp(c.fcor, *fcor, (size_t)E * 16);
+  cp(c.mp, *mp, (size_t)E * 16);
+  cp(c.spheremp, *spheremp, (size_t)E * 16);
+  cp(c.rspheremp, *rspheremp, (size_t)E * 16);
+  cp(c.metdet, *metdet, (size_t)E * 16);
+  cp(c.phis, *phis, (size_t)E * 16);
+  if (!c.consthv) {
+    cp(c.tensorvisc, *tensorvisc, (size_t)E * 64);
+    cp(c.vec_sph2cart, *vec_sph2cart, (size_t)E * 96);
+  }
+  const size_t N3 = (size_t)E * NP2 * NLEV;
+  const int Q = c.Q;
+  c.v.assign(N3 * NTL * 2, 0.0);
+  c.t.assign(N3 * NTL, 0.0);
+  c.dp3d.assign(N3 * NTL, 0.0);
+  c.ps_v.assign((size_t)E * NTL * NP2, 0.0);
+  c.qdp.assign(N3 * QTL * Q, 0.0);
+  c.Qc.assign(N3 * Q, 0.0);
+  for (auto* f : {&c.phi, &c.omega_p, &c.eta_dot_dpdn, &c.derived_dp, &c.divdp, &c.divdp_proj,
+                  &c.dpdiss_ave, &c.dpdiss_bih, &c.ttens, &c.dptens, &c.dpdissk, &c.dp_buf})
+    f->assign(N3, 0.0);
+  c.vn0.assign(2 * N3, 0.0);
+  c.vtens.assign(2 * N3, 0.0);
+  c.vstar.assign(2 * N3, 0.0);
+  c.qtens_bih.assign(N3 * Q, 0.0);
+  c.qlim.assign((size_t)E * Q * 2 * NLEV, 0.0);
+}
+
+void init_elements_states_c(const double* const* v, const double* const* T,
+                            const double* const* dp3d, const double* const* Qdp,
+                            const double* const* ps_v) {
+  Ctx& c = C();
+  const size_t B = (size_t)NP2 * NLEV;
+  for (int e = 0; e < c.E; ++e)
+    for (int tl = 0; tl < NTL; ++tl) {
+      pull_block(*v + ((size_t)e * NTL + tl) * 2 * B, &c.v[IV(e, tl, 0, 0, 0)], 2);
+      pull_block(*T + ((size_t)e * NTL + tl) * B, &c.t[IS(e, tl, 0, 0)], 1);
+      pull_block(*dp3d + ((size_t)e * NTL + tl) * B, &c.dp3d[IS(e, tl, 0, 0)], 1);
+    }
+  for (int e = 0; e < c.E; ++e)
+    for (int qt = 0; qt < QTL; ++qt)
+      for (int q = 0; q < c.Q; ++q)
+        pull_block(*Qdp + (((size_t)e * QTL + qt) * c.Q + q) * B, &c.qdp[IQ(e, qt, q, 0, 0, c.Q)], 1);
+  std::memcpy(c.ps_v.data(), *ps_v, sizeof(double) * c.E * NTL * NP2);
+}
+
+void init_diagnostics_c(double* const*, double* const*, double* const*, double* const*,
+                        double* const*, double* const*, double* const*, double* const*) {}
+
+void init_boundary_exchanges_c(void) { build_tables(); }
+
+void init_time_level_c(const int* nm1, const int* n0, const int* np1, const int* nstep,
+                       const int* nstep0) {
+  Ctx& c = C();
+  c.tl.nm1 = *nm1 - 1;
+  c.tl.n0 = *n0 - 1;
+  c.tl.np1 = *np1 - 1;
+  c.tl.nstep = *nstep;
+  c.tl.nstep0 = *nstep0;
+}
+
+void prim_run_subcycle_c(const double* dt, int* nstep, int* nm1, int* n0, int* np1, const int*) {
+  C().last_err = 0;
+  prim_run_subcycle(*dt, *nstep, *nm1, *n0, *np1);
+}
+
+void cxx_push_results_to_f90(double* const* v, double* const* T, double* const* dp3d,
+                             double* const* Qdp, double* const* Q, double* const* ps_v,
+                             double* const* omega_p) {
+  Ctx& c = C();
+  const size_t B = (size_t)NP2 * NLEV;
+  for (int e = 0; e < c.E; ++e)
+    for (int tl = 0; tl < NTL; ++tl) {
+      push_block(&c.v[IV(e, tl, 0, 0, 0)], *v + ((size_t)e * NTL + tl) * 2 * B, 2);
+      push_block(&c.t[IS(e, tl, 0, 0)], *T + ((size_t)e * NTL + tl) * B, 1);
+      push_block(&c.dp3d[IS(e, tl, 0, 0)], *dp3d + ((size_t)e * NTL + tl) * B, 1);
+    }
+  for (int e = 0; e < c.E; ++e)
+    for (int qt = 0; qt < QTL; ++qt)
+      for (int q = 0; q < c.Q; ++q)
+        push_block(&c.qdp[IQ(e, qt, q, 0, 0, c.Q)], *Qdp + (((size_t)e * QTL + qt) * c.Q + q) * B, 1);
+  for (int e = 0; e < c.E; ++e) {
+    for (int q = 0; q < c.Q; ++q)
+      push_block(&c.Qc[(((size_t)e * c.Q + q) * NP2) * NLEV], *Q + ((size_t)e * c.Q + q) * B, 1);
+    push_block(&c.omega_p[I3(e, 0, 0)], *omega_p + (size_t)e * B, 1);
+  }
+  std::memcpy(*ps_v, c.ps_v.data(), sizeof(double) * c.E * NTL * NP2);
+}
+
+int hx_last_error(char* buf, int buflen) {
+  Ctx& c = C();
+  if (buf && buflen > 0) {
+    std::strncpy(buf, c.last_msg.c_str(), buflen - 1);
+    buf[buflen - 1] = 0;
+  }
+  return c.last_err;
+}
+void hx_set_abort_on_error(int a) { C().abort_on_error = a != 0; }
+int hx_set_precision(int mode) {
+  if (mode != 0) {
+    set_error(12, "the oracle computes in FP64 only");
+    return 12;
+  }
+  return 0;
+}
+
+static double* field_ptr(const std::string& n, int tl, int& ncomp, size_t& estride, int& nblocks) {
+  Ctx& c = C();
+  const size_t B = (size_t)NP2 * NLEV;
+  ncomp = 1;
+  nblocks = 1;
+  if (n == "v") { ncomp = 2; estride = NTL * 2 * B; return &c.v[IV(0, tl, 0, 0, 0)]; }
+  if (n == "T") { estride = NTL * B; return &c.t[IS(0, tl, 0, 0)]; }
+  if (n == "dp3d") { estride = NTL * B; return &c.dp3d[IS(0, tl, 0, 0)]; }
+  if (n == "Qdp") { nblocks = c.Q; estride = (size_t)QTL * c.Q * B; return &c.qdp[IQ(0, tl, 0, 0, 0, c.Q)]; }
+  if (n == "Q") { nblocks = c.Q; estride = (size_t)c.Q * B; return c.Qc.data(); }
+  if (n == "vn0") { ncomp = 2; estride = 2 * B; return c.vn0.data(); }
+  estride = B;
+  if (n == "omega_p") return c.omega_p.data();
+  if (n == "phi") return c.phi.data();
+  if (n == "eta_dot_dpdn") return c.eta_dot_dpdn.data();
+  if (n == "derived_dp") return c.derived_dp.data();
+  if (n == "divdp") return c.divdp.data();
+  if (n == "divdp_proj") return c.divdp_proj.data();
+  if (n == "dpdiss_ave") return c.dpdiss_ave.data();
+  if (n == "dpdiss_biharmonic") return c.dpdiss_bih.data();
+  return nullptr;
+}
+
+int hx_get_field(const char* name, int tl, double* out) {
+  Ctx& c = C();
+  const std::string n(name);
+  if (n == "ps_v") {
+    for (int e = 0; e < c.E; ++e)
+      std::memcpy(out + (size_t)e * NP2, &c.ps_v[((size_t)e * NTL + tl) * NP2], sizeof(double) * NP2);
+    return 0;
+  }
+  int ncomp, nb;
+  size_t es;
+  double* base = field_ptr(n, tl, ncomp, es, nb);
+  if (!base) return HX_ERR_STATE;
+  const size_t B = (size_t)NP2 * NLEV * ncomp;
+  for (int e = 0; e < c.E; ++e)
+    for (int b = 0; b < nb; ++b) push_block(base + e * es + b * B, out + ((size_t)e * nb + b) * B, ncomp);
+  return 0;
+}
+
+int hx_set_field(const char* name, int tl, const double* in) {
+  Ctx& c = C();
+  const std::string n(name);
+  if (n == "ps_v") {
+    for (int e = 0; e < c.E; ++e)
+      std::memcpy(&c.ps_v[((size_t)e * NTL + tl) * NP2], in + (size_t)e * NP2, sizeof(double) * NP2);
+    return 0;
+  }
+  int ncomp, nb;
+  size_t es;
+  double* base = field_ptr(n, tl, ncomp, es, nb);
+  if (!base) return HX_ERR_STATE;
+  const size_t B = (size_t)NP2 * NLEV * ncomp;
+  for (int e = 0; e < c.E; ++e)
+    for (int b = 0; b < nb; ++b) pull_block(in + ((size_t)e * nb + b) * B, base + e * es + b * B, ncomp);
+  return 0;
+}
+
+int hx_run_caar_stage(int nm1, int n0, int np1, double dt, double w) {
+  caar_run(nm1, n0, np1, dt, w, -1);
+  return 0;
+}
+int hx_run_rk5(int nm1, int n0, int np1, int n0_qdp, double dt, double w) {
+  u3_5stage(nm1, n0, np1, n0_qdp, dt, w);
+  return 0;
+}
+int hx_run_hypervis(int np1, double dt, double w) {
+  hypervis_run(np1, dt, w);
+  return 0;
+}
+int hx_run_euler_step(int np1_qdp, int n0_qdp, double dt, double rhs, int dssopt) {
+  euler_step(np1_qdp, n0_qdp, dt, rhs, dssopt);
+  return 0;
+}
+int hx_run_tracers_rk2(double dt) {
+  tracers_rk2(dt);
+  return 0;
+}
+int hx_run_remap(int np1, int np1_qdp, double dt) {
+  remap_run(np1, np1_qdp, dt);
+  return C().valid_remap ? 0 : 101;
+}
+int hx_run_prim_step(double dt) {
+  prim_step(dt);
+  return 0;
+}
+int hx_run_dss(const char* name, int tl, int rsmp) {
+  int ncomp, nb;
+  size_t es;
+  double* base = field_ptr(name, tl, ncomp, es, nb);
+  if (!base) return HX_ERR_STATE;
+  std::vector<FieldRef> f;
+  for (int b = 0; b < nb * ncomp; ++b) f.push_back({base + (size_t)b * NP2 * NLEV, es});
+  dss(f, rsmp != 0);
+  return 0;
+}
+int hx_num_elems(void) { return C().E; }
+int hx_qsize(void) { return C().Q; }
+int hx_enable_timing(int) { return 0; }
+int hx_kernel_stats(char*, int, long long*, double*, int) { return 0; }
+long long hx_launch_count(void) { return 0; }
+int hx_synchronize(void) { return 0; }
+int hx_oracle_threads(void) {
+#ifdef _OPENMP
+  return omp_get_max_threads();
+#else
+  return 1;
+#endif
+}
+
+}  // extern "C"

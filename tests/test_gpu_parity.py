@@ -1,0 +1,189 @@
+"""Parity of the CUDA library (libhxgpu.so) with the CPU oracle, phase by phase and for
+whole remap intervals, through the C ABI, on the same seeded inputs.
+
+FP64 plain form: every field within 1e-12 relative (max |gpu - oracle| / max |oracle|),
+the bar the benchmark spec sets for the FP64 step.  The DSS sums in the reference's fixed
+order in double, so it is compared bit for bit.
+"""
+import numpy as np
+import pytest
+
+import hxtest as H
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-12
+DT = 300.0
+
+
+@pytest.fixture
+def pair(gpu_path, oracle_path):
+    def make(ne=4, Q=4, precision=0, **kw):
+        kw.setdefault("nu", 1e16)
+        g = H.setup(gpu_path, ne, Q, precision=precision, **kw)
+        o = H.setup(oracle_path, ne, Q, **kw)
+        return g, o
+    return make
+
+
+def _assert_close(errs, tol=TOL):
+    bad = {k: v for k, v in errs.items() if not (v <= tol)}
+    assert not bad, f"relative errors above {tol}: {bad} (all: {errs})"
+
+
+@pytest.mark.parametrize("name,rsmp", [("T", 1), ("dp3d", 0), ("v", 1)])
+def test_dss_bitwise(pair, name, rsmp):
+    g, o = pair()
+    rng = np.random.default_rng(11)
+    f = rng.standard_normal(g.field_shape(name))
+    for L in (g, o):
+        L.set(name, 1, f)
+        L.call("hx_run_dss", name.encode(), 1, rsmp)
+    a, b = g.get(name, 1), o.get(name, 1)
+    assert np.array_equal(a, b), f"max diff {np.max(np.abs(a - b))}"
+
+
+def test_dss_of_constant_is_multiplicity(pair):
+    g, _ = pair()
+    m = H.mesh(4)
+    ones = np.ones(g.field_shape("T"))
+    g.set("T", 0, ones)
+    g.call("hx_run_dss", b"T", 0, 0)
+    out = g.get("T", 0)
+    # multiplicity of each GLL point: 1 interior, 2 edge, 3 or 4 at element corners
+    mult = np.ones((m.nelem, 16))
+    groups = H.M.dss_point_sources(m)
+    for pts in groups.values():
+        for (e, i, j) in pts:
+            mult[e, 4 * i + j] = len(pts)
+    assert np.array_equal(out, np.broadcast_to(mult.reshape(m.nelem, 1, 4, 4), out.shape))
+
+
+def test_caar_stage(pair):
+    g, o = pair()
+    for L in (g, o):
+        L.call("hx_run_caar_stage", 0, 1, 2, DT / 5.0, 0.25)
+    errs = H.compare(g, o, ("v", "T", "dp3d"), tl=2)
+    errs.update(H.compare(g, o, ("vn0", "omega_p", "phi")))
+    _assert_close(errs)
+
+
+def test_caar_stage_in_place(pair):
+    """n0 == np1 (stages 3-5 of the RK5 scheme read and write the same level)."""
+    g, o = pair()
+    for L in (g, o):
+        L.call("hx_run_caar_stage", 0, 1, 1, DT / 3.0, 0.0)
+    _assert_close(H.compare(g, o, ("v", "T", "dp3d"), tl=1))
+
+
+def test_rk5(pair):
+    g, o = pair()
+    for L in (g, o):
+        L.call("hx_run_rk5", 0, 1, 2, -1, DT, 1.0)
+    errs = {}
+    for tl in range(3):
+        for k, v in H.compare(g, o, ("v", "T", "dp3d"), tl=tl).items():
+            errs[f"{k}[{tl}]"] = v
+    errs.update(H.compare(g, o, ("vn0", "omega_p")))
+    _assert_close(errs)
+
+
+@pytest.mark.parametrize("nu_top", [2.5e5, 0.0])
+def test_hypervis(pair, nu_top):
+    g, o = pair(nu_top=nu_top)
+    for L in (g, o):
+        L.call("hx_run_hypervis", 2, DT, 1.0)
+    errs = H.compare(g, o, ("v", "T", "dp3d"), tl=2)
+    errs.update(H.compare(g, o, ("dpdiss_ave", "dpdiss_biharmonic")))
+    _assert_close(errs)
+
+
+@pytest.mark.parametrize("limiter", [8, 9])
+def test_prim_step_with_tracers(pair, limiter):
+    g, o = pair(limiter_option=limiter)
+    for L in (g, o):
+        L.call("hx_run_prim_step", DT)
+    errs = {}
+    for tl in range(3):
+        for k, v in H.compare(g, o, ("v", "T", "dp3d"), tl=tl).items():
+            errs[f"{k}[{tl}]"] = v
+    for tl in range(2):
+        errs[f"Qdp[{tl}]"] = H.rel_err(g.get("Qdp", tl), o.get("Qdp", tl))
+    errs.update(H.compare(g, o, ("vn0", "omega_p", "divdp", "divdp_proj", "eta_dot_dpdn")))
+    _assert_close(errs)
+
+
+@pytest.mark.parametrize("rhs", [0.0, 1.0, 2.0])
+def test_euler_step_stage(pair, rhs):
+    g, o = pair()
+    for L in (g, o):
+        L.call("hx_run_rk5", 0, 1, 2, -1, DT, 1.0)
+        L.call("hx_run_tracers_rk2", DT)            # fills vn0 / divdp state
+        L.call("hx_run_euler_step", 1, 0, DT / 2.0, rhs, int(rhs) % 3)
+    errs = {f"Qdp[{tl}]": H.rel_err(g.get("Qdp", tl), o.get("Qdp", tl)) for tl in range(2)}
+    errs.update(H.compare(g, o, ("omega_p", "divdp_proj", "eta_dot_dpdn")))
+    _assert_close(errs)
+
+
+@pytest.mark.parametrize("remap_alg", [1, 2])
+def test_remap(pair, remap_alg):
+    g, o = pair(remap_alg=remap_alg)
+    for L in (g, o):
+        L.call("hx_run_rk5", 0, 1, 2, -1, DT, 1.0)
+        L.call("hx_run_remap", 2, 0, DT)
+    errs = H.compare(g, o, ("v", "T"), tl=2)
+    errs["Qdp[0]"] = H.rel_err(g.get("Qdp", 0), o.get("Qdp", 0))
+    errs["ps_v"] = H.rel_err(g.get("ps_v", 2), o.get("ps_v", 2))
+    _assert_close(errs)
+
+
+@pytest.mark.parametrize("rsplit,nsub", [(1, 1), (3, 2)])
+def test_subcycle(pair, rsplit, nsub):
+    """prim_run_subcycle_c end to end, results pushed through cxx_push_results_to_f90."""
+    g, o = pair(rsplit=rsplit)
+    for _ in range(nsub):
+        tg = g.run_subcycle(DT)
+        to = o.run_subcycle(DT)
+        assert tg == to
+    rg, ro = g.push_results(), o.push_results()
+    errs = {k: H.rel_err(rg[k], ro[k]) for k in rg}
+    _assert_close(errs)
+
+
+def test_mass_conservation_gpu(pair):
+    g, _ = pair(rsplit=3)
+    m = H.mesh(4)
+    st = H.state(4, 4)
+    g.run_subcycle(DT)
+    r = g.push_results()
+    n0 = g.tl[1]
+    ps0 = np.sum(st["ps_v"][:, 1] * m.spheremp)
+    ps1 = np.sum(r["ps_v"][:, n0] * m.spheremp)
+    assert abs(ps1 - ps0) / ps0 < 1e-13
+    q0 = np.sum(st["Qdp"][:, 0] * m.spheremp[:, None, None])
+    # tracer mass of the level holding the newest Qdp (np1_qdp of the last step)
+    qa = [np.sum(r["Qdp"][:, k] * m.spheremp[:, None, None]) for k in range(2)]
+    assert min(abs(x - q0) / q0 for x in qa) < 1e-12
+
+
+def test_mixed_precision_close(pair):
+    """Mixed form against the FP64 oracle after one remap interval (loose bound; the
+    per-day error is reported by the benchmark)."""
+    g, o = pair(precision=1, rsplit=3)
+    g.run_subcycle(DT)
+    o.run_subcycle(DT)
+    rg, ro = g.push_results(), o.push_results()
+    errs = {k: H.rel_err(rg[k], ro[k]) for k in ("T", "dp3d", "v", "Qdp", "ps_v")}
+    assert errs["T"] < 1e-5 and errs["dp3d"] < 1e-5, errs
+    assert errs["v"] < 1e-3 and errs["Qdp"] < 1e-4, errs
+
+
+def test_negative_thickness_reports_101(gpu_path):
+    """Host-side fault injection: a negative layer thickness in the input makes the
+    remap report the reference's error code 101 instead of continuing."""
+    L = H.setup(gpu_path, 4, 2, rsplit=1)
+    dp = L.get("dp3d", 1)
+    dp[0, 40, 1, 1] = -5.0e4
+    L.set("dp3d", 1, dp)
+    rc = L.lib.hx_run_remap(1, 0, DT)
+    assert rc == 101
