@@ -223,7 +223,7 @@ struct BackendT : Backend {
     *dpdiss_bih = 0, *vn0 = 0;
   // scratch
   R *caar_out = 0, *bufA = 0, *bufB = 0, *vstar = 0, *dpdissk = 0, *fscr = 0, *qtens = 0, *qscr = 0;
-  double *qlim = 0, *qlim_tmp = 0, *dp0 = 0, *staging = 0;
+  double *qlim = 0, *qlim_tmp = 0, *dp0 = 0, *staging = 0, *rsp_d = 0;
   R* gen_scr = 0;
   int *tab_cnt = 0, *tab_src = 0, *nbr = 0, *invalid = 0;
   int* h_invalid = nullptr;
@@ -233,7 +233,7 @@ struct BackendT : Backend {
     void* ptrs[] = {D, Dinv, metinv, metdet, spheremp, rspheremp, mp, fcor, phis, tensorvisc, vec_sph2cart,
                     v, T, dp, ps_v, qdp, Qc, phi, omega_p, eta, derived_dp, divdp, divdp_proj, dpdiss_ave,
                     dpdiss_bih, vn0, caar_out, bufA, bufB, vstar, dpdissk, fscr, qtens, qscr, qlim, qlim_tmp,
-                    dp0, staging, gen_scr, tab_cnt, tab_src, nbr, invalid};
+                    dp0, staging, rsp_d, gen_scr, tab_cnt, tab_src, nbr, invalid};
     for (void* p : ptrs)
       if (p) cudaFree(p);
     if (h_invalid) cudaFreeHost(h_invalid);
@@ -545,10 +545,9 @@ struct BackendT : Backend {
       std::vector<double> h;
       if (rs) {
         // rspheremp in double
-        static double* rsd = nullptr;
-        if (!rsd) rsd = dalloc<double>((size_t)E * 16);
-        k_r2d<R><<<(E * 16 + 255) / 256, 256, 0, g_stream>>>(rspheremp, rsd, (size_t)E * 16);
-        rd = rsd;
+        if (!rsp_d) rsp_d = dalloc<double>((size_t)E * 16);
+        k_r2d<R><<<(E * 16 + 255) / 256, 256, 0, g_stream>>>(rspheremp, rsp_d, (size_t)E * 16);
+        rd = rsp_d;
       }
       launch_dss_inplace_d(E, Q, qdp + (size_t)tl * Q * NLEV * 16, NLEV * 16, (long long)QTL * Q * NLEV * 16, 16, scr, rd, table(), g_stream);
     } else return HX_ERR_STATE;
