@@ -1,0 +1,398 @@
+"""Benchmark of the GB300 preqx dycore step: simulated years per day (SYPD) at ne30L72.
+
+Workload (the FP64 plain-form configuration): equiangular cubed sphere ne=30 (5400
+elements), np=4, 72 levels, 10 tracers, dt=300 s, rsplit=3 (remap every 3 dynamics
+steps), hyperviscosity nu=1e15 with 3 subcycles, nu_top=2.5e5, limiter 8, PPM
+mirrored remap; seeded smooth synthetic initial state (spherical harmonics of degree
+<= 6).  One benchmark step = one ``prim_run_subcycle_c`` call = one remap interval =
+3 dynamics steps = 900 simulated seconds.  SYPD = simulated years per wall-clock day.
+
+* ``value``: device time of K steps with the state resident in HBM (CUDA events on the
+  library's stream); the working set (~1.9 GB) is far larger than L2, so no flush.
+* ``e2e``: the same through the C ABI with host buffers, each step copying the state in
+  (``init_elements_states_c``) and the results out (``cxx_push_results_to_f90``) from
+  pinned host memory, wall clock.
+* ``mixed``: the mixed-precision form timed the same way, with its error against the
+  FP64 form after ``--error-days`` simulated days.
+* ``roofline``: the kernel with the largest share of device time; algorithmic bytes per
+  launch from the field-pass model below, divided by its CUDA-event launch time.
+* ``cpu_baseline``: the C++/OpenMP oracle (a restatement of the reference's algorithm;
+  the reference itself needs Kokkos and cannot be built here) on all host cores, on a
+  bounded sample of the same workload.
+
+``--impl reference`` times that CPU implementation alone and prints its own line.
+Multi-GPU: the step does not shard here (one GPU per box), so N>1 runs N independent
+replicas, one per rank, and reports their aggregate.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+NE, QSIZE, DT, RSPLIT, HSUB, NU = 30, 10, 300.0, 3, 3, 1e15
+SIM_SECONDS_PER_STEP = DT * RSPLIT
+MEASURED_PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
+FALLBACK_HBM_GBS = 6800.0
+
+
+def sypd(steps: int, seconds: float) -> float:
+    return steps * SIM_SECONDS_PER_STEP / (365.0 * seconds)
+
+
+# ---- algorithmic bytes per remap interval, per kernel -----------------------------------
+def kernel_bytes(E: int, Q: int, rsize: int, rsplit: int = RSPLIT, hsub: int = HSUB,
+                 nu_p_positive: bool = True):
+    """(launches, bytes) per remap interval for every kernel: each launch reads each
+    input field once and writes each output field once (one field = E*16*72 values;
+    dynamics fields in the form's type, tracer mass in double)."""
+    F = E * 16 * 72 * rsize
+    Fd = E * 16 * 72 * 8
+    qlim = E * Q * 2 * 72 * 8
+    d = {}
+
+    def add(name, launches, nbytes):
+        a, b = d.get(name, (0, 0))
+        d[name] = (a + launches, b + nbytes)
+
+    for _ in range(rsplit):
+        add("prim_step_init", 1, 8 * F)
+        # caar: stage 1 (19F: n0 4, nm1 4, vn0 4, omega_p 2, phi 1, out 4), stages 2-4
+        # (13F: no vn0/omega_p accumulation), stage 5 (27F: + RK combine 8F)
+        add("caar_stage", 5, (19 + 13 * 3 + 27) * F)
+        add("dss_caar", 5, 5 * 8 * F)
+        add("hv_laplace1", hsub, hsub * 8 * F)
+        add("hv_laplace2", hsub, hsub * 13 * F)
+        add("hv_dss_update", hsub, hsub * 11 * F)
+        if Q > 0:
+            add("precompute_divdp", 1, 4 * F)
+            for stage in range(3):
+                last = stage == 2
+                add("euler_qminmax", 1, Q * Fd + 2 * F + qlim + (Q * F if last else 0)
+                    + (qlim if stage == 1 else 0))
+                if stage != 1:
+                    add("euler_minmax_nbr", 1, 2 * qlim)
+                if last:
+                    add("euler_bih_pre", 1, 2 * Q * F + F)
+                    add("euler_bih_post", 1, 2 * Q * F)
+                add("euler_aal_setup", 1, 10 * F + (F if (last and nu_p_positive) else 0))
+                add("euler_aal_tracer", 1, Q * Fd + Q * F + 3 * F + (Q * F if last else 0) + 2 * qlim)
+                add("euler_dss_qdp", 1, Q * F + Q * Fd + (Q * Fd if last else 0))
+                add("euler_dss_fvar", 1, 2 * F)
+    add("dp3d_from_ps", 1, F)
+    add("ppm_remap", 1, 7 * F + 2 * Q * Fd)
+    add("update_q", 1, 2 * Q * Fd)
+    return d
+
+
+# ---- clocks sampled during the timed region ------------------------------------------------
+class ClockSampler:
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self):
+        self.samples = []
+        self._stop = threading.Event()
+        self._th = None
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", "-i", os.environ.get("HX_SMI_INDEX", "0"),
+                                      f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits"],
+                                     capture_output=True, text=True, timeout=5).stdout.strip()
+                if out:
+                    self.samples.append([x.strip() for x in out.split(",")])
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._th = threading.Thread(target=self._run, daemon=True)
+        self._th.start()
+        return self
+
+    def __exit__(self, *a):
+        self._stop.set()
+        if self._th:
+            self._th.join(timeout=10)
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4)
+                          if len(s) > 3 + i and s[3 + i].lower().startswith("active")})
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(self.samples)}
+
+
+def _peaks():
+    try:
+        with open(MEASURED_PEAKS) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+def _setup(lib_path, precision, mesh, hv, state, qsize=QSIZE):
+    from hommexx_gb300 import abi
+    L = abi.HxLibrary(lib_path)
+    p = abi.SimParams(qsize=qsize, nu=NU, rsplit=RSPLIT, hypervis_subcycle=HSUB, nu_top=2.5e5,
+                      limiter_option=8, remap_alg=1)
+    L.init(mesh, hv, p, state, precision=precision, abort_on_error=True)
+    return L
+
+
+def _device_time(L, steps):
+    L.lib.hx_timer_start()
+    for _ in range(steps):
+        L.run_subcycle(DT)
+    import ctypes
+    ms = ctypes.c_double(0)
+    L.lib.hx_timer_stop(ctypes.byref(ms))
+    return ms.value / 1e3
+
+
+def run_gpu(args, rank, world):
+    from hommexx_gb300 import build as B, mesh as M, state as S
+    lib_path = B.build()
+    mesh = M.build_mesh(NE)
+    hv = S.hybrid_coordinate()
+    state = S.initial_state(mesh, QSIZE, hv)
+    out = {}
+    import ctypes
+    for precision, tag in ((0, "fp64"), (1, "mixed")):
+        if tag == "mixed" and args.no_mixed:
+            continue
+        L = _setup(lib_path, precision, mesh, hv, state)
+        for _ in range(args.warmup):
+            L.run_subcycle(DT)
+        L.lib.hx_synchronize()
+        _barrier(world)
+        launches0 = L.lib.hx_launch_count()
+        L.lib.hx_enable_timing(1)
+        with ClockSampler() as cs:
+            t = _device_time(L, args.steps)
+        L.lib.hx_enable_timing(0)
+        launches = L.lib.hx_launch_count() - launches0
+        stats = L.kernel_stats()
+        t = _max_over_ranks(t, world)
+        # end-to-end through the C ABI with pinned host buffers
+        res = L.push_results()
+        host_in = {k: np.ascontiguousarray(state[k]) for k in ("v", "T", "dp3d", "Qdp", "ps_v")}
+        for a in list(host_in.values()) + list(res.values()):
+            L.lib.hx_host_register(ctypes.c_void_p(a.ctypes.data), ctypes.c_size_t(a.nbytes))
+        h2d = sum(a.nbytes for a in host_in.values())
+        d2h = sum(a.nbytes for a in res.values())
+        L.set_state(host_in)
+        L.run_subcycle(DT)
+        L.push_results(res)
+        _barrier(world)
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            L.set_state(host_in)
+            L.run_subcycle(DT)
+            L.push_results(res)
+        te = time.perf_counter() - t0
+        te = _max_over_ranks(te, world)
+        for a in list(host_in.values()) + list(res.values()):
+            L.lib.hx_host_unregister(ctypes.c_void_p(a.ctypes.data))
+        out[tag] = dict(t=t, te=te, launches=launches, stats=stats, clocks=cs.summary(),
+                        h2d=h2d, d2h=d2h)
+        if tag == "fp64":
+            out["fp64_state_after"] = None
+        L.finalize()
+    # error of the mixed form against the FP64 form after --error-days simulated days
+    if not args.no_mixed and args.error_days > 0 and rank == 0:
+        nsub = int(round(args.error_days * 86400.0 / SIM_SECONDS_PER_STEP))
+        finals = {}
+        for precision in (0, 1):
+            L = _setup(lib_path, precision, mesh, hv, state)
+            for _ in range(nsub):
+                L.run_subcycle(DT)
+            finals[precision] = L.push_results()
+            L.finalize()
+        a, b = finals[1], finals[0]
+        err = {}
+        for k, lab in (("v", "uv"), ("T", "T"), ("dp3d", "dp3d"), ("Qdp", "Qdp"), ("ps_v", "ps")):
+            err[lab] = float(np.max(np.abs(a[k] - b[k])) / np.max(np.abs(b[k])))
+        sm = mesh.spheremp
+        m0 = float(np.sum(state["ps_v"][:, 1] * sm))
+        out["mixed_error"] = dict(days=args.error_days, subcycles=nsub, rel_err=err,
+                                  mass_drift_fp64=float(np.sum(b["ps_v"][:, 1] * sm) / m0 - 1.0),
+                                  mass_drift_mixed=float(np.sum(a["ps_v"][:, 1] * sm) / m0 - 1.0))
+    return out, mesh
+
+
+def _barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def _max_over_ranks(x, world):
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def roofline(stats, E, Q, rsize, steps):
+    model = kernel_bytes(E, Q, rsize)
+    total = sum(ms for _, _, ms in stats) or 1.0
+    rows = []
+    for name, launches, ms in stats:
+        nb = model.get(name)
+        per_launch = nb[1] / nb[0] if nb else None
+        rows.append(dict(kernel=name, launches=launches, total_ms=ms, share=ms / total,
+                         bytes_per_launch=per_launch,
+                         gbs=(per_launch / (ms / launches * 1e-3) / 1e9) if (nb and launches) else None))
+    rows.sort(key=lambda r: -r["total_ms"])
+    return rows
+
+
+def _oracle(mesh=None, state=None):
+    from hommexx_gb300 import mesh as M, state as S
+    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle")], check=True)
+    mesh = mesh or M.build_mesh(NE)
+    hv = S.hybrid_coordinate()
+    state = state or S.initial_state(mesh, QSIZE, hv)
+    L = _setup(os.path.join(ROOT, "oracle", "liboracle.so"), 0, mesh, hv, state)
+    L.lib.hx_oracle_threads.restype = int
+    return L
+
+
+def cpu_baseline(seconds_budget: float = 20.0, L=None):
+    """Time the oracle on the machine's host cores on a bounded sample: ne30 with the same
+    parameters for as many remap intervals as fit the budget (at least one)."""
+    own = L is None
+    L = L or _oracle()
+    threads = L.lib.hx_oracle_threads()
+    t0 = time.perf_counter()
+    n = 0
+    while True:
+        L.run_subcycle(DT)
+        n += 1
+        if time.perf_counter() - t0 > seconds_budget / 2 or n >= 4:
+            break
+    t = time.perf_counter() - t0
+    if own:
+        L.finalize()
+    return dict(value=sypd(n, t), unit="SYPD", cores=threads, kind="port",
+                sample=f"ne30 L72 q10, {n} remap interval(s) of 3 x 300 s steps, "
+                       f"{t:.1f} s on {threads} OpenMP threads")
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
+    ap.add_argument("--no-mixed", action="store_true")
+    ap.add_argument("--error-days", type=float, default=1.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        os.environ["CUDA_VISIBLE_DEVICES"] = str(local_rank)
+        os.environ["HX_SMI_INDEX"] = str(local_rank)
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+
+    config = {"workload": "preqx step ne30 L72 np4 qsize10, dt 300 s, rsplit 3, hv nu 1e15 x3 subcycles, "
+                          "limiter 8, PPM mirrored remap",
+              "elements": 6 * NE * NE, "nlev": 72, "qsize": QSIZE, "step": "one remap interval "
+              "(prim_run_subcycle_c) = 3 x 300 s", "l2": "working set 1.9 GB >> 129 MB L2, no flush",
+              "parallelism": f"replicas x{world}" if world > 1 else "single GPU"}
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        L = _oracle()
+        threads = L.lib.hx_oracle_threads()
+        times = []
+        for i in range(args.warmup + args.steps):
+            t0 = time.perf_counter()
+            L.run_subcycle(DT)
+            if i >= args.warmup:
+                times.append(time.perf_counter() - t0)
+        L.finalize()
+        v = sypd(len(times), float(np.sum(times)))
+        per = [dict(value=v, unit="SYPD", cores=threads, kind="port",
+                    sample=f"ne30 L72 q10, one remap interval (3 x 300 s) per step, "
+                           f"{np.mean(times):.2f} s per step on {threads} OpenMP threads")]
+        line = {"metric": "ne30L72 SYPD (FP64 preqx step)", "value": v, "unit": "SYPD",
+                "impl": "reference", "n_gpus": 0, "steps": args.steps, "warmup": args.warmup,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic seeded spherical-harmonic state", "config": config,
+                "cpu_baseline": dict(per[-1], value=v),
+                "e2e": {"value": v, "unit": "SYPD", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+
+    out, mesh = run_gpu(args, rank, world)
+    if rank != 0:
+        return
+    E = mesh.nelem
+    f = out["fp64"]
+    rows = roofline(f["stats"], E, QSIZE, 8, args.steps)
+    peak, peak_kind = _peaks()
+    top = rows[0]
+    achieved = top["gbs"] or 0.0
+    value = sypd(args.steps, f["t"]) * world
+    line = {
+        "metric": "ne30L72 SYPD (FP64 preqx step)", "value": value, "unit": "SYPD",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": f["t"] / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic seeded spherical-harmonic state",
+        "config": config,
+        "e2e": {"value": sypd(args.steps, f["te"]) * world, "unit": "SYPD",
+                "h2d_bytes_per_step": f["h2d"], "d2h_bytes_per_step": f["d2h"]},
+        "gpu_launches": f["launches"],
+        "clocks": f["clocks"],
+        "roofline": {"bound": "hbm", "kernel": top["kernel"], "achieved": achieved, "peak": peak,
+                     "unit": "GB/s", "frac": achieved / peak, "traffic": None,
+                     "peak_source": peak_kind},
+        "kernels": [{k: (round(v, 4) if isinstance(v, float) else v) for k, v in r.items()} for r in rows],
+    }
+    if "mixed" in out:
+        mx = out["mixed"]
+        mrows = roofline(mx["stats"], E, QSIZE, 4, args.steps)
+        line["mixed"] = {"value": sypd(args.steps, mx["t"]) * world, "unit": "SYPD",
+                         "speedup_vs_fp64": f["t"] / mx["t"],
+                         "e2e": sypd(args.steps, mx["te"]) * world,
+                         "ms_per_step": mx["t"] / args.steps * 1e3,
+                         "top_kernel": {k: mrows[0][k] for k in ("kernel", "share", "gbs")},
+                         "clocks": mx["clocks"]}
+        if "mixed_error" in out:
+            line["mixed"]["error_vs_fp64"] = out["mixed_error"]
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline()
+    print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

@@ -419,21 +419,23 @@ struct BackendT : Backend {
   }
 
   // EulerStepFunctorImpl::euler_step; dssopt 0 = ETA, 1 = OMEGA, 2 = DIV_VDP_AVE
+  // tavg >= 0: the stage's DSS also applies qdp_time_avg against tracer level tavg.
   void euler_step(int np1_qdp, int n0_qdp, double dt, double rhs, int dssopt, int tavg) override {
     EulerArgs<R> a = euler_args();
     a.np1_qdp = np1_qdp; a.n0_qdp = n0_qdp; a.dt = dt; a.rhs_multiplier = rhs;
+    a.avg_n0_qdp = tavg;
     a.f_dss = dssopt == 0 ? eta : dssopt == 1 ? omega_p : divdp_proj;
-    launch_euler_step<R>(a, E, tavg, g_stream);
+    launch_euler_step<R>(a, E, tavg >= 0 ? 1 : 0, g_stream);
     post("euler_step");
   }
 
   void tracers_rk2(double dt) override {
     s.tl.update_tracers_levels(s.prm.qsplit);
     precompute_divdp();
-    euler_step(s.tl.np1_qdp, s.tl.n0_qdp, dt / 2.0, 0.0, 2, 0);
-    euler_step(s.tl.np1_qdp, s.tl.np1_qdp, dt / 2.0, 1.0, 0, 0);
+    euler_step(s.tl.np1_qdp, s.tl.n0_qdp, dt / 2.0, 0.0, 2, -1);
+    euler_step(s.tl.np1_qdp, s.tl.np1_qdp, dt / 2.0, 1.0, 0, -1);
     // the last stage's DSS applies qdp_time_avg (EulerStepFunctorImpl.hpp:379-403)
-    euler_step(s.tl.np1_qdp, s.tl.np1_qdp, dt / 2.0, 2.0, 1, 1);
+    euler_step(s.tl.np1_qdp, s.tl.np1_qdp, dt / 2.0, 2.0, 1, s.tl.n0_qdp);
   }
 
   void launch_remap(int np1, int np1_qdp) {
@@ -815,7 +817,7 @@ int hx_run_hypervis(int np1, double dt, double w) {
 int hx_run_euler_step(int np1_qdp, int n0_qdp, double dt, double rhs, int dssopt) {
   return run([&] {
     if (dssopt < 0 || dssopt > 2) fail(11, "dss_opt must be 0, 1 or 2");
-    B().euler_step(np1_qdp, n0_qdp, dt, rhs, dssopt, 0);
+    B().euler_step(np1_qdp, n0_qdp, dt, rhs, dssopt, -1);
     ck(cudaStreamSynchronize(g_stream), "sync");
   });
 }
@@ -867,6 +869,38 @@ long long hx_launch_count(void) { return g_tim.launches; }
 
 int hx_synchronize(void) {
   return run([] { if (g_stream) ck(cudaStreamSynchronize(g_stream), "cudaStreamSynchronize"); });
+}
+
+static cudaEvent_t g_t0 = nullptr, g_t1 = nullptr;
+
+int hx_timer_start(void) {
+  return run([] {
+    if (!g_stream) fail(HX_ERR_STATE, "no session");
+    if (!g_t0) {
+      ck(cudaEventCreate(&g_t0), "cudaEventCreate");
+      ck(cudaEventCreate(&g_t1), "cudaEventCreate");
+    }
+    ck(cudaEventRecord(g_t0, g_stream), "cudaEventRecord");
+  });
+}
+
+int hx_timer_stop(double* ms) {
+  return run([&] {
+    if (!g_t0) fail(HX_ERR_STATE, "hx_timer_start was not called");
+    ck(cudaEventRecord(g_t1, g_stream), "cudaEventRecord");
+    ck(cudaEventSynchronize(g_t1), "cudaEventSynchronize");
+    float f = 0.f;
+    ck(cudaEventElapsedTime(&f, g_t0, g_t1), "cudaEventElapsedTime");
+    *ms = f;
+  });
+}
+
+int hx_host_register(void* ptr, size_t bytes) {
+  return run([&] { ck(cudaHostRegister(ptr, bytes, cudaHostRegisterDefault), "cudaHostRegister"); });
+}
+
+int hx_host_unregister(void* ptr) {
+  return run([&] { ck(cudaHostUnregister(ptr), "cudaHostUnregister"); });
 }
 
 }  // extern "C"

@@ -258,9 +258,11 @@ __global__ void __launch_bounds__(LG * 16) k_caar(CaarArgs<R> a) {
     const R u = a.v[vN0 + l * 32 + p], w = a.v[vN0 + l * 32 + 16 + p];
     const R tt = a.T[sN0 + l * 16 + p], d = a.dp[sN0 + l * 16 + p];
     const R vd0 = u * d, vd1 = w * d;
-    const size_t iv = ((size_t)e * NLEV + l) * 32 + p;
-    a.vn0[iv] += eta * vd0;
-    a.vn0[iv + 16] += eta * vd1;
+    if (a.eta_ave_w != 0.0) {  // stages 2-4 accumulate nothing (eta_ave_w = 0)
+      const size_t iv = ((size_t)e * NLEV + l) * 32 + p;
+      a.vn0[iv] += eta * vd0;
+      a.vn0[iv + 16] += eta * vd1;
+    }
     const R div = divergence_sphere(t, m, vd0, vd1);
     R tv = tt;
     if (a.n0_qdp >= 0) {
@@ -342,7 +344,7 @@ __global__ void __launch_bounds__(LG * 16) k_caar(CaarArgs<R> a) {
     const R div = (R)s_div[l * SROW + p];
     const R vgp = u * gp0 + w * gp1;
     const R omega = (vgp - ((R)s_om[l * SROW + p] + R(0.5) * div)) / pr;
-    a.omega_p[((size_t)e * NLEV + l) * 16 + p] += eta * omega;
+    if (a.eta_ave_w != 0.0) a.omega_p[((size_t)e * NLEV + l) * 16 + p] += eta * omega;
     // time level "nm1" (RK combine of stage 5 fused here)
     R tm = a.T[sM + l * 16 + p], dm = a.dp[sM + l * 16 + p];
     R vm0 = a.v[vM + l * 32 + p], vm1 = a.v[vM + l * 32 + 16 + p];
@@ -861,7 +863,7 @@ __global__ void k_dss_tracers(EulerArgs<R> a, int E, int time_avg) {
   const double v = dss_gather(a.qscr + (size_t)q * NLEV * 16, (long long)a.Q * NLEV * 16, 16, e, l, p, a.dss) * rs;
   const size_t d = ((((size_t)e * QTL + a.np1_qdp) * a.Q + q) * NLEV + l) * 16 + p;
   if (time_avg) {
-    const size_t s0 = ((((size_t)e * QTL + a.n0_qdp) * a.Q + q) * NLEV + l) * 16 + p;
+    const size_t s0 = ((((size_t)e * QTL + a.avg_n0_qdp) * a.Q + q) * NLEV + l) * 16 + p;
     a.qdp[d] = (a.qdp[s0] + 2.0 * v) / 3.0;
   } else {
     a.qdp[d] = v;

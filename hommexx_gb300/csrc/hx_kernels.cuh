@@ -69,6 +69,7 @@ struct EulerArgs {
   const double* dp0;  // [72] device
   const int* conn;    // [E][8] neighbour element per connection slot, -1 if missing
   int Q, n0_qdp, np1_qdp, limiter_option, consthv;
+  int avg_n0_qdp;  // level averaged with np1 when the last RK2 stage fuses qdp_time_avg
   double dt, rhs_multiplier, rhs_viss, nu_p, nu_q;
 };
 

@@ -168,6 +168,13 @@ int hx_kernel_stats(char* names, int name_len, long long* launches, double* tota
 long long hx_launch_count(void);
 /* Block the host until all device work of the session has finished. */
 int hx_synchronize(void);
+/* CUDA-event timer on the library's stream: start records an event, stop records a
+ * second one, waits for it and returns the elapsed device time in *ms. */
+int hx_timer_start(void);
+int hx_timer_stop(double* ms);
+/* Page-lock (pin) host memory so init/push copies run at full link bandwidth. */
+int hx_host_register(void* ptr, size_t bytes);
+int hx_host_unregister(void* ptr);
 
 #ifdef __cplusplus
 }

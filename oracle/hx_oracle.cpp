@@ -1611,6 +1611,13 @@ int hx_enable_timing(int) { return 0; }
 int hx_kernel_stats(char*, int, long long*, double*, int) { return 0; }
 long long hx_launch_count(void) { return 0; }
 int hx_synchronize(void) { return 0; }
+int hx_timer_start(void) { return 0; }
+int hx_timer_stop(double* ms) {
+  *ms = 0.0;
+  return 0;
+}
+int hx_host_register(void*, size_t) { return 0; }
+int hx_host_unregister(void*) { return 0; }
 int hx_oracle_threads(void) {
 #ifdef _OPENMP
   return omp_get_max_threads();
