@@ -223,7 +223,7 @@ struct BackendT : Backend {
     *dpdiss_bih = 0, *vn0 = 0;
   // scratch
   R *caar_out = 0, *bufA = 0, *bufB = 0, *vstar = 0, *dpdissk = 0, *fscr = 0, *qtens = 0, *qscr = 0;
-  double *qlim = 0, *qlim_tmp = 0, *dp0 = 0, *staging = 0, *rsp_d = 0;
+  double *qlim = 0, *qlim_tmp = 0, *dp0 = 0, *staging = 0, *rsp_d = 0, *rsp_noalloc = 0;
   R* gen_scr = 0;
   int *tab_cnt = 0, *tab_src = 0, *nbr = 0, *invalid = 0;
   int* h_invalid = nullptr;
@@ -233,7 +233,7 @@ struct BackendT : Backend {
     void* ptrs[] = {D, Dinv, metinv, metdet, spheremp, rspheremp, mp, fcor, phis, tensorvisc, vec_sph2cart,
                     v, T, dp, ps_v, qdp, Qc, phi, omega_p, eta, derived_dp, divdp, divdp_proj, dpdiss_ave,
                     dpdiss_bih, vn0, caar_out, bufA, bufB, vstar, dpdissk, fscr, qtens, qscr, qlim, qlim_tmp,
-                    dp0, staging, rsp_d, gen_scr, tab_cnt, tab_src, nbr, invalid};
+                    dp0, staging, rsp_d, rsp_noalloc, gen_scr, tab_cnt, tab_src, nbr, invalid};
     for (void* p : ptrs)
       if (p) cudaFree(p);
     if (h_invalid) cudaFreeHost(h_invalid);
@@ -301,6 +301,8 @@ struct BackendT : Backend {
     to_dev(metdet, a[6], (size_t)E * 16);
     to_dev(metinv, a[7], (size_t)E * 64);
     to_dev(phis, a[8], (size_t)E * 16);
+    if (!rsp_noalloc) rsp_noalloc = dalloc<double>((size_t)E * 16);
+    ck(cudaMemcpyAsync(rsp_noalloc, a[5], (size_t)E * 16 * sizeof(double), cudaMemcpyHostToDevice, g_stream), "H2D");
     if (!consthv) {
       to_dev(tensorvisc, a[9], (size_t)E * 64);
       to_dev(vec_sph2cart, a[10], (size_t)E * 96);
@@ -340,6 +342,12 @@ struct BackendT : Backend {
     return m;
   }
   DssTable table() const { return DssTable{tab_cnt, tab_src}; }
+  bool dss_view(const int** c, const int** sr, const double** r) const {
+    *c = tab_cnt;
+    *sr = tab_src;
+    *r = rsp_noalloc;
+    return tab_cnt != nullptr && rsp_noalloc != nullptr;
+  }
 
   void set_tables(const std::vector<int>& cnt, const std::vector<int>& src, const std::vector<int>& nb) {
     if (!tab_cnt) {
@@ -591,6 +599,19 @@ Backend& B() {
 }
 
 }  // namespace
+
+// Session view used by the no-allocation DSS entry point (hx_noalloc.cu).
+bool session_dss_view(int* E, const int** cnt, const int** src, const double** rsp,
+                      cudaStream_t* stream) {
+  if (!g_s || !g_s->be || !g_stream) return false;
+  const bool ok = g_s->precision == 0
+                      ? static_cast<BackendT<double>&>(*g_s->be).dss_view(cnt, src, rsp)
+                      : static_cast<BackendT<float>&>(*g_s->be).dss_view(cnt, src, rsp);
+  *E = g_s->E;
+  *stream = g_stream;
+  return ok;
+}
+
 }  // namespace hx
 
 using namespace hx;

@@ -172,6 +172,18 @@ int hx_synchronize(void);
  * second one, waits for it and returns the elapsed device time in *ms. */
 int hx_timer_start(void);
 int hx_timer_stop(double* ms);
+/* No counterpart in the reference.  DSS of one caller-owned device field
+ * [nelem][nlev][np*np] (in and out may alias) without allocating device memory, for
+ * callers that cannot call cudaMalloc when they need it (a host model that reserves
+ * its GPU memory budget up front, code where allocation is forbidden).  Scratch is a
+ * fixed 4 MiB __device__ array (at most 455 elements of 72 levels); larger fields are
+ * rejected with code 13.  The first call on a device looks the array up and must come
+ * before any stream capture on that device.  Calls share the array, so calls that
+ * overlap on the GPU race; the array keeps the last call's contents and needs no
+ * clearing because every call overwrites what it reads.  Enqueued on the session's
+ * stream; returns 0, 13 or HX_ERR_STATE/HX_ERR_CUDA. */
+int hx_dss_noalloc(const double* in, double* out, int nelem, int apply_rspheremp);
+
 /* Page-lock (pin) host memory so init/push copies run at full link bandwidth. */
 int hx_host_register(void* ptr, size_t bytes);
 int hx_host_unregister(void* ptr);
