@@ -198,33 +198,23 @@ void build_tables(const std::vector<int>& conn, int E, std::vector<int>& cnt, st
 }
 
 template <typename R>
-__global__ void k_d2r(const double* __restrict__ a, R* b, size_t n) {
-  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) b[i] = (R)a[i];
-}
-template <typename R>
-__global__ void k_r2d(const R* __restrict__ a, double* b, size_t n) {
-  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) b[i] = (double)a[i];
-}
-
-template <typename R>
 struct BackendT : Backend {
   Session& s;
   explicit BackendT(Session& ss) : s(ss) {}
   int E = 0, Q = 0;
-  // metric
+  // metric in the arithmetic type R (operators) plus double spheremp/rspheremp
   R *D = 0, *Dinv = 0, *metinv = 0, *metdet = 0, *spheremp = 0, *rspheremp = 0, *mp = 0, *fcor = 0,
     *phis = 0, *tensorvisc = 0, *vec_sph2cart = 0;
-  // state
-  R *v = 0, *T = 0, *dp = 0;
+  double *sp_d = 0;
+  // state (all fields are stored in double in both forms)
+  double *v = 0, *T = 0, *dp = 0;
   double *ps_v = 0, *qdp = 0, *Qc = 0;
-  R *phi = 0, *omega_p = 0, *eta = 0, *derived_dp = 0, *divdp = 0, *divdp_proj = 0, *dpdiss_ave = 0,
-    *dpdiss_bih = 0, *vn0 = 0;
+  double *phi = 0, *omega_p = 0, *eta = 0, *derived_dp = 0, *divdp = 0, *divdp_proj = 0,
+         *dpdiss_ave = 0, *dpdiss_bih = 0, *vn0 = 0;
   // scratch
-  R *caar_out = 0, *bufA = 0, *bufB = 0, *vstar = 0, *dpdissk = 0, *fscr = 0, *qtens = 0, *qscr = 0;
+  double *caar_out = 0, *bufA = 0, *bufB = 0, *vstar = 0, *dpdissk = 0, *fscr = 0, *qtens = 0, *qscr = 0;
   double *qlim = 0, *qlim_tmp = 0, *dp0 = 0, *staging = 0, *rsp_d = 0, *rsp_noalloc = 0;
-  R* gen_scr = 0;
+  double* gen_scr = 0;
   int *tab_cnt = 0, *tab_src = 0, *nbr = 0, *invalid = 0;
   int* h_invalid = nullptr;
   size_t staging_n = 0;
@@ -233,7 +223,7 @@ struct BackendT : Backend {
     void* ptrs[] = {D, Dinv, metinv, metdet, spheremp, rspheremp, mp, fcor, phis, tensorvisc, vec_sph2cart,
                     v, T, dp, ps_v, qdp, Qc, phi, omega_p, eta, derived_dp, divdp, divdp_proj, dpdiss_ave,
                     dpdiss_bih, vn0, caar_out, bufA, bufB, vstar, dpdissk, fscr, qtens, qscr, qlim, qlim_tmp,
-                    dp0, staging, rsp_d, rsp_noalloc, gen_scr, tab_cnt, tab_src, nbr, invalid};
+                    dp0, staging, rsp_d, rsp_noalloc, gen_scr, tab_cnt, tab_src, nbr, invalid, sp_d};
     for (void* p : ptrs)
       if (p) cudaFree(p);
     if (h_invalid) cudaFreeHost(h_invalid);
@@ -250,62 +240,52 @@ struct BackendT : Backend {
     metdet = dalloc<R>((size_t)E * 16); spheremp = dalloc<R>((size_t)E * 16);
     rspheremp = dalloc<R>((size_t)E * 16); mp = dalloc<R>((size_t)E * 16);
     fcor = dalloc<R>((size_t)E * 16); phis = dalloc<R>((size_t)E * 16);
-    v = dalloc<R>(n3 * NTL * 2); T = dalloc<R>(n3 * NTL); dp = dalloc<R>(n3 * NTL);
+    sp_d = dalloc<double>((size_t)E * 16); rsp_d = dalloc<double>((size_t)E * 16);
+    v = dalloc<double>(n3 * NTL * 2); T = dalloc<double>(n3 * NTL); dp = dalloc<double>(n3 * NTL);
     ps_v = dalloc<double>((size_t)E * NTL * 16);
     qdp = dalloc<double>(n3 * QTL * Q); Qc = dalloc<double>(n3 * Q);
-    phi = dalloc<R>(n3); omega_p = dalloc<R>(n3); eta = dalloc<R>(n3); derived_dp = dalloc<R>(n3);
-    divdp = dalloc<R>(n3); divdp_proj = dalloc<R>(n3); dpdiss_ave = dalloc<R>(n3); dpdiss_bih = dalloc<R>(n3);
-    vn0 = dalloc<R>(2 * n3);
-    caar_out = dalloc<R>(4 * n3); bufA = dalloc<R>(4 * n3); bufB = dalloc<R>(4 * n3);
-    vstar = dalloc<R>(2 * n3); dpdissk = dalloc<R>(n3); fscr = dalloc<R>(n3);
-    qtens = dalloc<R>(n3 * Q); qscr = dalloc<R>(n3 * Q);
+    phi = dalloc<double>(n3); omega_p = dalloc<double>(n3); eta = dalloc<double>(n3);
+    derived_dp = dalloc<double>(n3); divdp = dalloc<double>(n3); divdp_proj = dalloc<double>(n3);
+    dpdiss_ave = dalloc<double>(n3); dpdiss_bih = dalloc<double>(n3); vn0 = dalloc<double>(2 * n3);
+    caar_out = dalloc<double>(4 * n3); bufA = dalloc<double>(4 * n3); bufB = dalloc<double>(4 * n3);
+    vstar = dalloc<double>(2 * n3); dpdissk = dalloc<double>(n3); fscr = dalloc<double>(n3);
+    qtens = dalloc<double>(n3 * Q); qscr = dalloc<double>(n3 * Q);
     qlim = dalloc<double>((size_t)E * Q * 2 * NLEV); qlim_tmp = dalloc<double>((size_t)E * Q * 2 * NLEV);
     dp0 = dalloc<double>(NLEV);
-    gen_scr = dalloc<R>(n3 * (Q > 2 ? Q : 2));
+    gen_scr = dalloc<double>(n3 * (Q > 2 ? Q : 2));
     invalid = dalloc<int>(1);
     ck(cudaMallocHost(&h_invalid, sizeof(int)), "cudaMallocHost");
-    if (std::is_same<R, float>::value) {
-      staging_n = n3 * (NTL * 2 > QTL * Q ? NTL * 2 : QTL * Q);
-      staging = dalloc<double>(staging_n);
-    }
   }
 
-  void to_dev(R* dst, const double* host, size_t n) {
-    if (std::is_same<R, double>::value) {
-      ck(cudaMemcpyAsync(dst, host, n * sizeof(double), cudaMemcpyHostToDevice, g_stream), "H2D");
-    } else {
-      if (n > staging_n) fail(HX_ERR_STATE, "staging buffer too small");
-      ck(cudaMemcpyAsync(staging, host, n * sizeof(double), cudaMemcpyHostToDevice, g_stream), "H2D");
-      k_d2r<R><<<(unsigned)((n + 255) / 256), 256, 0, g_stream>>>(staging, dst, n);
-      ck(cudaGetLastError(), "convert");
-    }
+  // metric arrays in R (host conversion: small arrays, once)
+  void to_dev_R(R* dst, const double* host, size_t n) {
+    std::vector<R> tmp(host, host + n);
+    ck(cudaMemcpy(dst, tmp.data(), n * sizeof(R), cudaMemcpyHostToDevice), "H2D metric");
   }
-  void to_host(double* host, const R* src, size_t n) {
-    if (std::is_same<R, double>::value) {
-      ck(cudaMemcpyAsync(host, src, n * sizeof(double), cudaMemcpyDeviceToHost, g_stream), "D2H");
-    } else {
-      if (n > staging_n) fail(HX_ERR_STATE, "staging buffer too small");
-      k_r2d<R><<<(unsigned)((n + 255) / 256), 256, 0, g_stream>>>(src, staging, n);
-      ck(cudaGetLastError(), "convert");
-      ck(cudaMemcpyAsync(host, staging, n * sizeof(double), cudaMemcpyDeviceToHost, g_stream), "D2H");
-    }
+  void to_dev(double* dst, const double* host, size_t n) {
+    ck(cudaMemcpyAsync(dst, host, n * sizeof(double), cudaMemcpyHostToDevice, g_stream), "H2D");
+  }
+  void to_host(double* host, const double* src, size_t n) {
+    ck(cudaMemcpyAsync(host, src, n * sizeof(double), cudaMemcpyDeviceToHost, g_stream), "D2H");
   }
 
   void upload_metric(const double* const* a, bool consthv) override {
-    to_dev(D, a[0], (size_t)E * 64);
-    to_dev(Dinv, a[1], (size_t)E * 64);
-    to_dev(fcor, a[2], (size_t)E * 16);
-    to_dev(mp, a[3], (size_t)E * 16);
-    to_dev(spheremp, a[4], (size_t)E * 16);
-    to_dev(rspheremp, a[5], (size_t)E * 16);
-    to_dev(metdet, a[6], (size_t)E * 16);
-    to_dev(metinv, a[7], (size_t)E * 64);
-    to_dev(phis, a[8], (size_t)E * 16);
+    to_dev_R(D, a[0], (size_t)E * 64);
+    to_dev_R(Dinv, a[1], (size_t)E * 64);
+    to_dev_R(fcor, a[2], (size_t)E * 16);
+    to_dev_R(mp, a[3], (size_t)E * 16);
+    to_dev_R(spheremp, a[4], (size_t)E * 16);
+    to_dev_R(rspheremp, a[5], (size_t)E * 16);
+    to_dev_R(metdet, a[6], (size_t)E * 16);
+    to_dev_R(metinv, a[7], (size_t)E * 64);
+    to_dev_R(phis, a[8], (size_t)E * 16);
+    to_dev(sp_d, a[4], (size_t)E * 16);
+    to_dev(rsp_d, a[5], (size_t)E * 16);
     if (!rsp_noalloc) rsp_noalloc = dalloc<double>((size_t)E * 16);
     ck(cudaMemcpyAsync(rsp_noalloc, a[5], (size_t)E * 16 * sizeof(double), cudaMemcpyHostToDevice, g_stream), "H2D");
     if (!consthv) {
-      to_dev(tensorvisc, a[9], (size_t)E * 64);
-      to_dev(vec_sph2cart, a[10], (size_t)E * 96);
+      to_dev_R(tensorvisc, a[9], (size_t)E * 64);
+      to_dev_R(vec_sph2cart, a[10], (size_t)E * 96);
     }
     ck(cudaStreamSynchronize(g_stream), "upload_metric");
   }
@@ -339,6 +319,7 @@ struct BackendT : Backend {
     m.D = D; m.Dinv = Dinv; m.metinv = metinv; m.metdet = metdet; m.spheremp = spheremp;
     m.rspheremp = rspheremp; m.mp = mp; m.fcor = fcor; m.phis = phis;
     m.tensorvisc = tensorvisc; m.vec_sph2cart = vec_sph2cart;
+    m.spheremp_d = sp_d; m.rspheremp_d = rsp_d;
     return m;
   }
   DssTable table() const { return DssTable{tab_cnt, tab_src}; }
@@ -379,7 +360,7 @@ struct BackendT : Backend {
     a.rk_combine = combine; a.n0orig = n0orig;
     launch_caar<R>(a, E, g_stream);
     post("caar");
-    launch_dss_state<R>(E, caar_out, v, T, dp, np1, rspheremp, table(), g_stream);
+    launch_dss_state(E, caar_out, v, T, dp, np1, rsp_d, table(), g_stream);
     post("dss_caar");
   }
 
@@ -447,12 +428,12 @@ struct BackendT : Backend {
   }
 
   void launch_remap(int np1, int np1_qdp) {
-    RemapArgs<R> a;
+    RemapArgs a;
     a.v = v; a.T = T; a.dp = dp; a.qdp = qdp; a.ps_v = ps_v;
     a.np1 = np1; a.n0_qdp = np1_qdp; a.Q = Q; a.remap_alg = s.prm.remap_alg; a.nelem = E;
     a.ps0 = s.ps0; a.hyai0 = s.hyai[0]; a.invalid = invalid;
     ck(cudaMemsetAsync(invalid, 0, sizeof(int), g_stream), "memset");
-    hx::launch_remap<R>(a, g_stream);
+    hx::launch_remap(a, g_stream);
     post("remap");
   }
   int remap_status() {
@@ -467,7 +448,7 @@ struct BackendT : Backend {
 
   void prim_step(double dt) override {
     const Params& p = s.prm;
-    launch_prim_step_init<R>(E, eta, vn0, omega_p, dpdiss_ave, dpdiss_bih, derived_dp, dp, s.tl.n0,
+    launch_prim_step_init(E, eta, vn0, omega_p, dpdiss_ave, dpdiss_bih, derived_dp, dp, s.tl.n0,
                              p.nu_p > 0 ? 1 : 0, g_stream);
     post("prim_step_init");
     for (int n = 0; n < p.qsplit; ++n) {
@@ -487,7 +468,7 @@ struct BackendT : Backend {
   void run_subcycle(double dt) override {
     const Params& p = s.prm;
     s.tl.update_tracers_levels(p.qsplit);
-    launch_dp_from_ps<R>(E, dp, ps_v, s.tl.n0, s.ps0, g_stream);
+    launch_dp_from_ps(E, dp, ps_v, s.tl.n0, s.ps0, g_stream);
     post("dp3d_from_ps");
     prim_step(dt);
     for (int r = 1; r < p.rsplit; ++r) {
@@ -496,7 +477,7 @@ struct BackendT : Backend {
     }
     s.tl.update_tracers_levels(p.qsplit);
     launch_remap(s.tl.np1, s.tl.np1_qdp);
-    launch_update_q<R>(E, Q, qdp, Qc, ps_v, s.tl.np1, s.tl.np1_qdp, s.ps0, g_stream);
+    launch_update_q(E, Q, qdp, Qc, ps_v, s.tl.np1, s.tl.np1_qdp, s.ps0, g_stream);
     post("update_q");
     const int st = remap_status();
     s.tl.update_dynamics_levels();
@@ -506,7 +487,7 @@ struct BackendT : Backend {
   // Field access in the Fortran layout of one time level.
   int field(const std::string& n, int tl, double* host, bool get) override {
     const size_t n3 = N3();
-    auto xfer_R = [&](R* base, long long es, int ncomp) {
+    auto xfer_R = [&](double* base, long long es, int ncomp) {
       // base + e*es holds ncomp*[72][16]... contiguous per element: [72][ncomp][16]
       const size_t per = (size_t)NLEV * 16 * ncomp;
       for (int e = 0; e < E; ++e) {
@@ -542,25 +523,13 @@ struct BackendT : Backend {
   }
 
   int dss_field(const std::string& n, int tl, bool rs) override {
-    const R* r = rs ? rspheremp : nullptr;
-    if (n == "v") launch_dss_inplace<R>(E, 2, v + (size_t)tl * NLEV * 32, 16, (long long)NTL * NLEV * 32, 32, gen_scr, r, table(), g_stream);
-    else if (n == "T") launch_dss_inplace<R>(E, 1, T + (size_t)tl * NLEV * 16, 0, (long long)NTL * NLEV * 16, 16, gen_scr, r, table(), g_stream);
-    else if (n == "dp3d") launch_dss_inplace<R>(E, 1, dp + (size_t)tl * NLEV * 16, 0, (long long)NTL * NLEV * 16, 16, gen_scr, r, table(), g_stream);
-    else if (n == "omega_p") launch_dss_inplace<R>(E, 1, omega_p, 0, NLEV * 16, 16, gen_scr, r, table(), g_stream);
-    else if (n == "Qdp") {
-      // FP64 tracer mass through the double path
-      double* scr = reinterpret_cast<double*>(qscr);
-      if (sizeof(R) != sizeof(double)) scr = staging;
-      const double* rd = nullptr;
-      std::vector<double> h;
-      if (rs) {
-        // rspheremp in double
-        if (!rsp_d) rsp_d = dalloc<double>((size_t)E * 16);
-        k_r2d<R><<<(E * 16 + 255) / 256, 256, 0, g_stream>>>(rspheremp, rsp_d, (size_t)E * 16);
-        rd = rsp_d;
-      }
-      launch_dss_inplace_d(E, Q, qdp + (size_t)tl * Q * NLEV * 16, NLEV * 16, (long long)QTL * Q * NLEV * 16, 16, scr, rd, table(), g_stream);
-    } else return HX_ERR_STATE;
+    const double* r = rs ? rsp_d : nullptr;
+    if (n == "v") launch_dss_inplace(E, 2, v + (size_t)tl * NLEV * 32, 16, (long long)NTL * NLEV * 32, 32, gen_scr, r, table(), g_stream);
+    else if (n == "T") launch_dss_inplace(E, 1, T + (size_t)tl * NLEV * 16, 0, (long long)NTL * NLEV * 16, 16, gen_scr, r, table(), g_stream);
+    else if (n == "dp3d") launch_dss_inplace(E, 1, dp + (size_t)tl * NLEV * 16, 0, (long long)NTL * NLEV * 16, 16, gen_scr, r, table(), g_stream);
+    else if (n == "omega_p") launch_dss_inplace(E, 1, omega_p, 0, NLEV * 16, 16, gen_scr, r, table(), g_stream);
+    else if (n == "Qdp") launch_dss_inplace(E, Q, qdp + (size_t)tl * Q * NLEV * 16, NLEV * 16, (long long)QTL * Q * NLEV * 16, 16, qscr, r, table(), g_stream);
+    else return HX_ERR_STATE;
     post("dss_field");
     ck(cudaStreamSynchronize(g_stream), "dss_field");
     return 0;

@@ -39,6 +39,8 @@ struct MetricP {
   const R* phis;
   const R* tensorvisc;     // [E][2][2][16] or null
   const R* vec_sph2cart;   // [E][2][3][16] or null
+  const double* spheremp_d;   // double copies for the state updates and the DSS
+  const double* rspheremp_d;
 };
 
 // DSS gather table: for (e, p) the ordered sources src[(e*16+p)*3 + k] = se*16 + sp,

@@ -42,6 +42,18 @@ template <typename R> __device__ __forceinline__ R sh16(R v, int src) {
 
 template <typename R> __device__ __forceinline__ R rre() { return R(kRrearth); }
 
+template <typename R> constexpr bool kF32 = sizeof(R) == 4;
+
+// A double field value as operator input.  In the mixed form the value at point 0 of the
+// same level and element is subtracted first (in double): the sphere operators annihilate
+// constants, and the FP32 operand then carries the horizontal variation instead of the
+// large mean (pressure, geopotential, temperature, layer thickness).  In the FP64 form the
+// value is used as is, so the arithmetic follows the reference formulas.
+template <typename R> __device__ __forceinline__ R rel(double x) {
+  if constexpr (kF32<R>) return (R)(x - sh16(x, 0));
+  else return x;
+}
+
 // Per-thread GLL point data: index, dvv rows/columns for the four contractions.
 template <typename R>
 struct Pt {
@@ -255,24 +267,25 @@ __global__ void __launch_bounds__(LG * 16) k_caar(CaarArgs<R> a) {
 #pragma unroll 1
   for (int k = 0; k < NL; ++k) {
     const int l = lg + LG * k;
-    const R u = a.v[vN0 + l * 32 + p], w = a.v[vN0 + l * 32 + 16 + p];
-    const R tt = a.T[sN0 + l * 16 + p], d = a.dp[sN0 + l * 16 + p];
+    const R u = (R)a.v[vN0 + l * 32 + p], w = (R)a.v[vN0 + l * 32 + 16 + p];
+    const double td = a.T[sN0 + l * 16 + p], dd = a.dp[sN0 + l * 16 + p];
+    const R d = (R)dd;
     const R vd0 = u * d, vd1 = w * d;
     if (a.eta_ave_w != 0.0) {  // stages 2-4 accumulate nothing (eta_ave_w = 0)
       const size_t iv = ((size_t)e * NLEV + l) * 32 + p;
-      a.vn0[iv] += eta * vd0;
-      a.vn0[iv + 16] += eta * vd1;
+      a.vn0[iv] += (double)(eta * vd0);
+      a.vn0[iv + 16] += (double)(eta * vd1);
     }
     const R div = divergence_sphere(t, m, vd0, vd1);
-    R tv = tt;
-    if (a.n0_qdp >= 0) {
-      R Qt = R(a.qdp[((((size_t)e * QTL + a.n0_qdp) * a.qsize) * NLEV + l) * 16 + p]) / d;
-      Qt *= R(kRwaterVapor / kRgas - 1.0);
-      Qt += R(1);
-      tv = tt * Qt;
+    double tv = td;
+    if (a.n0_qdp >= 0) {  // moist virtual temperature, in double
+      double Qt = a.qdp[((((size_t)e * QTL + a.n0_qdp) * a.qsize) * NLEV + l) * 16 + p] / dd;
+      Qt *= (kRwaterVapor / kRgas - 1.0);
+      Qt += 1.0;
+      tv = td * Qt;
     }
-    s_dp[l * SROW + p] = (double)d;
-    s_tv[l * SROW + p] = (double)tv;
+    s_dp[l * SROW + p] = dd;
+    s_tv[l * SROW + p] = tv;
     s_div[l * SROW + p] = (double)div;
   }
   __syncthreads();
@@ -305,13 +318,13 @@ __global__ void __launch_bounds__(LG * 16) k_caar(CaarArgs<R> a) {
     for (int k = 0; k < 9; ++k) rt += r[k];
     double integ = seg_excl_suffix(rt, seg);
     const double phis = (double)a.m.phis[(size_t)e * 16 + col];
-    R* phig = a.phi + (size_t)e * NLEV * 16;
+    double* phig = a.phi + (size_t)e * NLEV * 16;
 #pragma unroll
     for (int k = 8; k >= 0; --k) {
       const double ph = phis + 2.0 * integ + r[k];
       integ = integ + r[k];
       s_dp[(l0 + k) * SROW + col] = ph;  // dp no longer needed: holds phi now
-      phig[(l0 + k) * 16 + col] = (R)ph;
+      phig[(l0 + k) * 16 + col] = ph;
     }
     // omega integral: exclusive prefix of div_vdp
     double dt_ = 0.0;
@@ -332,27 +345,29 @@ __global__ void __launch_bounds__(LG * 16) k_caar(CaarArgs<R> a) {
   const size_t sM = ((size_t)e * NTL + a.nm1) * NLEV * 16;
   const size_t vO = ((size_t)e * NTL + a.n0orig) * NLEV * 32;
   const size_t sO = ((size_t)e * NTL + a.n0orig) * NLEV * 16;
-  R* out = a.out + (size_t)e * NLEV * 64;
+  double* out = a.out + (size_t)e * NLEV * 64;
+  const double spd = a.m.spheremp_d[(size_t)e * 16 + p];
 #pragma unroll 1
   for (int k = 0; k < NL; ++k) {
     const int l = lg + LG * k;
-    const R pr = (R)s_p[l * SROW + p];
+    const double pd = s_p[l * SROW + p];
+    const R pr = (R)pd;
     R gp0, gp1;
-    gradient_sphere(t, m, pr, gp0, gp1);
-    const R u = a.v[vN0 + l * 32 + p], w = a.v[vN0 + l * 32 + 16 + p];
-    const R tt = a.T[sN0 + l * 16 + p];
+    gradient_sphere(t, m, rel<R>(pd), gp0, gp1);
+    const R u = (R)a.v[vN0 + l * 32 + p], w = (R)a.v[vN0 + l * 32 + 16 + p];
+    const double td = a.T[sN0 + l * 16 + p];
     const R div = (R)s_div[l * SROW + p];
     const R vgp = u * gp0 + w * gp1;
     const R omega = (vgp - ((R)s_om[l * SROW + p] + R(0.5) * div)) / pr;
-    if (a.eta_ave_w != 0.0) a.omega_p[((size_t)e * NLEV + l) * 16 + p] += eta * omega;
-    // time level "nm1" (RK combine of stage 5 fused here)
-    R tm = a.T[sM + l * 16 + p], dm = a.dp[sM + l * 16 + p];
-    R vm0 = a.v[vM + l * 32 + p], vm1 = a.v[vM + l * 32 + 16 + p];
+    if (a.eta_ave_w != 0.0) a.omega_p[((size_t)e * NLEV + l) * 16 + p] += (double)(eta * omega);
+    // time level "nm1" (RK combine of stage 5 fused here), in double
+    double tm = a.T[sM + l * 16 + p], dm = a.dp[sM + l * 16 + p];
+    double vm0 = a.v[vM + l * 32 + p], vm1 = a.v[vM + l * 32 + 16 + p];
     if (a.rk_combine) {
-      tm = (R(5) * tm - a.T[sO + l * 16 + p]) / R(4);
-      dm = (R(5) * dm - a.dp[sO + l * 16 + p]) / R(4);
-      vm0 = (R(5) * vm0 - a.v[vO + l * 32 + p]) / R(4);
-      vm1 = (R(5) * vm1 - a.v[vO + l * 32 + 16 + p]) / R(4);
+      tm = (5.0 * tm - a.T[sO + l * 16 + p]) / 4.0;
+      dm = (5.0 * dm - a.dp[sO + l * 16 + p]) / 4.0;
+      vm0 = (5.0 * vm0 - a.v[vO + l * 32 + p]) / 4.0;
+      vm1 = (5.0 * vm1 - a.v[vO + l * 32 + 16 + p]) / 4.0;
       a.T[sM + l * 16 + p] = tm;
       a.dp[sM + l * 16 + p] = dm;
       a.v[vM + l * 32 + p] = vm0;
@@ -360,15 +375,15 @@ __global__ void __launch_bounds__(LG * 16) k_caar(CaarArgs<R> a) {
     }
     // temperature (compute_temperature_np1)
     R gt0, gt1;
-    gradient_sphere(t, m, tt, gt0, gt1);
+    gradient_sphere(t, m, rel<R>(td), gt0, gt1);
     const R tv = (R)s_tv[l * SROW + p];
     const R vgt = u * gt0 + w * gt1;
     const R ttens = -vgt + R(kKappa) * tv * omega;
-    const R tnew = m.sp * (ttens * dt + tm);
+    const double tnew = spd * ((double)(ttens * dt) + tm);
     // velocity (compute_velocity_np1 with compute_energy_grad)
     const R rr = R(kRgas) * (tv / pr);
     R eg0 = rr * gp0, eg1 = rr * gp1;
-    const R ephi = R(0.5) * (u * u + w * w) + (R)s_dp[l * SROW + p];
+    const R ephi = R(0.5) * (u * u + w * w) + rel<R>(s_dp[l * SROW + p]);
     R ge0, ge1;
     gradient_sphere(t, m, ephi, ge0, ge1);
     eg0 += ge0;
@@ -376,10 +391,10 @@ __global__ void __launch_bounds__(LG * 16) k_caar(CaarArgs<R> a) {
     const R vort = vorticity_sphere(t, m, u, w) + fcor;
     eg0 = -eg0 + w * vort;
     eg1 = -eg1 - u * vort;
-    const R vn0_ = m.sp * (eg0 * dt + vm0);
-    const R vn1_ = m.sp * (eg1 * dt + vm1);
+    const double vn0_ = spd * ((double)(eg0 * dt) + vm0);
+    const double vn1_ = spd * ((double)(eg1 * dt) + vm1);
     // dp3d (compute_dp3d_np1, eta_dot_dpdn = 0 for rsplit > 0)
-    const R dnew = m.sp * (dm - div * dt);
+    const double dnew = spd * (dm - (double)(div * dt));
     out[l * 64 + p] = vn0_;
     out[l * 64 + 16 + p] = vn1_;
     out[l * 64 + 32 + p] = tnew;
@@ -389,23 +404,22 @@ __global__ void __launch_bounds__(LG * 16) k_caar(CaarArgs<R> a) {
 
 // DSS of the Caar output into the state of time level np1, times rspheremp
 // (BoundaryExchange::exchange(rspheremp) on v, T, dp3d: CaarFunctor.cpp:114).
-template <typename R>
-__global__ void k_dss_state(int E, const R* __restrict__ src, R* v, R* T, R* dp, int np1,
-                            const R* __restrict__ rsmp, DssTable tab) {
+__global__ void k_dss_state(int E, const double* __restrict__ src, double* v, double* T, double* dp,
+                            int np1, const double* __restrict__ rsmp, DssTable tab) {
   const int idx = blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= E * NLEV * 16) return;
   const int e = idx / (NLEV * 16), l = (idx / 16) % NLEV, p = idx & 15;
-  const double r = (double)rsmp[e * 16 + p];
+  const double r = rsmp[e * 16 + p];
   const double a0 = dss_gather(src, NLEV * 64, 64, e, l, p, tab) * r;
   const double a1 = dss_gather(src + 16, NLEV * 64, 64, e, l, p, tab) * r;
   const double a2 = dss_gather(src + 32, NLEV * 64, 64, e, l, p, tab) * r;
   const double a3 = dss_gather(src + 48, NLEV * 64, 64, e, l, p, tab) * r;
   const size_t vb = (((size_t)e * NTL + np1) * NLEV + l) * 32 + p;
   const size_t sb = (((size_t)e * NTL + np1) * NLEV + l) * 16 + p;
-  v[vb] = (R)a0;
-  v[vb + 16] = (R)a1;
-  T[sb] = (R)a2;
-  dp[sb] = (R)a3;
+  v[vb] = a0;
+  v[vb + 16] = a1;
+  T[sb] = a2;
+  dp[sb] = a3;
 }
 
 // ======================================================================================
@@ -422,19 +436,19 @@ __global__ void __launch_bounds__(LG * 16) k_hv_lap1(HvArgs<R> a) {
   m.load(a.m, e, p);
   const size_t vb = ((size_t)e * NTL + a.np1) * NLEV * 32;
   const size_t sb = ((size_t)e * NTL + a.np1) * NLEV * 16;
-  R* out = a.bufA + (size_t)e * NLEV * 64;
+  double* out = a.bufA + (size_t)e * NLEV * 64;
   const R nr = R(a.nu_ratio1);
 #pragma unroll 1
   for (int k = 0; k < NL; ++k) {
     const int l = lg + LG * k;
-    const R lt = laplace_simple(t, m, a.T[sb + l * 16 + p]);
-    const R ld = laplace_simple(t, m, a.dp[sb + l * 16 + p]);
+    const R lt = laplace_simple(t, m, rel<R>(a.T[sb + l * 16 + p]));
+    const R ld = laplace_simple(t, m, rel<R>(a.dp[sb + l * 16 + p]));
     R l0, l1;
-    vlaplace_contra(t, m, nr, a.v[vb + l * 32 + p], a.v[vb + l * 32 + 16 + p], l0, l1);
-    out[l * 64 + p] = l0;
-    out[l * 64 + 16 + p] = l1;
-    out[l * 64 + 32 + p] = lt;
-    out[l * 64 + 48 + p] = ld;
+    vlaplace_contra(t, m, nr, (R)a.v[vb + l * 32 + p], (R)a.v[vb + l * 32 + 16 + p], l0, l1);
+    out[l * 64 + p] = (double)l0;
+    out[l * 64 + 16 + p] = (double)l1;
+    out[l * 64 + 32 + p] = (double)lt;
+    out[l * 64 + 48 + p] = (double)ld;
   }
 }
 
@@ -456,8 +470,9 @@ __global__ void __launch_bounds__(LG * 16) k_hv_lap2(HvArgs<R> a) {
   }
   const size_t vb = ((size_t)e * NTL + a.np1) * NLEV * 32;
   const size_t sb = ((size_t)e * NTL + a.np1) * NLEV * 16;
-  R* out = a.bufB + (size_t)e * NLEV * 64;
-  const double rs = (double)m.rsp;
+  double* out = a.bufB + (size_t)e * NLEV * 64;
+  const double rs = a.m.rspheremp_d[(size_t)e * 16 + p];
+  const double spd = a.m.spheremp_d[(size_t)e * 16 + p];
   const R eta_h = R(a.eta_ave_w);
   const R hs = R(a.hsub);
   const R dt = R(a.dt);
@@ -479,18 +494,18 @@ __global__ void __launch_bounds__(LG * 16) k_hv_lap2(HvArgs<R> a) {
       vlaplace_cartesian(t, m, tv, s2c, v0, v1, l0, l1);
     }
     const size_t i3 = ((size_t)e * NLEV + l) * 16 + p;
-    const R dpn = a.dp[sb + l * 16 + p];
-    a.dpdiss_ave[i3] += eta_h * dpn / hs;
-    a.dpdiss_bih[i3] += eta_h * ld / hs;
+    const double dpn = a.dp[sb + l * 16 + p];
+    a.dpdiss_ave[i3] += a.eta_ave_w * dpn / a.hsub;
+    a.dpdiss_bih[i3] += (double)(eta_h * ld / hs);
     R vt0 = l0 * R(-a.nu), vt1 = l1 * R(-a.nu);
     R ttn = lt * R(-a.nu_s), dpt = ld * R(-a.nu_p);
     if (a.nu_top > 0 && __any_sync(FULL, l < 3)) {
       // nu_top sponge on the top three levels, applied to the np1 state
-      const R un = a.v[vb + l * 32 + p], wn = a.v[vb + l * 32 + 16 + p];
+      const R un = (R)a.v[vb + l * 32 + p], wn = (R)a.v[vb + l * 32 + 16 + p];
       R lv0, lv1;
       vlaplace_contra(t, m, R(1), un, wn, lv0, lv1);
-      const R ltt = laplace_simple(t, m, a.T[sb + l * 16 + p]);
-      const R ldd = laplace_simple(t, m, dpn);
+      const R ltt = laplace_simple(t, m, rel<R>(a.T[sb + l * 16 + p]));
+      const R ldd = laplace_simple(t, m, rel<R>(dpn));
       if (l < 3) {
         const R sc = R((l == 0 ? 4.0 : l == 1 ? 2.0 : 1.0) * a.nu_top);
         vt0 += sc * lv0;
@@ -499,11 +514,10 @@ __global__ void __launch_bounds__(LG * 16) k_hv_lap2(HvArgs<R> a) {
         dpt += sc * ldd;
       }
     }
-    dpt = dpt * dt + dpn * m.sp;
-    out[l * 64 + p] = vt0;
-    out[l * 64 + 16 + p] = vt1;
-    out[l * 64 + 32 + p] = ttn;
-    out[l * 64 + 48 + p] = dpt;
+    out[l * 64 + p] = (double)vt0;
+    out[l * 64 + 16 + p] = (double)vt1;
+    out[l * 64 + 32 + p] = (double)ttn;
+    out[l * 64 + 48 + p] = (double)(dpt * dt) + dpn * spd;
   }
 }
 
@@ -513,31 +527,33 @@ __global__ void k_hv_update(HvArgs<R> a, int E) {
   const int idx = blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= E * NLEV * 16) return;
   const int e = idx / (NLEV * 16), l = (idx / 16) % NLEV, p = idx & 15;
-  const R rs = a.m.rspheremp[e * 16 + p];
+  const double rsd = a.m.rspheremp_d[e * 16 + p];
+  const R rs = (R)rsd;
   const R dt = R(a.dt);
   R vt0 = (R)dss_gather(a.bufB, NLEV * 64, 64, e, l, p, a.dss);
   R vt1 = (R)dss_gather(a.bufB + 16, NLEV * 64, 64, e, l, p, a.dss);
   R tt = (R)dss_gather(a.bufB + 32, NLEV * 64, 64, e, l, p, a.dss);
-  const R dpt = (R)dss_gather(a.bufB + 48, NLEV * 64, 64, e, l, p, a.dss);
+  const double dpt = dss_gather(a.bufB + 48, NLEV * 64, 64, e, l, p, a.dss);
   const size_t vb = (((size_t)e * NTL + a.np1) * NLEV + l) * 32 + p;
   const size_t sb = (((size_t)e * NTL + a.np1) * NLEV + l) * 16 + p;
   vt0 = dt * vt0 * rs;
   vt1 = dt * vt1 * rs;
-  const R v0 = a.v[vb] + vt0, v1 = a.v[vb + 16] + vt1;
+  const double v0 = a.v[vb] + (double)vt0, v1 = a.v[vb + 16] + (double)vt1;
   a.v[vb] = v0;
   a.v[vb + 16] = v1;
   tt = dt * tt * rs;
-  const R heating = vt0 * v0 + vt1 * v1;
-  a.T[sb] = a.T[sb] + tt - heating / R(kCp);
-  a.dp[sb] = dpt * rs;
+  const R heating = vt0 * (R)v0 + vt1 * (R)v1;
+  if constexpr (kF32<R>) a.T[sb] = a.T[sb] + (double)(tt - heating / R(kCp));
+  else a.T[sb] = a.T[sb] + tt - heating / R(kCp);
+  a.dp[sb] = dpt * rsd;
 }
 
 // ======================================================================================
 // Small element-wise kernels
 // ======================================================================================
-template <typename R>
-__global__ void k_prim_step_init(int E, R* eta, R* vn0, R* omega_p, R* dpa, R* dpb, R* derived_dp,
-                                 const R* dp, int n0, int zero_diss) {
+__global__ void k_prim_step_init(int E, double* eta, double* vn0, double* omega_p, double* dpa,
+                                 double* dpb, double* derived_dp, const double* dp, int n0,
+                                 int zero_diss) {
   const int idx = blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= E * NLEV * 16) return;
   const int e = idx / (NLEV * 16), r = idx % (NLEV * 16), l = r / 16, p = r & 15;
@@ -552,16 +568,14 @@ __global__ void k_prim_step_init(int E, R* eta, R* vn0, R* omega_p, R* dpa, R* d
   derived_dp[idx] = dp[((size_t)e * NTL + n0) * NLEV * 16 + r];
 }
 
-template <typename R>
-__global__ void k_dp_from_ps(int E, R* dp, const double* ps_v, int n0, double ps0) {
+__global__ void k_dp_from_ps(int E, double* dp, const double* ps_v, int n0, double ps0) {
   const int idx = blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= E * NLEV * 16) return;
   const int e = idx / (NLEV * 16), r = idx % (NLEV * 16), l = r / 16, p = r & 15;
   dp[((size_t)e * NTL + n0) * NLEV * 16 + r] =
-      (R)(c_ai_delta[l] * ps0 + c_bi_delta[l] * ps_v[((size_t)e * NTL + n0) * 16 + p]);
+      c_ai_delta[l] * ps0 + c_bi_delta[l] * ps_v[((size_t)e * NTL + n0) * 16 + p];
 }
 
-template <typename R>
 __global__ void k_update_q(int E, int Q, const double* qdp, double* Qc, const double* ps_v, int np1,
                            int np1_qdp, double ps0) {
   const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -590,10 +604,10 @@ __global__ void __launch_bounds__(LG * 16) k_precompute_divdp(EulerArgs<R> a) {
   for (int k = 0; k < NL; ++k) {
     const int l = lg + LG * k;
     const size_t iv = ((size_t)e * NLEV + l) * 32 + p;
-    const R d = divergence_sphere(t, m, a.vn0[iv], a.vn0[iv + 16]);
+    const R d = divergence_sphere(t, m, (R)a.vn0[iv], (R)a.vn0[iv + 16]);
     const size_t i3 = ((size_t)e * NLEV + l) * 16 + p;
-    a.divdp[i3] = d;
-    a.divdp_proj[i3] = d;
+    a.divdp[i3] = (double)d;
+    a.divdp_proj[i3] = (double)d;
   }
 }
 
@@ -609,10 +623,10 @@ __global__ void __launch_bounds__(LG * 16) k_qminmax(EulerArgs<R> a, double* qli
   for (int k = 0; k < NL; ++k) {
     const int l = lg + LG * k;
     const size_t i3 = ((size_t)e * NLEV + l) * 16 + p;
-    const R dpt = a.derived_dp[i3] - rhsdt * a.divdp_proj[i3];
+    const R dpt = (R)a.derived_dp[i3] - rhsdt * (R)a.divdp_proj[i3];
     const double qv = a.qdp[((((size_t)e * QTL + a.n0_qdp) * a.Q + q) * NLEV + l) * 16 + p];
     const R val = R(qv) / dpt;
-    if (store_q) a.qtens[(((size_t)e * a.Q + q) * NLEV + l) * 16 + p] = val;
+    if (store_q) a.qtens[(((size_t)e * a.Q + q) * NLEV + l) * 16 + p] = (double)val;
     double mn = (double)val, mx = (double)val;
 #pragma unroll
     for (int off = 8; off >= 1; off >>= 1) {
@@ -664,9 +678,9 @@ __global__ void __launch_bounds__(LG * 16) k_bih_pre(EulerArgs<R> a) {
 #pragma unroll 1
   for (int k = 0; k < NL; ++k) {
     const int l = lg + LG * k;
-    R s = a.qtens[qb + l * 16 + p];
-    if (a.nu_p > 0) s = s * a.dpdiss_ave[((size_t)e * NLEV + l) * 16 + p] / R(a.dp0[l]);
-    a.qscr[qb + l * 16 + p] = laplace_simple(t, m, s);
+    R s = (R)a.qtens[qb + l * 16 + p];
+    if (a.nu_p > 0) s = s * (R)a.dpdiss_ave[((size_t)e * NLEV + l) * 16 + p] / R(a.dp0[l]);
+    a.qscr[qb + l * 16 + p] = (double)laplace_simple(t, m, s);
   }
 }
 
@@ -686,15 +700,15 @@ __global__ void __launch_bounds__(LG * 16) k_bih_post(EulerArgs<R> a) {
     for (int c = 0; c < 4; ++c) tv[c] = a.m.tensorvisc[(size_t)e * 64 + c * 16 + p];
   }
   const size_t qb = ((size_t)e * a.Q + q) * NLEV * 16;
-  const R* fbase = a.qscr + (size_t)q * NLEV * 16;
+  const double* fbase = a.qscr + (size_t)q * NLEV * 16;
   const R fac = R(-a.rhs_viss * a.dt * a.nu_q);
-  const double rs = (double)m.rsp;
+  const double rs = a.m.rspheremp_d[(size_t)e * 16 + p];
 #pragma unroll 1
   for (int k = 0; k < NL; ++k) {
     const int l = lg + LG * k;
     const R s = (R)(dss_gather(fbase, (long long)a.Q * NLEV * 16, 16, e, l, p, a.dss) * rs);
     const R lap = a.consthv ? laplace_simple(t, m, s) : laplace_tensor(t, m, tv, s);
-    a.qtens[qb + l * 16 + p] = (fac * R(a.dp0[l]) * lap / m.sp);
+    a.qtens[qb + l * 16 + p] = (double)(fac * R(a.dp0[l]) * lap / m.sp);
   }
 }
 
@@ -705,15 +719,15 @@ __global__ void k_aal_setup(EulerArgs<R> a, int E) {
   if (idx >= E * NLEV * 16) return;
   const int e = idx / (NLEV * 16), l = (idx / 16) % NLEV, p = idx & 15;
   const R rhsdt = R(a.rhs_multiplier * a.dt);
-  const R dpt = a.derived_dp[idx] - rhsdt * a.divdp_proj[idx];
+  const R dpt = (R)a.derived_dp[idx] - rhsdt * (R)a.divdp_proj[idx];
   const size_t iv = ((size_t)e * NLEV + l) * 32 + p;
-  a.vstar[iv] = a.vn0[iv] / dpt;
-  a.vstar[iv + 16] = a.vn0[iv + 16] / dpt;
-  R dk = dpt - R(a.dt) * a.divdp[idx];
+  a.vstar[iv] = (double)((R)a.vn0[iv] / dpt);
+  a.vstar[iv + 16] = (double)((R)a.vn0[iv + 16] / dpt);
+  R dk = dpt - R(a.dt) * (R)a.divdp[idx];
   if (a.nu_p > 0 && a.rhs_viss != 0.0)
-    dk += R(-a.rhs_viss * a.dt * a.nu_q) * a.dpdiss_bih[idx] / a.m.spheremp[e * 16 + p];
-  a.dpdissk[idx] = dk;
-  a.fscr[idx] = a.f_dss[idx] * a.m.spheremp[e * 16 + p];
+    dk += R(-a.rhs_viss * a.dt * a.nu_q) * (R)a.dpdiss_bih[idx] / a.m.spheremp[e * 16 + p];
+  a.dpdissk[idx] = (double)dk;
+  a.fscr[idx] = a.f_dss[idx] * a.m.spheremp_d[e * 16 + p];
 }
 
 // The quasi-monotone limiters of with_limiter_shell (EulerStepFunctorImpl.hpp:693-884)
@@ -797,7 +811,7 @@ __device__ void limiter_level(int option, R* x, const R* c, double& minp_io, dou
 template <typename R, int LG>
 __global__ void __launch_bounds__(LG * 16) k_aal_tracer(EulerArgs<R> a) {
   constexpr int NL = NLEV / LG;
-  __shared__ R s_q[NLEV * SROW];
+  __shared__ double s_q[NLEV * SROW];
   __shared__ R s_dm[NLEV * SROW];
   __shared__ R s_sp[16];
   const int eq = blockIdx.x, e = eq / a.Q, q = eq % a.Q;
@@ -814,13 +828,15 @@ __global__ void __launch_bounds__(LG * 16) k_aal_tracer(EulerArgs<R> a) {
 #pragma unroll 1
   for (int k = 0; k < NL; ++k) {
     const int l = lg + LG * k;
-    const R qd = (R)a.qdp[qn0 + l * 16 + p];
+    const double qdd = a.qdp[qn0 + l * 16 + p];
+    const R qd = (R)qdd;
     const size_t iv = ((size_t)e * NLEV + l) * 32 + p;
-    const R g0 = a.vstar[iv] * qd, g1 = a.vstar[iv + 16] * qd;
+    const R g0 = (R)a.vstar[iv] * qd, g1 = (R)a.vstar[iv + 16] * qd;
     const R dv = divergence_sphere(t, m, g0, g1);
-    const R q0 = add_hv ? a.qtens[qb + l * 16 + p] : R(0);
-    s_q[l * SROW + p] = (qd + mdt * dv + q0);
-    s_dm[l * SROW + p] = a.dpdissk[((size_t)e * NLEV + l) * 16 + p];
+    const double q0 = add_hv ? a.qtens[qb + l * 16 + p] : 0.0;
+    if constexpr (kF32<R>) s_q[l * SROW + p] = qdd + (double)(mdt * dv) + q0;
+    else s_q[l * SROW + p] = (qdd + mdt * dv + q0);
+    s_dm[l * SROW + p] = (R)a.dpdissk[((size_t)e * NLEV + l) * 16 + p];
   }
   __syncthreads();
   for (int l = tid; l < NLEV; l += blockDim.x) {
@@ -830,7 +846,7 @@ __global__ void __launch_bounds__(LG * 16) k_aal_tracer(EulerArgs<R> a) {
     for (int k = 0; k < 16; ++k) {
       const R dpm = s_dm[l * SROW + k];
       c[k] = s_sp[k] * dpm;
-      x[k] = s_q[l * SROW + k] / dpm;
+      x[k] = (R)s_q[l * SROW + k] / dpm;
       s1 += c[k];
     }
     if (s1 > R(0)) {
@@ -840,14 +856,14 @@ __global__ void __launch_bounds__(LG * 16) k_aal_tracer(EulerArgs<R> a) {
       ql[l] = mn;
       ql[NLEV + l] = mx;
 #pragma unroll
-      for (int k = 0; k < 16; ++k) s_q[l * SROW + k] = x[k] * s_dm[l * SROW + k];
+      for (int k = 0; k < 16; ++k) s_q[l * SROW + k] = (double)(x[k] * s_dm[l * SROW + k]);
     }
   }
   __syncthreads();
 #pragma unroll 1
   for (int k = 0; k < NL; ++k) {
     const int l = lg + LG * k;
-    a.qscr[qb + l * 16 + p] = m.sp * s_q[l * SROW + p];
+    a.qscr[qb + l * 16 + p] = a.m.spheremp_d[(size_t)e * 16 + p] * s_q[l * SROW + p];
   }
 }
 
@@ -859,7 +875,7 @@ __global__ void k_dss_tracers(EulerArgs<R> a, int E, int time_avg) {
   if (idx >= (long long)E * a.Q * NLEV * 16) return;
   const int p = idx & 15, l = (idx / 16) % NLEV, q = (idx / (16 * NLEV)) % a.Q;
   const int e = idx / (16LL * NLEV * a.Q);
-  const double rs = (double)a.m.rspheremp[e * 16 + p];
+  const double rs = a.m.rspheremp_d[e * 16 + p];
   const double v = dss_gather(a.qscr + (size_t)q * NLEV * 16, (long long)a.Q * NLEV * 16, 16, e, l, p, a.dss) * rs;
   const size_t d = ((((size_t)e * QTL + a.np1_qdp) * a.Q + q) * NLEV + l) * 16 + p;
   if (time_avg) {
@@ -870,36 +886,34 @@ __global__ void k_dss_tracers(EulerArgs<R> a, int E, int time_avg) {
   }
 }
 
-template <typename R>
-__global__ void k_dss_field(int E, const R* __restrict__ src, R* dst, const R* __restrict__ rsmp,
-                            DssTable tab) {
+__global__ void k_dss_field(int E, const double* __restrict__ src, double* dst,
+                            const double* __restrict__ rsmp, DssTable tab) {
   const int idx = blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= E * NLEV * 16) return;
   const int e = idx / (NLEV * 16), l = (idx / 16) % NLEV, p = idx & 15;
   double v = dss_gather(src, NLEV * 16, 16, e, l, p, tab);
-  if (rsmp) v *= (double)rsmp[e * 16 + p];
-  dst[idx] = (R)v;
+  if (rsmp) v *= rsmp[e * 16 + p];
+  dst[idx] = v;
 }
 
 // Generic in-place DSS through a scratch copy.
-template <typename R>
-__global__ void k_copy_fields(int E, int nf, const R* base, long long fs, long long es, int ls, R* scr) {
+__global__ void k_copy_fields(int E, int nf, const double* base, long long fs, long long es, int ls,
+                              double* scr) {
   const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= (long long)E * nf * NLEV * 16) return;
   const int p = idx & 15, l = (idx / 16) % NLEV, f = (idx / (16 * NLEV)) % nf;
   const int e = idx / (16LL * NLEV * nf);
   scr[idx] = base[(size_t)f * fs + (size_t)e * es + (size_t)l * ls + p];
 }
-template <typename R>
-__global__ void k_dss_from_copy(int E, int nf, R* base, long long fs, long long es, int ls, const R* scr,
-                                const R* rsmp, DssTable tab) {
+__global__ void k_dss_from_copy(int E, int nf, double* base, long long fs, long long es, int ls,
+                                const double* scr, const double* rsmp, DssTable tab) {
   const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= (long long)E * nf * NLEV * 16) return;
   const int p = idx & 15, l = (idx / 16) % NLEV, f = (idx / (16 * NLEV)) % nf;
   const int e = idx / (16LL * NLEV * nf);
   double v = dss_gather(scr + (size_t)f * NLEV * 16, (long long)nf * NLEV * 16, 16, e, l, p, tab);
-  if (rsmp) v *= (double)rsmp[e * 16 + p];
-  base[(size_t)f * fs + (size_t)e * es + (size_t)l * ls + p] = (R)v;
+  if (rsmp) v *= rsmp[e * 16 + p];
+  base[(size_t)f * fs + (size_t)e * es + (size_t)l * ls + p] = v;
 }
 
 // ======================================================================================
@@ -933,8 +947,7 @@ __device__ void warp_scan_incl(double* x, int n) {
   }
 }
 
-template <typename R>
-__global__ void __launch_bounds__(RT) k_remap(RemapArgs<R> a) {
+__global__ void __launch_bounds__(RT) k_remap(RemapArgs a) {
   __shared__ double src[NLEV], tgt[NLEV], pio[NLEV + 2], pin[NLEV + 1], Dp[NLEV + 4], z2[NLEV];
   __shared__ int kid[NLEV];
   __shared__ double g[10][NLEV + 2];
@@ -944,7 +957,7 @@ __global__ void __launch_bounds__(RT) k_remap(RemapArgs<R> a) {
   double* D = Dp + 2;
   double* A = Ap + 2;
   const size_t sb = ((size_t)e * NTL + a.np1) * NLEV * 16 + p;
-  for (int l = tid; l < NLEV; l += RT) src[l] = (double)a.dp[sb + (size_t)l * 16];
+  for (int l = tid; l < NLEV; l += RT) src[l] = a.dp[sb + (size_t)l * 16];
   __syncthreads();
   if (tid == 0) {  // compute_ps_v, sequential as in the reference
     double ps = 0.0;
@@ -1013,8 +1026,8 @@ __global__ void __launch_bounds__(RT) k_remap(RemapArgs<R> a) {
     // the mass below interface m: mass[1] = 0, mass[m + 1] = sum_{j<m} x_j
     for (int l = tid; l < NLEV; l += RT) {
       double x;
-      if (var < 2) x = (double)a.v[((size_t)e * NTL + a.np1) * NLEV * 32 + (size_t)l * 32 + var * 16 + p] * src[l];
-      else if (var == 2) x = (double)a.T[sb + (size_t)l * 16] * src[l];
+      if (var < 2) x = a.v[((size_t)e * NTL + a.np1) * NLEV * 32 + (size_t)l * 32 + var * 16 + p] * src[l];
+      else if (var == 2) x = a.T[sb + (size_t)l * 16] * src[l];
       else x = a.qdp[((((size_t)e * QTL + a.n0_qdp) * a.Q + (var - 3)) * NLEV + l) * 16 + p];
       col[l] = x;
       A[l] = x / D[l];
@@ -1087,8 +1100,8 @@ __global__ void __launch_bounds__(RT) k_remap(RemapArgs<R> a) {
                         coef[2][kk] * (x2 * x2 * x2 - x1 * x1 * x1) / 3.0;
       const double m2 = mass[kk + 1] + in * D[kk];
       const double out = m2 - m1;
-      if (var < 2) a.v[((size_t)e * NTL + a.np1) * NLEV * 32 + (size_t)k * 32 + var * 16 + p] = (R)(out / tgt[k]);
-      else if (var == 2) a.T[sb + (size_t)k * 16] = (R)(out / tgt[k]);
+      if (var < 2) a.v[((size_t)e * NTL + a.np1) * NLEV * 32 + (size_t)k * 32 + var * 16 + p] = (out / tgt[k]);
+      else if (var == 2) a.T[sb + (size_t)k * 16] = (out / tgt[k]);
       else a.qdp[((((size_t)e * QTL + a.n0_qdp) * a.Q + (var - 3)) * NLEV + k) * 16 + p] = out;
     }
     __syncthreads();
@@ -1145,18 +1158,16 @@ void upload_constants(const double* dvv16, const double* hyai, const double* hyb
   cudaStreamSynchronize(s);
 }
 
-template <typename R>
-void launch_prim_step_init(int E, R* eta, R* vn0, R* omega_p, R* dpa, R* dpb, R* derived_dp, const R* dp,
-                           int n0, int zero_diss, cudaStream_t s) {
+void launch_prim_step_init(int E, double* eta, double* vn0, double* omega_p, double* dpa, double* dpb,
+                           double* derived_dp, const double* dp, int n0, int zero_diss, cudaStream_t s) {
   KScope k("prim_step_init", s);
-  k_prim_step_init<R><<<nblk((long long)E * NLEV * 16, 256), 256, 0, s>>>(E, eta, vn0, omega_p, dpa, dpb,
-                                                                          derived_dp, dp, n0, zero_diss);
+  k_prim_step_init<<<nblk((long long)E * NLEV * 16, 256), 256, 0, s>>>(E, eta, vn0, omega_p, dpa, dpb,
+                                                                       derived_dp, dp, n0, zero_diss);
 }
 
-template <typename R>
-void launch_dp_from_ps(int E, R* dp, const double* ps_v, int n0, double ps0, cudaStream_t s) {
+void launch_dp_from_ps(int E, double* dp, const double* ps_v, int n0, double ps0, cudaStream_t s) {
   KScope k("dp3d_from_ps", s);
-  k_dp_from_ps<R><<<nblk((long long)E * NLEV * 16, 256), 256, 0, s>>>(E, dp, ps_v, n0, ps0);
+  k_dp_from_ps<<<nblk((long long)E * NLEV * 16, 256), 256, 0, s>>>(E, dp, ps_v, n0, ps0);
 }
 
 template <typename R>
@@ -1172,11 +1183,10 @@ void launch_caar(const CaarArgs<R>& a, int E, cudaStream_t s) {
   k_caar<R, LG><<<E, LG * 16, smem, s>>>(a);
 }
 
-template <typename R>
-void launch_dss_state(int E, const R* src, R* v, R* T, R* dp, int np1, const R* rsmp, DssTable t,
-                      cudaStream_t s) {
+void launch_dss_state(int E, const double* src, double* v, double* T, double* dp, int np1,
+                      const double* rsmp, DssTable t, cudaStream_t s) {
   KScope k("dss_caar", s);
-  k_dss_state<R><<<nblk((long long)E * NLEV * 16, 256), 256, 0, s>>>(E, src, v, T, dp, np1, rsmp, t);
+  k_dss_state<<<nblk((long long)E * NLEV * 16, 256), 256, 0, s>>>(E, src, v, T, dp, np1, rsmp, t);
 }
 
 template <typename R>
@@ -1248,51 +1258,35 @@ void launch_euler_step(EulerArgs<R>& a, int E, int time_avg, cudaStream_t s) {
   }
   {
     KScope k("euler_dss_fvar", s);
-    k_dss_field<R><<<nblk((long long)E * NLEV * 16, 256), 256, 0, s>>>(E, a.fscr, a.f_dss, a.m.rspheremp, a.dss);
+    k_dss_field<<<nblk((long long)E * NLEV * 16, 256), 256, 0, s>>>(E, a.fscr, a.f_dss, a.m.rspheremp_d, a.dss);
   }
 }
 
-template <typename R>
-void launch_remap(const RemapArgs<R>& a, cudaStream_t s) {
+void launch_remap(const RemapArgs& a, cudaStream_t s) {
   KScope k("ppm_remap", s);
-  k_remap<R><<<a.nelem * 16, RT, 0, s>>>(a);
+  k_remap<<<a.nelem * 16, RT, 0, s>>>(a);
 }
 
-template <typename R>
 void launch_update_q(int E, int Q, const double* qdp, double* Qc, const double* ps_v, int np1, int np1_qdp,
                      double ps0, cudaStream_t s) {
   if (Q == 0) return;
   KScope k("update_q", s);
-  k_update_q<R><<<nblk((long long)E * Q * NLEV * 16, 256), 256, 0, s>>>(E, Q, qdp, Qc, ps_v, np1, np1_qdp, ps0);
+  k_update_q<<<nblk((long long)E * Q * NLEV * 16, 256), 256, 0, s>>>(E, Q, qdp, Qc, ps_v, np1, np1_qdp, ps0);
 }
 
-template <typename R>
-void launch_dss_inplace(int E, int nf, R* base, long long fs, long long es, int ls, R* scr, const R* rsmp,
-                        DssTable t, cudaStream_t s) {
+void launch_dss_inplace(int E, int nf, double* base, long long fs, long long es, int ls, double* scr,
+                        const double* rsmp, DssTable t, cudaStream_t s) {
   KScope k("dss_generic", s);
   const long long n = (long long)E * nf * NLEV * 16;
-  k_copy_fields<R><<<nblk(n, 256), 256, 0, s>>>(E, nf, base, fs, es, ls, scr);
-  k_dss_from_copy<R><<<nblk(n, 256), 256, 0, s>>>(E, nf, base, fs, es, ls, scr, rsmp, t);
+  k_copy_fields<<<nblk(n, 256), 256, 0, s>>>(E, nf, base, fs, es, ls, scr);
+  k_dss_from_copy<<<nblk(n, 256), 256, 0, s>>>(E, nf, base, fs, es, ls, scr, rsmp, t);
 }
 
-void launch_dss_inplace_d(int E, int nf, double* base, long long fs, long long es, int ls, double* scr,
-                          const double* rsmp, DssTable t, cudaStream_t s) {
-  launch_dss_inplace<double>(E, nf, base, fs, es, ls, scr, rsmp, t, s);
-}
-
-#define HX_INST(R)                                                                                      \
-  template void launch_prim_step_init<R>(int, R*, R*, R*, R*, R*, R*, const R*, int, int, cudaStream_t); \
-  template void launch_dp_from_ps<R>(int, R*, const double*, int, double, cudaStream_t);                \
-  template void launch_caar<R>(const CaarArgs<R>&, int, cudaStream_t);                                  \
-  template void launch_dss_state<R>(int, const R*, R*, R*, R*, int, const R*, DssTable, cudaStream_t);  \
-  template void launch_hv<R>(const HvArgs<R>&, int, cudaStream_t);                                      \
-  template void launch_precompute_divdp<R>(const EulerArgs<R>&, int, cudaStream_t);                     \
-  template void launch_euler_step<R>(EulerArgs<R>&, int, int, cudaStream_t);                            \
-  template void launch_remap<R>(const RemapArgs<R>&, cudaStream_t);                                     \
-  template void launch_update_q<R>(int, int, const double*, double*, const double*, int, int, double,   \
-                                   cudaStream_t);                                                       \
-  template void launch_dss_inplace<R>(int, int, R*, long long, long long, int, R*, const R*, DssTable,  \
-                                      cudaStream_t);
+#define HX_INST(R)                                                                  \
+  template void launch_caar<R>(const CaarArgs<R>&, int, cudaStream_t);              \
+  template void launch_hv<R>(const HvArgs<R>&, int, cudaStream_t);                  \
+  template void launch_precompute_divdp<R>(const EulerArgs<R>&, int, cudaStream_t); \
+  template void launch_euler_step<R>(EulerArgs<R>&, int, int, cudaStream_t);
 HX_INST(double)
 HX_INST(float)
 

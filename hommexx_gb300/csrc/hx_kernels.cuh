@@ -1,9 +1,10 @@
 // hx_kernels.cuh — launch interface of the preqx kernels (implemented in hx_kernels.cu).
 //
-// Every kernel is templated on R, the floating type of the dynamics state and of the
+// Every field lives in HBM in double.  Kernels are templated on R, the type of the
 // sphere-operator arithmetic: double for the FP64 plain form, float for the mixed
-// form.  Vertical scans (pressure, geopotential, omega), DSS accumulation and the PPM
-// remap always run in double; tracer mass Qdp is always stored in double.
+// form.  In both forms the vertical scans (pressure, geopotential, omega), the DSS
+// accumulation, the PPM remap and the final state updates x = spheremp (x0 + dt f)
+// run in double; only tendencies and operators are computed in R.
 #pragma once
 #include <cuda_runtime.h>
 
@@ -18,15 +19,15 @@ void upload_constants(const double* dvv16, const double* hyai73, const double* h
 template <typename R>
 struct CaarArgs {
   MetricP<R> m;
-  R* v;        // [E][3][72][2][16]
-  R* T;        // [E][3][72][16]
-  R* dp;       // [E][3][72][16]
-  R* vn0;      // [E][72][2][16]
-  R* omega_p;  // [E][72][16]
-  R* phi;      // [E][72][16]
+  double* v;        // [E][3][72][2][16]
+  double* T;        // [E][3][72][16]
+  double* dp;       // [E][3][72][16]
+  double* vn0;      // [E][72][2][16]
+  double* omega_p;  // [E][72][16]
+  double* phi;      // [E][72][16]
   const double* qdp;  // [E][2][Q][72][16] (moist only)
   int qsize, n0_qdp;  // n0_qdp < 0: dry
-  R* out;      // pre-DSS result [E][72][4][16]: v0, v1, T, dp3d
+  double* out;      // pre-DSS result [E][72][4][16]: v0, v1, T, dp3d
   int nm1, n0;
   double dt, eta_ave_w, p_top;  // p_top = hyai(0)*ps0
   int rk_combine, n0orig;       // stage 5: nm1 := (5 nm1 - n0orig)/4 first
@@ -36,13 +37,13 @@ template <typename R>
 struct HvArgs {
   MetricP<R> m;
   DssTable dss;
-  R* v;
-  R* T;
-  R* dp;
-  R* dpdiss_ave;
-  R* dpdiss_bih;
-  R* bufA;   // [E][72][4][16]
-  R* bufB;
+  double* v;
+  double* T;
+  double* dp;
+  double* dpdiss_ave;
+  double* dpdiss_bih;
+  double* bufA;   // [E][72][4][16]
+  double* bufB;
   int np1, hsub, consthv;
   double dt, eta_ave_w, nu, nu_s, nu_p, nu_top, nu_ratio1, nu_ratio2;
 };
@@ -51,19 +52,19 @@ template <typename R>
 struct EulerArgs {
   MetricP<R> m;
   DssTable dss;
-  const R* derived_dp;
-  R* divdp;
-  R* divdp_proj;
-  R* vn0;
-  R* dpdiss_ave;
-  R* dpdiss_bih;
-  R* f_dss;     // eta_dot_dpdn / omega_p / divdp_proj selected by the DSS option
-  R* vstar;     // [E][72][2][16]
-  R* dpdissk;   // [E][72][16]
-  R* fscr;      // [E][72][16] scratch for the DSS of f_dss
+  const double* derived_dp;
+  double* divdp;
+  double* divdp_proj;
+  double* vn0;
+  double* dpdiss_ave;
+  double* dpdiss_bih;
+  double* f_dss;     // eta_dot_dpdn / omega_p / divdp_proj selected by the DSS option
+  double* vstar;     // [E][72][2][16]
+  double* dpdissk;   // [E][72][16]
+  double* fscr;      // [E][72][16] scratch for the DSS of f_dss
   double* qdp;  // [E][2][Q][72][16]
-  R* qtens;     // [E][Q][72][16] qtens_biharmonic
-  R* qscr;      // [E][Q][72][16] pre-DSS scratch
+  double* qtens;     // [E][Q][72][16] qtens_biharmonic
+  double* qscr;      // [E][Q][72][16] pre-DSS scratch
   double* qlim;     // [E][Q][2][72]
   double* qlim_tmp;
   const double* dp0;  // [72] device
@@ -73,11 +74,10 @@ struct EulerArgs {
   double dt, rhs_multiplier, rhs_viss, nu_p, nu_q;
 };
 
-template <typename R>
 struct RemapArgs {
-  R* v;
-  R* T;
-  const R* dp;
+  double* v;
+  double* T;
+  const double* dp;
   double* qdp;
   double* ps_v;   // [E][3][16]
   int np1, n0_qdp, Q, remap_alg, nelem;
@@ -85,28 +85,22 @@ struct RemapArgs {
   int* invalid;   // set to 1 on a negative or NaN source thickness
 };
 
-template <typename R> void launch_prim_step_init(int E, R* eta, R* vn0, R* omega_p, R* dpa,
-                                                 R* dpb, R* derived_dp, const R* dp, int n0,
-                                                 int zero_diss, cudaStream_t s);
-template <typename R> void launch_dp_from_ps(int E, R* dp, const double* ps_v, int n0, double ps0,
-                                             cudaStream_t s);
+void launch_prim_step_init(int E, double* eta, double* vn0, double* omega_p, double* dpa,
+                           double* dpb, double* derived_dp, const double* dp, int n0, int zero_diss,
+                           cudaStream_t s);
+void launch_dp_from_ps(int E, double* dp, const double* ps_v, int n0, double ps0, cudaStream_t s);
 template <typename R> void launch_caar(const CaarArgs<R>& a, int E, cudaStream_t s);
-template <typename R> void launch_dss_state(int E, const R* src, R* v, R* T, R* dp, int np1,
-                                            const R* rsmp, DssTable t, cudaStream_t s);
+void launch_dss_state(int E, const double* src, double* v, double* T, double* dp, int np1,
+                      const double* rsmp, DssTable t, cudaStream_t s);
 template <typename R> void launch_hv(const HvArgs<R>& a, int E, cudaStream_t s);
 template <typename R> void launch_precompute_divdp(const EulerArgs<R>& a, int E, cudaStream_t s);
-template <typename R> void launch_euler_step(EulerArgs<R>& a, int E, int dss_opt_time_avg,
-                                             cudaStream_t s);
-template <typename R> void launch_remap(const RemapArgs<R>& a, cudaStream_t s);
-template <typename R> void launch_update_q(int E, int Q, const double* qdp, double* Qc,
-                                           const double* ps_v, int np1, int np1_qdp, double ps0,
-                                           cudaStream_t s);
+template <typename R> void launch_euler_step(EulerArgs<R>& a, int E, int time_avg, cudaStream_t s);
+void launch_remap(const RemapArgs& a, cudaStream_t s);
+void launch_update_q(int E, int Q, const double* qdp, double* Qc, const double* ps_v, int np1,
+                     int np1_qdp, double ps0, cudaStream_t s);
 // Generic DSS of nf fields (field f at base + f*fs, element stride es, level stride ls).
-template <typename R> void launch_dss_inplace(int E, int nf, R* base, long long fs, long long es,
-                                              int ls, R* scratch, const R* rsmp, DssTable t,
-                                              cudaStream_t s);
-void launch_dss_inplace_d(int E, int nf, double* base, long long fs, long long es, int ls,
-                          double* scratch, const double* rsmp, DssTable t, cudaStream_t s);
+void launch_dss_inplace(int E, int nf, double* base, long long fs, long long es, int ls,
+                        double* scratch, const double* rsmp, DssTable t, cudaStream_t s);
 
 // Name of the last kernel launched by the wrappers above (for per-kernel timing).
 const char* last_kernel_name();

@@ -179,8 +179,8 @@ def test_mixed_precision_close(pair):
     o.run_subcycle(DT)
     rg, ro = g.push_results(), o.push_results()
     errs = {k: H.rel_err(rg[k], ro[k]) for k in ("T", "dp3d", "v", "Qdp", "ps_v")}
-    assert errs["T"] < 1e-5 and errs["dp3d"] < 1e-5, errs
-    assert errs["v"] < 1e-3 and errs["Qdp"] < 1e-4, errs
+    assert errs["T"] < 1e-6 and errs["dp3d"] < 1e-6 and errs["ps_v"] < 1e-7, errs
+    assert errs["v"] < 1e-5 and errs["Qdp"] < 1e-5, errs
 
 
 def test_negative_thickness_reports_101(gpu_path):
