@@ -386,6 +386,8 @@ def main():
                          "e2e": sypd(args.steps, mx["te"]) * world,
                          "ms_per_step": mx["t"] / args.steps * 1e3,
                          "top_kernel": {k: mrows[0][k] for k in ("kernel", "share", "gbs")},
+                         "kernels": [{k: (round(v, 4) if isinstance(v, float) else v)
+                                      for k, v in r.items()} for r in mrows],
                          "clocks": mx["clocks"]}
         if "mixed_error" in out:
             line["mixed"]["error_vs_fp64"] = out["mixed_error"]

@@ -433,7 +433,7 @@ struct BackendT : Backend {
     a.np1 = np1; a.n0_qdp = np1_qdp; a.Q = Q; a.remap_alg = s.prm.remap_alg; a.nelem = E;
     a.ps0 = s.ps0; a.hyai0 = s.hyai[0]; a.invalid = invalid;
     ck(cudaMemsetAsync(invalid, 0, sizeof(int), g_stream), "memset");
-    hx::launch_remap(a, g_stream);
+    hx::launch_remap<R>(a, g_stream);
     post("remap");
   }
   int remap_status() {

@@ -919,127 +919,190 @@ __global__ void k_dss_from_copy(int E, int nf, double* base, long long fs, long 
 // ======================================================================================
 // PPM vertical remap (RemapFunctor + PpmVertRemap, rsplit > 0), one CTA per column.
 // ======================================================================================
-constexpr int RT = 64;  // threads per column CTA
+constexpr int RCOLS = 4;            // columns (warps) per CTA
+constexpr int RT = RCOLS * 32;
+// Shared-memory slots of one column (doubles).
+constexpr int R_D = 0;                 // D[-2 .. 73]  (source thickness, ghosts)
+constexpr int R_PIO = R_D + 76;        // pio[0 .. 73]
+constexpr int R_PIN = R_PIO + 74;      // pin[0 .. 72]
+constexpr int R_Z2 = R_PIN + 74;       // z2[0 .. 71]
+constexpr int R_KID = R_Z2 + 72;       // kid[0 .. 71] (ints, 36 doubles)
+constexpr int R_TGT = R_KID + 36;      // target thickness
+constexpr int R_G = R_TGT + 72;        // ppmdx grids g[10][74]
+constexpr int R_A = R_G + 740;         // cell means A[-2 .. 73]
+constexpr int R_MASS = R_A + 76;       // mass[0 .. 73]
+constexpr int R_DMA = R_MASS + 74;     // dma[0 .. 73]
+constexpr int R_AI = R_DMA + 74;       // ai[0 .. 72]
+constexpr int R_COEF = R_AI + 74;      // coef[3][72]
+constexpr int R_COL = R_COEF + 216;    // doubles per column
 
-// Warp-0 inclusive scan of n <= 96 values in place (lanes own 3 consecutive values).
-__device__ void warp_scan_incl(double* x, int n) {
-  const int lane = threadIdx.x & 31;
-  double v[3], run = 0.0;
-#pragma unroll
-  for (int k = 0; k < 3; ++k) {
-    const int i = lane * 3 + k;
-    v[k] = i < n ? x[i] : 0.0;
-    run += v[k];
-  }
-  double incl = run;
+// Exclusive prefix over the warp of one value per lane.
+__device__ __forceinline__ double warp_excl_scan(double v, int lane) {
+  double incl = v;
 #pragma unroll
   for (int off = 1; off < 32; off <<= 1) {
     const double y = __shfl_up_sync(FULL, incl, off);
     if (lane >= off) incl += y;
   }
-  double ex = __shfl_up_sync(FULL, incl, 1);
-  if (lane == 0) ex = 0.0;
+  const double ex = __shfl_up_sync(FULL, incl, 1);
+  return lane == 0 ? 0.0 : ex;
+}
+__device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
-  for (int k = 0; k < 3; ++k) {
-    const int i = lane * 3 + k;
-    ex += v[k];
-    if (i < n) x[i] = ex;
-  }
+  for (int off = 16; off >= 1; off >>= 1) v += __shfl_xor_sync(FULL, v, off);
+  return v;
 }
 
+// PPM vertical remap (RemapFunctor + PpmVertRemap, rsplit > 0), one warp per column:
+// lane L owns levels 3L .. 3L+2 (L < 24) for level work and interfaces j = 3L .. 3L+2
+// (L < 25) for the grid quantities; column scans are warp shuffles, phases are
+// separated by __syncwarp only.  The reconstruction (cell means, slopes, edge values,
+// parabola coefficients, ppmdx grids) runs in R; the cumulative masses and the
+// integrals of the parabolas run in double, so the remap conserves mass in FP64 in
+// both forms.
+template <typename R>
 __global__ void __launch_bounds__(RT) k_remap(RemapArgs a) {
-  __shared__ double src[NLEV], tgt[NLEV], pio[NLEV + 2], pin[NLEV + 1], Dp[NLEV + 4], z2[NLEV];
-  __shared__ int kid[NLEV];
-  __shared__ double g[10][NLEV + 2];
-  __shared__ double Ap[NLEV + 4], mass[NLEV + 2], dma[NLEV + 2], ai[NLEV + 1], coef[3][NLEV], col[NLEV];
-  __shared__ double ps_s;
-  const int cidx = blockIdx.x, e = cidx >> 4, p = cidx & 15, tid = threadIdx.x;
-  double* D = Dp + 2;
-  double* A = Ap + 2;
+  extern __shared__ double rsm[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int cidx = blockIdx.x * RCOLS + warp;
+  if (cidx >= a.nelem * 16) return;  // whole warp leaves together; no CTA barriers below
+  const int e = cidx >> 4, p = cidx & 15;
+  double* sm = rsm + warp * R_COL;
+  double* D = sm + R_D + 2;
+  double* pio = sm + R_PIO;
+  double* pin = sm + R_PIN;
+  double* z2 = sm + R_Z2;
+  int* kid = reinterpret_cast<int*>(sm + R_KID);
+  double* tgt = sm + R_TGT;
+  double* g = sm + R_G;  // g[c * 74 + j]
+  double* A = sm + R_A + 2;
+  double* mass = sm + R_MASS;
+  double* dma = sm + R_DMA;
+  double* ai = sm + R_AI;
+  double* coef = sm + R_COEF;  // coef[c * 72 + j]
+  const bool own = lane < 24;
+  const int l0 = 3 * lane;
   const size_t sb = ((size_t)e * NTL + a.np1) * NLEV * 16 + p;
-  for (int l = tid; l < NLEV; l += RT) src[l] = a.dp[sb + (size_t)l * 16];
-  __syncthreads();
-  if (tid == 0) {  // compute_ps_v, sequential as in the reference
-    double ps = 0.0;
-    for (int l = 0; l < NLEV; ++l) ps += src[l];
-    ps += a.hyai0 * a.ps0;
-    ps_s = ps;
-    a.ps_v[((size_t)e * NTL + a.np1) * 16 + p] = ps;
+  const size_t vb = ((size_t)e * NTL + a.np1) * NLEV * 32 + p;
+  // source thickness and surface pressure (compute_ps_v)
+  double s3[3] = {0.0, 0.0, 0.0};
+  if (own) {
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      s3[k] = a.dp[sb + (size_t)(l0 + k) * 16];
+      D[l0 + k] = s3[k];
+      if (isnan(s3[k]) || s3[k] < 0.0) atomicExch(a.invalid, 1);
+    }
   }
-  __syncthreads();
-  const double ps = ps_s;
-  for (int l = tid; l < NLEV; l += RT) {
-    tgt[l] = (c_hyai[l + 1] - c_hyai[l]) * a.ps0 + (c_hybi[l + 1] - c_hybi[l]) * ps;
-    const double s = src[l];
-    if (isnan(s) || s < 0.0) atomicExch(a.invalid, 1);
-    D[l] = s;
-    pio[l + 1] = s;   // inclusive-scan input shifted by one
-    pin[l + 1] = tgt[l];
+  const double ps = warp_sum(s3[0] + s3[1] + s3[2]) + a.hyai0 * a.ps0;
+  if (lane == 0) a.ps_v[((size_t)e * NTL + a.np1) * 16 + p] = ps;
+  double t3[3] = {0.0, 0.0, 0.0};
+  if (own) {
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const int l = l0 + k;
+      t3[k] = (c_hyai[l + 1] - c_hyai[l]) * a.ps0 + (c_hybi[l + 1] - c_hybi[l]) * ps;
+      tgt[l] = t3[k];
+    }
   }
-  __syncthreads();
-  if (tid < 32) {
-    warp_scan_incl(pio + 1, NLEV);
-    warp_scan_incl(pin + 1, NLEV);
+  // compute_partitions: pio, pin cumulative thickness
+  {
+    double ex = warp_excl_scan(s3[0] + s3[1] + s3[2], lane);
+    double ey = warp_excl_scan(t3[0] + t3[1] + t3[2], lane);
+    if (own) {
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        pio[l0 + k] = ex;
+        pin[l0 + k] = ey;
+        ex += s3[k];
+        ey += t3[k];
+      }
+    }
+    if (lane == 23) {
+      pio[NLEV] = ex;
+      pio[NLEV + 1] = ex + 1.0;
+      pin[NLEV] = ex;  // the column's total mass does not change
+    }
   }
-  __syncthreads();
-  if (tid == 0) {
-    pio[0] = 0.0;
-    pin[0] = 0.0;
-    pio[NLEV + 1] = pio[NLEV] + 1.0;
-    pin[NLEV] = pio[NLEV];
+  __syncwarp();
+  if (lane == 0) {
     D[-1] = D[0];
     D[-2] = D[1];
     D[NLEV] = D[NLEV - 1];
     D[NLEV + 1] = D[NLEV - 2];
   }
-  __syncthreads();
-  for (int k = tid; k < NLEV; k += RT) {  // compute_integral_bounds
-    int kk = k + 1;
-    while (kk < NLEV + 2 && pio[kk - 1] <= pin[k + 1]) kk++;
-    kk--;
-    if (kk == NLEV + 1) kk = NLEV;
-    if (kk < 1) {  // only reachable with a non-monotone (invalid) source grid
-      kk = 1;
-      atomicExch(a.invalid, 1);
-    }
-    kid[k] = kk - 1;
-    z2[k] = (pin[k + 1] - (pio[kk - 1] + pio[kk]) * 0.5) / D[kk - 1];
-  }
-  for (int j = tid; j < NLEV + 2; j += RT) {  // compute_grids
-    g[0][j] = D[j - 1] / (D[j - 2] + D[j - 1] + D[j]);
-    g[1][j] = (2.0 * D[j - 2] + D[j - 1]) / (D[j - 1] + D[j]);
-    g[2][j] = (D[j - 1] + 2.0 * D[j]) / (D[j - 2] + D[j - 1]);
-    if (j < NLEV + 1) {
-      g[3][j] = D[j - 1] / (D[j - 1] + D[j]);
-      g[4][j] = 1.0 / (D[j - 2] + D[j - 1] + D[j] + D[j + 1]);
-      g[5][j] = (2.0 * D[j - 1] * D[j]) / (D[j - 1] + D[j]);
-      g[6][j] = (D[j - 2] + D[j - 1]) / (2.0 * D[j - 1] + D[j]);
-      g[7][j] = (D[j + 1] + D[j]) / (2.0 * D[j] + D[j - 1]);
-      g[8][j] = D[j - 1] * (D[j - 2] + D[j - 1]) / (2.0 * D[j - 1] + D[j]);
-      g[9][j] = D[j] * (D[j] + D[j + 1]) / (D[j - 1] + 2.0 * D[j]);
+  __syncwarp();
+  // compute_integral_bounds
+  if (own) {
+#pragma unroll
+    for (int k3 = 0; k3 < 3; ++k3) {
+      const int k = l0 + k3;
+      int kk = k + 1;
+      while (kk < NLEV + 2 && pio[kk - 1] <= pin[k + 1]) kk++;
+      kk--;
+      if (kk == NLEV + 1) kk = NLEV;
+      if (kk < 1) {  // only reachable with a non-monotone (invalid) source grid
+        kk = 1;
+        atomicExch(a.invalid, 1);
+      }
+      kid[k] = kk - 1;
+      z2[k] = (pin[k + 1] - (pio[kk - 1] + pio[kk]) * 0.5) / D[kk - 1];
     }
   }
-  __syncthreads();
+  // compute_grids (in R)
+  if (lane < 25) {
+#pragma unroll
+    for (int k3 = 0; k3 < 3; ++k3) {
+      const int j = 3 * lane + k3;
+      if (j < NLEV + 2) {
+        const R dm2 = (R)D[j - 2], dm1 = (R)D[j - 1], d0 = (R)D[j];
+        g[0 * 74 + j] = (double)(dm1 / (dm2 + dm1 + d0));
+        g[1 * 74 + j] = (double)((R(2) * dm2 + dm1) / (dm1 + d0));
+        g[2 * 74 + j] = (double)((dm1 + R(2) * d0) / (dm2 + dm1));
+        if (j < NLEV + 1) {
+          const R dp1 = (R)D[j + 1];
+          g[3 * 74 + j] = (double)(dm1 / (dm1 + d0));
+          g[4 * 74 + j] = (double)(R(1) / (dm2 + dm1 + d0 + dp1));
+          g[5 * 74 + j] = (double)((R(2) * dm1 * d0) / (dm1 + d0));
+          g[6 * 74 + j] = (double)((dm2 + dm1) / (R(2) * dm1 + d0));
+          g[7 * 74 + j] = (double)((dp1 + d0) / (R(2) * d0 + dm1));
+          g[8 * 74 + j] = (double)(dm1 * (dm2 + dm1) / (R(2) * dm1 + d0));
+          g[9 * 74 + j] = (double)(d0 * (d0 + dp1) / (dm1 + R(2) * d0));
+        }
+      }
+    }
+  }
+  __syncwarp();
   const int nvar = 3 + a.Q;
+#pragma unroll 1
   for (int var = 0; var < nvar; ++var) {
-    // load the field (states in extrinsic form v dp, T dp); mass[1 + m] is scanned into
-    // the mass below interface m: mass[1] = 0, mass[m + 1] = sum_{j<m} x_j
-    for (int l = tid; l < NLEV; l += RT) {
-      double x;
-      if (var < 2) x = a.v[((size_t)e * NTL + a.np1) * NLEV * 32 + (size_t)l * 32 + var * 16 + p] * src[l];
-      else if (var == 2) x = a.T[sb + (size_t)l * 16] * src[l];
-      else x = a.qdp[((((size_t)e * QTL + a.n0_qdp) * a.Q + (var - 3)) * NLEV + l) * 16 + p];
-      col[l] = x;
-      A[l] = x / D[l];
-      if (l < NLEV - 1) mass[l + 2] = x;
+    // extrinsic values (v dp, T dp for the states; Qdp as is), cell means, masses
+    double x3[3] = {0.0, 0.0, 0.0};
+    if (own) {
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        const int l = l0 + k;
+        if (var < 2) x3[k] = a.v[vb + (size_t)l * 32 + var * 16] * s3[k];
+        else if (var == 2) x3[k] = a.T[sb + (size_t)l * 16] * s3[k];
+        else x3[k] = a.qdp[((((size_t)e * QTL + a.n0_qdp) * a.Q + (var - 3)) * NLEV + l) * 16 + p];
+        if constexpr (kF32<R>) A[l] = (double)((R)x3[k] / (R)s3[k]);
+        else A[l] = x3[k] / s3[k];
+      }
     }
-    if (tid == 0) {
-      mass[0] = 0.0;
-      mass[1] = 0.0;
+    {
+      double ex = warp_excl_scan(x3[0] + x3[1] + x3[2], lane);
+      if (own) {
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+          mass[l0 + k + 1] = ex;
+          ex += x3[k];
+        }
+      }
+      if (lane == 23) mass[NLEV + 1] = ex;  // mass[NLEV] + x[NLEV-1]
+      if (lane == 0) mass[0] = 0.0;
     }
-    __syncthreads();
-    if (tid < 32) warp_scan_incl(mass + 1, NLEV);
-    if (tid == 32) {
+    __syncwarp();
+    if (lane == 0) {
       if (a.remap_alg == 3) {
         A[-1] = A[-2] = A[0];
         A[NLEV] = A[NLEV + 1] = A[NLEV - 1];
@@ -1050,61 +1113,88 @@ __global__ void __launch_bounds__(RT) k_remap(RemapArgs a) {
         A[NLEV + 1] = A[NLEV - 2];
       }
     }
-    __syncthreads();
-    for (int j = tid; j < NLEV + 2; j += RT) {
-      if ((A[j] - A[j - 1]) * (A[j - 1] - A[j - 2]) > 0.0) {
-        const double da = g[0][j] * (g[1][j] * (A[j] - A[j - 1]) + g[2][j] * (A[j - 1] - A[j - 2]));
-        dma[j] = fmin(fmin(fabs(da), 2.0 * fabs(A[j - 1] - A[j - 2])), 2.0 * fabs(A[j] - A[j - 1])) *
-                 copysign(1.0, da);
-      } else {
-        dma[j] = 0.0;
+    __syncwarp();
+    // compute_ppm: slopes dma (j in 0 .. 73)
+    if (lane < 25) {
+#pragma unroll
+      for (int k3 = 0; k3 < 3; ++k3) {
+        const int j = 3 * lane + k3;
+        if (j < NLEV + 2) {
+          const R a0 = (R)A[j], am1 = (R)A[j - 1], am2 = (R)A[j - 2];
+          R r = R(0);
+          if ((a0 - am1) * (am1 - am2) > R(0)) {
+            const R da = (R)g[0 * 74 + j] * ((R)g[1 * 74 + j] * (a0 - am1) + (R)g[2 * 74 + j] * (am1 - am2));
+            r = fmin(fmin(fabs(da), R(2) * fabs(am1 - am2)), R(2) * fabs(a0 - am1)) * copysign(R(1), da);
+          }
+          dma[j] = (double)r;
+        }
       }
     }
-    if (tid == 0) mass[NLEV + 1] = mass[NLEV] + col[NLEV - 1];
-    __syncthreads();
-    for (int j = tid; j < NLEV + 1; j += RT) {
-      ai[j] = A[j - 1] + g[3][j] * (A[j] - A[j - 1]) +
-              g[4][j] * (g[5][j] * (g[6][j] - g[7][j]) * (A[j] - A[j - 1]) - g[8][j] * dma[j + 1] +
-                         g[9][j] * dma[j]);
-    }
-    __syncthreads();
-    for (int jp = tid; jp < NLEV; jp += RT) {
-      const int j = jp + 1;
-      double al = ai[j - 1], ar = ai[j];
-      const double cm = A[j - 1];
-      if ((ar - cm) * (cm - al) <= 0.) { al = cm; ar = cm; }
-      if ((ar - al) * (cm - (al + ar) / 2.0) > (ar - al) * (ar - al) / 6.0) al = 3.0 * cm - 2.0 * ar;
-      if ((ar - al) * (cm - (al + ar) / 2.0) < -(ar - al) * (ar - al) / 6.0) ar = 3.0 * cm - 2.0 * al;
-      coef[0][jp] = 1.5 * cm - (al + ar) / 4.0;
-      coef[1][jp] = ar - al;
-      coef[2][jp] = 3.0 * (-2.0 * cm + (al + ar));
-      if (a.remap_alg == 2 && (jp < 2 || jp >= NLEV - 2)) {  // PpmFixedParabola
-        coef[0][jp] = A[jp];
-        coef[1][jp] = 0.0;
-        coef[2][jp] = 0.0;
+    __syncwarp();
+    // edge values ai (j in 0 .. 72)
+    if (lane < 25) {
+#pragma unroll
+      for (int k3 = 0; k3 < 3; ++k3) {
+        const int j = 3 * lane + k3;
+        if (j < NLEV + 1) {
+          const R a0 = (R)A[j], am1 = (R)A[j - 1];
+          ai[j] = (double)(am1 + (R)g[3 * 74 + j] * (a0 - am1) +
+                           (R)g[4 * 74 + j] * ((R)g[5 * 74 + j] * ((R)g[6 * 74 + j] - (R)g[7 * 74 + j]) * (a0 - am1) -
+                                               (R)g[8 * 74 + j] * (R)dma[j + 1] + (R)g[9 * 74 + j] * (R)dma[j]));
+        }
       }
     }
-    __syncthreads();
-    for (int k = tid; k < NLEV; k += RT) {  // compute_remap, GPU form
-      double m1 = 0.0;
-      if (k > 0) {
-        const int kk = kid[k - 1];
-        const double x2 = z2[k - 1], x1 = -0.5;
-        const double in = (coef[0][kk] * (x2 - x1) + coef[1][kk] * (x2 * x2 - x1 * x1) / 2.0) +
-                          coef[2][kk] * (x2 * x2 * x2 - x1 * x1 * x1) / 3.0;
-        m1 = mass[kk + 1] + in * D[kk];
+    __syncwarp();
+    // monotone parabola coefficients per cell
+    if (own) {
+#pragma unroll
+      for (int k3 = 0; k3 < 3; ++k3) {
+        const int jp = l0 + k3;
+        R al = (R)ai[jp], ar = (R)ai[jp + 1];
+        const R cm = (R)A[jp];
+        if ((ar - cm) * (cm - al) <= R(0)) { al = cm; ar = cm; }
+        if ((ar - al) * (cm - (al + ar) / R(2)) > (ar - al) * (ar - al) / R(6)) al = R(3) * cm - R(2) * ar;
+        if ((ar - al) * (cm - (al + ar) / R(2)) < -(ar - al) * (ar - al) / R(6)) ar = R(3) * cm - R(2) * al;
+        R c0 = R(1.5) * cm - (al + ar) / R(4), c1 = ar - al, c2 = R(3) * (R(-2) * cm + (al + ar));
+        if (a.remap_alg == 2 && (jp < 2 || jp >= NLEV - 2)) {  // PpmFixedParabola
+          c0 = cm;
+          c1 = R(0);
+          c2 = R(0);
+        }
+        coef[0 * 72 + jp] = (double)c0;
+        coef[1 * 72 + jp] = (double)c1;
+        coef[2 * 72 + jp] = (double)c2;
       }
-      const int kk = kid[k];
-      const double x2 = z2[k], x1 = -0.5;
-      const double in = (coef[0][kk] * (x2 - x1) + coef[1][kk] * (x2 * x2 - x1 * x1) / 2.0) +
-                        coef[2][kk] * (x2 * x2 * x2 - x1 * x1 * x1) / 3.0;
-      const double m2 = mass[kk + 1] + in * D[kk];
-      const double out = m2 - m1;
-      if (var < 2) a.v[((size_t)e * NTL + a.np1) * NLEV * 32 + (size_t)k * 32 + var * 16 + p] = (out / tgt[k]);
-      else if (var == 2) a.T[sb + (size_t)k * 16] = (out / tgt[k]);
-      else a.qdp[((((size_t)e * QTL + a.n0_qdp) * a.Q + (var - 3)) * NLEV + k) * 16 + p] = out;
     }
-    __syncthreads();
+    __syncwarp();
+    // compute_remap: mass below each new interface, in double; new cell masses are
+    // differences of consecutive interface masses (the lower one from the next lane).
+    double m2[3] = {0.0, 0.0, 0.0};
+    if (own) {
+#pragma unroll
+      for (int k3 = 0; k3 < 3; ++k3) {
+        const int k = l0 + k3;
+        const int kk = kid[k];
+        const double x2 = z2[k], x1 = -0.5;
+        const double in = (coef[kk] * (x2 - x1) + coef[72 + kk] * (x2 * x2 - x1 * x1) / 2.0) +
+                          coef[144 + kk] * (x2 * x2 * x2 - x1 * x1 * x1) / 3.0;
+        m2[k3] = mass[kk + 1] + in * D[kk];
+      }
+    }
+    double below = __shfl_up_sync(FULL, m2[2], 1);
+    if (lane == 0) below = 0.0;
+    if (own) {
+#pragma unroll
+      for (int k3 = 0; k3 < 3; ++k3) {
+        const int k = l0 + k3;
+        const double m1 = k3 == 0 ? below : m2[k3 - 1];
+        const double out = m2[k3] - m1;
+        if (var < 2) a.v[vb + (size_t)k * 32 + var * 16] = out / t3[k3];
+        else if (var == 2) a.T[sb + (size_t)k * 16] = out / t3[k3];
+        else a.qdp[((((size_t)e * QTL + a.n0_qdp) * a.Q + (var - 3)) * NLEV + k) * 16 + p] = out;
+      }
+    }
+    __syncwarp();
   }
 }
 
@@ -1262,9 +1352,16 @@ void launch_euler_step(EulerArgs<R>& a, int E, int time_avg, cudaStream_t s) {
   }
 }
 
+template <typename R>
 void launch_remap(const RemapArgs& a, cudaStream_t s) {
+  const size_t smem = (size_t)RCOLS * R_COL * sizeof(double);
+  static bool init = false;
+  if (!init) {
+    cudaFuncSetAttribute(k_remap<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    init = true;
+  }
   KScope k("ppm_remap", s);
-  k_remap<<<a.nelem * 16, RT, 0, s>>>(a);
+  k_remap<R><<<(a.nelem * 16 + RCOLS - 1) / RCOLS, RT, smem, s>>>(a);
 }
 
 void launch_update_q(int E, int Q, const double* qdp, double* Qc, const double* ps_v, int np1, int np1_qdp,
@@ -1286,7 +1383,8 @@ void launch_dss_inplace(int E, int nf, double* base, long long fs, long long es,
   template void launch_caar<R>(const CaarArgs<R>&, int, cudaStream_t);              \
   template void launch_hv<R>(const HvArgs<R>&, int, cudaStream_t);                  \
   template void launch_precompute_divdp<R>(const EulerArgs<R>&, int, cudaStream_t); \
-  template void launch_euler_step<R>(EulerArgs<R>&, int, int, cudaStream_t);
+  template void launch_euler_step<R>(EulerArgs<R>&, int, int, cudaStream_t);  \
+  template void launch_remap<R>(const RemapArgs&, cudaStream_t);
 HX_INST(double)
 HX_INST(float)
 

@@ -95,7 +95,7 @@ void launch_dss_state(int E, const double* src, double* v, double* T, double* dp
 template <typename R> void launch_hv(const HvArgs<R>& a, int E, cudaStream_t s);
 template <typename R> void launch_precompute_divdp(const EulerArgs<R>& a, int E, cudaStream_t s);
 template <typename R> void launch_euler_step(EulerArgs<R>& a, int E, int time_avg, cudaStream_t s);
-void launch_remap(const RemapArgs& a, cudaStream_t s);
+template <typename R> void launch_remap(const RemapArgs& a, cudaStream_t s);
 void launch_update_q(int E, int Q, const double* qdp, double* Qc, const double* ps_v, int np1,
                      int np1_qdp, double ps0, cudaStream_t s);
 // Generic DSS of nf fields (field f at base + f*fs, element stride es, level stride ls).
