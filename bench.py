@@ -297,11 +297,12 @@ def cpu_baseline(seconds_budget: float = 20.0, L=None):
     if own:
         L.finalize()
     return dict(value=sypd(n, t), unit="SYPD", cores=threads, kind="port",
-                sample=f"ne30 L72 q10, {n} remap interval(s) of 3 x 300 s steps, "
+                sample=f"ne{NE} L72 q{QSIZE}, {n} remap interval(s) of 3 x 300 s steps, "
                        f"{t:.1f} s on {threads} OpenMP threads")
 
 
 def main():
+    global NE, QSIZE
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
@@ -310,8 +311,11 @@ def main():
     ap.add_argument("--no-mixed", action="store_true")
     ap.add_argument("--error-days", type=float, default=1.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--ne", type=int, default=NE, help="cubed-sphere resolution (profiling cases)")
+    ap.add_argument("--qsize", type=int, default=QSIZE, help="tracer count (profiling cases)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    NE, QSIZE = args.ne, args.qsize
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -322,8 +326,8 @@ def main():
         import torch.distributed as dist
         dist.init_process_group("gloo")
 
-    config = {"workload": "preqx step ne30 L72 np4 qsize10, dt 300 s, rsplit 3, hv nu 1e15 x3 subcycles, "
-                          "limiter 8, PPM mirrored remap",
+    config = {"workload": f"preqx step ne{NE} L72 np4 qsize{QSIZE}, dt 300 s, rsplit 3, hv nu 1e15 x3 "
+                          "subcycles, limiter 8, PPM mirrored remap",
               "elements": 6 * NE * NE, "nlev": 72, "qsize": QSIZE, "step": "one remap interval "
               "(prim_run_subcycle_c) = 3 x 300 s", "l2": "working set 1.9 GB >> 129 MB L2, no flush",
               "parallelism": f"replicas x{world}" if world > 1 else "single GPU"}
@@ -342,7 +346,7 @@ def main():
         L.finalize()
         v = sypd(len(times), float(np.sum(times)))
         per = [dict(value=v, unit="SYPD", cores=threads, kind="port",
-                    sample=f"ne30 L72 q10, one remap interval (3 x 300 s) per step, "
+                    sample=f"ne{NE} L72 q{QSIZE}, one remap interval (3 x 300 s) per step, "
                            f"{np.mean(times):.2f} s per step on {threads} OpenMP threads")]
         line = {"metric": "ne30L72 SYPD (FP64 preqx step)", "value": v, "unit": "SYPD",
                 "impl": "reference", "n_gpus": 0, "steps": args.steps, "warmup": args.warmup,
@@ -380,7 +384,7 @@ def main():
     }
     if "mixed" in out:
         mx = out["mixed"]
-        mrows = roofline(mx["stats"], E, QSIZE, 4, args.steps)
+        mrows = roofline(mx["stats"], E, QSIZE, 8, args.steps)
         line["mixed"] = {"value": sypd(args.steps, mx["t"]) * world, "unit": "SYPD",
                          "speedup_vs_fp64": f["t"] / mx["t"],
                          "e2e": sypd(args.steps, mx["te"]) * world,

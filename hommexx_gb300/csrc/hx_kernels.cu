@@ -105,6 +105,7 @@ struct Pt {
 template <typename R>
 struct PM {
   R di00, di01, di10, di11, d00, d01, d10, d11, md, fdiv, sp, mp, a00, a01, a10, a11, rsp;
+  R l00, l01, l10, l11;  // spheremp * (Dinv Dinv^T) * rrearth, for laplace_simple
   __device__ __forceinline__ void load(const MetricP<R>& m, int e, int p) {
     const R* Di = m.Dinv + (size_t)e * 64;
     const R* D = m.D + (size_t)e * 64;
@@ -117,6 +118,12 @@ struct PM {
     rsp = m.rspheremp[(size_t)e * 16 + p];
     mp = m.mp[(size_t)e * 16 + p];
     a00 = Mi[p] * md; a01 = Mi[16 + p] * md; a10 = Mi[32 + p] * md; a11 = Mi[48 + p] * md;
+    // c = (Dinv^T-contraction of the Dinv-contraction): c_a = sum_b K_ab v_b with
+    // K_ab = sum_c Dinv(c,a) Dinv(c,b) in the reference's C++ indices.
+    l00 = sp * (di00 * di00 + di10 * di10) * rre<R>();
+    l01 = sp * (di00 * di01 + di10 * di11) * rre<R>();
+    l10 = sp * (di01 * di00 + di11 * di10) * rre<R>();
+    l11 = sp * (di01 * di01 + di11 * di11) * rre<R>();
   }
 };
 
@@ -151,11 +158,15 @@ __device__ __forceinline__ R divergence_sphere_wk(const Pt<R>& t, const PM<R>& m
   return -(t.wrow(w0) + t.wcol(w1)) * rre<R>();
 }
 
+// laplace_simple = divergence_sphere_wk(gradient_sphere(s)).  The two metric
+// transforms compose to Dinv Dinv^T = metinv, so the weak-form operands are
+// spheremp metinv rrearth (d s/dx, d s/dy); m.l00/l01/l10/l11 hold that product.
 template <typename R>
 __device__ __forceinline__ R laplace_simple(const Pt<R>& t, const PM<R>& m, R s) {
-  R g0, g1;
-  gradient_sphere(t, m, s, g0, g1);
-  return divergence_sphere_wk(t, m, g0, g1);
+  const R sx = t.ddx(s), sy = t.ddy(s);
+  const R w0 = m.l00 * sx + m.l01 * sy;
+  const R w1 = m.l10 * sx + m.l11 * sy;
+  return -(t.wrow(w0) + t.wcol(w1)) * rre<R>();
 }
 
 template <typename R>
@@ -255,6 +266,7 @@ __global__ void __launch_bounds__(LG * 16) k_caar(CaarArgs<R> a) {
   double* s_div = sm + 2 * NLEV * SROW; // div(v dp)
   double* s_p = sm + 3 * NLEV * SROW;   // pressure
   double* s_om = sm + 4 * NLEV * SROW;  // sum_{j<k} div_vdp_j
+  double* s_rp = sm + 5 * NLEV * SROW;  // 1 / pressure
   const int e = blockIdx.x, tid = threadIdx.x, p = tid & 15, lg = tid >> 4;
   Pt<R> t;
   t.init(p);
@@ -309,8 +321,10 @@ __global__ void __launch_bounds__(LG * 16) k_caar(CaarArgs<R> a) {
       const double d = s_dp[(l0 + k) * SROW + col];
       pr = pr + 0.5 * (prev + d);
       prev = d;
+      const double rp = 1.0 / pr;
       s_p[(l0 + k) * SROW + col] = pr;
-      r[k] = kRgas * s_tv[(l0 + k) * SROW + col] * (d * 0.5 / pr);
+      s_rp[(l0 + k) * SROW + col] = rp;
+      r[k] = kRgas * s_tv[(l0 + k) * SROW + col] * (d * 0.5 * rp);
     }
     // geopotential: phi_k = phis + 2 sum_{j>k} r_j + r_k
     double rt = 0.0;
@@ -351,14 +365,14 @@ __global__ void __launch_bounds__(LG * 16) k_caar(CaarArgs<R> a) {
   for (int k = 0; k < NL; ++k) {
     const int l = lg + LG * k;
     const double pd = s_p[l * SROW + p];
-    const R pr = (R)pd;
+    const R rp = (R)s_rp[l * SROW + p];
     R gp0, gp1;
     gradient_sphere(t, m, rel<R>(pd), gp0, gp1);
     const R u = (R)a.v[vN0 + l * 32 + p], w = (R)a.v[vN0 + l * 32 + 16 + p];
     const double td = a.T[sN0 + l * 16 + p];
     const R div = (R)s_div[l * SROW + p];
     const R vgp = u * gp0 + w * gp1;
-    const R omega = (vgp - ((R)s_om[l * SROW + p] + R(0.5) * div)) / pr;
+    const R omega = (vgp - ((R)s_om[l * SROW + p] + R(0.5) * div)) * rp;
     if (a.eta_ave_w != 0.0) a.omega_p[((size_t)e * NLEV + l) * 16 + p] += (double)(eta * omega);
     // time level "nm1" (RK combine of stage 5 fused here), in double
     double tm = a.T[sM + l * 16 + p], dm = a.dp[sM + l * 16 + p];
@@ -381,7 +395,7 @@ __global__ void __launch_bounds__(LG * 16) k_caar(CaarArgs<R> a) {
     const R ttens = -vgt + R(kKappa) * tv * omega;
     const double tnew = spd * ((double)(ttens * dt) + tm);
     // velocity (compute_velocity_np1 with compute_energy_grad)
-    const R rr = R(kRgas) * (tv / pr);
+    const R rr = R(kRgas) * (tv * rp);
     R eg0 = rr * gp0, eg1 = rr * gp1;
     const R ephi = R(0.5) * (u * u + w * w) + rel<R>(s_dp[l * SROW + p]);
     R ge0, ge1;
@@ -611,37 +625,49 @@ __global__ void __launch_bounds__(LG * 16) k_precompute_divdp(EulerArgs<R> a) {
   }
 }
 
-// compute_dp + compute_qmin_qmax for one (element, tracer): qlim out, Q into qtens when
-// the biharmonic needs it.  Reads qlim (rhs_multiplier == 1) or writes qlim_out.
+// compute_dp + compute_qmin_qmax for one element and all its tracers: the layer
+// thickness dp = derived_dp - rhs_multiplier dt divdp_proj and its reciprocal are formed
+// once per point and level and reused for every tracer; Q = Qdp / dp goes to qtens when
+// the biharmonic needs it; per-level min/max over the 16 points (in R, exact) to
+// qlim_out, combined with the previous qlim when rhs_multiplier == 1.
 template <typename R, int LG>
 __global__ void __launch_bounds__(LG * 16) k_qminmax(EulerArgs<R> a, double* qlim_out, int store_q) {
   constexpr int NL = NLEV / LG;
-  const int eq = blockIdx.x, e = eq / a.Q, q = eq % a.Q;
+  const int e = blockIdx.x;
   const int tid = threadIdx.x, p = tid & 15, lg = tid >> 4;
   const R rhsdt = R(a.rhs_multiplier * a.dt);
-#pragma unroll 1
-  for (int k = 0; k < NL; ++k) {
-    const int l = lg + LG * k;
-    const size_t i3 = ((size_t)e * NLEV + l) * 16 + p;
-    const R dpt = (R)a.derived_dp[i3] - rhsdt * (R)a.divdp_proj[i3];
-    const double qv = a.qdp[((((size_t)e * QTL + a.n0_qdp) * a.Q + q) * NLEV + l) * 16 + p];
-    const R val = R(qv) / dpt;
-    if (store_q) a.qtens[(((size_t)e * a.Q + q) * NLEV + l) * 16 + p] = (double)val;
-    double mn = (double)val, mx = (double)val;
+  R rdp[NL];
 #pragma unroll
-    for (int off = 8; off >= 1; off >>= 1) {
-      mn = fmin(mn, __shfl_xor_sync(FULL, mn, off, 16));
-      mx = fmax(mx, __shfl_xor_sync(FULL, mx, off, 16));
-    }
-    if (p == 0) {
-      double* ql = qlim_out + ((size_t)e * a.Q + q) * 2 * NLEV;
-      if (a.rhs_multiplier == 1.0) {
-        const double* qo = a.qlim + ((size_t)e * a.Q + q) * 2 * NLEV;
-        mn = fmin(qo[l], mn);
-        mx = fmax(qo[NLEV + l], mx);
+  for (int k = 0; k < NL; ++k) {
+    const size_t i3 = ((size_t)e * NLEV + lg + LG * k) * 16 + p;
+    rdp[k] = R(1) / ((R)a.derived_dp[i3] - rhsdt * (R)a.divdp_proj[i3]);
+  }
+#pragma unroll 1
+  for (int q = 0; q < a.Q; ++q) {
+    const double* qsrc = a.qdp + (((size_t)e * QTL + a.n0_qdp) * a.Q + q) * NLEV * 16;
+    double* qt = a.qtens + ((size_t)e * a.Q + q) * NLEV * 16;
+    double* ql = qlim_out + ((size_t)e * a.Q + q) * 2 * NLEV;
+    const double* qo = a.qlim + ((size_t)e * a.Q + q) * 2 * NLEV;
+#pragma unroll
+    for (int k = 0; k < NL; ++k) {
+      const int l = lg + LG * k;
+      const R val = (R)qsrc[l * 16 + p] * rdp[k];
+      if (store_q) qt[l * 16 + p] = (double)val;
+      R mn = val, mx = val;
+#pragma unroll
+      for (int off = 8; off >= 1; off >>= 1) {
+        mn = fmin(mn, __shfl_xor_sync(FULL, mn, off, 16));
+        mx = fmax(mx, __shfl_xor_sync(FULL, mx, off, 16));
       }
-      ql[l] = mn;
-      ql[NLEV + l] = mx;
+      if (p == 0) {
+        double dmn = (double)mn, dmx = (double)mx;
+        if (a.rhs_multiplier == 1.0) {
+          dmn = fmin(qo[l], dmn);
+          dmx = fmax(qo[NLEV + l], dmx);
+        }
+        ql[l] = dmn;
+        ql[NLEV + l] = dmx;
+      }
     }
   }
 }
@@ -807,64 +833,93 @@ __device__ void limiter_level(int option, R* x, const R* c, double& minp_io, dou
 }
 
 // AALTracerPhase: qtens = Qdp - dt div(vstar Qdp) [+ qtens_biharmonic], limiter,
-// spheremp -> qscr (pre-DSS).  One CTA per (element, tracer).
+// spheremp -> qscr (pre-DSS).  One CTA per element loops over the tracers: vstar, the
+// limiter weights c = spheremp dpdissk, 1/dpdissk and sum(c) are formed once per element
+// and reused by every tracer.
 template <typename R, int LG>
 __global__ void __launch_bounds__(LG * 16) k_aal_tracer(EulerArgs<R> a) {
   constexpr int NL = NLEV / LG;
-  __shared__ double s_q[NLEV * SROW];
-  __shared__ R s_dm[NLEV * SROW];
-  __shared__ R s_sp[16];
-  const int eq = blockIdx.x, e = eq / a.Q, q = eq % a.Q;
+  extern __shared__ double tsm[];
+  double* s_q = tsm;                                            // [72][17] double
+  R* s_dm = reinterpret_cast<R*>(tsm + NLEV * SROW);            // dpdissk
+  R* s_rdm = s_dm + NLEV * SROW;                                // 1 / dpdissk
+  R* s_c = s_rdm + NLEV * SROW;                                 // spheremp * dpdissk
+  R* s_c1 = s_c + NLEV * SROW;                                  // sum of c per level
+  const int e = blockIdx.x;
   const int tid = threadIdx.x, p = tid & 15, lg = tid >> 4;
   Pt<R> t;
   t.init(p);
   PM<R> m;
   m.load(a.m, e, p);
-  if (tid < 16) s_sp[tid] = m.sp;
-  const size_t qn0 = (((size_t)e * QTL + a.n0_qdp) * a.Q + q) * NLEV * 16;
-  const size_t qb = ((size_t)e * a.Q + q) * NLEV * 16;
-  const bool add_hv = a.rhs_viss != 0.0;
-  const R mdt = R(-a.dt);
-#pragma unroll 1
+  const double spd = a.m.spheremp_d[(size_t)e * 16 + p];
+  // tracer-independent part of div(vstar Qdp): the contravariant flux per unit Qdp,
+  // (Dinv-contraction of vstar) * metdet
+  R w0[NL], w1[NL];
+#pragma unroll
   for (int k = 0; k < NL; ++k) {
     const int l = lg + LG * k;
-    const double qdd = a.qdp[qn0 + l * 16 + p];
-    const R qd = (R)qdd;
     const size_t iv = ((size_t)e * NLEV + l) * 32 + p;
-    const R g0 = (R)a.vstar[iv] * qd, g1 = (R)a.vstar[iv + 16] * qd;
-    const R dv = divergence_sphere(t, m, g0, g1);
-    const double q0 = add_hv ? a.qtens[qb + l * 16 + p] : 0.0;
-    if constexpr (kF32<R>) s_q[l * SROW + p] = qdd + (double)(mdt * dv) + q0;
-    else s_q[l * SROW + p] = (qdd + mdt * dv + q0);
-    s_dm[l * SROW + p] = (R)a.dpdissk[((size_t)e * NLEV + l) * 16 + p];
+    const R vs0 = (R)a.vstar[iv], vs1 = (R)a.vstar[iv + 16];
+    w0[k] = (m.di00 * vs0 + m.di10 * vs1) * m.md;
+    w1[k] = (m.di01 * vs0 + m.di11 * vs1) * m.md;
+    const R dm = (R)a.dpdissk[((size_t)e * NLEV + l) * 16 + p];
+    s_dm[l * SROW + p] = dm;
+    s_rdm[l * SROW + p] = R(1) / dm;
+    s_c[l * SROW + p] = m.sp * dm;
   }
   __syncthreads();
   for (int l = tid; l < NLEV; l += blockDim.x) {
-    R x[16], c[16];
     R s1 = 0;
 #pragma unroll
-    for (int k = 0; k < 16; ++k) {
-      const R dpm = s_dm[l * SROW + k];
-      c[k] = s_sp[k] * dpm;
-      x[k] = (R)s_q[l * SROW + k] / dpm;
-      s1 += c[k];
-    }
-    if (s1 > R(0)) {
-      double* ql = a.qlim + ((size_t)e * a.Q + q) * 2 * NLEV;
-      double mn = ql[l], mx = ql[NLEV + l];
-      limiter_level<R>(a.limiter_option, x, c, mn, mx);
-      ql[l] = mn;
-      ql[NLEV + l] = mx;
-#pragma unroll
-      for (int k = 0; k < 16; ++k) s_q[l * SROW + k] = (double)(x[k] * s_dm[l * SROW + k]);
-    }
+    for (int k = 0; k < 16; ++k) s1 += s_c[l * SROW + k];
+    s_c1[l] = s1;
   }
-  __syncthreads();
+  const bool add_hv = a.rhs_viss != 0.0;
+  const R mdt = R(-a.dt);
 #pragma unroll 1
-  for (int k = 0; k < NL; ++k) {
-    const int l = lg + LG * k;
-    a.qscr[qb + l * 16 + p] = a.m.spheremp_d[(size_t)e * 16 + p] * s_q[l * SROW + p];
+  for (int q = 0; q < a.Q; ++q) {
+    const size_t qn0 = (((size_t)e * QTL + a.n0_qdp) * a.Q + q) * NLEV * 16;
+    const size_t qb = ((size_t)e * a.Q + q) * NLEV * 16;
+#pragma unroll
+    for (int k = 0; k < NL; ++k) {
+      const int l = lg + LG * k;
+      const double qdd = a.qdp[qn0 + l * 16 + p];
+      const R qd = (R)qdd;
+      const R dv = (t.ddx(w0[k] * qd) + t.ddy(w1[k] * qd)) * m.fdiv;
+      const double q0 = add_hv ? a.qtens[qb + l * 16 + p] : 0.0;
+      if constexpr (kF32<R>) s_q[l * SROW + p] = qdd + (double)(mdt * dv) + q0;
+      else s_q[l * SROW + p] = (qdd + mdt * dv + q0);
+    }
+    __syncthreads();
+    for (int l = tid; l < NLEV; l += blockDim.x) {
+      if (s_c1[l] > R(0)) {
+        R x[16], c[16];
+#pragma unroll
+        for (int k = 0; k < 16; ++k) {
+          c[k] = s_c[l * SROW + k];
+          x[k] = (R)s_q[l * SROW + k] * s_rdm[l * SROW + k];
+        }
+        double* ql = a.qlim + ((size_t)e * a.Q + q) * 2 * NLEV;
+        double mn = ql[l], mx = ql[NLEV + l];
+        limiter_level<R>(a.limiter_option, x, c, mn, mx);
+        ql[l] = mn;
+        ql[NLEV + l] = mx;
+#pragma unroll
+        for (int k = 0; k < 16; ++k) s_q[l * SROW + k] = (double)(x[k] * s_dm[l * SROW + k]);
+      }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < NL; ++k) {
+      const int l = lg + LG * k;
+      a.qscr[qb + l * 16 + p] = spd * s_q[l * SROW + p];
+    }
+    __syncthreads();
   }
+}
+
+template <typename R> constexpr size_t aal_smem() {
+  return NLEV * SROW * sizeof(double) + (4 * NLEV * SROW) * sizeof(R);
 }
 
 // DSS(rspheremp) of the tracer scratch into Qdp(np1); with time_avg the last RK2 stage
@@ -934,7 +989,8 @@ constexpr int R_MASS = R_A + 76;       // mass[0 .. 73]
 constexpr int R_DMA = R_MASS + 74;     // dma[0 .. 73]
 constexpr int R_AI = R_DMA + 74;       // ai[0 .. 72]
 constexpr int R_COEF = R_AI + 74;      // coef[3][72]
-constexpr int R_COL = R_COEF + 216;    // doubles per column
+constexpr int R_RD = R_COEF + 216;     // 1 / D[0 .. 71]
+constexpr int R_COL = R_RD + 72;       // doubles per column
 
 // Exclusive prefix over the warp of one value per lane.
 __device__ __forceinline__ double warp_excl_scan(double v, int lane) {
@@ -956,10 +1012,9 @@ __device__ __forceinline__ double warp_sum(double v) {
 // PPM vertical remap (RemapFunctor + PpmVertRemap, rsplit > 0), one warp per column:
 // lane L owns levels 3L .. 3L+2 (L < 24) for level work and interfaces j = 3L .. 3L+2
 // (L < 25) for the grid quantities; column scans are warp shuffles, phases are
-// separated by __syncwarp only.  The reconstruction (cell means, slopes, edge values,
-// parabola coefficients, ppmdx grids) runs in R; the cumulative masses and the
-// integrals of the parabolas run in double, so the remap conserves mass in FP64 in
-// both forms.
+// separated by __syncwarp only.  Everything runs in double in both forms (R is double
+// at every launch); the remap conserves mass to round-off.  Divisions by the layer
+// thickness and by the constants 3 and 6 are multiplications by reciprocals.
 template <typename R>
 __global__ void __launch_bounds__(RT) k_remap(RemapArgs a) {
   extern __shared__ double rsm[];
@@ -980,6 +1035,7 @@ __global__ void __launch_bounds__(RT) k_remap(RemapArgs a) {
   double* dma = sm + R_DMA;
   double* ai = sm + R_AI;
   double* coef = sm + R_COEF;  // coef[c * 72 + j]
+  double* rD = sm + R_RD;
   const bool own = lane < 24;
   const int l0 = 3 * lane;
   const size_t sb = ((size_t)e * NTL + a.np1) * NLEV * 16 + p;
@@ -991,6 +1047,7 @@ __global__ void __launch_bounds__(RT) k_remap(RemapArgs a) {
     for (int k = 0; k < 3; ++k) {
       s3[k] = a.dp[sb + (size_t)(l0 + k) * 16];
       D[l0 + k] = s3[k];
+      rD[l0 + k] = 1.0 / s3[k];
       if (isnan(s3[k]) || s3[k] < 0.0) atomicExch(a.invalid, 1);
     }
   }
@@ -1085,8 +1142,7 @@ __global__ void __launch_bounds__(RT) k_remap(RemapArgs a) {
         if (var < 2) x3[k] = a.v[vb + (size_t)l * 32 + var * 16] * s3[k];
         else if (var == 2) x3[k] = a.T[sb + (size_t)l * 16] * s3[k];
         else x3[k] = a.qdp[((((size_t)e * QTL + a.n0_qdp) * a.Q + (var - 3)) * NLEV + l) * 16 + p];
-        if constexpr (kF32<R>) A[l] = (double)((R)x3[k] / (R)s3[k]);
-        else A[l] = x3[k] / s3[k];
+        A[l] = x3[k] * rD[l];
       }
     }
     {
@@ -1153,8 +1209,9 @@ __global__ void __launch_bounds__(RT) k_remap(RemapArgs a) {
         R al = (R)ai[jp], ar = (R)ai[jp + 1];
         const R cm = (R)A[jp];
         if ((ar - cm) * (cm - al) <= R(0)) { al = cm; ar = cm; }
-        if ((ar - al) * (cm - (al + ar) / R(2)) > (ar - al) * (ar - al) / R(6)) al = R(3) * cm - R(2) * ar;
-        if ((ar - al) * (cm - (al + ar) / R(2)) < -(ar - al) * (ar - al) / R(6)) ar = R(3) * cm - R(2) * al;
+        constexpr R sixth = R(1.0 / 6.0);
+        if ((ar - al) * (cm - (al + ar) * R(0.5)) > (ar - al) * (ar - al) * sixth) al = R(3) * cm - R(2) * ar;
+        if ((ar - al) * (cm - (al + ar) * R(0.5)) < -(ar - al) * (ar - al) * sixth) ar = R(3) * cm - R(2) * al;
         R c0 = R(1.5) * cm - (al + ar) / R(4), c1 = ar - al, c2 = R(3) * (R(-2) * cm + (al + ar));
         if (a.remap_alg == 2 && (jp < 2 || jp >= NLEV - 2)) {  // PpmFixedParabola
           c0 = cm;
@@ -1176,8 +1233,8 @@ __global__ void __launch_bounds__(RT) k_remap(RemapArgs a) {
         const int k = l0 + k3;
         const int kk = kid[k];
         const double x2 = z2[k], x1 = -0.5;
-        const double in = (coef[kk] * (x2 - x1) + coef[72 + kk] * (x2 * x2 - x1 * x1) / 2.0) +
-                          coef[144 + kk] * (x2 * x2 * x2 - x1 * x1 * x1) / 3.0;
+        const double in = (coef[kk] * (x2 - x1) + coef[72 + kk] * (x2 * x2 - x1 * x1) * 0.5) +
+                          coef[144 + kk] * (x2 * x2 * x2 - x1 * x1 * x1) * (1.0 / 3.0);
         m2[k3] = mass[kk + 1] + in * D[kk];
       }
     }
@@ -1263,7 +1320,7 @@ void launch_dp_from_ps(int E, double* dp, const double* ps_v, int n0, double ps0
 template <typename R>
 void launch_caar(const CaarArgs<R>& a, int E, cudaStream_t s) {
   constexpr int LG = LG_CAAR<R>();
-  const size_t smem = 5 * NLEV * SROW * sizeof(double);
+  const size_t smem = 6 * NLEV * SROW * sizeof(double);
   static bool init = false;
   if (!init) {
     cudaFuncSetAttribute(k_caar<R, LG>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -1314,7 +1371,7 @@ void launch_euler_step(EulerArgs<R>& a, int E, int time_avg, cudaStream_t s) {
     const bool nbr = (a.rhs_multiplier == 0.0 || a.rhs_multiplier == 2.0);
     {
       KScope k("euler_qminmax", s);
-      k_qminmax<R, LG><<<EQ, LG * 16, 0, s>>>(a, nbr ? a.qlim_tmp : a.qlim, a.rhs_multiplier == 2.0);
+      k_qminmax<R, LG><<<E, LG * 16, 0, s>>>(a, nbr ? a.qlim_tmp : a.qlim, a.rhs_multiplier == 2.0);
     }
     if (a.rhs_multiplier == 2.0) {
       a.rhs_viss = 3.0;
@@ -1338,8 +1395,14 @@ void launch_euler_step(EulerArgs<R>& a, int E, int time_avg, cudaStream_t s) {
   }
   if (a.Q > 0) {
     {
+      constexpr size_t smem = aal_smem<R>();
+      static bool init = false;
+      if (!init) {
+        cudaFuncSetAttribute(k_aal_tracer<R, LG>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        init = true;
+      }
       KScope k("euler_aal_tracer", s);
-      k_aal_tracer<R, LG><<<EQ, LG * 16, 0, s>>>(a);
+      k_aal_tracer<R, LG><<<E, LG * 16, smem, s>>>(a);
     }
     {
       KScope k("euler_dss_qdp", s);
@@ -1357,11 +1420,11 @@ void launch_remap(const RemapArgs& a, cudaStream_t s) {
   const size_t smem = (size_t)RCOLS * R_COL * sizeof(double);
   static bool init = false;
   if (!init) {
-    cudaFuncSetAttribute(k_remap<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(k_remap<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     init = true;
   }
   KScope k("ppm_remap", s);
-  k_remap<R><<<(a.nelem * 16 + RCOLS - 1) / RCOLS, RT, smem, s>>>(a);
+  k_remap<double><<<(a.nelem * 16 + RCOLS - 1) / RCOLS, RT, smem, s>>>(a);
 }
 
 void launch_update_q(int E, int Q, const double* qdp, double* Qc, const double* ps_v, int np1, int np1_qdp,
