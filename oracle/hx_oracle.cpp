@@ -1618,6 +1618,50 @@ int hx_timer_stop(double* ms) {
 }
 int hx_host_register(void*, size_t) { return 0; }
 int hx_host_unregister(void*) { return 0; }
+// Test hooks of the oracle only (no counterpart in the GPU library).
+
+// One level of the quasi-monotone limiter exactly as with_limiter_shell applies it
+// (EulerStepFunctorImpl.hpp:693-757): ptens[16] (mass), sphweights[16], dpmass[16],
+// qlim[2] (min, max) in/out.
+void hx_oracle_limiter(int option, double* ptens, const double* sphweights,
+                       const double* dpmass, double* qlim) {
+  double x[NP2], cw[NP2], s1 = 0;
+  for (int k = 0; k < NP2; ++k) {
+    cw[k] = sphweights[k] * dpmass[k];
+    x[k] = ptens[k] / dpmass[k];
+    s1 += cw[k];
+  }
+  if (s1 <= 0) return;
+  limiter_level(option, x, cw, qlim[0], qlim[1]);
+  for (int k = 0; k < NP2; ++k) ptens[k] = x[k] * dpmass[k];
+}
+
+// Apply a sphere operator to every level of a field given in the Fortran layout of
+// one time level ([E][72][16]; vectors [E][72][2][16]):
+//   op 0: laplace_simple (weak), 1: divergence_sphere, 2: vorticity_sphere,
+//   3: gradient_sphere (out is a vector), 4: vlaplace_sphere_wk_contra (in/out vectors).
+int hx_oracle_sphere_op(int op, const double* in, double* out) {
+  Ctx& c = C();
+  const size_t B = (size_t)NP2 * NLEV;
+#pragma omp parallel for
+  for (int e = 0; e < c.E; ++e) {
+    const EM m = metric(e);
+    std::vector<double> a(2 * B), b(2 * B);
+    const int nin = (op == 1 || op == 2 || op == 4) ? 2 : 1;
+    const int nout = (op == 3 || op == 4) ? 2 : 1;
+    pull_block(in + (size_t)e * nin * B, a.data(), nin);
+    switch (op) {
+      case 0: laplace_simple(m, a.data(), b.data(), NLEV); break;
+      case 1: divergence_sphere(m, a.data(), b.data(), NLEV); break;
+      case 2: vorticity_sphere(m, a.data(), b.data(), NLEV); break;
+      case 3: gradient_sphere(m, a.data(), b.data(), NLEV); break;
+      default: vlaplace_sphere_wk_contra(m, 1.0, a.data(), b.data(), NLEV); break;
+    }
+    push_block(b.data(), out + (size_t)e * nout * B, nout);
+  }
+  return 0;
+}
+
 int hx_oracle_threads(void) {
 #ifdef _OPENMP
   return omp_get_max_threads();

@@ -30,3 +30,10 @@ def gpu_path():
     code, msg = L.last_error()
     assert code == 0, f"CUDA device unavailable for the GPU tests: {msg}"
     return path
+
+
+@pytest.fixture(scope="session")
+def gpu_lib_cpu():
+    """The CUDA library, built here and loaded without using a GPU (host-only calls)."""
+    import hxtest
+    return hxtest.build_gpu_lib()

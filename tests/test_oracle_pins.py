@@ -1,0 +1,238 @@
+"""Pins of the CPU oracle.  The reference ships no golden vectors and cannot be built
+here (Kokkos, gfortran and MPI are missing), so the oracle is held to the reference's
+own property tests and to analytic identities:
+
+* limiter 8 and CAAS (limiter 9): bounds within (1 +- 10 eps) and mass within
+  1e2 eps, on the reference's feasible random problems, and equal 1-norm of the
+  corrections (src/preqx/unit_tests/preqx_ut.cpp:1330-1527);
+* DSS of a constant gives the point multiplicity, DSS is symmetric, mass-weighted DSS
+  conserves the global integral;
+* the weak Laplacian of a spherical harmonic (after DSS and the inverse mass matrix)
+  approaches -l(l+1)/a^2 Y; divergence of solid-body rotation vanishes and its
+  vorticity is 2 w sin(lat);
+* a remap interval conserves dry mass and tracer mass, and a constant mixing ratio
+  stays constant;
+* option checks return the reference's error codes.
+"""
+import ctypes as C
+import math
+
+import numpy as np
+import pytest
+
+import hxtest as H
+
+EPS = np.finfo(np.float64).eps
+DT = 300.0
+
+
+@pytest.fixture(scope="module")
+def ora(oracle_path):
+    return H.lib(oracle_path)
+
+
+def _lim(L, option, ptens, sph, dpm, qlim):
+    dp = C.POINTER(C.c_double)
+    L.lib.hx_oracle_limiter(C.c_int(option), ptens.ctypes.data_as(dp), sph.ctypes.data_as(dp),
+                            dpm.ctypes.data_as(dp), qlim.ctypes.data_as(dp))
+
+
+def _feasible(rng):
+    """LimiterTester::init_feasible (preqx_ut.cpp:1337-1380), one level."""
+    sph = rng.uniform(1.0 / 16, 2.0 / 16, 16)
+    dpm = rng.uniform(0.5, 1.0, 16)
+    ptens = rng.uniform(0.0, 1.0, 16)
+    q = np.sort(rng.uniform(0.0, 1.0, 2))
+    ptens = ptens * dpm
+    m = np.sum(sph * ptens)
+    lo = np.sum(sph * q[0] * dpm)
+    hi = np.sum(sph * q[1] * dpm)
+    dm = lo - m if m < lo else (hi - m if m > hi else 0.0)
+    if dm:
+        ptens = ptens + (1 + 1e2 * EPS) * dm / (16 * sph)
+    m = np.sum(sph * ptens)
+    assert m >= (1 - 1e1 * EPS) * lo and m <= (1 + 1e1 * EPS) * hi
+    return ptens, sph, dpm, q.copy(), m
+
+
+@pytest.mark.parametrize("option", [8, 9])
+def test_limiter_bounds_and_mass(ora, option):
+    rng = np.random.default_rng(1330 + option)
+    for _ in range(400):
+        ptens, sph, dpm, qlim, mass = _feasible(rng)
+        _lim(ora, option, ptens, sph, dpm, qlim)
+        assert (ptens >= (1 - 1e1 * EPS) * qlim[0] * dpm).all()
+        assert (ptens <= (1 + 1e1 * EPS) * qlim[1] * dpm).all()
+        assert abs(np.sum(sph * ptens) - mass) <= 1e2 * EPS * mass
+
+
+def test_limiter_one_norm_minimal(ora):
+    """Limiter 8 and CAAS both give 1-norm-minimal corrections (preqx_ut.cpp:1459-1527)."""
+    rng = np.random.default_rng(1459)
+    for _ in range(200):
+        ptens, sph, dpm, qlim, _ = _feasible(rng)
+        a, b = ptens.copy(), ptens.copy()
+        qa, qb = qlim.copy(), qlim.copy()
+        _lim(ora, 8, a, sph, dpm, qa)
+        _lim(ora, 9, b, sph, dpm, qb)
+        na = np.sum(np.abs(a - ptens) * sph)
+        nb = np.sum(np.abs(b - ptens) * sph)
+        assert abs(na - nb) <= 1e3 * EPS * max(nb, 1e-300)
+
+
+def test_limiter_relaxes_infeasible_bounds(ora):
+    """If the level's mean lies outside [qmin, qmax] the bound is moved to the mean and
+    the result is the constant mean (with_limiter_shell, EulerStepFunctorImpl.hpp:727-739)."""
+    sph = np.full(16, 1.0 / 16)
+    dpm = np.ones(16)
+    ptens = np.linspace(0.5, 1.5, 16)
+    qlim = np.array([2.0, 3.0])
+    _lim(ora, 8, ptens, sph, dpm, qlim)
+    assert qlim[0] == pytest.approx(1.0, rel=1e-15)
+    assert np.allclose(ptens, 1.0, rtol=1e-14)
+
+
+def _setup(path, ne=4, Q=2, **kw):
+    kw.setdefault("nu", 1e16)
+    return H.setup(path, ne, Q, **kw)
+
+
+def test_dss_constant_multiplicity(oracle_path):
+    L = _setup(oracle_path)
+    m = H.mesh(4)
+    L.set("T", 0, np.ones(L.field_shape("T")))
+    L.call("hx_run_dss", b"T", 0, 0)
+    out = L.get("T", 0)
+    mult = np.ones((m.nelem, 16))
+    for pts in H.M.dss_point_sources(m).values():
+        for (e, i, j) in pts:
+            mult[e, 4 * i + j] = len(pts)
+    assert np.array_equal(out, np.broadcast_to(mult.reshape(m.nelem, 1, 4, 4), out.shape))
+
+
+def test_dss_with_rspheremp_is_projection(oracle_path):
+    """DSS(spheremp f) * rspheremp is a projection: applying it twice changes nothing,
+    and it preserves the spheremp-weighted global integral."""
+    L = _setup(oracle_path)
+    m = H.mesh(4)
+    rng = np.random.default_rng(3)
+    f = rng.standard_normal(L.field_shape("T"))
+    sm = m.spheremp[:, None]
+    L.set("T", 0, f * sm)
+    L.call("hx_run_dss", b"T", 0, 1)
+    g = L.get("T", 0)
+    L.set("T", 0, g * sm)
+    L.call("hx_run_dss", b"T", 0, 1)
+    g2 = L.get("T", 0)
+    assert np.abs(g2 - g).max() <= 1e-13 * np.abs(g).max()
+    # the spheremp-weighted integral over all element points is unchanged
+    tot_g = (g * sm).sum(axis=(0, 2, 3))
+    tot_f = (f * sm).sum(axis=(0, 2, 3))
+    assert np.abs(tot_g - tot_f).max() <= 1e-12 * np.abs(tot_f).max()
+
+
+def _sphere_op(L, op, arr, out_shape):
+    out = np.empty(out_shape)
+    a = np.ascontiguousarray(arr)
+    L.lib.hx_oracle_sphere_op(C.c_int(op), C.c_void_p(a.ctypes.data), C.c_void_p(out.ctypes.data))
+    return out
+
+
+def _lap_err(path, ne):
+    L = _setup(path, ne=ne)
+    m = H.mesh(ne)
+    y = 0.5 * (3 * np.sin(m.lat) ** 2 - 1)                     # P_2(sin lat)
+    f = np.broadcast_to(y[:, None], (m.nelem, 72, 4, 4)).copy()
+    lap = _sphere_op(L, 0, f, f.shape)
+    L.set("T", 0, lap)
+    L.call("hx_run_dss", b"T", 0, 1)
+    lap = L.get("T", 0)
+    exact = -6.0 / 6.376e6 ** 2 * f
+    return float(np.sqrt(np.mean((lap - exact) ** 2) / np.mean(exact ** 2)))
+
+
+def test_laplacian_of_spherical_harmonic(oracle_path):
+    """Weak Laplacian + DSS + inverse mass matrix of Y_2^0 -> -6/a^2 Y_2^0, with the
+    error falling by more than 4x per doubling of resolution (ne 4 -> 8)."""
+    e4, e8 = _lap_err(oracle_path, 4), _lap_err(oracle_path, 8)
+    assert e8 < 1e-3 and e4 / e8 > 4.0, (e4, e8)
+
+
+def test_solid_body_rotation(oracle_path):
+    ne = 8
+    L = _setup(oracle_path, ne=ne)
+    m = H.mesh(ne)
+    u0 = 20.0
+    u = u0 * np.cos(m.lat)
+    vel = np.zeros((m.nelem, 72, 2, 4, 4))
+    vel[:, :, 0] = u[:, None]
+    div = _sphere_op(L, 1, vel, (m.nelem, 72, 4, 4))
+    vort = _sphere_op(L, 2, vel, (m.nelem, 72, 4, 4))
+    a = 6.376e6
+    scale = u0 / a
+    # discretisation error only (sign or orientation mistakes give O(1) errors)
+    assert np.abs(div).max() < 1e-2 * scale
+    exact = 2 * u0 / a * np.sin(m.lat)
+    assert np.abs(vort - exact[:, None]).max() < 1e-2 * scale
+
+
+@pytest.mark.parametrize("rsplit", [1, 3])
+def test_subcycle_conserves_mass(oracle_path, rsplit):
+    L = _setup(oracle_path, ne=4, Q=3, rsplit=rsplit)
+    m = H.mesh(4)
+    st = H.state(4, 3)
+    L.run_subcycle(DT)
+    r = L.push_results()
+    n0 = L.tl[1]
+    ps0 = np.sum(st["ps_v"][:, 1] * m.spheremp)
+    ps1 = np.sum(r["ps_v"][:, n0] * m.spheremp)
+    assert abs(ps1 / ps0 - 1) < 1e-14
+    q0 = np.sum(st["Qdp"][:, 0] * m.spheremp[:, None, None], axis=(0, 2, 3, 4))
+    newest = [np.sum(r["Qdp"][:, k] * m.spheremp[:, None, None], axis=(0, 2, 3, 4)) for k in range(2)]
+    assert min(np.abs(x / q0 - 1).max() for x in newest) < 1e-13
+
+
+def test_constant_mixing_ratio_survives_remap(oracle_path):
+    """q = const stays close to const through advection, limiter and remap.  It is not
+    exact in the reference algorithm: the dynamics' dp3d carries the nu_top sponge and
+    the nu_p hyperviscosity, which the tracer mass flux reproduces only approximately,
+    so the bound is the size of that inconsistency, largest at the model top."""
+    ne, Q = 4, 1
+    m = H.mesh(ne)
+    st = {k: v.copy() for k, v in H.state(ne, Q).items()}
+    st["Qdp"][:] = 0.003 * st["dp3d"][:, 1][:, None, None]
+    L = H.lib(oracle_path)
+    if L.nelem:
+        L.finalize()
+    from hommexx_gb300 import abi
+    L.init(m, H.hvc(), abi.SimParams(qsize=Q, nu=1e16, rsplit=3), st)
+    L.run_subcycle(DT)
+    r = L.push_results()
+    dev = np.abs(r["Q"] / 0.003 - 1)
+    assert dev.max() < 1e-3
+    assert dev[:, :, 36:].max() < 1e-5     # lower half of the column
+
+
+@pytest.mark.parametrize("field,value,code", [
+    ("limiter_option", 4, 11), ("remap_alg", 3, 11), ("time_step_type", 1, 11),
+    ("hypervis_order", 1, 11), ("ftype", 2, 12), ("rsplit", 0, 12),
+])
+def test_option_checks(oracle_path, gpu_lib_cpu, field, value, code):
+    """cxx_f90_interface.cpp:43-52 option checks; the same codes from both libraries."""
+    from hommexx_gb300 import abi
+    for path in (oracle_path, gpu_lib_cpu):
+        L = H.lib(path)
+        L.lib.hx_set_abort_on_error(0)
+        p = abi.SimParams(qsize=2, nu=1e16, **{field: value}).resolved()
+        L.lib.init_simulation_params_c(*[abi._i(x) if isinstance(x, (bool, int)) and not isinstance(x, bool)
+                                         else (abi._b(x) if isinstance(x, bool) else abi._d(x))
+                                         for x in _param_list(p)])
+        assert L.last_error()[0] == code, (path, field, L.last_error())
+
+
+def _param_list(p):
+    return [p.remap_alg, p.limiter_option, p.rsplit, p.qsplit, p.time_step_type, p.energy_fixer,
+            p.qsize, p.state_frequency, float(p.nu), float(p.nu_p), float(p.nu_q), float(p.nu_s),
+            float(p.nu_div), float(p.nu_top), p.hypervis_order, p.hypervis_subcycle,
+            float(p.hypervis_scaling), p.ftype, bool(p.prescribed_wind), bool(p.moisture),
+            bool(p.disable_diagnostics), bool(p.use_cpstar), bool(p.use_semi_lagrangian_transport)]
