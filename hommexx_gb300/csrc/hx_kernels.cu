@@ -487,8 +487,8 @@ __global__ void __launch_bounds__(LG * 16) k_hv_lap2(HvArgs<R> a) {
   double* out = a.bufB + (size_t)e * NLEV * 64;
   const double rs = a.m.rspheremp_d[(size_t)e * 16 + p];
   const double spd = a.m.spheremp_d[(size_t)e * 16 + p];
-  const R eta_h = R(a.eta_ave_w);
-  const R hs = R(a.hsub);
+  const double wh = a.eta_ave_w / a.hsub;  // eta_ave_w / hypervis_subcycle
+  const R whr = R(wh);
   const R dt = R(a.dt);
 #pragma unroll 1
   for (int k = 0; k < NL; ++k) {
@@ -509,8 +509,8 @@ __global__ void __launch_bounds__(LG * 16) k_hv_lap2(HvArgs<R> a) {
     }
     const size_t i3 = ((size_t)e * NLEV + l) * 16 + p;
     const double dpn = a.dp[sb + l * 16 + p];
-    a.dpdiss_ave[i3] += a.eta_ave_w * dpn / a.hsub;
-    a.dpdiss_bih[i3] += (double)(eta_h * ld / hs);
+    a.dpdiss_ave[i3] += wh * dpn;
+    a.dpdiss_bih[i3] += (double)(whr * ld);
     R vt0 = l0 * R(-a.nu), vt1 = l1 * R(-a.nu);
     R ttn = lt * R(-a.nu_s), dpt = ld * R(-a.nu_p);
     if (a.nu_top > 0 && __any_sync(FULL, l < 3)) {
@@ -557,8 +557,9 @@ __global__ void k_hv_update(HvArgs<R> a, int E) {
   a.v[vb + 16] = v1;
   tt = dt * tt * rs;
   const R heating = vt0 * (R)v0 + vt1 * (R)v1;
-  if constexpr (kF32<R>) a.T[sb] = a.T[sb] + (double)(tt - heating / R(kCp));
-  else a.T[sb] = a.T[sb] + tt - heating / R(kCp);
+  constexpr R rcp = R(1.0 / kCp);
+  if constexpr (kF32<R>) a.T[sb] = a.T[sb] + (double)(tt - heating * rcp);
+  else a.T[sb] = a.T[sb] + tt - heating * rcp;
   a.dp[sb] = dpt * rsd;
 }
 
@@ -705,7 +706,7 @@ __global__ void __launch_bounds__(LG * 16) k_bih_pre(EulerArgs<R> a) {
   for (int k = 0; k < NL; ++k) {
     const int l = lg + LG * k;
     R s = (R)a.qtens[qb + l * 16 + p];
-    if (a.nu_p > 0) s = s * (R)a.dpdiss_ave[((size_t)e * NLEV + l) * 16 + p] / R(a.dp0[l]);
+    if (a.nu_p > 0) s = s * (R)a.dpdiss_ave[((size_t)e * NLEV + l) * 16 + p] * R(1.0 / a.dp0[l]);
     a.qscr[qb + l * 16 + p] = (double)laplace_simple(t, m, s);
   }
 }
@@ -729,12 +730,13 @@ __global__ void __launch_bounds__(LG * 16) k_bih_post(EulerArgs<R> a) {
   const double* fbase = a.qscr + (size_t)q * NLEV * 16;
   const R fac = R(-a.rhs_viss * a.dt * a.nu_q);
   const double rs = a.m.rspheremp_d[(size_t)e * 16 + p];
+  const R rsp_local = R(1) / m.sp;
 #pragma unroll 1
   for (int k = 0; k < NL; ++k) {
     const int l = lg + LG * k;
     const R s = (R)(dss_gather(fbase, (long long)a.Q * NLEV * 16, 16, e, l, p, a.dss) * rs);
     const R lap = a.consthv ? laplace_simple(t, m, s) : laplace_tensor(t, m, tv, s);
-    a.qtens[qb + l * 16 + p] = (double)(fac * R(a.dp0[l]) * lap / m.sp);
+    a.qtens[qb + l * 16 + p] = (double)(fac * R(a.dp0[l]) * lap * rsp_local);
   }
 }
 
@@ -747,8 +749,9 @@ __global__ void k_aal_setup(EulerArgs<R> a, int E) {
   const R rhsdt = R(a.rhs_multiplier * a.dt);
   const R dpt = (R)a.derived_dp[idx] - rhsdt * (R)a.divdp_proj[idx];
   const size_t iv = ((size_t)e * NLEV + l) * 32 + p;
-  a.vstar[iv] = (double)((R)a.vn0[iv] / dpt);
-  a.vstar[iv + 16] = (double)((R)a.vn0[iv + 16] / dpt);
+  const R rdpt = R(1) / dpt;
+  a.vstar[iv] = (double)((R)a.vn0[iv] * rdpt);
+  a.vstar[iv + 16] = (double)((R)a.vn0[iv + 16] * rdpt);
   R dk = dpt - R(a.dt) * (R)a.divdp[idx];
   if (a.nu_p > 0 && a.rhs_viss != 0.0)
     dk += R(-a.rhs_viss * a.dt * a.nu_q) * (R)a.dpdiss_bih[idx] / a.m.spheremp[e * 16 + p];
@@ -935,7 +938,7 @@ __global__ void k_dss_tracers(EulerArgs<R> a, int E, int time_avg) {
   const size_t d = ((((size_t)e * QTL + a.np1_qdp) * a.Q + q) * NLEV + l) * 16 + p;
   if (time_avg) {
     const size_t s0 = ((((size_t)e * QTL + a.avg_n0_qdp) * a.Q + q) * NLEV + l) * 16 + p;
-    a.qdp[d] = (a.qdp[s0] + 2.0 * v) / 3.0;
+    a.qdp[d] = (a.qdp[s0] + 2.0 * v) * (1.0 / 3.0);
   } else {
     a.qdp[d] = v;
   }
@@ -1113,18 +1116,21 @@ __global__ void __launch_bounds__(RT) k_remap(RemapArgs a) {
       const int j = 3 * lane + k3;
       if (j < NLEV + 2) {
         const R dm2 = (R)D[j - 2], dm1 = (R)D[j - 1], d0 = (R)D[j];
+        const R r10 = R(1) / (dm1 + d0);  // shared by g1, g3, g5
         g[0 * 74 + j] = (double)(dm1 / (dm2 + dm1 + d0));
-        g[1 * 74 + j] = (double)((R(2) * dm2 + dm1) / (dm1 + d0));
+        g[1 * 74 + j] = (double)((R(2) * dm2 + dm1) * r10);
         g[2 * 74 + j] = (double)((dm1 + R(2) * d0) / (dm2 + dm1));
         if (j < NLEV + 1) {
           const R dp1 = (R)D[j + 1];
-          g[3 * 74 + j] = (double)(dm1 / (dm1 + d0));
+          const R r6 = R(1) / (R(2) * dm1 + d0);  // shared by g6, g8
+          const R r7 = R(1) / (R(2) * d0 + dm1);  // shared by g7, g9
+          g[3 * 74 + j] = (double)(dm1 * r10);
           g[4 * 74 + j] = (double)(R(1) / (dm2 + dm1 + d0 + dp1));
-          g[5 * 74 + j] = (double)((R(2) * dm1 * d0) / (dm1 + d0));
-          g[6 * 74 + j] = (double)((dm2 + dm1) / (R(2) * dm1 + d0));
-          g[7 * 74 + j] = (double)((dp1 + d0) / (R(2) * d0 + dm1));
-          g[8 * 74 + j] = (double)(dm1 * (dm2 + dm1) / (R(2) * dm1 + d0));
-          g[9 * 74 + j] = (double)(d0 * (d0 + dp1) / (dm1 + R(2) * d0));
+          g[5 * 74 + j] = (double)((R(2) * dm1 * d0) * r10);
+          g[6 * 74 + j] = (double)((dm2 + dm1) * r6);
+          g[7 * 74 + j] = (double)((dp1 + d0) * r7);
+          g[8 * 74 + j] = (double)(dm1 * (dm2 + dm1) * r6);
+          g[9 * 74 + j] = (double)(d0 * (d0 + dp1) * r7);
         }
       }
     }

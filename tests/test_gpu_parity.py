@@ -192,3 +192,35 @@ def test_negative_thickness_reports_101(gpu_path):
     L.set("dp3d", 1, dp)
     rc = L.lib.hx_run_remap(1, 0, DT)
     assert rc == 101
+
+
+def test_moist_virtual_temperature(pair):
+    """moisture='moist': T_v = T (1 + (Rv/R - 1) Qdp/dp) in caar
+    (CaarFunctorImpl.hpp:345-360)."""
+    g, o = pair(moisture=True, rsplit=1)
+    for L in (g, o):
+        L.call("hx_run_prim_step", DT)
+    errs = {}
+    for tl in range(3):
+        for k, v in H.compare(g, o, ("v", "T", "dp3d"), tl=tl).items():
+            errs[f"{k}[{tl}]"] = v
+    _assert_close(errs)
+
+
+def test_tensor_hyperviscosity(gpu_path, oracle_path):
+    """hypervis_scaling != 0: laplace_tensor and vlaplace_sphere_wk_cartesian
+    (TagSecondLaplaceTensorHV, HyperviscosityFunctorImpl.hpp:105-125)."""
+    from hommexx_gb300 import abi
+    m = H.M.build_mesh(4, hypervis_scaling=3.2)
+    st = H.state(4, 2)
+    p = abi.SimParams(qsize=2, nu=3.0e-8, nu_div=3.0e-8, hypervis_scaling=3.2, rsplit=1)
+    libs = []
+    for path in (gpu_path, oracle_path):
+        L = H.lib(path)
+        if L.nelem:
+            L.finalize()
+        L.init(m, H.hvc(), p, st)
+        L.call("hx_run_hypervis", 1, DT, 1.0)
+        libs.append(L)
+    g, o = libs
+    _assert_close(H.compare(g, o, ("v", "T", "dp3d"), tl=1))
