@@ -19,6 +19,13 @@ mirrored remap; seeded smooth synthetic initial state (spherical harmonics of de
 * ``cpu_baseline``: the C++/OpenMP oracle (a restatement of the reference's algorithm;
   the reference itself needs Kokkos and cannot be built here) on all host cores, on a
   bounded sample of the same workload.
+* ``adjoint``: the hand-written adjoint of the dry dynamics (RK5 caar + hyperviscosity
+  + PPM remap) at ne16 L72, 24 steps of 300 s: device time of the forward trajectory
+  and of the vector-Jacobian product (state on the device, CUDA events), the cost of
+  a gradient relative to a forward run, and its checks: central finite differences of
+  J = sum spheremp T_final^2 along 10 seeded smooth directions (eps = 1e-6), the
+  dot-product test against the oracle's tangent-linear model, and the mixed form's
+  gradient error against the FP64 one.
 
 ``--impl reference`` times that CPU implementation alone and prints its own line.
 Multi-GPU: the step does not shard here (one GPU per box), so N>1 runs N independent
@@ -240,6 +247,127 @@ def run_gpu(args, rank, world):
     return out, mesh
 
 
+ADJ_NE, ADJ_STEPS, ADJ_QSIZE = 16, 24, 4
+
+
+def _traj_call(fn, ins, outs, *mid):
+    import ctypes
+    a = [ctypes.c_void_p(t.data_ptr()) for t in ins]
+    b = [ctypes.c_void_p(t.data_ptr()) for t in outs]
+    rc = fn(*a, *mid, *b)
+    if rc:
+        raise RuntimeError(f"{fn.__name__} -> {rc}")
+
+
+def _timed(L, f, reps=3):
+    import ctypes
+    ts = []
+    for _ in range(reps):
+        L.lib.hx_timer_start()
+        f()
+        ms = ctypes.c_double(0)
+        L.lib.hx_timer_stop(ctypes.byref(ms))
+        ts.append(ms.value)
+    return float(np.median(ts))
+
+
+def run_adjoint(lib_path, dot_check=True):
+    """Adjoint leg: timings with the state resident on the device, then the checks."""
+    import ctypes
+    import torch
+    from hommexx_gb300 import abi, mesh as M, state as S
+    mesh = M.build_mesh(ADJ_NE)
+    hv = S.hybrid_coordinate()
+    st = S.initial_state(mesh, ADJ_QSIZE, hv)
+    x0 = {"v": st["v"][:, 1], "T": st["T"][:, 1], "dp3d": st["dp3d"][:, 1]}
+    w = mesh.spheremp[:, None]
+    keys = ("v", "T", "dp3d")
+    dev = lambda d: [torch.from_numpy(np.ascontiguousarray(d[k])).cuda() for k in keys]
+    params = abi.SimParams(qsize=ADJ_QSIZE, nu=NU, rsplit=RSPLIT, hypervis_subcycle=HSUB,
+                           nu_top=2.5e5)
+    if dot_check:
+        subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle")], check=True)
+    res = {}
+    grads = {}
+    for precision, tag in ((0, "fp64"), (1, "mixed")):
+        L = abi.HxLibrary(lib_path)
+        L.init(mesh, hv, params, st, precision=precision, abort_on_error=True)
+        xin = dev(x0)
+        xout = [torch.empty_like(t) for t in xin]
+        gout = [torch.empty_like(t) for t in xin]
+        torch.cuda.synchronize()
+        fwd = lambda: _traj_call(L.lib.hx_traj_forward, xin, xout, ctypes.c_int(ADJ_STEPS),
+                                 ctypes.c_double(DT))
+        L.traj_checkpointing(2)
+        fwd()
+        t_plain = _timed(L, fwd)
+        xf = {k: t.cpu().numpy() for k, t in zip(keys, xout)}
+        bar = {"v": np.zeros_like(xf["v"]), "T": 2.0 * w * xf["T"], "dp3d": np.zeros_like(xf["dp3d"])}
+        bard = dev(bar)
+        torch.cuda.synchronize()
+        vjp = lambda: _traj_call(L.lib.hx_traj_vjp, bard, gout)
+        t_b2 = _timed(L, vjp)
+        L.traj_checkpointing(1)
+        fwd()
+        t_f1 = _timed(L, fwd)
+        t_b1 = _timed(L, vjp)
+        L.lib.hx_enable_timing(1)
+        vjp()
+        L.lib.hx_enable_timing(0)
+        stats = sorted(L.kernel_stats(), key=lambda r: -r[2])
+        tot = sum(r[2] for r in stats) or 1.0
+        grads[tag] = {k: t.cpu().numpy() for k, t in zip(keys, gout)}
+        res[tag] = dict(forward_ms=t_plain, forward_checkpointed_ms=t_f1, vjp_ms=t_b1,
+                        vjp_recompute_ms=t_b2,
+                        gradient_cost_vs_forward=(t_f1 + t_b1) / t_plain,
+                        reverse_sweep_vs_forward=t_b1 / t_plain,
+                        recompute_mode_cost_vs_forward=(t_plain + t_b2) / t_plain,
+                        vjp_kernels=[dict(kernel=n, launches=c, total_ms=round(ms, 3),
+                                          share=round(ms / tot, 4)) for n, c, ms in stats[:6]])
+        if tag == "fp64":
+            # central finite differences of J along 10 smooth directions (host API)
+            eps, worst = 1e-6, 0.0
+            g = grads["fp64"]
+            L.traj_checkpointing(2)
+            for i in range(10):
+                d = S.dynamics_direction(mesh, 7000 + i, hv)
+                tp = L.traj_forward({k: x0[k] + eps * d[k] for k in keys}, ADJ_STEPS, DT)["T"]
+                tm = L.traj_forward({k: x0[k] - eps * d[k] for k in keys}, ADJ_STEPS, DT)["T"]
+                fd = float(np.sum(w * (tp - tm) * (tp + tm))) / (2 * eps)
+                ad = sum(float(np.vdot(g[k], d[k])) for k in keys)
+                worst = max(worst, abs(fd - ad) / abs(fd))
+            res["fd_max_rel_err"] = worst
+            if dot_check:
+                rng = np.random.default_rng(2024)
+                dx = {k: rng.standard_normal(x0[k].shape) for k in keys}
+                dy = {k: rng.standard_normal(x0[k].shape) for k in keys}
+                L.traj_forward(x0, ADJ_STEPS, DT)
+                rhs = sum(float(np.vdot(dx[k], v)) for k, v in L.traj_vjp(dy).items())
+                O = abi.HxLibrary(os.path.join(ROOT, "oracle", "liboracle.so"))
+                O.init(mesh, hv, params, st, abort_on_error=True)
+                O.lib.hx_oracle_threads.restype = int
+                t0 = time.perf_counter()
+                O.traj_forward(x0, ADJ_STEPS, DT)
+                lhs = sum(float(np.vdot(v, dy[k])) for k, v in O.traj_jvp(dx).items())
+                res["dot_product"] = dict(tlm_dot=lhs, adjoint_dot=rhs, rel_err=abs(lhs - rhs) / abs(lhs),
+                                          tlm="CPU oracle (dual-number instantiation of its step), "
+                                              f"{O.lib.hx_oracle_threads()} threads, "
+                                              f"{time.perf_counter() - t0:.1f} s")
+                O.finalize()
+        L.finalize()
+    res["mixed_gradient_rel_err"] = {
+        k: float(np.max(np.abs(grads["mixed"][k] - grads["fp64"][k])) / np.max(np.abs(grads["fp64"][k])))
+        for k in keys}
+    res["workload"] = (f"dry dynamics ne{ADJ_NE} L72 ({6 * ADJ_NE * ADJ_NE} elements), {ADJ_STEPS} steps "
+                       f"of {DT:.0f} s, RK5 caar + hyperviscosity (nu {NU:g}, {HSUB} subcycles) + PPM "
+                       f"remap every {RSPLIT} steps; J = sum spheremp T_final^2; gradient w.r.t. "
+                       "initial u, v, T, dp3d")
+    res["checkpoints"] = ("forward_checkpointed keeps every RK-stage, hyperviscosity-subcycle and "
+                          "remap input; vjp_recompute keeps the step inputs only and recomputes each "
+                          "step's stage inputs while reversing it")
+    return res
+
+
 def _barrier(world):
     if world > 1:
         import torch.distributed as dist
@@ -316,6 +444,9 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--ne", type=int, default=NE, help="cubed-sphere resolution (profiling cases)")
     ap.add_argument("--qsize", type=int, default=QSIZE, help="tracer count (profiling cases)")
+    ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint leg")
+    ap.add_argument("--no-dot-check", action="store_true",
+                    help="skip the oracle tangent-linear dot-product check of the adjoint leg")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     NE, QSIZE = args.ne, args.qsize
@@ -404,6 +535,9 @@ def main():
                          "clocks": mx["clocks"]}
         if "mixed_error" in out:
             line["mixed"]["error_vs_fp64"] = out["mixed_error"]
+    if not args.no_adjoint:
+        line["adjoint"] = run_adjoint(os.path.join(ROOT, "hommexx_gb300", "libhxgpu.so"),
+                                      dot_check=not args.no_dot_check)
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline()
     print(json.dumps(line))

@@ -233,5 +233,51 @@ class HxLibrary:
             out.append((nm, int(la[i]), float(ms[i])))
         return out
 
+    # -- dry-dynamics trajectory and its adjoint -----------------------------------------
+    def _dyn_arrays(self, st=None):
+        E = self.nelem
+        shapes = {"v": (E, NLEV, 2, NP, NP), "T": (E, NLEV, NP, NP), "dp3d": (E, NLEV, NP, NP)}
+        if st is None:
+            return {k: np.empty(s) for k, s in shapes.items()}
+        return {k: np.ascontiguousarray(st[k], dtype=np.float64).reshape(shapes[k])
+                for k in shapes}
+
+    def _traj(self, fn: str, inp: dict):
+        a = self._dyn_arrays(inp)
+        out = self._dyn_arrays()
+        rc = fn(C.c_void_p(a["v"].ctypes.data), C.c_void_p(a["T"].ctypes.data),
+                C.c_void_p(a["dp3d"].ctypes.data), C.c_void_p(out["v"].ctypes.data),
+                C.c_void_p(out["T"].ctypes.data), C.c_void_p(out["dp3d"].ctypes.data))
+        if rc:
+            raise RuntimeError(f"{fn.__name__} -> {rc}: {self.last_error()[1]}")
+        return out
+
+    def traj_forward(self, x0: dict, nsteps: int, dt: float) -> dict:
+        """hx_traj_forward: ``x0``/result hold one time level of v, T, dp3d."""
+        a = self._dyn_arrays(x0)
+        out = self._dyn_arrays()
+        rc = self.lib.hx_traj_forward(
+            C.c_void_p(a["v"].ctypes.data), C.c_void_p(a["T"].ctypes.data),
+            C.c_void_p(a["dp3d"].ctypes.data), C.c_int(nsteps), C.c_double(dt),
+            C.c_void_p(out["v"].ctypes.data), C.c_void_p(out["T"].ctypes.data),
+            C.c_void_p(out["dp3d"].ctypes.data))
+        if rc:
+            raise RuntimeError(f"hx_traj_forward -> {rc}: {self.last_error()[1]}")
+        return out
+
+    def traj_vjp(self, bar: dict) -> dict:
+        """hx_traj_vjp: cotangent of the final state -> gradient w.r.t. the initial one."""
+        return self._traj(self.lib.hx_traj_vjp, bar)
+
+    def traj_jvp(self, tan: dict) -> dict:
+        """hx_traj_jvp: tangent of the initial state -> tangent of the final one."""
+        return self._traj(self.lib.hx_traj_jvp, tan)
+
+    def traj_checkpointing(self, mode: int):
+        """hx_traj_set_checkpointing: 0 automatic, 1 every stage input, 2 step inputs."""
+        rc = self.lib.hx_traj_set_checkpointing(C.c_int(mode))
+        if rc:
+            raise RuntimeError(f"hx_traj_set_checkpointing -> {rc}: {self.last_error()[1]}")
+
     def finalize(self):
         self.lib.finalize_hommexx_session()

@@ -1,6 +1,6 @@
 """Builds libhxgpu.so in place (hommexx_gb300/libhxgpu.so) with nvcc for sm_103a.
 
-The two translation units compile in parallel; the library links only the CUDA
+The translation units compile in parallel; the library links only the CUDA
 runtime.  ``HX_NVCC`` overrides the compiler path and ``HX_ARCH`` the -gencode
 argument (default ``arch=compute_103a,code=sm_103a``).
 """
@@ -16,7 +16,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libhxgpu.so")
-SOURCES = ["hx_kernels.cu", "hx_abi.cu", "hx_noalloc.cu"]
+SOURCES = ["hx_kernels.cu", "hx_adjoint.cu", "hx_abi.cu", "hx_noalloc.cu"]
 
 
 def nvcc() -> str:

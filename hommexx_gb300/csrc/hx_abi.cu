@@ -132,6 +132,10 @@ struct Backend {
   virtual void prim_step(double dt) = 0;
   virtual int field(const std::string& name, int tl, double* host, bool get) = 0;
   virtual int dss_field(const std::string& name, int tl, bool rsmp) = 0;
+  virtual void traj_forward(const double* v, const double* T, const double* dp, int nsteps, double dt,
+                            double* vo, double* To, double* dpo) = 0;
+  virtual void traj_vjp(const double* vb, const double* Tb, const double* dpb, double* vg, double* Tg,
+                        double* dpg) = 0;
 };
 
 struct Session;
@@ -151,6 +155,7 @@ struct Session {
   int last_err = 0;
   std::string last_msg;
   bool abort_on_error = true;
+  int traj_mode = 0;  // checkpointing of the dry trajectory (hx_traj_set_checkpointing)
   ~Session() {}
 };
 
@@ -218,6 +223,11 @@ struct BackendT : Backend {
   int *tab_cnt = 0, *tab_src = 0, *nbr = 0, *invalid = 0;
   int* h_invalid = nullptr;
   size_t staging_n = 0;
+  // The state arrays the caar, hyperviscosity and remap launches work on: the model
+  // state (default) or the dry trajectory's own levels.
+  struct Work {
+    double *v, *T, *dp, *phi, *dpdiss_ave, *dpdiss_bih, *ps_v;
+  } wk{};
 
   ~BackendT() override {
     void* ptrs[] = {D, Dinv, metinv, metdet, spheremp, rspheremp, mp, fcor, phis, tensorvisc, vec_sph2cart,
@@ -227,6 +237,7 @@ struct BackendT : Backend {
     for (void* p : ptrs)
       if (p) cudaFree(p);
     if (h_invalid) cudaFreeHost(h_invalid);
+    free_traj();
   }
 
   size_t N3() const { return (size_t)E * NLEV * 16; }
@@ -255,6 +266,7 @@ struct BackendT : Backend {
     gen_scr = dalloc<double>(n3 * (Q > 2 ? Q : 2));
     invalid = dalloc<int>(1);
     ck(cudaMallocHost(&h_invalid, sizeof(int)), "cudaMallocHost");
+    wk = Work{v, T, dp, phi, dpdiss_ave, dpdiss_bih, ps_v};
   }
 
   // metric arrays in R (host conversion: small arrays, once)
@@ -353,14 +365,14 @@ struct BackendT : Backend {
   void caar_stage(int nm1, int n0, int np1, double dt, double w, int n0_qdp, int combine, int n0orig) override {
     CaarArgs<R> a;
     a.m = metric();
-    a.v = v; a.T = T; a.dp = dp; a.vn0 = vn0; a.omega_p = omega_p; a.phi = phi;
+    a.v = wk.v; a.T = wk.T; a.dp = wk.dp; a.vn0 = vn0; a.omega_p = omega_p; a.phi = wk.phi;
     a.qdp = qdp; a.qsize = Q; a.n0_qdp = n0_qdp;
     a.out = caar_out; a.nm1 = nm1; a.n0 = n0;
     a.dt = dt; a.eta_ave_w = w; a.p_top = s.hyai[0] * s.ps0;
     a.rk_combine = combine; a.n0orig = n0orig;
     launch_caar<R>(a, E, g_stream);
     post("caar");
-    launch_dss_state(E, caar_out, v, T, dp, np1, rsp_d, table(), g_stream);
+    launch_dss_state(E, caar_out, wk.v, wk.T, wk.dp, np1, rsp_d, table(), g_stream);
     post("dss_caar");
   }
 
@@ -373,13 +385,16 @@ struct BackendT : Backend {
     caar_stage(nm1, np1, np1, 3.0 * dt / 4.0, 3.0 * w / 4.0, n0_qdp, 1, n0);
   }
 
-  void hypervis(int np1, double dt, double w) override {
+  void hypervis(int np1, double dt, double w) override { hypervis_cycles(np1, dt, w, s.prm.hypervis_subcycle); }
+
+  // ncyc of the hypervis_subcycle subcycles of HyperviscosityFunctorImpl::run
+  void hypervis_cycles(int np1, double dt, double w, int ncyc) {
     HvArgs<R> a;
     a.m = metric();
     a.dss = table();
-    a.v = v; a.T = T; a.dp = dp; a.dpdiss_ave = dpdiss_ave; a.dpdiss_bih = dpdiss_bih;
+    a.v = wk.v; a.T = wk.T; a.dp = wk.dp; a.dpdiss_ave = wk.dpdiss_ave; a.dpdiss_bih = wk.dpdiss_bih;
     a.bufA = bufA; a.bufB = bufB;
-    a.np1 = np1; a.hsub = s.prm.hypervis_subcycle; a.consthv = s.consthv ? 1 : 0;
+    a.np1 = np1; a.hsub = s.prm.hypervis_subcycle; a.ncyc = ncyc; a.consthv = s.consthv ? 1 : 0;
     a.dt = dt / s.prm.hypervis_subcycle; a.eta_ave_w = w;
     a.nu = s.prm.nu; a.nu_s = s.prm.nu_s; a.nu_p = s.prm.nu_p; a.nu_top = s.prm.nu_top;
     a.nu_ratio1 = s.prm.nu_ratio1; a.nu_ratio2 = s.prm.nu_ratio2;
@@ -427,12 +442,13 @@ struct BackendT : Backend {
     euler_step(s.tl.np1_qdp, s.tl.np1_qdp, dt / 2.0, 2.0, 1, s.tl.n0_qdp);
   }
 
-  void launch_remap(int np1, int np1_qdp) {
+  // reset = false keeps an invalid-thickness flag raised by an earlier remap.
+  void launch_remap(int np1, int np1_qdp, bool reset = true) {
     RemapArgs a;
-    a.v = v; a.T = T; a.dp = dp; a.qdp = qdp; a.ps_v = ps_v;
-    a.np1 = np1; a.n0_qdp = np1_qdp; a.Q = Q; a.remap_alg = s.prm.remap_alg; a.nelem = E;
+    a.v = wk.v; a.T = wk.T; a.dp = wk.dp; a.qdp = qdp; a.ps_v = wk.ps_v;
+    a.np1 = np1; a.n0_qdp = np1_qdp; a.Q = wk.v == v ? Q : 0; a.remap_alg = s.prm.remap_alg; a.nelem = E;
     a.ps0 = s.ps0; a.hyai0 = s.hyai[0]; a.invalid = invalid;
-    ck(cudaMemsetAsync(invalid, 0, sizeof(int), g_stream), "memset");
+    if (reset) ck(cudaMemsetAsync(invalid, 0, sizeof(int), g_stream), "memset");
     hx::launch_remap<R>(a, g_stream);
     post("remap");
   }
@@ -534,6 +550,261 @@ struct BackendT : Backend {
     ck(cudaStreamSynchronize(g_stream), "dss_field");
     return 0;
   }
+  // ---- dry-dynamics trajectory and its adjoint --------------------------------------
+  // Work levels [E][3][...] of the trajectory (the model state is left untouched), a
+  // checkpoint pool of single-level states and five single-level cotangent/io states.
+  struct Traj {
+    double *v3 = nullptr, *T3 = nullptr, *dp3 = nullptr, *phi = nullptr, *dpa = nullptr,
+           *dpb = nullptr, *ps = nullptr, *cot = nullptr, *pool = nullptr;
+    size_t pool_states = 0;
+    int nsteps = 0, mode = 1, cur = 1;
+    double dt = 0;
+    bool have = false;
+  } tj;
+
+  void free_traj() {
+    void* ptrs[] = {tj.v3, tj.T3, tj.dp3, tj.phi, tj.dpa, tj.dpb, tj.ps, tj.cot, tj.pool};
+    for (void* q : ptrs)
+      if (q) cudaFree(q);
+    tj = Traj();
+  }
+
+  size_t state_doubles() const { return 4 * N3(); }
+  DynV single(double* b) const {
+    return DynV{b, b + 2 * N3(), b + 3 * N3(), (long long)NLEV * 32, (long long)NLEV * 16};
+  }
+  DynV level3(int tl) const {
+    return DynV{tj.v3 + (size_t)tl * NLEV * 32, tj.T3 + (size_t)tl * NLEV * 16,
+                tj.dp3 + (size_t)tl * NLEV * 16, (long long)NTL * NLEV * 32, (long long)NTL * NLEV * 16};
+  }
+  DynV cot(int i) const { return single(tj.cot + (size_t)i * state_doubles()); }
+  DynV ckpt(size_t i) const { return single(tj.pool + i * state_doubles()); }
+
+  int stage_states() const { return 5 + s.prm.hypervis_subcycle + 1; }
+  bool remaps_after(int step) const { return s.prm.rsplit > 0 && (step + 1) % s.prm.rsplit == 0; }
+
+  void traj_alloc_work() {
+    if (tj.v3) return;
+    const size_t n3 = N3();
+    tj.v3 = dalloc<double>(n3 * NTL * 2);
+    tj.T3 = dalloc<double>(n3 * NTL);
+    tj.dp3 = dalloc<double>(n3 * NTL);
+    tj.phi = dalloc<double>(n3);
+    tj.dpa = dalloc<double>(n3);
+    tj.dpb = dalloc<double>(n3);
+    tj.ps = dalloc<double>((size_t)E * NTL * 16);
+    tj.cot = dalloc<double>(5 * state_doubles());
+  }
+
+  // Checkpoint pool: mode 1 keeps every stage input of every step; mode 2 keeps the
+  // step inputs plus one step's stage inputs (recomputed when reversing that step).
+  void traj_alloc_pool(int nsteps) {
+    const size_t per = state_doubles() * sizeof(double);
+    const size_t all = (size_t)nsteps * stage_states();
+    const size_t lean = (size_t)nsteps + stage_states();
+    int mode = s.traj_mode;
+    if (mode == 0) {
+      size_t fr = 0, tot = 0;
+      ck(cudaMemGetInfo(&fr, &tot), "cudaMemGetInfo");
+      const size_t have = fr + tj.pool_states * per;
+      const size_t reserve = (size_t)4 << 30;  // headroom for the rest of the process
+      mode = (all * per + reserve <= have) ? 1 : 2;
+    }
+    const size_t need = mode == 1 ? all : lean;
+    if (need > tj.pool_states) {
+      if (tj.pool) cudaFree(tj.pool);
+      tj.pool = nullptr;
+      tj.pool_states = 0;
+      void* q = nullptr;
+      if (cudaMalloc(&q, need * per) != cudaSuccess) {
+        cudaGetLastError();
+        fail(HX_ERR_CUDA, "hx_traj_forward: not enough device memory for the checkpoints (" +
+                              std::to_string(need * per >> 20) + " MiB)");
+      }
+      tj.pool = static_cast<double*>(q);
+      tj.pool_states = need;
+    }
+    tj.mode = mode;
+  }
+
+  // Selects the trajectory's work arrays for the caar / hyperviscosity / remap launches.
+  struct WorkScope {
+    BackendT& b;
+    Work saved;
+    explicit WorkScope(BackendT& bb) : b(bb), saved(bb.wk) {
+      b.wk = Work{b.tj.v3, b.tj.T3, b.tj.dp3, b.tj.phi, b.tj.dpa, b.tj.dpb, b.tj.ps};
+    }
+    ~WorkScope() { b.wk = saved; }
+  };
+
+  // One dry step on the work levels; the state enters and leaves at level tj.cur.  When
+  // keep is non-null it receives the stage inputs: 0-4 the RK stage inputs, 5 .. 4+hsub
+  // the hyperviscosity subcycle inputs, 5+hsub the remap input.
+  void traj_step(double dt, bool remap, size_t keep) {
+    const int n0 = tj.cur, nm1 = (n0 + 2) % 3, np1 = (n0 + 1) % 3;
+    const bool k = keep != (size_t)-1;
+    auto save = [&](int i, int tl) {
+      if (k) launch_copy_dyn(E, ckpt(keep + i), level3(tl), g_stream);
+    };
+    save(0, n0);
+    caar_stage(n0, n0, nm1, dt / 5.0, 0.0, -1, 0, n0);
+    save(1, nm1);
+    caar_stage(n0, nm1, np1, dt / 5.0, 0.0, -1, 0, n0);
+    save(2, np1);
+    caar_stage(n0, np1, np1, dt / 3.0, 0.0, -1, 0, n0);
+    save(3, np1);
+    caar_stage(n0, np1, np1, 2.0 * dt / 3.0, 0.0, -1, 0, n0);
+    save(4, np1);
+    caar_stage(nm1, np1, np1, 3.0 * dt / 4.0, 0.0, -1, 1, n0);
+    const int hsub = s.prm.hypervis_subcycle;
+    for (int i = 0; i < hsub; ++i) {
+      save(5 + i, np1);
+      hypervis_cycles(np1, dt, 0.0, 1);
+    }
+    if (remap) {
+      save(5 + hsub, np1);
+      launch_remap(np1, 0, false);
+      launch_dp_from_ps(E, tj.dp3, tj.ps, np1, s.ps0, g_stream);
+      post("dp3d_from_ps");
+    }
+    tj.cur = np1;
+  }
+
+  void traj_forward(const double* hv, const double* hT, const double* hdp, int nsteps, double dt,
+                    double* ov, double* oT, double* odp) override {
+    if (!s.consthv) fail(12, "trajectory: tensor hyperviscosity (hypervis_scaling != 0) has no adjoint");
+    if (nsteps < 0 || !(dt > 0)) fail(HX_ERR_STATE, "hx_traj_forward: nsteps must be >= 0 and dt > 0");
+    tj.have = false;
+    traj_alloc_work();
+    traj_alloc_pool(nsteps);
+    const size_t n3 = N3();
+    DynV io = cot(4);
+    ck(cudaMemcpyAsync(io.v, hv, 2 * n3 * sizeof(double), cudaMemcpyDefault, g_stream), "traj in");
+    ck(cudaMemcpyAsync(io.T, hT, n3 * sizeof(double), cudaMemcpyDefault, g_stream), "traj in");
+    ck(cudaMemcpyAsync(io.dp, hdp, n3 * sizeof(double), cudaMemcpyDefault, g_stream), "traj in");
+    tj.cur = 1;
+    launch_copy_dyn(E, level3(tj.cur), io, g_stream);
+    ck(cudaMemsetAsync(invalid, 0, sizeof(int), g_stream), "memset");
+    {
+      WorkScope ws(*this);
+      for (int st = 0; st < nsteps; ++st) {
+        const size_t keep = tj.mode == 1 ? (size_t)st * stage_states() : (size_t)-1;
+        if (tj.mode == 2) launch_copy_dyn(E, ckpt(st), level3(tj.cur), g_stream);
+        traj_step(dt, remaps_after(st), keep);
+      }
+    }
+    launch_copy_dyn(E, io, level3(tj.cur), g_stream);
+    ck(cudaMemcpyAsync(ov, io.v, 2 * n3 * sizeof(double), cudaMemcpyDefault, g_stream), "traj out");
+    ck(cudaMemcpyAsync(oT, io.T, n3 * sizeof(double), cudaMemcpyDefault, g_stream), "traj out");
+    ck(cudaMemcpyAsync(odp, io.dp, n3 * sizeof(double), cudaMemcpyDefault, g_stream), "traj out");
+    if (remap_status()) fail(101, "Negative (or nan) layer thickness detected, aborting!");
+    tj.nsteps = nsteps;
+    tj.dt = dt;
+    tj.have = true;
+  }
+
+  void zero(DynV d) {
+    ck(cudaMemsetAsync(d.v, 0, state_doubles() * sizeof(double), g_stream), "memset");
+  }
+
+  // caar stage reversed: aout -> xm_bar (+=), x0_bar (+=)
+  void caar_vjp(DynV x, DynV aout, DynV xm_bar, DynV x0_bar, double dt) {
+    CaarVjpArgs<R> a;
+    a.m = metric();
+    a.dss = table();
+    a.x = x; a.aout = aout; a.xm_bar = xm_bar; a.x0_bar = x0_bar;
+    a.dt = dt; a.p_top = s.hyai[0] * s.ps0;
+    launch_caar_vjp<R>(a, E, g_stream);
+    post("caar_vjp");
+  }
+
+  // One step reversed; st(i) are its stage inputs; the cotangent is in cot(0) on entry
+  // and on exit.  Uses cot(1..3) as scratch.
+  template <typename ST>
+  void step_vjp(ST&& st, double dt, bool remap) {
+    const int hsub = s.prm.hypervis_subcycle;
+    DynV A = cot(0), P = cot(1), Qb = cot(2), B1 = cot(3);
+    if (remap) {
+      RemapVjpArgs r;
+      r.x = st(5 + hsub); r.a = A; r.remap_alg = s.prm.remap_alg; r.nelem = E;
+      r.ps0 = s.ps0; r.hyai0 = s.hyai[0];
+      launch_remap_vjp(r, g_stream);
+      post("remap_vjp");
+    }
+    for (int i = hsub - 1; i >= 0; --i) {
+      // recompute the subcycle's output on a work level
+      const int w = (tj.cur + 1) % 3;
+      launch_copy_dyn(E, level3(w), st(5 + i), g_stream);
+      {
+        WorkScope ws(*this);
+        hypervis_cycles(w, dt, 0.0, 1);
+      }
+      HvVjpArgs<R> h;
+      h.m = metric();
+      h.dss = table();
+      h.x = st(5 + i); h.xo = level3(w); h.a = A; h.xb = P;
+      h.pre = bufA; h.mid = bufB;
+      h.dt = dt / hsub; h.nu = s.prm.nu; h.nu_s = s.prm.nu_s; h.nu_p = s.prm.nu_p;
+      h.nu_top = s.prm.nu_top; h.nu_ratio1 = s.prm.nu_ratio1; h.nu_ratio2 = s.prm.nu_ratio2;
+      launch_hv_vjp<R>(h, E, g_stream);
+      post("hv_vjp");
+      std::swap(A, P);
+    }
+    if (A.v != cot(0).v) {  // odd number of subcycles: bring the cotangent back to cot(0)
+      launch_copy_dyn(E, cot(0), A, g_stream);
+      A = cot(0);
+      P = cot(1);
+    }
+    // RK5: X1 = C(X0,X0), X2 = C(X0,X1), X3 = C(X0,X2), X4 = C(X0,X3),
+    // X5 = C((5 X1 - X0)/4, X4)
+    zero(P);
+    zero(Qb);
+    caar_vjp(st(4), A, Qb, P, 3.0 * dt / 4.0);          // Qb = Y_bar, P = X4_bar
+    zero(A);
+    zero(B1);
+    launch_rk5_comb_vjp(E, Qb, B1, A, g_stream);         // A = X0_bar, B1 = X1_bar
+    post("rk5_comb_vjp");
+    zero(Qb);
+    caar_vjp(st(3), P, A, Qb, 2.0 * dt / 3.0);           // Qb = X3_bar
+    zero(P);
+    caar_vjp(st(2), Qb, A, P, dt / 3.0);                 // P = X2_bar
+    caar_vjp(st(1), P, A, B1, dt / 5.0);
+    caar_vjp(st(0), B1, A, A, dt / 5.0);
+  }
+
+  void traj_vjp(const double* hvb, const double* hTb, const double* hdpb, double* gv, double* gT,
+                double* gdp) override {
+    if (!tj.have) fail(HX_ERR_STATE, "trajectory: run hx_traj_forward first");
+    const size_t n3 = N3();
+    DynV A = cot(0);
+    ck(cudaMemcpyAsync(A.v, hvb, 2 * n3 * sizeof(double), cudaMemcpyDefault, g_stream), "vjp in");
+    ck(cudaMemcpyAsync(A.T, hTb, n3 * sizeof(double), cudaMemcpyDefault, g_stream), "vjp in");
+    ck(cudaMemcpyAsync(A.dp, hdpb, n3 * sizeof(double), cudaMemcpyDefault, g_stream), "vjp in");
+    for (int st = tj.nsteps - 1; st >= 0; --st) {
+      const bool rm = remaps_after(st);
+      if (tj.mode == 1) {
+        const size_t base = (size_t)st * stage_states();
+        step_vjp([&](int i) { return ckpt(base + i); }, tj.dt, rm);
+      } else {
+        // recompute the step's stage inputs from its checkpointed input state
+        const size_t base = (size_t)tj.nsteps;
+        const int keep_cur = tj.cur;
+        tj.cur = 1;
+        launch_copy_dyn(E, level3(1), ckpt(st), g_stream);
+        {
+          WorkScope ws(*this);
+          traj_step(tj.dt, rm, base);
+        }
+        tj.cur = keep_cur;
+        step_vjp([&](int i) { return ckpt(base + i); }, tj.dt, rm);
+      }
+    }
+    ck(cudaMemcpyAsync(gv, A.v, 2 * n3 * sizeof(double), cudaMemcpyDefault, g_stream), "vjp out");
+    ck(cudaMemcpyAsync(gT, A.T, n3 * sizeof(double), cudaMemcpyDefault, g_stream), "vjp out");
+    ck(cudaMemcpyAsync(gdp, A.dp, n3 * sizeof(double), cudaMemcpyDefault, g_stream), "vjp out");
+    ck(cudaStreamSynchronize(g_stream), "vjp");
+  }
+
 };
 
 
@@ -882,6 +1153,29 @@ int hx_timer_stop(double* ms) {
     float f = 0.f;
     ck(cudaEventElapsedTime(&f, g_t0, g_t1), "cudaEventElapsedTime");
     *ms = f;
+  });
+}
+
+int hx_traj_forward(const double* v, const double* T, const double* dp3d, int nsteps, double dt,
+                    double* v_out, double* T_out, double* dp3d_out) {
+  return run([&] { B().traj_forward(v, T, dp3d, nsteps, dt, v_out, T_out, dp3d_out); });
+}
+
+int hx_traj_vjp(const double* v_bar, const double* T_bar, const double* dp3d_bar, double* v_grad,
+                double* T_grad, double* dp3d_grad) {
+  return run([&] { B().traj_vjp(v_bar, T_bar, dp3d_bar, v_grad, T_grad, dp3d_grad); });
+}
+
+int hx_traj_jvp(const double*, const double*, const double*, double*, double*, double*) {
+  return run([&] {
+    fail(HX_ERR_STATE, "hx_traj_jvp: the tangent-linear model is provided by the CPU oracle only");
+  });
+}
+
+int hx_traj_set_checkpointing(int mode) {
+  return run([&] {
+    if (mode < 0 || mode > 2) fail(HX_ERR_STATE, "hx_traj_set_checkpointing: mode must be 0, 1 or 2");
+    S().traj_mode = mode;
   });
 }
 

@@ -16,242 +16,11 @@
 //   prim_driver.cpp:90-206, prim_step.cpp:42-66, prim_advance_exp.cpp:138-156.
 #include <cstdio>
 
-#include "hx_kernels.cuh"
+#include "hx_device.cuh"
 
 namespace hx {
 
 namespace {
-
-constexpr unsigned FULL = 0xffffffffu;
-constexpr int SROW = 17;  // padded shared-memory row of 16 points
-
-__constant__ double c_dvv[16];
-__constant__ float c_dvvf[16];
-__constant__ double c_hyai[NLEV + 1];
-__constant__ double c_hybi[NLEV + 1];
-__constant__ double c_ai_delta[NLEV];
-__constant__ double c_bi_delta[NLEV];
-
-template <typename R> __device__ __forceinline__ R dvv_at(int a, int b);
-template <> __device__ __forceinline__ double dvv_at<double>(int a, int b) { return c_dvv[a * 4 + b]; }
-template <> __device__ __forceinline__ float dvv_at<float>(int a, int b) { return c_dvvf[a * 4 + b]; }
-
-template <typename R> __device__ __forceinline__ R sh16(R v, int src) {
-  return __shfl_sync(FULL, v, src, 16);
-}
-
-template <typename R> __device__ __forceinline__ R rre() { return R(kRrearth); }
-
-template <typename R> constexpr bool kF32 = sizeof(R) == 4;
-
-// A double field value as operator input.  In the mixed form the value at point 0 of the
-// same level and element is subtracted first (in double): the sphere operators annihilate
-// constants, and the FP32 operand then carries the horizontal variation instead of the
-// large mean (pressure, geopotential, temperature, layer thickness).  In the FP64 form the
-// value is used as is, so the arithmetic follows the reference formulas.
-template <typename R> __device__ __forceinline__ R rel(double x) {
-  if constexpr (kF32<R>) return (R)(x - sh16(x, 0));
-  else return x;
-}
-
-// Per-thread GLL point data: index, dvv rows/columns for the four contractions.
-template <typename R>
-struct Pt {
-  int p, i, j;
-  R dx[4], dy[4], tx[4], ty[4];
-  __device__ __forceinline__ void init(int p_) {
-    p = p_;
-    i = p >> 2;
-    j = p & 3;
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-      dx[k] = dvv_at<R>(j, k);
-      dy[k] = dvv_at<R>(i, k);
-      tx[k] = dvv_at<R>(k, j);
-      ty[k] = dvv_at<R>(k, i);
-    }
-  }
-  // sum_k dvv[j][k] s(i,k)  — derivative along jgp (x1)
-  __device__ __forceinline__ R ddx(R s) const {
-    R a = 0;
-#pragma unroll
-    for (int k = 0; k < 4; ++k) a += dx[k] * sh16(s, 4 * i + k);
-    return a;
-  }
-  // sum_k dvv[i][k] s(k,j)  — derivative along igp (x2)
-  __device__ __forceinline__ R ddy(R s) const {
-    R a = 0;
-#pragma unroll
-    for (int k = 0; k < 4; ++k) a += dy[k] * sh16(s, 4 * k + j);
-    return a;
-  }
-  // sum_k w(i,k) dvv[k][j]  — weak-form row contraction
-  __device__ __forceinline__ R wrow(R w) const {
-    R a = 0;
-#pragma unroll
-    for (int k = 0; k < 4; ++k) a += sh16(w, 4 * i + k) * tx[k];
-    return a;
-  }
-  // sum_k w(k,j) dvv[k][i]  — weak-form column contraction
-  __device__ __forceinline__ R wcol(R w) const {
-    R a = 0;
-#pragma unroll
-    for (int k = 0; k < 4; ++k) a += sh16(w, 4 * k + j) * ty[k];
-    return a;
-  }
-};
-
-// Metric of one GLL point of one element.
-template <typename R>
-struct PM {
-  R di00, di01, di10, di11, d00, d01, d10, d11, md, fdiv, sp, mp, a00, a01, a10, a11, rsp;
-  R l00, l01, l10, l11;  // spheremp * (Dinv Dinv^T) * rrearth, for laplace_simple
-  __device__ __forceinline__ void load(const MetricP<R>& m, int e, int p) {
-    const R* Di = m.Dinv + (size_t)e * 64;
-    const R* D = m.D + (size_t)e * 64;
-    const R* Mi = m.metinv + (size_t)e * 64;
-    di00 = Di[p]; di01 = Di[16 + p]; di10 = Di[32 + p]; di11 = Di[48 + p];
-    d00 = D[p]; d01 = D[16 + p]; d10 = D[32 + p]; d11 = D[48 + p];
-    md = m.metdet[(size_t)e * 16 + p];
-    fdiv = R(1.0) / md * rre<R>();
-    sp = m.spheremp[(size_t)e * 16 + p];
-    rsp = m.rspheremp[(size_t)e * 16 + p];
-    mp = m.mp[(size_t)e * 16 + p];
-    a00 = Mi[p] * md; a01 = Mi[16 + p] * md; a10 = Mi[32 + p] * md; a11 = Mi[48 + p] * md;
-    // c = (Dinv^T-contraction of the Dinv-contraction): c_a = sum_b K_ab v_b with
-    // K_ab = sum_c Dinv(c,a) Dinv(c,b) in the reference's C++ indices.
-    l00 = sp * (di00 * di00 + di10 * di10) * rre<R>();
-    l01 = sp * (di00 * di01 + di10 * di11) * rre<R>();
-    l10 = sp * (di01 * di00 + di11 * di10) * rre<R>();
-    l11 = sp * (di01 * di01 + di11 * di11) * rre<R>();
-  }
-};
-
-// ---- sphere operators on one point-level (SphereOperators.hpp) ------------------------
-template <typename R>
-__device__ __forceinline__ void gradient_sphere(const Pt<R>& t, const PM<R>& m, R s, R& g0, R& g1) {
-  const R v0 = t.ddx(s) * rre<R>();
-  const R v1 = t.ddy(s) * rre<R>();
-  g0 = m.di00 * v0 + m.di01 * v1;
-  g1 = m.di10 * v0 + m.di11 * v1;
-}
-
-template <typename R>
-__device__ __forceinline__ R divergence_sphere(const Pt<R>& t, const PM<R>& m, R v0, R v1) {
-  const R gv0 = (m.di00 * v0 + m.di10 * v1) * m.md;
-  const R gv1 = (m.di01 * v0 + m.di11 * v1) * m.md;
-  return (t.ddx(gv0) + t.ddy(gv1)) * m.fdiv;
-}
-
-template <typename R>
-__device__ __forceinline__ R vorticity_sphere(const Pt<R>& t, const PM<R>& m, R v0, R v1) {
-  const R c0 = m.d00 * v0 + m.d01 * v1;
-  const R c1 = m.d10 * v0 + m.d11 * v1;
-  return (t.ddx(c1) - t.ddy(c0)) * m.fdiv;
-}
-
-// divergence_sphere_wk of the vector (g0, g1)
-template <typename R>
-__device__ __forceinline__ R divergence_sphere_wk(const Pt<R>& t, const PM<R>& m, R g0, R g1) {
-  const R w0 = m.sp * (m.di00 * g0 + m.di10 * g1);
-  const R w1 = m.sp * (m.di01 * g0 + m.di11 * g1);
-  return -(t.wrow(w0) + t.wcol(w1)) * rre<R>();
-}
-
-// laplace_simple = divergence_sphere_wk(gradient_sphere(s)).  The two metric
-// transforms compose to Dinv Dinv^T = metinv, so the weak-form operands are
-// spheremp metinv rrearth (d s/dx, d s/dy); m.l00/l01/l10/l11 hold that product.
-template <typename R>
-__device__ __forceinline__ R laplace_simple(const Pt<R>& t, const PM<R>& m, R s) {
-  const R sx = t.ddx(s), sy = t.ddy(s);
-  const R w0 = m.l00 * sx + m.l01 * sy;
-  const R w1 = m.l10 * sx + m.l11 * sy;
-  return -(t.wrow(w0) + t.wcol(w1)) * rre<R>();
-}
-
-template <typename R>
-__device__ __forceinline__ R laplace_tensor(const Pt<R>& t, const PM<R>& m, const R* tv, R s) {
-  R g0, g1;
-  gradient_sphere(t, m, s, g0, g1);
-  const R t0 = tv[0] * g0 + tv[2] * g1;
-  const R t1 = tv[1] * g0 + tv[3] * g1;
-  return divergence_sphere_wk(t, m, t0, t1);
-}
-
-// vlaplace_sphere_wk_contra (SphereOperators.hpp:816-862)
-template <typename R>
-__device__ __forceinline__ void vlaplace_contra(const Pt<R>& t, const PM<R>& m, R nu_ratio, R v0, R v1,
-                                                R& l0, R& l1) {
-  R div = divergence_sphere(t, m, v0, v1);
-  if (nu_ratio > R(0) && nu_ratio != R(1)) div *= nu_ratio;
-  // grad_sphere_wk_testcov(div)
-  const R w = m.mp * div;
-  const R X = t.wrow(w), Y = t.wcol(w);
-  const R b0 = -(m.a00 * X + m.a01 * Y);
-  const R b1 = -(m.a10 * X + m.a11 * Y);
-  R g0 = (m.d00 * b0 + m.d10 * b1) * rre<R>();
-  R g1 = (m.d01 * b0 + m.d11 * b1) * rre<R>();
-  // curl_sphere_wk_testcov_update(-1, 1, vort, g)
-  const R vort = vorticity_sphere(t, m, v0, v1);
-  const R wv = m.mp * vort;
-  const R sb0 = -t.wcol(wv), sb1 = t.wrow(wv);
-  g0 = g0 - (m.d00 * sb0 + m.d10 * sb1) * rre<R>();
-  g1 = g1 - (m.d01 * sb0 + m.d11 * sb1) * rre<R>();
-  const R f = R(2) * m.sp * rre<R>() * rre<R>();
-  l0 = f * v0 + g0;
-  l1 = f * v1 + g1;
-}
-
-// vlaplace_sphere_wk_cartesian (SphereOperators.hpp:750-814); tv = tensorVisc[0..3],
-// s2c = vec_sph2cart[2][3] of this point.
-template <typename R>
-__device__ __forceinline__ void vlaplace_cartesian(const Pt<R>& t, const PM<R>& m, const R* tv, const R* s2c,
-                                                   R v0, R v1, R& l0, R& l1) {
-  R lc[3];
-#pragma unroll
-  for (int c = 0; c < 3; ++c) lc[c] = laplace_tensor(t, m, tv, s2c[c] * v0 + s2c[3 + c] * v1);
-  const R f = R(2) * m.sp * rre<R>() * rre<R>();
-  l0 = s2c[0] * lc[0] + s2c[1] * lc[1] + s2c[2] * lc[2] + f * v0;
-  l1 = s2c[3] * lc[0] + s2c[4] * lc[1] + s2c[5] * lc[2] + f * v1;
-}
-
-// DSS gather of one point-level: own value plus the table's sources, in order, in double.
-template <typename T>
-__device__ __forceinline__ double dss_gather(const T* base, long long es, int ls, int e, int l, int p,
-                                             const DssTable& tab) {
-  const int ep = e * 16 + p;
-  double acc = (double)base[(size_t)e * es + (size_t)l * ls + p];
-  const int n = tab.cnt[ep];
-  for (int k = 0; k < n; ++k) {
-    const int s = tab.src[ep * MAXSRC + k];
-    acc += (double)base[(size_t)(s >> 4) * es + (size_t)l * ls + (s & 15)];
-  }
-  return acc;
-}
-
-// ---- segmented column scans (128 threads: 16 columns x 8 segments of 9 levels) ------
-// Exclusive prefix of the per-segment totals within an 8-lane group.
-__device__ __forceinline__ double seg_excl_prefix(double tot, int seg) {
-  double incl = tot;
-#pragma unroll
-  for (int off = 1; off < 8; off <<= 1) {
-    const double y = __shfl_up_sync(FULL, incl, off, 8);
-    if (seg >= off) incl += y;
-  }
-  double ex = __shfl_up_sync(FULL, incl, 1, 8);
-  return seg == 0 ? 0.0 : ex;
-}
-// Exclusive suffix (sum of later segments).
-__device__ __forceinline__ double seg_excl_suffix(double tot, int seg) {
-  double incl = tot;
-#pragma unroll
-  for (int off = 1; off < 8; off <<= 1) {
-    const double y = __shfl_down_sync(FULL, incl, off, 8);
-    if (seg + off < 8) incl += y;
-  }
-  double ex = __shfl_down_sync(FULL, incl, 1, 8);
-  return seg == 7 ? 0.0 : ex;
-}
 
 // ======================================================================================
 // Caar RK stage (CaarFunctorImpl::operator(), rsplit > 0), one CTA per element.
@@ -995,23 +764,6 @@ constexpr int R_COEF = R_AI + 74;      // coef[3][72]
 constexpr int R_RD = R_COEF + 216;     // 1 / D[0 .. 71]
 constexpr int R_COL = R_RD + 72;       // doubles per column
 
-// Exclusive prefix over the warp of one value per lane.
-__device__ __forceinline__ double warp_excl_scan(double v, int lane) {
-  double incl = v;
-#pragma unroll
-  for (int off = 1; off < 32; off <<= 1) {
-    const double y = __shfl_up_sync(FULL, incl, off);
-    if (lane >= off) incl += y;
-  }
-  const double ex = __shfl_up_sync(FULL, incl, 1);
-  return lane == 0 ? 0.0 : ex;
-}
-__device__ __forceinline__ double warp_sum(double v) {
-#pragma unroll
-  for (int off = 16; off >= 1; off >>= 1) v += __shfl_xor_sync(FULL, v, off);
-  return v;
-}
-
 // PPM vertical remap (RemapFunctor + PpmVertRemap, rsplit > 0), one warp per column:
 // lane L owns levels 3L .. 3L+2 (L < 24) for level work and interfaces j = 3L .. 3L+2
 // (L < 25) for the grid quantities; column scans are warp shuffles, phases are
@@ -1261,31 +1013,25 @@ __global__ void __launch_bounds__(RT) k_remap(RemapArgs a) {
   }
 }
 
-// ---- launch bookkeeping --------------------------------------------------------------
-const char* g_last = "";
-void (*g_before)(const char*, cudaStream_t) = nullptr;
-void (*g_after)(const char*, cudaStream_t) = nullptr;
-
-struct KScope {
-  const char* n;
-  cudaStream_t s;
-  KScope(const char* name, cudaStream_t st) : n(name), s(st) {
-    g_last = name;
-    if (g_before) g_before(name, st);
-  }
-  ~KScope() {
-    if (g_after) g_after(n, s);
-  }
-};
-
-inline int nblk(long long n, int b) { return (int)((n + b - 1) / b); }
-
 template <typename R> constexpr int LG_CAAR() { return 8; }
 template <typename R> constexpr int LG_HV() { return 8; }
 template <typename R> constexpr int LG_TR() { return 8; }
 
 }  // namespace
 
+namespace {
+const char* g_last = "";
+void (*g_before)(const char*, cudaStream_t) = nullptr;
+void (*g_after)(const char*, cudaStream_t) = nullptr;
+}  // namespace
+
+void kernel_enter(const char* name, cudaStream_t s) {
+  g_last = name;
+  if (g_before) g_before(name, s);
+}
+void kernel_leave(const char* name, cudaStream_t s) {
+  if (g_after) g_after(name, s);
+}
 const char* last_kernel_name() { return g_last; }
 void set_kernel_hook(void (*b)(const char*, cudaStream_t), void (*a)(const char*, cudaStream_t)) {
   g_before = b;
@@ -1308,6 +1054,7 @@ void upload_constants(const double* dvv16, const double* hyai, const double* hyb
   cudaMemcpyToSymbolAsync(c_hybi, hybi, sizeof(double) * (NLEV + 1), 0, cudaMemcpyHostToDevice, s);
   cudaMemcpyToSymbolAsync(c_ai_delta, ad, sizeof(double) * NLEV, 0, cudaMemcpyHostToDevice, s);
   cudaMemcpyToSymbolAsync(c_bi_delta, bd, sizeof(double) * NLEV, 0, cudaMemcpyHostToDevice, s);
+  upload_adjoint_constants(dvv16, hyai, hybi, s);
   cudaStreamSynchronize(s);
 }
 
@@ -1345,7 +1092,7 @@ void launch_dss_state(int E, const double* src, double* v, double* T, double* dp
 template <typename R>
 void launch_hv(const HvArgs<R>& a, int E, cudaStream_t s) {
   constexpr int LG = LG_HV<R>();
-  for (int c = 0; c < a.hsub; ++c) {
+  for (int c = 0; c < a.ncyc; ++c) {
     {
       KScope k("hv_laplace1", s);
       k_hv_lap1<R, LG><<<E, LG * 16, 0, s>>>(a);

@@ -45,6 +45,7 @@ struct HvArgs {
   double* bufA;   // [E][72][4][16]
   double* bufB;
   int np1, hsub, consthv;
+  int ncyc;  // subcycles this launch runs (hsub for a whole HyperviscosityFunctorImpl::run)
   double dt, eta_ave_w, nu, nu_s, nu_p, nu_top, nu_ratio1, nu_ratio2;
 };
 
@@ -101,6 +102,62 @@ void launch_update_q(int E, int Q, const double* qdp, double* Qc, const double* 
 // Generic DSS of nf fields (field f at base + f*fs, element stride es, level stride ls).
 void launch_dss_inplace(int E, int nf, double* base, long long fs, long long es, int ls,
                         double* scratch, const double* rsmp, DssTable t, cudaStream_t s);
+
+// ---- adjoint of the dry dynamics (hx_adjoint.cu) ------------------------------------
+
+void upload_adjoint_constants(const double* dvv16, const double* hyai73, const double* hybi73,
+                              cudaStream_t s);
+
+// One time level of the dynamics state: v component c of element e, level l, point p
+// at v[e*ev + l*32 + c*16 + p]; T and dp3d at T[e*es + l*16 + p].  A time level tl of
+// the [E][3][72]... state arrays is (base + tl*72*32, base + tl*72*16, ev = 3*72*32,
+// es = 3*72*16); a stand-alone level has ev = 72*32, es = 72*16.
+struct DynV {
+  double* v;
+  double* T;
+  double* dp;
+  long long ev, es;
+};
+
+template <typename R>
+struct CaarVjpArgs {
+  MetricP<R> m;
+  DssTable dss;
+  DynV x;       // stage input (its n0 state)
+  DynV aout;    // cotangent of the stage output (after its DSS)
+  DynV xm_bar;  // += spheremp * pre-DSS cotangent
+  DynV x0_bar;  // += tendency^T (dt spheremp pre-DSS cotangent); may alias xm_bar
+  double dt, p_top;
+};
+
+template <typename R>
+struct HvVjpArgs {
+  MetricP<R> m;
+  DssTable dss;
+  DynV x;      // subcycle input
+  DynV xo;     // subcycle output (recomputed)
+  DynV a;      // cotangent of the output
+  DynV xb;     // cotangent of the input (written)
+  double* pre; // scratch [E][72][4][16]
+  double* mid; // scratch [E][72][4][16]
+  double dt, nu, nu_s, nu_p, nu_top, nu_ratio1, nu_ratio2;
+};
+
+struct RemapVjpArgs {
+  DynV x;   // remap input
+  DynV a;   // in: cotangent of the remapped v, T and of dp3d = target thickness;
+            // out (in place): cotangent of the remap input
+  int remap_alg, nelem;
+  double ps0, hyai0;
+};
+
+template <typename R> void launch_caar_vjp(const CaarVjpArgs<R>& a, int E, cudaStream_t s);
+template <typename R> void launch_hv_vjp(const HvVjpArgs<R>& a, int E, cudaStream_t s);
+void launch_remap_vjp(const RemapVjpArgs& a, cudaStream_t s);
+// b1 += 5/4 by, b0 -= 1/4 by (reverse of the RK5 combination (5 X1 - X0)/4).
+void launch_rk5_comb_vjp(int E, DynV by, DynV b1, DynV b0, cudaStream_t s);
+// Copy one time level (dst and src may have different element strides).
+void launch_copy_dyn(int E, DynV dst, DynV src, cudaStream_t s);
 
 // Name of the last kernel launched by the wrappers above (for per-kernel timing).
 const char* last_kernel_name();

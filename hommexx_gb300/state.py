@@ -88,6 +88,22 @@ def _smooth_fields(basis: np.ndarray, nfields: int, seed: int) -> np.ndarray:
     return f
 
 
+def dynamics_direction(mesh, seed: int, hv: HVCoord | None = None, lmax: int = LMAX):
+    """Seeded smooth perturbation of the dynamics state (one time level): u, v of
+    1 m/s, T of 1 K and dp3d of 1 % of the layer thickness, each a random sum of
+    spherical harmonics up to degree ``lmax`` per level (continuous across elements)."""
+    hv = hv or hybrid_coordinate()
+    E = mesh.nelem
+    basis = _sph_basis(mesh.lat, mesh.lon, lmax)
+    shp = (E, 4, 4)
+    f = _smooth_fields(basis, 4 * NLEV, seed).reshape(4, NLEV, *shp).transpose(0, 2, 1, 3, 4)
+    dp = (np.diff(hv.hyai)[None, :, None, None] * hv.ps0
+          + np.diff(hv.hybi)[None, :, None, None] * PS0)
+    return dict(v=np.ascontiguousarray(np.stack([f[0], f[1]], axis=2)),
+                T=np.ascontiguousarray(f[2]),
+                dp3d=np.ascontiguousarray(0.01 * dp * f[3]))
+
+
 def initial_state(mesh, qsize: int, hv: HVCoord | None = None):
     """Seeded smooth state on ``mesh``; every time level holds the same values."""
     hv = hv or hybrid_coordinate()

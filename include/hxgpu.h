@@ -184,6 +184,38 @@ int hx_timer_stop(double* ms);
  * stream; returns 0, 13 or HX_ERR_STATE/HX_ERR_CUDA. */
 int hx_dss_noalloc(const double* in, double* out, int nelem, int apply_rspheremp);
 
+/* ---- Dry-dynamics trajectory and its adjoint (no counterpart in the reference) ----
+ * A trajectory of nsteps steps, each the dynamics part of prim_step for rsplit > 0:
+ * u3_5stage caar with DSS (src/share/cxx/prim_advance_exp.cpp:113-161), the
+ * hyperviscosity subcycles (src/share/cxx/HyperviscosityFunctorImpl.cpp:56-84) and,
+ * after every rsplit-th step, the PPM remap of v and T (src/share/cxx/RemapFunctor.hpp:
+ * 299-331) with dp3d reset to the hybrid thickness from ps, as the next remap interval
+ * starts (src/share/cxx/prim_driver.cpp:90-113).  Dry: tracers are not advected, T_v = T.
+ * Uses the session's mesh, hybrid coordinate and namelist values (nu, nu_p, nu_s,
+ * nu_top, hypervis_subcycle, rsplit, remap_alg); tensor hyperviscosity is rejected
+ * with code 12.  States are one time level in the Fortran layout: v (np,np,2,nlev,
+ * nelemd), T and dp3d (np,np,nlev,nelemd); pointers may be host or device memory.
+ *
+ * hx_traj_forward runs the trajectory from (v, T, dp3d), writes the final state and
+ * keeps the checkpoints its adjoint needs (returns 101 on a negative layer
+ * thickness).  hx_traj_vjp takes the cotangent of the final state and returns the
+ * gradient with respect to the initial state (a vector-Jacobian product), reversing
+ * the last forward trajectory: each caar stage, hyperviscosity subcycle and remap is
+ * differentiated by hand, with its inputs checkpointed and its intermediates
+ * recomputed.  hx_traj_jvp is the tangent-linear model along the same trajectory
+ * (CPU oracle only; the GPU library returns HX_ERR_STATE).
+ * hx_traj_set_checkpointing: 0 = automatic (every RK stage and hyperviscosity
+ * subcycle input of every step when that fits in device memory, else mode 2), 1 =
+ * keep every stage input, 2 = keep the step inputs only and recompute each step's
+ * stage inputs when reversing it (one extra forward step of work per step). */
+int hx_traj_forward(const double* v, const double* T, const double* dp3d, int nsteps,
+                    double dt, double* v_out, double* T_out, double* dp3d_out);
+int hx_traj_vjp(const double* v_bar, const double* T_bar, const double* dp3d_bar,
+                double* v_grad, double* T_grad, double* dp3d_grad);
+int hx_traj_jvp(const double* dv, const double* dT, const double* ddp3d, double* v_tan,
+                double* T_tan, double* dp3d_tan);
+int hx_traj_set_checkpointing(int mode);
+
 /* Page-lock (pin) host memory so init/push copies run at full link bandwidth. */
 int hx_host_register(void* ptr, size_t bytes);
 int hx_host_unregister(void* ptr);

@@ -51,6 +51,38 @@ constexpr double cp = 1005.0;
 constexpr double kappa = Rgas / cp;
 constexpr double rrearth = 1.0 / 6.376e6;
 
+// Forward-mode dual number: the element and column routines below are templates over
+// the field scalar, so instantiating them with Dual gives the exact tangent-linear model
+// of the same code (value part bit-identical to the double instantiation).  Branches and
+// index searches follow the value part.
+struct Dual {
+  double v, d;
+  Dual(double a = 0.0) : v(a), d(0.0) {}
+  Dual(double a, double b) : v(a), d(b) {}
+  Dual& operator+=(const Dual& o) { v += o.v; d += o.d; return *this; }
+  Dual& operator-=(const Dual& o) { v -= o.v; d -= o.d; return *this; }
+  Dual& operator*=(const Dual& o) { d = d * o.v + v * o.d; v *= o.v; return *this; }
+  Dual& operator/=(const Dual& o) {
+    const double q = v / o.v;
+    d = (d - q * o.d) / o.v;
+    v = q;
+    return *this;
+  }
+};
+inline Dual operator+(Dual a, const Dual& b) { return a += b; }
+inline Dual operator-(Dual a, const Dual& b) { return a -= b; }
+inline Dual operator*(Dual a, const Dual& b) { return a *= b; }
+inline Dual operator/(Dual a, const Dual& b) { return a /= b; }
+inline Dual operator-(const Dual& a) { return {-a.v, -a.d}; }
+inline bool operator<(const Dual& a, const Dual& b) { return a.v < b.v; }
+inline bool operator>(const Dual& a, const Dual& b) { return a.v > b.v; }
+inline bool operator<=(const Dual& a, const Dual& b) { return a.v <= b.v; }
+inline bool operator>=(const Dual& a, const Dual& b) { return a.v >= b.v; }
+inline double val(double x) { return x; }
+inline double val(const Dual& x) { return x.v; }
+inline double sabs(double x) { return std::fabs(x); }
+inline Dual sabs(const Dual& x) { return x.v < 0.0 ? -x : x; }
+
 struct Params {
   int remap_alg = 1, limiter_option = 8, rsplit = 1, qsplit = 1, time_step_type = 5;
   int qsize = 0, state_frequency = 1, hypervis_order = 2, hypervis_subcycle = 1, ftype = -1;
@@ -153,11 +185,12 @@ inline int P(int i, int j) { return i * NP + j; }
 #define FV(arr, c, p, k) (arr)[((c) * NP2 + (p)) * NLEV + (k)]
 
 // SphereOperators.hpp:291-319
-void gradient_sphere(const EM& m, const double* s, double* g, int nl) {
+template <class S>
+void gradient_sphere(const EM& m, const S* s, S* g, int nl) {
   for (int igp = 0; igp < NP; ++igp)
     for (int jgp = 0; jgp < NP; ++jgp)
       for (int l = 0; l < nl; ++l) {
-        double v0 = 0, v1 = 0;
+        S v0 = 0.0, v1 = 0.0;
         for (int k = 0; k < NP; ++k) {
           v0 += m.dvv[jgp][k] * F(s, P(igp, k), l);
           v1 += m.dvv[igp][k] * F(s, P(k, jgp), l);
@@ -171,11 +204,12 @@ void gradient_sphere(const EM& m, const double* s, double* g, int nl) {
 }
 
 // SphereOperators.hpp:321-348
-void gradient_sphere_update(const EM& m, const double* s, double* g, int nl) {
+template <class S>
+void gradient_sphere_update(const EM& m, const S* s, S* g, int nl) {
   for (int igp = 0; igp < NP; ++igp)
     for (int jgp = 0; jgp < NP; ++jgp)
       for (int l = 0; l < nl; ++l) {
-        double dsdx = 0, dsdy = 0;
+        S dsdx = 0.0, dsdy = 0.0;
         for (int k = 0; k < NP; ++k) {
           dsdx += m.dvv[jgp][k] * F(s, P(igp, k), l);
           dsdy += m.dvv[igp][k] * F(s, P(k, jgp), l);
@@ -189,18 +223,19 @@ void gradient_sphere_update(const EM& m, const double* s, double* g, int nl) {
 }
 
 // SphereOperators.hpp:350-392
-void divergence_sphere(const EM& m, const double* v, double* div, int nl) {
-  std::vector<double> gv(2 * NP2 * NLEV);
+template <class S>
+void divergence_sphere(const EM& m, const S* v, S* div, int nl) {
+  std::vector<S> gv(2 * NP2 * NLEV);
   for (int p = 0; p < NP2; ++p)
     for (int l = 0; l < nl; ++l) {
-      const double v0 = FV(v, 0, p, l), v1 = FV(v, 1, p, l);
+      const S v0 = FV(v, 0, p, l), v1 = FV(v, 1, p, l);
       FV(gv.data(), 0, p, l) = (m.di(0, 0, p) * v0 + m.di(1, 0, p) * v1) * m.metdet[p];
       FV(gv.data(), 1, p, l) = (m.di(0, 1, p) * v0 + m.di(1, 1, p) * v1) * m.metdet[p];
     }
   for (int igp = 0; igp < NP; ++igp)
     for (int jgp = 0; jgp < NP; ++jgp)
       for (int l = 0; l < nl; ++l) {
-        double dudx = 0, dvdy = 0;
+        S dudx = 0.0, dvdy = 0.0;
         for (int k = 0; k < NP; ++k) {
           dudx += m.dvv[jgp][k] * FV(gv.data(), 0, P(igp, k), l);
           dvdy += m.dvv[igp][k] * FV(gv.data(), 1, P(k, jgp), l);
@@ -211,45 +246,47 @@ void divergence_sphere(const EM& m, const double* v, double* div, int nl) {
 }
 
 // SphereOperators.hpp:394-444: qtens = qdp + alpha*div(vstar*qdp) [+ qtens]
-void divergence_sphere_update(const EM& m, double alpha, bool add_hv, const double* vstar,
-                              const double* qdp, double* qtens, int nl) {
-  std::vector<double> gv(2 * NP2 * NLEV);
+template <class S>
+void divergence_sphere_update(const EM& m, double alpha, bool add_hv, const S* vstar,
+                              const S* qdp, S* qtens, int nl) {
+  std::vector<S> gv(2 * NP2 * NLEV);
   for (int p = 0; p < NP2; ++p)
     for (int l = 0; l < nl; ++l) {
-      const double q = F(qdp, p, l);
-      const double v0 = FV(vstar, 0, p, l) * q;
-      const double v1 = FV(vstar, 1, p, l) * q;
+      const S q = F(qdp, p, l);
+      const S v0 = FV(vstar, 0, p, l) * q;
+      const S v1 = FV(vstar, 1, p, l) * q;
       FV(gv.data(), 0, p, l) = (m.di(0, 0, p) * v0 + m.di(1, 0, p) * v1) * m.metdet[p];
       FV(gv.data(), 1, p, l) = (m.di(0, 1, p) * v0 + m.di(1, 1, p) * v1) * m.metdet[p];
     }
   for (int igp = 0; igp < NP; ++igp)
     for (int jgp = 0; jgp < NP; ++jgp)
       for (int l = 0; l < nl; ++l) {
-        double dudx = 0, dvdy = 0;
+        S dudx = 0.0, dvdy = 0.0;
         for (int k = 0; k < NP; ++k) {
           dudx += m.dvv[jgp][k] * FV(gv.data(), 0, P(igp, k), l);
           dvdy += m.dvv[igp][k] * FV(gv.data(), 1, P(k, jgp), l);
         }
         const int p = P(igp, jgp);
-        const double q0 = add_hv ? F(qtens, p, l) : 0.0;
+        const S q0 = add_hv ? F(qtens, p, l) : S(0.0);
         F(qtens, p, l) =
             (F(qdp, p, l) + alpha * ((dudx + dvdy) * (1.0 / m.metdet[p] * rrearth)) + q0);
       }
 }
 
 // SphereOperators.hpp:492-533
-void vorticity_sphere(const EM& m, const double* v, double* vort, int nl) {
-  std::vector<double> vc(2 * NP2 * NLEV);
+template <class S>
+void vorticity_sphere(const EM& m, const S* v, S* vort, int nl) {
+  std::vector<S> vc(2 * NP2 * NLEV);
   for (int p = 0; p < NP2; ++p)
     for (int l = 0; l < nl; ++l) {
-      const double v0 = FV(v, 0, p, l), v1 = FV(v, 1, p, l);
+      const S v0 = FV(v, 0, p, l), v1 = FV(v, 1, p, l);
       FV(vc.data(), 0, p, l) = m.d(0, 0, p) * v0 + m.d(0, 1, p) * v1;
       FV(vc.data(), 1, p, l) = m.d(1, 0, p) * v0 + m.d(1, 1, p) * v1;
     }
   for (int igp = 0; igp < NP; ++igp)
     for (int jgp = 0; jgp < NP; ++jgp)
       for (int l = 0; l < nl; ++l) {
-        double dudy = 0, dvdx = 0;
+        S dudy = 0.0, dvdx = 0.0;
         for (int k = 0; k < NP; ++k) {
           dvdx += m.dvv[jgp][k] * FV(vc.data(), 1, P(igp, k), l);
           dudy += m.dvv[igp][k] * FV(vc.data(), 0, P(k, jgp), l);
@@ -260,17 +297,18 @@ void vorticity_sphere(const EM& m, const double* v, double* vort, int nl) {
 }
 
 // SphereOperators.hpp:536-583 (the input vector is overwritten, as in the reference)
-void divergence_sphere_wk(const EM& m, double* v, double* div, int nl) {
+template <class S>
+void divergence_sphere_wk(const EM& m, S* v, S* div, int nl) {
   for (int p = 0; p < NP2; ++p)
     for (int l = 0; l < nl; ++l) {
-      const double v0 = FV(v, 0, p, l), v1 = FV(v, 1, p, l);
+      const S v0 = FV(v, 0, p, l), v1 = FV(v, 1, p, l);
       FV(v, 0, p, l) = m.di(0, 0, p) * v0 + m.di(1, 0, p) * v1;
       FV(v, 1, p, l) = m.di(0, 1, p) * v0 + m.di(1, 1, p) * v1;
     }
   for (int ngp = 0; ngp < NP; ++ngp)
     for (int mgp = 0; mgp < NP; ++mgp)
       for (int l = 0; l < nl; ++l) {
-        double dd = 0;
+        S dd = 0.0;
         for (int jgp = 0; jgp < NP; ++jgp) {
           dd -= (m.spheremp[P(ngp, jgp)] * FV(v, 0, P(ngp, jgp), l) * m.dvv[jgp][mgp] +
                  m.spheremp[P(jgp, mgp)] * FV(v, 1, P(jgp, mgp), l) * m.dvv[jgp][ngp]) *
@@ -281,8 +319,9 @@ void divergence_sphere_wk(const EM& m, double* v, double* div, int nl) {
 }
 
 // SphereOperators.hpp:585-597
-void laplace_simple(const EM& m, const double* field, double* lap, int nl) {
-  std::vector<double> gs(2 * NP2 * NLEV);
+template <class S>
+void laplace_simple(const EM& m, const S* field, S* lap, int nl) {
+  std::vector<S> gs(2 * NP2 * NLEV);
   gradient_sphere(m, field, gs.data(), nl);
   divergence_sphere_wk(m, gs.data(), lap, nl);
 }
@@ -301,12 +340,13 @@ void laplace_tensor(const EM& m, const double* field, double* lap, int nl) {
 }
 
 // SphereOperators.hpp:680-710: curls = beta*curls + alpha*curl(scalar)
+template <class S>
 void curl_sphere_wk_testcov_update(const EM& m, double alpha, double beta,
-                                   const double* scalar, double* curls, int nl) {
+                                   const S* scalar, S* curls, int nl) {
   for (int ngp = 0; ngp < NP; ++ngp)
     for (int mgp = 0; mgp < NP; ++mgp)
       for (int l = 0; l < nl; ++l) {
-        double sb0 = 0, sb1 = 0;
+        S sb0 = 0.0, sb1 = 0.0;
         for (int j = 0; j < NP; ++j) {
           sb0 -= m.mp[P(j, mgp)] * F(scalar, P(j, mgp), l) * m.dvv[j][ngp];
           sb1 += m.mp[P(ngp, j)] * F(scalar, P(ngp, j), l) * m.dvv[j][mgp];
@@ -320,18 +360,19 @@ void curl_sphere_wk_testcov_update(const EM& m, double alpha, double beta,
 }
 
 // SphereOperators.hpp:712-748
-void grad_sphere_wk_testcov(const EM& m, const double* scalar, double* grads, int nl) {
+template <class S>
+void grad_sphere_wk_testcov(const EM& m, const S* scalar, S* grads, int nl) {
   for (int ngp = 0; ngp < NP; ++ngp)
     for (int mgp = 0; mgp < NP; ++mgp)
       for (int l = 0; l < nl; ++l) {
-        double b0 = 0, b1 = 0;
+        S b0 = 0.0, b1 = 0.0;
         const int p = P(ngp, mgp);
         for (int j = 0; j < NP; ++j) {
           const double mpnj = m.mp[P(ngp, j)];
           const double mpjm = m.mp[P(j, mgp)];
           const double md = m.metdet[p];
-          const double snj = F(scalar, P(ngp, j), l);
-          const double sjm = F(scalar, P(j, mgp), l);
+          const S snj = F(scalar, P(ngp, j), l);
+          const S sjm = F(scalar, P(j, mgp), l);
           const double djm = m.dvv[j][mgp];
           const double djn = m.dvv[j][ngp];
           b0 -= (mpnj * m.mi(0, 0, p) * md * snj * djm + mpjm * m.mi(0, 1, p) * md * sjm * djn);
@@ -343,23 +384,24 @@ void grad_sphere_wk_testcov(const EM& m, const double* scalar, double* grads, in
 }
 
 // SphereOperators.hpp:816-862 (input and output may alias)
-void vlaplace_sphere_wk_contra(const EM& m, double nu_ratio, const double* vec, double* lap,
+template <class S>
+void vlaplace_sphere_wk_contra(const EM& m, double nu_ratio, const S* vec, S* lap,
                                int nl) {
-  std::vector<double> div(NP2 * NLEV), gcc(2 * NP2 * NLEV);
+  std::vector<S> div(NP2 * NLEV), gcc(2 * NP2 * NLEV);
   divergence_sphere(m, vec, div.data(), nl);
   if (nu_ratio > 0 && nu_ratio != 1.0)
     for (int p = 0; p < NP2; ++p)
       for (int l = 0; l < nl; ++l) F(div.data(), p, l) *= nu_ratio;
   grad_sphere_wk_testcov(m, div.data(), gcc.data(), nl);
-  std::vector<double>& vort = div;
+  std::vector<S>& vort = div;
   vorticity_sphere(m, vec, vort.data(), nl);
   curl_sphere_wk_testcov_update(m, -1.0, 1.0, vort.data(), gcc.data(), nl);
   const double re2 = rrearth * rrearth;
   for (int p = 0; p < NP2; ++p)
     for (int l = 0; l < nl; ++l) {
       const double f = 2.0 * m.spheremp[p];
-      const double a0 = f * FV(vec, 0, p, l) * re2 + FV(gcc.data(), 0, p, l);
-      const double a1 = f * FV(vec, 1, p, l) * re2 + FV(gcc.data(), 1, p, l);
+      const S a0 = f * FV(vec, 0, p, l) * re2 + FV(gcc.data(), 0, p, l);
+      const S a1 = f * FV(vec, 1, p, l) * re2 + FV(gcc.data(), 1, p, l);
       FV(lap, 0, p, l) = a0;
       FV(lap, 1, p, l) = a1;
     }
@@ -445,31 +487,34 @@ void build_tables() {
 }
 
 // One registered 3-D field: element block of [16][NLEV] at base + e*estride.
-struct FieldRef {
-  double* base;
+template <class S>
+struct FieldRefT {
+  S* base;
   size_t estride;
 };
+using FieldRef = FieldRefT<double>;
 
 // BoundaryExchange::exchange: pack all (pre-exchange values), unpack in the fixed order,
 // then optionally multiply by rspheremp.
-void dss(const std::vector<FieldRef>& fields, bool rsmp) {
+template <class S>
+void dss_t(const std::vector<FieldRefT<S>>& fields, bool rsmp) {
   Ctx& c = C();
   const int E = c.E;
-  for (const FieldRef& f : fields) {
-    std::vector<double> pre((size_t)E * NP2 * NLEV);
+  for (const FieldRefT<S>& f : fields) {
+    std::vector<S> pre((size_t)E * NP2 * NLEV);
 #pragma omp parallel for
     for (int e = 0; e < E; ++e)
-      std::memcpy(&pre[(size_t)e * NP2 * NLEV], f.base + (size_t)e * f.estride,
-                  sizeof(double) * NP2 * NLEV);
+      std::copy(f.base + (size_t)e * f.estride, f.base + (size_t)e * f.estride + NP2 * NLEV,
+                &pre[(size_t)e * NP2 * NLEV]);
 #pragma omp parallel for
     for (int e = 0; e < E; ++e) {
-      double* dst = f.base + (size_t)e * f.estride;
+      S* dst = f.base + (size_t)e * f.estride;
       for (int p = 0; p < NP2; ++p) {
         const int n = c.g_cnt[(size_t)e * 16 + p];
         for (int s = 0; s < n; ++s) {
           const int se = c.g_src_e[((size_t)e * 16 + p) * 3 + s];
           const int sp = c.g_src_p[((size_t)e * 16 + p) * 3 + s];
-          const double* src = &pre[((size_t)se * NP2 + sp) * NLEV];
+          const S* src = &pre[((size_t)se * NP2 + sp) * NLEV];
           for (int l = 0; l < NLEV; ++l) dst[p * NLEV + l] += src[l];
         }
       }
@@ -481,6 +526,7 @@ void dss(const std::vector<FieldRef>& fields, bool rsmp) {
     }
   }
 }
+void dss(const std::vector<FieldRef>& fields, bool rsmp) { dss_t<double>(fields, rsmp); }
 
 // BoundaryExchange.cpp:620-849 on qlim [E][Q][2][NLEV]
 void dss_minmax() {
@@ -504,16 +550,139 @@ void dss_minmax() {
 // ----------------------------------------------------------------------------------
 // Caar (src/share/cxx/CaarFunctorImpl.hpp), rsplit > 0 path, one element.
 // ----------------------------------------------------------------------------------
+// Element constants the caar tendency reads.
+struct CaarElem {
+  const EM* m;
+  const double* phis;      // [16]
+  const double* fcor;      // [16]
+  const double* spheremp;  // [16]
+  double p_top;            // hyai(0) * ps0
+};
+
+CaarElem caar_elem(const EM& m, int e) {
+  Ctx& c = C();
+  return {&m, &c.phis[(size_t)e * 16], &c.fcor[(size_t)e * 16], &c.spheremp[(size_t)e * 16],
+          c.hyai0 * c.ps0};
+}
+
+// One caar stage of one element, rsplit > 0 (CaarFunctorImpl.hpp:97-493):
+// new = spheremp * (state(nm1) + dt * tendency(state(n0))), before the DSS.  TV is the
+// virtual temperature (T itself when dry).  The outputs must not alias the inputs; vn0,
+// omega_p and phi_out (diagnostics) may be null.
+template <class S>
+void caar_core(const CaarElem& ce, const S* V0, const S* T0, const S* DP0, const S* TV,
+               const S* Vm, const S* Tm, const S* DPm, double dt, S* v_new, S* t_new,
+               S* dp_new, double eta_ave_w, S* vn0, S* omega_p, S* phi_out) {
+  const EM& m = *ce.m;
+  const size_t N3 = NP2 * NLEV;
+  std::vector<S> vdp(2 * N3), div_vdp(N3), pressure(N3), gradp(2 * N3), omega(N3),
+      gradt(2 * N3), eg(2 * N3), ephi(N3), vort(N3), phi(N3);
+  // compute_temperature_div_vdp: CaarFunctorImpl.hpp:330-409
+  for (int p = 0; p < NP2; ++p)
+    for (int l = 0; l < NLEV; ++l) {
+      FV(vdp.data(), 0, p, l) = FV(V0, 0, p, l) * F(DP0, p, l);
+      FV(vdp.data(), 1, p, l) = FV(V0, 1, p, l) * F(DP0, p, l);
+      if (vn0) {
+        FV(vn0, 0, p, l) += eta_ave_w * FV(vdp.data(), 0, p, l);
+        FV(vn0, 1, p, l) += eta_ave_w * FV(vdp.data(), 1, p, l);
+      }
+    }
+  divergence_sphere(m, vdp.data(), div_vdp.data(), NLEV);
+  // compute_pressure (serial form, CaarFunctorImpl.hpp:618-647)
+  for (int p = 0; p < NP2; ++p) {
+    S dp_prev = 0.0;
+    S p_prev = ce.p_top;
+    for (int l = 0; l < NLEV; ++l) {
+      F(pressure.data(), p, l) = p_prev + 0.5 * (dp_prev + F(DP0, p, l));
+      p_prev = F(pressure.data(), p, l);
+      dp_prev = F(DP0, p, l);
+    }
+  }
+  // preq_hydrostatic (serial form, :686-730)
+  for (int p = 0; p < NP2; ++p) {
+    const double phis = ce.phis[p];
+    S integration = 0.0;
+    for (int l = NLEV - 1; l >= 0; --l) {
+      const S r = Rgas * F(TV, p, l) * (F(DP0, p, l) * 0.5 / F(pressure.data(), p, l));
+      F(phi.data(), p, l) = phis + 2.0 * integration + r;
+      integration = integration + r;
+    }
+  }
+  if (phi_out) std::copy(phi.begin(), phi.end(), phi_out);
+  // preq_omega_ps (serial form, :848-889)
+  gradient_sphere(m, pressure.data(), gradp.data(), NLEV);
+  for (int p = 0; p < NP2; ++p) {
+    S integration = 0.0;
+    for (int l = 0; l < NLEV; ++l) {
+      const S vgrad_p = FV(V0, 0, p, l) * FV(gradp.data(), 0, p, l) +
+                        FV(V0, 1, p, l) * FV(gradp.data(), 1, p, l);
+      const S dv = F(div_vdp.data(), p, l);
+      F(omega.data(), p, l) = (vgrad_p - (integration + 0.5 * dv)) / F(pressure.data(), p, l);
+      integration = integration + dv;
+    }
+  }
+  // compute_phase_3 (:136-148): omega_p, T, v, dp3d
+  if (omega_p)
+    for (int p = 0; p < NP2; ++p)
+      for (int l = 0; l < NLEV; ++l) F(omega_p, p, l) += eta_ave_w * F(omega.data(), p, l);
+  // compute_temperature_np1 (:424-460)
+  gradient_sphere(m, T0, gradt.data(), NLEV);
+  for (int p = 0; p < NP2; ++p)
+    for (int l = 0; l < NLEV; ++l) {
+      const S vgrad_t = FV(V0, 0, p, l) * FV(gradt.data(), 0, p, l) +
+                        FV(V0, 1, p, l) * FV(gradt.data(), 1, p, l);
+      const S ttens = (0.0 - vgrad_t) + kappa * F(TV, p, l) * F(omega.data(), p, l);
+      S temp_np1 = ttens * dt + F(Tm, p, l);
+      temp_np1 *= ce.spheremp[p];
+      F(t_new, p, l) = temp_np1;
+    }
+  // compute_velocity_np1 (:183-232) with compute_energy_grad (:97-132)
+  for (int p = 0; p < NP2; ++p)
+    for (int l = 0; l < NLEV; ++l) {
+      const S r = Rgas * (F(TV, p, l) / F(pressure.data(), p, l));
+      FV(eg.data(), 0, p, l) = r * FV(gradp.data(), 0, p, l);
+      FV(eg.data(), 1, p, l) = r * FV(gradp.data(), 1, p, l);
+      const S ke = 0.5 * (FV(V0, 0, p, l) * FV(V0, 0, p, l) + FV(V0, 1, p, l) * FV(V0, 1, p, l));
+      F(ephi.data(), p, l) = ke + F(phi.data(), p, l);
+    }
+  gradient_sphere_update(m, ephi.data(), eg.data(), NLEV);
+  vorticity_sphere(m, V0, vort.data(), NLEV);
+  for (int p = 0; p < NP2; ++p)
+    for (int l = 0; l < NLEV; ++l) {
+      F(vort.data(), p, l) += ce.fcor[p];
+      S e0 = FV(eg.data(), 0, p, l), e1 = FV(eg.data(), 1, p, l);
+      const S vo = F(vort.data(), p, l);
+      e0 *= -1.0;
+      e0 += 0.0 + FV(V0, 1, p, l) * vo;
+      e1 *= -1.0;
+      e1 += 0.0 - FV(V0, 0, p, l) * vo;
+      e0 *= dt;
+      e0 += FV(Vm, 0, p, l);
+      e1 *= dt;
+      e1 += FV(Vm, 1, p, l);
+      const double smp = ce.spheremp[p];
+      FV(v_new, 0, p, l) = smp * e0;
+      FV(v_new, 1, p, l) = smp * e1;
+    }
+  // compute_dp3d_np1 (:462-493), eta_dot_dpdn buffer is zero when rsplit > 0
+  for (int p = 0; p < NP2; ++p)
+    for (int l = 0; l < NLEV; ++l) {
+      S tmp = 0.0;
+      tmp += F(div_vdp.data(), p, l);
+      tmp -= 0.0;
+      tmp = F(DPm, p, l) - tmp * dt;
+      F(dp_new, p, l) = ce.spheremp[p] * tmp;
+    }
+}
+
 void caar_element(int e, int nm1, int n0, int np1, double dt, double eta_ave_w, int n0_qdp) {
   Ctx& c = C();
   const EM m = metric(e);
   const size_t N3 = NP2 * NLEV;
-  std::vector<double> tv(N3), vdp(2 * N3), div_vdp(N3), pressure(N3), gradp(2 * N3),
-      omega(N3), gradt(2 * N3), eg(2 * N3), ephi(N3), vort(N3);
-  const double* V0 = &c.v[IV(e, n0, 0, 0, 0)];
+  std::vector<double> tv(N3), t_new(N3), v_new(2 * N3), dp_new(N3);
   const double* T0 = &c.t[IS(e, n0, 0, 0)];
   const double* DP0 = &c.dp3d[IS(e, n0, 0, 0)];
-  // compute_temperature_div_vdp: CaarFunctorImpl.hpp:330-409
+  // virtual temperature (CaarFunctorImpl.hpp:330-360)
   for (int p = 0; p < NP2; ++p)
     for (int l = 0; l < NLEV; ++l) {
       if (n0_qdp < 0) {
@@ -525,102 +694,10 @@ void caar_element(int e, int nm1, int n0, int np1, double dt, double eta_ave_w, 
         F(tv.data(), p, l) = F(T0, p, l) * Qt;
       }
     }
-  for (int p = 0; p < NP2; ++p)
-    for (int l = 0; l < NLEV; ++l) {
-      FV(vdp.data(), 0, p, l) = FV(V0, 0, p, l) * F(DP0, p, l);
-      FV(vdp.data(), 1, p, l) = FV(V0, 1, p, l) * F(DP0, p, l);
-      c.vn0[I3V(e, 0, p, l)] += eta_ave_w * FV(vdp.data(), 0, p, l);
-      c.vn0[I3V(e, 1, p, l)] += eta_ave_w * FV(vdp.data(), 1, p, l);
-    }
-  divergence_sphere(m, vdp.data(), div_vdp.data(), NLEV);
-  // compute_pressure (serial form, CaarFunctorImpl.hpp:618-647)
-  for (int p = 0; p < NP2; ++p) {
-    double dp_prev = 0;
-    double p_prev = c.hyai0 * c.ps0;
-    for (int l = 0; l < NLEV; ++l) {
-      F(pressure.data(), p, l) = p_prev + 0.5 * (dp_prev + F(DP0, p, l));
-      p_prev = F(pressure.data(), p, l);
-      dp_prev = F(DP0, p, l);
-    }
-  }
-  // preq_hydrostatic (serial form, :686-730)
-  double* PHI = &c.phi[I3(e, 0, 0)];
-  for (int p = 0; p < NP2; ++p) {
-    const double phis = c.phis[(size_t)e * 16 + p];
-    double integration = 0;
-    for (int l = NLEV - 1; l >= 0; --l) {
-      const double r = Rgas * F(tv.data(), p, l) * (F(DP0, p, l) * 0.5 / F(pressure.data(), p, l));
-      F(PHI, p, l) = phis + 2.0 * integration + r;
-      integration = integration + r;
-    }
-  }
-  // preq_omega_ps (serial form, :848-889)
-  gradient_sphere(m, pressure.data(), gradp.data(), NLEV);
-  for (int p = 0; p < NP2; ++p) {
-    double integration = 0;
-    for (int l = 0; l < NLEV; ++l) {
-      const double vgrad_p = FV(V0, 0, p, l) * FV(gradp.data(), 0, p, l) +
-                             FV(V0, 1, p, l) * FV(gradp.data(), 1, p, l);
-      const double dv = F(div_vdp.data(), p, l);
-      F(omega.data(), p, l) = (vgrad_p - (integration + 0.5 * dv)) / F(pressure.data(), p, l);
-      integration = integration + dv;
-    }
-  }
-  // compute_phase_3 (:136-148): omega_p, T, v, dp3d
-  for (int p = 0; p < NP2; ++p)
-    for (int l = 0; l < NLEV; ++l) c.omega_p[I3(e, p, l)] += eta_ave_w * F(omega.data(), p, l);
-  // compute_temperature_np1 (:424-460)
-  gradient_sphere(m, T0, gradt.data(), NLEV);
-  std::vector<double> t_new(N3), v_new(2 * N3), dp_new(N3);
-  const double* Tm = &c.t[IS(e, nm1, 0, 0)];
-  for (int p = 0; p < NP2; ++p)
-    for (int l = 0; l < NLEV; ++l) {
-      const double vgrad_t = FV(V0, 0, p, l) * FV(gradt.data(), 0, p, l) +
-                             FV(V0, 1, p, l) * FV(gradt.data(), 1, p, l);
-      const double ttens = (0.0 - vgrad_t) + kappa * F(tv.data(), p, l) * F(omega.data(), p, l);
-      double temp_np1 = ttens * dt + F(Tm, p, l);
-      temp_np1 *= c.spheremp[(size_t)e * 16 + p];
-      F(t_new.data(), p, l) = temp_np1;
-    }
-  // compute_velocity_np1 (:183-232) with compute_energy_grad (:97-132)
-  for (int p = 0; p < NP2; ++p)
-    for (int l = 0; l < NLEV; ++l) {
-      const double r = Rgas * (F(tv.data(), p, l) / F(pressure.data(), p, l));
-      FV(eg.data(), 0, p, l) = r * FV(gradp.data(), 0, p, l);
-      FV(eg.data(), 1, p, l) = r * FV(gradp.data(), 1, p, l);
-      const double ke = 0.5 * (FV(V0, 0, p, l) * FV(V0, 0, p, l) + FV(V0, 1, p, l) * FV(V0, 1, p, l));
-      F(ephi.data(), p, l) = ke + F(PHI, p, l);
-    }
-  gradient_sphere_update(m, ephi.data(), eg.data(), NLEV);
-  vorticity_sphere(m, V0, vort.data(), NLEV);
-  const double* Vm = &c.v[IV(e, nm1, 0, 0, 0)];
-  for (int p = 0; p < NP2; ++p)
-    for (int l = 0; l < NLEV; ++l) {
-      F(vort.data(), p, l) += c.fcor[(size_t)e * 16 + p];
-      double e0 = FV(eg.data(), 0, p, l), e1 = FV(eg.data(), 1, p, l);
-      const double vo = F(vort.data(), p, l);
-      e0 *= -1;
-      e0 += 0.0 + FV(V0, 1, p, l) * vo;
-      e1 *= -1;
-      e1 += 0.0 - FV(V0, 0, p, l) * vo;
-      e0 *= dt;
-      e0 += FV(Vm, 0, p, l);
-      e1 *= dt;
-      e1 += FV(Vm, 1, p, l);
-      const double smp = c.spheremp[(size_t)e * 16 + p];
-      FV(v_new.data(), 0, p, l) = smp * e0;
-      FV(v_new.data(), 1, p, l) = smp * e1;
-    }
-  // compute_dp3d_np1 (:462-493), eta_dot_dpdn buffer is zero when rsplit > 0
-  const double* DPm = &c.dp3d[IS(e, nm1, 0, 0)];
-  for (int p = 0; p < NP2; ++p)
-    for (int l = 0; l < NLEV; ++l) {
-      double tmp = 0.0;
-      tmp += F(div_vdp.data(), p, l);
-      tmp -= 0.0;
-      tmp = F(DPm, p, l) - tmp * dt;
-      F(dp_new.data(), p, l) = c.spheremp[(size_t)e * 16 + p] * tmp;
-    }
+  caar_core<double>(caar_elem(m, e), &c.v[IV(e, n0, 0, 0, 0)], T0, DP0, tv.data(),
+                    &c.v[IV(e, nm1, 0, 0, 0)], &c.t[IS(e, nm1, 0, 0)], &c.dp3d[IS(e, nm1, 0, 0)],
+                    dt, v_new.data(), t_new.data(), dp_new.data(), eta_ave_w,
+                    &c.vn0[I3V(e, 0, 0, 0)], &c.omega_p[I3(e, 0, 0)], &c.phi[I3(e, 0, 0)]);
   std::memcpy(&c.t[IS(e, np1, 0, 0)], t_new.data(), sizeof(double) * N3);
   std::memcpy(&c.v[IV(e, np1, 0, 0, 0)], v_new.data(), sizeof(double) * 2 * N3);
   std::memcpy(&c.dp3d[IS(e, np1, 0, 0)], dp_new.data(), sizeof(double) * N3);
@@ -663,23 +740,96 @@ void u3_5stage(int nm1, int n0, int np1, int n0_qdp, double dt, double w) {
 // ----------------------------------------------------------------------------------
 // Hyperviscosity (src/share/cxx/HyperviscosityFunctorImpl.{hpp,cpp})
 // ----------------------------------------------------------------------------------
+// TagFirstLaplaceHV, one element (HyperviscosityFunctorImpl.hpp:72-90).
+template <class S>
+void hv_first_laplace(const EM& m, double nu_ratio1, const S* T, const S* DP, const S* V,
+                      S* ttens, S* dptens, S* vtens) {
+  laplace_simple(m, T, ttens, NLEV);
+  laplace_simple(m, DP, dptens, NLEV);
+  vlaplace_sphere_wk_contra(m, nu_ratio1, V, vtens, NLEV);
+}
+
+// TagSecondLaplaceConstHV, one element, in place (HyperviscosityFunctorImpl.hpp:92-109).
+template <class S>
+void hv_second_laplace_const(const EM& m, double nu_ratio2, S* ttens, S* dptens, S* vtens) {
+  laplace_simple(m, ttens, ttens, NLEV);
+  laplace_simple(m, dptens, dptens, NLEV);
+  vlaplace_sphere_wk_contra(m, nu_ratio2, vtens, vtens, NLEV);
+}
+
+// TagHyperPreExchange without the dpdiss diagnostics (HyperviscosityFunctorImpl.hpp:
+// 161-257): scale by -nu, add the nu_top sponge on the top 3 levels, and form the
+// spheremp-weighted dp3d update.
+template <class S>
+void hv_pre_exchange(const EM& m, const Params& pr, double dt, const S* T, const S* DP,
+                     const S* V, S* ttens, S* dptens, S* vtens) {
+  const size_t N3 = NP2 * NLEV;
+  const double nu_scale_top[3] = {4.0 * pr.nu_top, 2.0 * pr.nu_top, 1.0 * pr.nu_top};
+  std::vector<S> lap_v(2 * N3), lap_t(N3), lap_dp(N3);
+  if (pr.nu_top > 0) {
+    vlaplace_sphere_wk_contra(m, 1.0, V, lap_v.data(), 3);
+    laplace_simple(m, T, lap_t.data(), 3);
+    laplace_simple(m, DP, lap_dp.data(), 3);
+  }
+  for (int p = 0; p < NP2; ++p) {
+    for (int l = 0; l < NLEV; ++l) {
+      FV(vtens, 0, p, l) *= -pr.nu;
+      FV(vtens, 1, p, l) *= -pr.nu;
+      F(ttens, p, l) *= -pr.nu_s;
+      F(dptens, p, l) *= -pr.nu_p;
+    }
+    if (pr.nu_top > 0)
+      for (int l = 0; l < 3; ++l) {
+        FV(vtens, 0, p, l) += nu_scale_top[l] * FV(lap_v.data(), 0, p, l);
+        FV(vtens, 1, p, l) += nu_scale_top[l] * FV(lap_v.data(), 1, p, l);
+        F(ttens, p, l) += nu_scale_top[l] * F(lap_t.data(), p, l);
+        F(dptens, p, l) += nu_scale_top[l] * F(lap_dp.data(), p, l);
+      }
+    for (int l = 0; l < NLEV; ++l) {
+      F(dptens, p, l) *= dt;
+      F(dptens, p, l) += F(DP, p, l) * m.spheremp[p];
+    }
+  }
+}
+
+// TagUpdateStates, one element (HyperviscosityFunctorImpl.hpp:134-158), after the DSS.
+template <class S>
+void hv_update(const double* rsmp_e, double dt, S* V, S* T, S* DP, S* vtens, S* ttens,
+               const S* dptens) {
+  for (int p = 0; p < NP2; ++p) {
+    const double rsmp = rsmp_e[p];
+    for (int l = 0; l < NLEV; ++l) {
+      S& vt0 = FV(vtens, 0, p, l);
+      S& vt1 = FV(vtens, 1, p, l);
+      vt0 = (dt * vt0 * rsmp);
+      vt1 = (dt * vt1 * rsmp);
+      S& v0 = FV(V, 0, p, l);
+      S& v1 = FV(V, 1, p, l);
+      v0 += vt0;
+      v1 += vt1;
+      S& tt = F(ttens, p, l);
+      tt = (dt * tt * rsmp);
+      const S heating = vt0 * v0 + vt1 * v1;
+      S& t = F(T, p, l);
+      t = t + tt - heating / cp;
+      F(DP, p, l) = (F(dptens, p, l) * rsmp);
+    }
+  }
+}
+
 void hypervis_run(int np1, double dt_in, double eta_ave_w) {
   Ctx& c = C();
   const Params& pr = c.prm;
   const int hsub = pr.hypervis_subcycle;
   const double dt = dt_in / hsub;
   const size_t N3 = NP2 * NLEV;
-  double nu_scale_top[3] = {4.0 * pr.nu_top, 2.0 * pr.nu_top, 1.0 * pr.nu_top};
   for (int icycle = 0; icycle < hsub; ++icycle) {
     // TagFirstLaplaceHV
 #pragma omp parallel for
-    for (int e = 0; e < c.E; ++e) {
-      const EM m = metric(e);
-      laplace_simple(m, &c.t[IS(e, np1, 0, 0)], &c.ttens[I3(e, 0, 0)], NLEV);
-      laplace_simple(m, &c.dp3d[IS(e, np1, 0, 0)], &c.dptens[I3(e, 0, 0)], NLEV);
-      vlaplace_sphere_wk_contra(m, pr.nu_ratio1, &c.v[IV(e, np1, 0, 0, 0)],
-                                &c.vtens[I3V(e, 0, 0, 0)], NLEV);
-    }
+    for (int e = 0; e < c.E; ++e)
+      hv_first_laplace(metric(e), pr.nu_ratio1, &c.t[IS(e, np1, 0, 0)],
+                       &c.dp3d[IS(e, np1, 0, 0)], &c.v[IV(e, np1, 0, 0, 0)],
+                       &c.ttens[I3(e, 0, 0)], &c.dptens[I3(e, 0, 0)], &c.vtens[I3V(e, 0, 0, 0)]);
     const std::vector<FieldRef> tens = {{&c.vtens[I3V(0, 0, 0, 0)], 2 * N3},
                                         {&c.vtens[I3V(0, 1, 0, 0)], 2 * N3},
                                         {&c.ttens[0], N3},
@@ -690,10 +840,8 @@ void hypervis_run(int np1, double dt_in, double eta_ave_w) {
     for (int e = 0; e < c.E; ++e) {
       const EM m = metric(e);
       if (c.consthv) {
-        laplace_simple(m, &c.ttens[I3(e, 0, 0)], &c.ttens[I3(e, 0, 0)], NLEV);
-        laplace_simple(m, &c.dptens[I3(e, 0, 0)], &c.dptens[I3(e, 0, 0)], NLEV);
-        vlaplace_sphere_wk_contra(m, pr.nu_ratio2, &c.vtens[I3V(e, 0, 0, 0)],
-                                  &c.vtens[I3V(e, 0, 0, 0)], NLEV);
+        hv_second_laplace_const(m, pr.nu_ratio2, &c.ttens[I3(e, 0, 0)], &c.dptens[I3(e, 0, 0)],
+                                &c.vtens[I3V(e, 0, 0, 0)]);
       } else {
         laplace_tensor(m, &c.ttens[I3(e, 0, 0)], &c.ttens[I3(e, 0, 0)], NLEV);
         laplace_tensor(m, &c.dptens[I3(e, 0, 0)], &c.dptens[I3(e, 0, 0)], NLEV);
@@ -704,61 +852,22 @@ void hypervis_run(int np1, double dt_in, double eta_ave_w) {
     // TagHyperPreExchange (HyperviscosityFunctorImpl.hpp:161-257)
 #pragma omp parallel for
     for (int e = 0; e < c.E; ++e) {
-      const EM m = metric(e);
       for (int p = 0; p < NP2; ++p)
         for (int l = 0; l < NLEV; ++l) {
           c.dpdiss_ave[I3(e, p, l)] += eta_ave_w * c.dp3d[IS(e, np1, p, l)] / hsub;
           c.dpdiss_bih[I3(e, p, l)] += eta_ave_w * c.dptens[I3(e, p, l)] / hsub;
         }
-      std::vector<double> lap_v(2 * N3), lap_t(N3), lap_dp(N3);
-      if (pr.nu_top > 0) {
-        vlaplace_sphere_wk_contra(m, 1.0, &c.v[IV(e, np1, 0, 0, 0)], lap_v.data(), 3);
-        laplace_simple(m, &c.t[IS(e, np1, 0, 0)], lap_t.data(), 3);
-        laplace_simple(m, &c.dp3d[IS(e, np1, 0, 0)], lap_dp.data(), 3);
-      }
-      for (int p = 0; p < NP2; ++p) {
-        for (int l = 0; l < NLEV; ++l) {
-          c.vtens[I3V(e, 0, p, l)] *= -pr.nu;
-          c.vtens[I3V(e, 1, p, l)] *= -pr.nu;
-          c.ttens[I3(e, p, l)] *= -pr.nu_s;
-          c.dptens[I3(e, p, l)] *= -pr.nu_p;
-        }
-        if (pr.nu_top > 0)
-          for (int l = 0; l < 3; ++l) {
-            c.vtens[I3V(e, 0, p, l)] += nu_scale_top[l] * FV(lap_v.data(), 0, p, l);
-            c.vtens[I3V(e, 1, p, l)] += nu_scale_top[l] * FV(lap_v.data(), 1, p, l);
-            c.ttens[I3(e, p, l)] += nu_scale_top[l] * F(lap_t.data(), p, l);
-            c.dptens[I3(e, p, l)] += nu_scale_top[l] * F(lap_dp.data(), p, l);
-          }
-        for (int l = 0; l < NLEV; ++l) {
-          c.dptens[I3(e, p, l)] *= dt;
-          c.dptens[I3(e, p, l)] += c.dp3d[IS(e, np1, p, l)] * m.spheremp[p];
-        }
-      }
+      hv_pre_exchange(metric(e), pr, dt, &c.t[IS(e, np1, 0, 0)], &c.dp3d[IS(e, np1, 0, 0)],
+                      &c.v[IV(e, np1, 0, 0, 0)], &c.ttens[I3(e, 0, 0)], &c.dptens[I3(e, 0, 0)],
+                      &c.vtens[I3V(e, 0, 0, 0)]);
     }
     dss(tens, false);
     // TagUpdateStates (HyperviscosityFunctorImpl.hpp:134-158)
 #pragma omp parallel for
     for (int e = 0; e < c.E; ++e)
-      for (int p = 0; p < NP2; ++p) {
-        const double rsmp = c.rspheremp[(size_t)e * 16 + p];
-        for (int l = 0; l < NLEV; ++l) {
-          double& vt0 = c.vtens[I3V(e, 0, p, l)];
-          double& vt1 = c.vtens[I3V(e, 1, p, l)];
-          vt0 = (dt * vt0 * rsmp);
-          vt1 = (dt * vt1 * rsmp);
-          double& v0 = c.v[IV(e, np1, 0, p, l)];
-          double& v1 = c.v[IV(e, np1, 1, p, l)];
-          v0 += vt0;
-          v1 += vt1;
-          double& tt = c.ttens[I3(e, p, l)];
-          tt = (dt * tt * rsmp);
-          const double heating = vt0 * v0 + vt1 * v1;
-          double& t = c.t[IS(e, np1, p, l)];
-          t = t + tt - heating / cp;
-          c.dp3d[IS(e, np1, p, l)] = (c.dptens[I3(e, p, l)] * rsmp);
-        }
-      }
+      hv_update(&c.rspheremp[(size_t)e * 16], dt, &c.v[IV(e, np1, 0, 0, 0)],
+                &c.t[IS(e, np1, 0, 0)], &c.dp3d[IS(e, np1, 0, 0)], &c.vtens[I3V(e, 0, 0, 0)],
+                &c.ttens[I3(e, 0, 0)], &c.dptens[I3(e, 0, 0)]);
   }
 }
 
@@ -1003,20 +1112,23 @@ void tracers_rk2(double dt) {  // prim_advec_tracers_remap.cpp:32-90
 // PPM vertical remap (src/share/cxx/RemapFunctor.hpp, PpmRemap.hpp); rsplit > 0.
 // Padded arrays use A(m) = a[m + 2] for m in [-2, NLEV+1].
 // ----------------------------------------------------------------------------------
-struct ColumnGrid {
-  double pio[NLEV + 2], pin[NLEV + 1], dpo[NLEV + 4], z2[NLEV];
+template <class S>
+struct ColumnGridT {
+  S pio[NLEV + 2], pin[NLEV + 1], dpo[NLEV + 4], z2[NLEV];
   int kid[NLEV];
-  double g[10][NLEV + 2];
+  S g[10][NLEV + 2];
 };
+using ColumnGrid = ColumnGridT<double>;
 
-void ppm_grids(const double* src, const double* tgt, ColumnGrid& G) {
+template <class S>
+void ppm_grids(const S* src, const S* tgt, ColumnGridT<S>& G) {
   // compute_partitions (PpmRemap.hpp:488-575)
-  double acc = 0;
+  S acc = 0.0;
   for (int k = 0; k < NLEV; ++k) {
     G.pio[k] = acc;
     acc += src[k];
   }
-  acc = 0;
+  acc = 0.0;
   for (int k = 0; k < NLEV; ++k) {
     G.pin[k] = acc;
     acc += tgt[k];
@@ -1025,7 +1137,7 @@ void ppm_grids(const double* src, const double* tgt, ColumnGrid& G) {
   G.pin[NLEV] = G.pin[NLEV - 1] + tgt[NLEV - 1];
   G.pio[NLEV + 1] = G.pio[NLEV] + 1.0;
   G.pin[NLEV] = G.pio[NLEV];
-  double* D = G.dpo + 2;
+  S* D = G.dpo + 2;
   for (int k = 0; k < NLEV; ++k) D[k] = src[k];
   for (int k = 0; k < 2; ++k) {
     D[-1 - k] = D[k];
@@ -1058,17 +1170,19 @@ void ppm_grids(const double* src, const double* tgt, ColumnGrid& G) {
   }
 }
 
-inline double integrate_parabola(double sq, double lin, double cst, double x1, double x2) {
+template <class S>
+inline S integrate_parabola(const S& sq, const S& lin, const S& cst, double x1, const S& x2) {
   return (cst * (x2 - x1) + lin * (x2 * x2 - x1 * x1) / 2.0) + sq * (x2 * x2 * x2 - x1 * x1 * x1) / 3.0;
 }
 
 // compute_remap_phase + compute_ppm + compute_remap (PpmRemap.hpp:202-483)
-void ppm_remap_column(const ColumnGrid& G, int remap_alg, double* q /* [NLEV] */) {
-  const double* D = G.dpo + 2;
-  double a_[NLEV + 4];
-  double* A = a_ + 2;
-  double mass[NLEV + 2];
-  double dma[NLEV + 2], ai[NLEV + 1], coef[3][NLEV];
+template <class S>
+void ppm_remap_column(const ColumnGridT<S>& G, int remap_alg, S* q /* [NLEV] */) {
+  const S* D = G.dpo + 2;
+  S a_[NLEV + 4];
+  S* A = a_ + 2;
+  S mass[NLEV + 2];
+  S dma[NLEV + 2], ai[NLEV + 1], coef[3][NLEV];
   for (int k = 0; k < NLEV; ++k) A[k] = q[k] / D[k];
   if (remap_alg == 3) {
     for (int k = 0; k < 2; ++k) {
@@ -1081,7 +1195,7 @@ void ppm_remap_column(const ColumnGrid& G, int remap_alg, double* q /* [NLEV] */
       A[NLEV + k] = A[NLEV - 1 - k];
     }
   }
-  double acc = 0;
+  S acc = 0.0;
   for (int k = 0; k < NLEV; ++k) {
     mass[k + 1] = acc;
     acc += q[k];
@@ -1090,10 +1204,10 @@ void ppm_remap_column(const ColumnGrid& G, int remap_alg, double* q /* [NLEV] */
   mass[NLEV + 1] = mass[NLEV] + q[NLEV - 1];
   for (int j = 0; j < NLEV + 2; ++j) {
     if ((A[j] - A[j - 1]) * (A[j - 1] - A[j - 2]) > 0.0) {
-      const double da = G.g[0][j] * (G.g[1][j] * (A[j] - A[j - 1]) + G.g[2][j] * (A[j - 1] - A[j - 2]));
-      dma[j] = std::min(std::min(std::fabs(da), 2.0 * std::fabs(A[j - 1] - A[j - 2])),
-                        2.0 * std::fabs(A[j] - A[j - 1])) *
-               std::copysign(1.0, da);
+      const S da = G.g[0][j] * (G.g[1][j] * (A[j] - A[j - 1]) + G.g[2][j] * (A[j - 1] - A[j - 2]));
+      dma[j] = std::min(std::min(sabs(da), 2.0 * sabs(A[j - 1] - A[j - 2])),
+                        2.0 * sabs(A[j] - A[j - 1])) *
+               std::copysign(1.0, val(da));
     } else {
       dma[j] = 0.0;
     }
@@ -1105,8 +1219,8 @@ void ppm_remap_column(const ColumnGrid& G, int remap_alg, double* q /* [NLEV] */
   }
   for (int jp = 0; jp < NLEV; ++jp) {
     const int j = jp + 1;
-    double al = ai[j - 1], ar = ai[j];
-    const double cm = A[j - 1];
+    S al = ai[j - 1], ar = ai[j];
+    const S cm = A[j - 1];
     if ((ar - cm) * (cm - al) <= 0.) {
       al = cm;
       ar = cm;
@@ -1126,17 +1240,43 @@ void ppm_remap_column(const ColumnGrid& G, int remap_alg, double* q /* [NLEV] */
     coef[1][NLEV - 2] = coef[1][NLEV - 1] = coef[2][NLEV - 2] = coef[2][NLEV - 1] = 0.0;
   }
   // compute_remap, GPU form (each level recomputes the lower interface mass)
-  auto cmass = [&](int kk, double x2) {
-    const double integral = integrate_parabola(coef[2][kk], coef[1][kk], coef[0][kk], -0.5, x2);
+  auto cmass = [&](int kk, const S& x2) {
+    const S integral = integrate_parabola(coef[2][kk], coef[1][kk], coef[0][kk], -0.5, x2);
     return mass[kk + 1] + integral * D[kk];
   };
-  double out[NLEV];
+  S out[NLEV];
   for (int k = 0; k < NLEV; ++k) {
-    const double m1 = k > 0 ? cmass(G.kid[k - 1], G.z2[k - 1]) : 0.0;
-    const double m2 = cmass(G.kid[k], G.z2[k]);
+    const S m1 = k > 0 ? cmass(G.kid[k - 1], G.z2[k - 1]) : S(0.0);
+    const S m2 = cmass(G.kid[k], G.z2[k]);
     out[k] = m2 - m1;
   }
   for (int k = 0; k < NLEV; ++k) q[k] = out[k];
+}
+
+// compute_ps_v, the target thicknesses from the hybrid coordinate and the PPM grids of
+// one column (RemapFunctor.hpp:225-240, 364-384; PpmRemap.hpp:488-648); returns ps.
+template <class S>
+S remap_target(const S* src, S* tgt, ColumnGridT<S>& G) {
+  Ctx& c = C();
+  S ps = 0.0;
+  for (int l = 0; l < NLEV; ++l) ps += src[l];
+  ps += c.hyai0 * c.ps0;
+  for (int l = 0; l < NLEV; ++l)
+    tgt[l] = (c.hyai[l + 1] - c.hyai[l]) * c.ps0 + (c.hybi[l + 1] - c.hybi[l]) * ps;
+  ppm_grids(src, tgt, G);
+  return ps;
+}
+
+// Remap of one state variable of a column as a mass-weighted quantity: v and T are
+// multiplied by dp3d before and divided by the target thickness after
+// (RemapFunctor.hpp:243-256, 285-297, 386-420).
+template <class S>
+void remap_state_var(const ColumnGridT<S>& G, int remap_alg, const S* src, const S* tgt,
+                     S* x) {
+  S col[NLEV];
+  for (int l = 0; l < NLEV; ++l) col[l] = x[l] * src[l];
+  ppm_remap_column(G, remap_alg, col);
+  for (int l = 0; l < NLEV; ++l) x[l] = col[l] / tgt[l];
 }
 
 void remap_run(int np1, int n0_qdp, double dt) {  // RemapFunctor::run_remap, rsplit > 0
@@ -1148,25 +1288,16 @@ void remap_run(int np1, int n0_qdp, double dt) {  // RemapFunctor::run_remap, rs
   for (int e = 0; e < E; ++e) {
     for (int p = 0; p < NP2; ++p) {
       double src[NLEV], tgt[NLEV];
-      // compute_ps_v
-      double ps = 0.0;
-      for (int l = 0; l < NLEV; ++l) ps += c.dp3d[IS(e, np1, p, l)];
-      ps += c.hyai0 * c.ps0;
-      c.ps_v[((size_t)e * NTL + np1) * NP2 + p] = ps;
       for (int l = 0; l < NLEV; ++l) {
-        tgt[l] = (c.hyai[l + 1] - c.hyai[l]) * c.ps0 + (c.hybi[l + 1] - c.hybi[l]) * ps;
         src[l] = c.dp3d[IS(e, np1, p, l)];
         if (std::isnan(src[l]) || src[l] < 0.0) valid = 0;
       }
       ColumnGrid G;
-      ppm_grids(src, tgt, G);
+      c.ps_v[((size_t)e * NTL + np1) * NP2 + p] = remap_target(src, tgt, G);
+      remap_state_var(G, c.prm.remap_alg, src, tgt, &c.v[IV(e, np1, 0, p, 0)]);
+      remap_state_var(G, c.prm.remap_alg, src, tgt, &c.v[IV(e, np1, 1, p, 0)]);
+      remap_state_var(G, c.prm.remap_alg, src, tgt, &c.t[IS(e, np1, p, 0)]);
       double col[NLEV];
-      for (int var = 0; var < 3; ++var) {
-        double* base = var < 2 ? &c.v[IV(e, np1, var, p, 0)] : &c.t[IS(e, np1, p, 0)];
-        for (int l = 0; l < NLEV; ++l) col[l] = base[l] * src[l];
-        ppm_remap_column(G, c.prm.remap_alg, col);
-        for (int l = 0; l < NLEV; ++l) base[l] = col[l] / tgt[l];
-      }
       for (int q = 0; q < Q; ++q) {
         double* base = &c.qdp[IQ(e, n0_qdp, q, p, 0, Q)];
         for (int l = 0; l < NLEV; ++l) col[l] = base[l];
@@ -1266,6 +1397,8 @@ void push_block(const double* in, double* f, int ncomp) {
       for (int p = 0; p < NP2; ++p) f[(l * ncomp + cc) * NP2 + p] = in[(cc * NP2 + p) * NLEV + l];
 }
 
+#include "hx_oracle_traj.inc"
+
 }  // namespace
 
 // ====================================================================================
@@ -1277,6 +1410,7 @@ void initialize_hommexx_session(void) { C(); }
 void finalize_hommexx_session(void) {
   delete g;
   g = nullptr;
+  TC() = TrajCtx();
 }
 void reset_cxx_comm(const int*) {}
 
@@ -1660,6 +1794,88 @@ int hx_oracle_sphere_op(int op, const double* in, double* out) {
     push_block(b.data(), out + (size_t)e * nout * B, nout);
   }
   return 0;
+}
+
+// Dry-dynamics trajectory (include/hxgpu.h).  The oracle keeps the input state of every
+// step and recomputes each step's stage inputs on the way back.
+int hx_traj_forward(const double* v, const double* T, const double* dp3d, int nsteps,
+                    double dt, double* v_out, double* T_out, double* dp3d_out) {
+  C().last_err = 0;
+  if (!traj_ready(false)) return C().last_err;
+  if (nsteps < 0 || !(dt > 0)) {
+    set_error(HX_ERR_STATE, "hx_traj_forward: nsteps must be >= 0 and dt > 0");
+    return C().last_err;
+  }
+  TrajCtx& tc = TC();
+  tc.have = false;
+  tc.steps.clear();
+  DryState<double> x;
+  traj_pull(v, T, dp3d, x);
+  for (int s = 0; s < nsteps; ++s) {
+    tc.steps.push_back(x);
+    if (!dry_step(x, dt, traj_remaps_after(s), (std::vector<DryState<double>>*)nullptr)) {
+      set_error(101, "Negative (or nan) layer thickness detected, aborting!");
+      return C().last_err;
+    }
+  }
+  tc.nsteps = nsteps;
+  tc.dt = dt;
+  tc.have = true;
+  traj_push(x, v_out, T_out, dp3d_out);
+  return 0;
+}
+
+int hx_traj_vjp(const double* v_bar, const double* T_bar, const double* dp3d_bar,
+                double* v_grad, double* T_grad, double* dp3d_grad) {
+  C().last_err = 0;
+  if (!traj_ready(true)) return C().last_err;
+  TrajCtx& tc = TC();
+  DryState<double> a;
+  traj_pull(v_bar, T_bar, dp3d_bar, a);
+  for (int s = tc.nsteps - 1; s >= 0; --s)
+    dry_step_vjp(tc.steps[(size_t)s], tc.dt, traj_remaps_after(s), a);
+  traj_push(a, v_grad, T_grad, dp3d_grad);
+  return 0;
+}
+
+int hx_traj_jvp(const double* dv, const double* dT, const double* ddp3d, double* v_tan,
+                double* T_tan, double* dp3d_tan) {
+  C().last_err = 0;
+  if (!traj_ready(true)) return C().last_err;
+  TrajCtx& tc = TC();
+  DryState<double> d;
+  traj_pull(dv, dT, ddp3d, d);
+  if (tc.nsteps == 0) {
+    traj_push(d, v_tan, T_tan, dp3d_tan);
+    return 0;
+  }
+  DryState<Dual> x;
+  x.alloc(C().E);
+  const DryState<double>& x0 = tc.steps[0];
+  for (size_t i = 0; i < x.v.size(); ++i) x.v[i] = Dual(x0.v[i], d.v[i]);
+  for (size_t i = 0; i < x.t.size(); ++i) {
+    x.t[i] = Dual(x0.t[i], d.t[i]);
+    x.dp[i] = Dual(x0.dp[i], d.dp[i]);
+  }
+  for (int s = 0; s < tc.nsteps; ++s)
+    dry_step(x, tc.dt, traj_remaps_after(s), (std::vector<DryState<Dual>>*)nullptr);
+  DryState<double> out;
+  out.alloc(C().E);
+  for (size_t i = 0; i < x.v.size(); ++i) out.v[i] = x.v[i].d;
+  for (size_t i = 0; i < x.t.size(); ++i) {
+    out.t[i] = x.t[i].d;
+    out.dp[i] = x.dp[i].d;
+  }
+  traj_push(out, v_tan, T_tan, dp3d_tan);
+  return 0;
+}
+
+int hx_traj_set_checkpointing(int mode) {
+  if (mode < 0 || mode > 2) {
+    set_error(HX_ERR_STATE, "hx_traj_set_checkpointing: mode must be 0, 1 or 2");
+    return C().last_err;
+  }
+  return 0;  // the oracle always keeps step states and recomputes the stages
 }
 
 int hx_oracle_threads(void) {
