@@ -24,6 +24,7 @@ __constant__ double c_hyai[NLEV + 1];
 __constant__ double c_hybi[NLEV + 1];
 __constant__ double c_ai_delta[NLEV];
 __constant__ double c_bi_delta[NLEV];
+__constant__ double c_rdp0[NLEV];  // 1 / reference layer thickness (hybrid coordinate at ps0)
 
 template <typename R> __device__ __forceinline__ R dvv_at(int a, int b);
 template <> __device__ __forceinline__ double dvv_at<double>(int a, int b) { return c_dvv[a * 4 + b]; }
@@ -262,6 +263,21 @@ __device__ __forceinline__ double warp_sum(double v) {
   for (int off = 16; off >= 1; off >>= 1) v += __shfl_xor_sync(FULL, v, off);
   return v;
 }
+
+// ---- exact FP64 operations on the integer pipe ------------------------------------
+// The GB300's FP64 pipe issues 2 thread-instructions per cycle per SM (1/64 of FP32),
+// and min/max and compares issue there like arithmetic.  Exact ones move to the integer
+// pipe: a non-NaN double's bit pattern, with the magnitude bits flipped when the sign
+// bit is set, orders like the value as a signed 64-bit integer (-0 below +0).
+__device__ __forceinline__ long long dkey(double x) {
+  const long long b = __double_as_longlong(x);
+  return b ^ ((b >> 63) & 0x7fffffffffffffffLL);
+}
+__device__ __forceinline__ double dkey_value(long long k) {
+  return __longlong_as_double(k ^ ((k >> 63) & 0x7fffffffffffffffLL));
+}
+__device__ __forceinline__ long long kmin(long long a, long long b) { return b < a ? b : a; }
+__device__ __forceinline__ long long kmax(long long a, long long b) { return b > a ? b : a; }
 
 // Brackets one launch for the per-kernel timing hooks.
 struct KScope {

@@ -360,16 +360,28 @@ __global__ void k_dp_from_ps(int E, double* dp, const double* ps_v, int n0, doub
       c_ai_delta[l] * ps0 + c_bi_delta[l] * ps_v[((size_t)e * NTL + n0) * 16 + p];
 }
 
-__global__ void k_update_q(int E, int Q, const double* qdp, double* Qc, const double* ps_v, int np1,
-                           int np1_qdp, double ps0) {
-  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= (long long)E * Q * NLEV * 16) return;
-  const int p = idx & 15;
-  const int l = (idx / 16) % NLEV;
-  const int q = (idx / (16 * NLEV)) % Q;
-  const int e = idx / (16LL * NLEV * Q);
+// Grid of the per-(element, tracer) pointwise kernels: blockIdx.x = e*nq + q, blockIdx.y
+// = a group of EQ_LEVELS levels, threadIdx.x = level-in-group * 16 + point.  Only
+// 32-bit divisions by the tracer count (64-bit division by a runtime value is a long
+// emulated sequence).
+constexpr int EQ_LEVELS = 8;
+constexpr int EQ_THREADS = EQ_LEVELS * 16;
+__device__ __forceinline__ void eq_index(int nq, int& e, int& q, int& l, int& p) {
+  const int eq = blockIdx.x;
+  e = eq / nq;
+  q = eq - e * nq;
+  l = blockIdx.y * EQ_LEVELS + (threadIdx.x >> 4);
+  p = threadIdx.x & 15;
+}
+
+__global__ void __launch_bounds__(EQ_THREADS) k_update_q(int Q, const double* qdp, double* Qc,
+                                                          const double* ps_v, int np1, int np1_qdp,
+                                                          double ps0) {
+  int e, q, l, p;
+  eq_index(Q, e, q, l, p);
   const double dp = c_ai_delta[l] * ps0 + c_bi_delta[l] * ps_v[((size_t)e * NTL + np1) * 16 + p];
-  Qc[idx] = qdp[((((size_t)e * QTL + np1_qdp) * Q + q) * NLEV + l) * 16 + p] / dp;
+  Qc[(((size_t)e * Q + q) * NLEV + l) * 16 + p] =
+      qdp[((((size_t)e * QTL + np1_qdp) * Q + q) * NLEV + l) * 16 + p] / dp;
 }
 
 // ======================================================================================
@@ -423,14 +435,27 @@ __global__ void __launch_bounds__(LG * 16) k_qminmax(EulerArgs<R> a, double* qli
       const int l = lg + LG * k;
       const R val = (R)qsrc[l * 16 + p] * rdp[k];
       if (store_q) qt[l * 16 + p] = (double)val;
-      R mn = val, mx = val;
+      double dmn, dmx;
+      if constexpr (kF32<R>) {
+        R mn = val, mx = val;
 #pragma unroll
-      for (int off = 8; off >= 1; off >>= 1) {
-        mn = fmin(mn, __shfl_xor_sync(FULL, mn, off, 16));
-        mx = fmax(mx, __shfl_xor_sync(FULL, mx, off, 16));
+        for (int off = 8; off >= 1; off >>= 1) {
+          mn = fminf(mn, __shfl_xor_sync(FULL, mn, off, 16));
+          mx = fmaxf(mx, __shfl_xor_sync(FULL, mx, off, 16));
+        }
+        dmn = (double)mn;
+        dmx = (double)mx;
+      } else {  // exact min/max on the integer pipe
+        long long mn = dkey(val), mx = mn;
+#pragma unroll
+        for (int off = 8; off >= 1; off >>= 1) {
+          mn = kmin(mn, __shfl_xor_sync(FULL, mn, off, 16));
+          mx = kmax(mx, __shfl_xor_sync(FULL, mx, off, 16));
+        }
+        dmn = dkey_value(mn);
+        dmx = dkey_value(mx);
       }
       if (p == 0) {
-        double dmn = (double)mn, dmx = (double)mx;
         if (a.rhs_multiplier == 1.0) {
           dmn = fmin(qo[l], dmn);
           dmx = fmax(qo[NLEV + l], dmx);
@@ -448,16 +473,16 @@ __global__ void k_minmax_nbr(int E, int Q, const double* __restrict__ pre, doubl
   const int idx = blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= E * Q * NLEV) return;
   const int l = idx % NLEV, q = (idx / NLEV) % Q, e = idx / (NLEV * Q);
-  double mn = pre[((size_t)e * Q + q) * 2 * NLEV + l];
-  double mx = pre[((size_t)e * Q + q) * 2 * NLEV + NLEV + l];
+  long long mn = dkey(pre[((size_t)e * Q + q) * 2 * NLEV + l]);
+  long long mx = dkey(pre[((size_t)e * Q + q) * 2 * NLEV + NLEV + l]);
   for (int s = 0; s < 8; ++s) {
     const int r = conn[e * 8 + s];
     if (r < 0) continue;
-    mn = fmin(mn, pre[((size_t)r * Q + q) * 2 * NLEV + l]);
-    mx = fmax(mx, pre[((size_t)r * Q + q) * 2 * NLEV + NLEV + l]);
+    mn = kmin(mn, dkey(pre[((size_t)r * Q + q) * 2 * NLEV + l]));
+    mx = kmax(mx, dkey(pre[((size_t)r * Q + q) * 2 * NLEV + NLEV + l]));
   }
-  qlim[((size_t)e * Q + q) * 2 * NLEV + l] = mn;
-  qlim[((size_t)e * Q + q) * 2 * NLEV + NLEV + l] = mx;
+  qlim[((size_t)e * Q + q) * 2 * NLEV + l] = dkey_value(mn);
+  qlim[((size_t)e * Q + q) * 2 * NLEV + NLEV + l] = dkey_value(mx);
 }
 
 // BIHPre: qtens (Q) [* dpdiss_ave / dp0] -> laplace -> qscr (pre-DSS).
@@ -475,7 +500,7 @@ __global__ void __launch_bounds__(LG * 16) k_bih_pre(EulerArgs<R> a) {
   for (int k = 0; k < NL; ++k) {
     const int l = lg + LG * k;
     R s = (R)a.qtens[qb + l * 16 + p];
-    if (a.nu_p > 0) s = s * (R)a.dpdiss_ave[((size_t)e * NLEV + l) * 16 + p] * R(1.0 / a.dp0[l]);
+    if (a.nu_p > 0) s = s * (R)a.dpdiss_ave[((size_t)e * NLEV + l) * 16 + p] * R(c_rdp0[l]);
     a.qscr[qb + l * 16 + p] = (double)laplace_simple(t, m, s);
   }
 }
@@ -697,11 +722,9 @@ template <typename R> constexpr size_t aal_smem() {
 // DSS(rspheremp) of the tracer scratch into Qdp(np1); with time_avg the last RK2 stage
 // also applies qdp_time_avg: Qdp(np1) = (Qdp(n0) + 2 Qdp(np1)) / 3.
 template <typename R>
-__global__ void k_dss_tracers(EulerArgs<R> a, int E, int time_avg) {
-  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= (long long)E * a.Q * NLEV * 16) return;
-  const int p = idx & 15, l = (idx / 16) % NLEV, q = (idx / (16 * NLEV)) % a.Q;
-  const int e = idx / (16LL * NLEV * a.Q);
+__global__ void __launch_bounds__(EQ_THREADS) k_dss_tracers(EulerArgs<R> a, int time_avg) {
+  int e, q, l, p;
+  eq_index(a.Q, e, q, l, p);
   const double rs = a.m.rspheremp_d[e * 16 + p];
   const double v = dss_gather(a.qscr + (size_t)q * NLEV * 16, (long long)a.Q * NLEV * 16, 16, e, l, p, a.dss) * rs;
   const size_t d = ((((size_t)e * QTL + a.np1_qdp) * a.Q + q) * NLEV + l) * 16 + p;
@@ -724,20 +747,17 @@ __global__ void k_dss_field(int E, const double* __restrict__ src, double* dst,
 }
 
 // Generic in-place DSS through a scratch copy.
-__global__ void k_copy_fields(int E, int nf, const double* base, long long fs, long long es, int ls,
-                              double* scr) {
-  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= (long long)E * nf * NLEV * 16) return;
-  const int p = idx & 15, l = (idx / 16) % NLEV, f = (idx / (16 * NLEV)) % nf;
-  const int e = idx / (16LL * NLEV * nf);
-  scr[idx] = base[(size_t)f * fs + (size_t)e * es + (size_t)l * ls + p];
+__global__ void __launch_bounds__(EQ_THREADS) k_copy_fields(int nf, const double* base, long long fs,
+                                                             long long es, int ls, double* scr) {
+  int e, f, l, p;
+  eq_index(nf, e, f, l, p);
+  scr[(((size_t)e * nf + f) * NLEV + l) * 16 + p] = base[(size_t)f * fs + (size_t)e * es + (size_t)l * ls + p];
 }
-__global__ void k_dss_from_copy(int E, int nf, double* base, long long fs, long long es, int ls,
-                                const double* scr, const double* rsmp, DssTable tab) {
-  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= (long long)E * nf * NLEV * 16) return;
-  const int p = idx & 15, l = (idx / 16) % NLEV, f = (idx / (16 * NLEV)) % nf;
-  const int e = idx / (16LL * NLEV * nf);
+__global__ void __launch_bounds__(EQ_THREADS) k_dss_from_copy(int nf, double* base, long long fs,
+                                                               long long es, int ls, const double* scr,
+                                                               const double* rsmp, DssTable tab) {
+  int e, f, l, p;
+  eq_index(nf, e, f, l, p);
   double v = dss_gather(scr + (size_t)f * NLEV * 16, (long long)nf * NLEV * 16, 16, e, l, p, tab);
   if (rsmp) v *= rsmp[e * 16 + p];
   base[(size_t)f * fs + (size_t)e * es + (size_t)l * ls + p] = v;
@@ -762,7 +782,67 @@ constexpr int R_DMA = R_MASS + 74;     // dma[0 .. 73]
 constexpr int R_AI = R_DMA + 74;       // ai[0 .. 72]
 constexpr int R_COEF = R_AI + 74;      // coef[3][72]
 constexpr int R_RD = R_COEF + 216;     // 1 / D[0 .. 71]
-constexpr int R_COL = R_RD + 72;       // doubles per column
+constexpr int R_GF = R_RD + 72;        // mixed form: float g[10][74], z2[72], 1/D[72]
+// doubles per column
+template <typename R> constexpr int r_col() { return kF32<R> ? R_GF + (740 + 72 + 72) / 2 : R_GF; }
+
+// compute_ppm and the monotone parabola coefficients (PpmRemap.hpp:202-353) for one
+// variable of one column in T: slopes dma (j in 0 .. 73), edge values ai (j in 0 .. 72),
+// coefficients coef[3][72].  A has its ghost cells; g holds the grid weights [10][74].
+template <typename T>
+__device__ __forceinline__ void ppm_coefs(int lane, bool own, int l0, int remap_alg, const T* A,
+                                          const T* g, T* dma, T* ai, T* coef) {
+  if (lane < 25) {
+#pragma unroll
+    for (int k3 = 0; k3 < 3; ++k3) {
+      const int j = 3 * lane + k3;
+      if (j < NLEV + 2) {
+        const T a0 = A[j], am1 = A[j - 1], am2 = A[j - 2];
+        T r = T(0);
+        if ((a0 - am1) * (am1 - am2) > T(0)) {
+          const T da = g[0 * 74 + j] * (g[1 * 74 + j] * (a0 - am1) + g[2 * 74 + j] * (am1 - am2));
+          r = fmin(fmin(fabs(da), T(2) * fabs(am1 - am2)), T(2) * fabs(a0 - am1)) * copysign(T(1), da);
+        }
+        dma[j] = r;
+      }
+    }
+  }
+  __syncwarp();
+  if (lane < 25) {
+#pragma unroll
+    for (int k3 = 0; k3 < 3; ++k3) {
+      const int j = 3 * lane + k3;
+      if (j < NLEV + 1) {
+        const T a0 = A[j], am1 = A[j - 1];
+        ai[j] = am1 + g[3 * 74 + j] * (a0 - am1) +
+                g[4 * 74 + j] * (g[5 * 74 + j] * (g[6 * 74 + j] - g[7 * 74 + j]) * (a0 - am1) -
+                                 g[8 * 74 + j] * dma[j + 1] + g[9 * 74 + j] * dma[j]);
+      }
+    }
+  }
+  __syncwarp();
+  if (own) {
+#pragma unroll
+    for (int k3 = 0; k3 < 3; ++k3) {
+      const int jp = l0 + k3;
+      T al = ai[jp], ar = ai[jp + 1];
+      const T cm = A[jp];
+      if ((ar - cm) * (cm - al) <= T(0)) { al = cm; ar = cm; }
+      constexpr T sixth = T(1.0 / 6.0);
+      if ((ar - al) * (cm - (al + ar) * T(0.5)) > (ar - al) * (ar - al) * sixth) al = T(3) * cm - T(2) * ar;
+      if ((ar - al) * (cm - (al + ar) * T(0.5)) < -(ar - al) * (ar - al) * sixth) ar = T(3) * cm - T(2) * al;
+      T c0 = T(1.5) * cm - (al + ar) / T(4), c1 = ar - al, c2 = T(3) * (T(-2) * cm + (al + ar));
+      if (remap_alg == 2 && (jp < 2 || jp >= NLEV - 2)) {  // PpmFixedParabola
+        c0 = cm;
+        c1 = T(0);
+        c2 = T(0);
+      }
+      coef[0 * 72 + jp] = c0;
+      coef[1 * 72 + jp] = c1;
+      coef[2 * 72 + jp] = c2;
+    }
+  }
+}
 
 // PPM vertical remap (RemapFunctor + PpmVertRemap, rsplit > 0), one warp per column:
 // lane L owns levels 3L .. 3L+2 (L < 24) for level work and interfaces j = 3L .. 3L+2
@@ -777,7 +857,7 @@ __global__ void __launch_bounds__(RT) k_remap(RemapArgs a) {
   const int cidx = blockIdx.x * RCOLS + warp;
   if (cidx >= a.nelem * 16) return;  // whole warp leaves together; no CTA barriers below
   const int e = cidx >> 4, p = cidx & 15;
-  double* sm = rsm + warp * R_COL;
+  double* sm = rsm + warp * r_col<R>();
   double* D = sm + R_D + 2;
   double* pio = sm + R_PIO;
   double* pin = sm + R_PIN;
@@ -808,13 +888,14 @@ __global__ void __launch_bounds__(RT) k_remap(RemapArgs a) {
   }
   const double ps = warp_sum(s3[0] + s3[1] + s3[2]) + a.hyai0 * a.ps0;
   if (lane == 0) a.ps_v[((size_t)e * NTL + a.np1) * 16 + p] = ps;
-  double t3[3] = {0.0, 0.0, 0.0};
+  double t3[3] = {0.0, 0.0, 0.0}, rt3[3] = {0.0, 0.0, 0.0};
   if (own) {
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
       const int l = l0 + k;
       t3[k] = (c_hyai[l + 1] - c_hyai[l]) * a.ps0 + (c_hybi[l + 1] - c_hybi[l]) * ps;
       tgt[l] = t3[k];
+      rt3[k] = 1.0 / t3[k];
     }
   }
   // compute_partitions: pio, pin cumulative thickness
@@ -861,36 +942,60 @@ __global__ void __launch_bounds__(RT) k_remap(RemapArgs a) {
       z2[k] = (pin[k + 1] - (pio[kk - 1] + pio[kk]) * 0.5) / D[kk - 1];
     }
   }
-  // compute_grids (in R)
+  // compute_grids (double)
   if (lane < 25) {
 #pragma unroll
     for (int k3 = 0; k3 < 3; ++k3) {
       const int j = 3 * lane + k3;
       if (j < NLEV + 2) {
-        const R dm2 = (R)D[j - 2], dm1 = (R)D[j - 1], d0 = (R)D[j];
-        const R r10 = R(1) / (dm1 + d0);  // shared by g1, g3, g5
-        g[0 * 74 + j] = (double)(dm1 / (dm2 + dm1 + d0));
-        g[1 * 74 + j] = (double)((R(2) * dm2 + dm1) * r10);
-        g[2 * 74 + j] = (double)((dm1 + R(2) * d0) / (dm2 + dm1));
+        const double dm2 = D[j - 2], dm1 = D[j - 1], d0 = D[j];
+        const double r10 = 1.0 / (dm1 + d0);  // shared by g1, g3, g5
+        g[0 * 74 + j] = dm1 / (dm2 + dm1 + d0);
+        g[1 * 74 + j] = (2.0 * dm2 + dm1) * r10;
+        g[2 * 74 + j] = (dm1 + 2.0 * d0) / (dm2 + dm1);
         if (j < NLEV + 1) {
-          const R dp1 = (R)D[j + 1];
-          const R r6 = R(1) / (R(2) * dm1 + d0);  // shared by g6, g8
-          const R r7 = R(1) / (R(2) * d0 + dm1);  // shared by g7, g9
-          g[3 * 74 + j] = (double)(dm1 * r10);
-          g[4 * 74 + j] = (double)(R(1) / (dm2 + dm1 + d0 + dp1));
-          g[5 * 74 + j] = (double)((R(2) * dm1 * d0) * r10);
-          g[6 * 74 + j] = (double)((dm2 + dm1) * r6);
-          g[7 * 74 + j] = (double)((dp1 + d0) * r7);
-          g[8 * 74 + j] = (double)(dm1 * (dm2 + dm1) * r6);
-          g[9 * 74 + j] = (double)(d0 * (d0 + dp1) * r7);
+          const double dp1 = D[j + 1];
+          const double r6 = 1.0 / (2.0 * dm1 + d0);  // shared by g6, g8
+          const double r7 = 1.0 / (2.0 * d0 + dm1);  // shared by g7, g9
+          g[3 * 74 + j] = dm1 * r10;
+          g[4 * 74 + j] = 1.0 / (dm2 + dm1 + d0 + dp1);
+          g[5 * 74 + j] = (2.0 * dm1 * d0) * r10;
+          g[6 * 74 + j] = (dm2 + dm1) * r6;
+          g[7 * 74 + j] = (dp1 + d0) * r7;
+          g[8 * 74 + j] = dm1 * (dm2 + dm1) * r6;
+          g[9 * 74 + j] = d0 * (d0 + dp1) * r7;
         }
       }
     }
   }
   __syncwarp();
+  // Mixed form: the tracers' reconstructions run in FP32 from float copies of the grid
+  // weights, z2 and 1/D; their cell integrals and the mass below each interface stay in
+  // FP64, and the bottom interface carries the exact column mass (mass fixer).
+  float* gf = reinterpret_cast<float*>(sm + R_GF);  // [10][74]
+  float* z2f = gf + 740;
+  float* rDf = z2f + 72;
+  float* Af = reinterpret_cast<float*>(sm + R_A) + 2;
+  float* dmaf = reinterpret_cast<float*>(sm + R_DMA);
+  float* aif = reinterpret_cast<float*>(sm + R_AI);
+  float* coeff = reinterpret_cast<float*>(sm + R_COEF);
+  if constexpr (kF32<R>) {
+    if (a.Q > 0) {
+      for (int i = lane; i < 740; i += 32) gf[i] = (float)g[i];
+      if (own) {
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+          z2f[l0 + k] = (float)z2[l0 + k];
+          rDf[l0 + k] = (float)rD[l0 + k];
+        }
+      }
+      __syncwarp();
+    }
+  }
   const int nvar = 3 + a.Q;
 #pragma unroll 1
   for (int var = 0; var < nvar; ++var) {
+    const bool lo = kF32<R> && var >= 3;
     // extrinsic values (v dp, T dp for the states; Qdp as is), cell means, masses
     double x3[3] = {0.0, 0.0, 0.0};
     if (own) {
@@ -900,7 +1005,8 @@ __global__ void __launch_bounds__(RT) k_remap(RemapArgs a) {
         if (var < 2) x3[k] = a.v[vb + (size_t)l * 32 + var * 16] * s3[k];
         else if (var == 2) x3[k] = a.T[sb + (size_t)l * 16] * s3[k];
         else x3[k] = a.qdp[((((size_t)e * QTL + a.n0_qdp) * a.Q + (var - 3)) * NLEV + l) * 16 + p];
-        A[l] = x3[k] * rD[l];
+        if (lo) Af[l] = (float)x3[k] * rDf[l];
+        else A[l] = x3[k] * rD[l];
       }
     }
     {
@@ -916,71 +1022,22 @@ __global__ void __launch_bounds__(RT) k_remap(RemapArgs a) {
       if (lane == 0) mass[0] = 0.0;
     }
     __syncwarp();
-    if (lane == 0) {
-      if (a.remap_alg == 3) {
-        A[-1] = A[-2] = A[0];
-        A[NLEV] = A[NLEV + 1] = A[NLEV - 1];
+    if (lane == 0) {  // ghost cells: mirrored (remap_alg 1, 2) or constant (3)
+      if (lo) {
+        Af[-1] = Af[0];
+        Af[-2] = a.remap_alg == 3 ? Af[0] : Af[1];
+        Af[NLEV] = Af[NLEV - 1];
+        Af[NLEV + 1] = a.remap_alg == 3 ? Af[NLEV - 1] : Af[NLEV - 2];
       } else {
         A[-1] = A[0];
-        A[-2] = A[1];
+        A[-2] = a.remap_alg == 3 ? A[0] : A[1];
         A[NLEV] = A[NLEV - 1];
-        A[NLEV + 1] = A[NLEV - 2];
+        A[NLEV + 1] = a.remap_alg == 3 ? A[NLEV - 1] : A[NLEV - 2];
       }
     }
     __syncwarp();
-    // compute_ppm: slopes dma (j in 0 .. 73)
-    if (lane < 25) {
-#pragma unroll
-      for (int k3 = 0; k3 < 3; ++k3) {
-        const int j = 3 * lane + k3;
-        if (j < NLEV + 2) {
-          const R a0 = (R)A[j], am1 = (R)A[j - 1], am2 = (R)A[j - 2];
-          R r = R(0);
-          if ((a0 - am1) * (am1 - am2) > R(0)) {
-            const R da = (R)g[0 * 74 + j] * ((R)g[1 * 74 + j] * (a0 - am1) + (R)g[2 * 74 + j] * (am1 - am2));
-            r = fmin(fmin(fabs(da), R(2) * fabs(am1 - am2)), R(2) * fabs(a0 - am1)) * copysign(R(1), da);
-          }
-          dma[j] = (double)r;
-        }
-      }
-    }
-    __syncwarp();
-    // edge values ai (j in 0 .. 72)
-    if (lane < 25) {
-#pragma unroll
-      for (int k3 = 0; k3 < 3; ++k3) {
-        const int j = 3 * lane + k3;
-        if (j < NLEV + 1) {
-          const R a0 = (R)A[j], am1 = (R)A[j - 1];
-          ai[j] = (double)(am1 + (R)g[3 * 74 + j] * (a0 - am1) +
-                           (R)g[4 * 74 + j] * ((R)g[5 * 74 + j] * ((R)g[6 * 74 + j] - (R)g[7 * 74 + j]) * (a0 - am1) -
-                                               (R)g[8 * 74 + j] * (R)dma[j + 1] + (R)g[9 * 74 + j] * (R)dma[j]));
-        }
-      }
-    }
-    __syncwarp();
-    // monotone parabola coefficients per cell
-    if (own) {
-#pragma unroll
-      for (int k3 = 0; k3 < 3; ++k3) {
-        const int jp = l0 + k3;
-        R al = (R)ai[jp], ar = (R)ai[jp + 1];
-        const R cm = (R)A[jp];
-        if ((ar - cm) * (cm - al) <= R(0)) { al = cm; ar = cm; }
-        constexpr R sixth = R(1.0 / 6.0);
-        if ((ar - al) * (cm - (al + ar) * R(0.5)) > (ar - al) * (ar - al) * sixth) al = R(3) * cm - R(2) * ar;
-        if ((ar - al) * (cm - (al + ar) * R(0.5)) < -(ar - al) * (ar - al) * sixth) ar = R(3) * cm - R(2) * al;
-        R c0 = R(1.5) * cm - (al + ar) / R(4), c1 = ar - al, c2 = R(3) * (R(-2) * cm + (al + ar));
-        if (a.remap_alg == 2 && (jp < 2 || jp >= NLEV - 2)) {  // PpmFixedParabola
-          c0 = cm;
-          c1 = R(0);
-          c2 = R(0);
-        }
-        coef[0 * 72 + jp] = (double)c0;
-        coef[1 * 72 + jp] = (double)c1;
-        coef[2 * 72 + jp] = (double)c2;
-      }
-    }
+    if (lo) ppm_coefs<float>(lane, own, l0, a.remap_alg, Af, gf, dmaf, aif, coeff);
+    else ppm_coefs<double>(lane, own, l0, a.remap_alg, A, g, dma, ai, coef);
     __syncwarp();
     // compute_remap: mass below each new interface, in double; new cell masses are
     // differences of consecutive interface masses (the lower one from the next lane).
@@ -990,10 +1047,17 @@ __global__ void __launch_bounds__(RT) k_remap(RemapArgs a) {
       for (int k3 = 0; k3 < 3; ++k3) {
         const int k = l0 + k3;
         const int kk = kid[k];
-        const double x2 = z2[k], x1 = -0.5;
-        const double in = (coef[kk] * (x2 - x1) + coef[72 + kk] * (x2 * x2 - x1 * x1) * 0.5) +
-                          coef[144 + kk] * (x2 * x2 * x2 - x1 * x1 * x1) * (1.0 / 3.0);
-        m2[k3] = mass[kk + 1] + in * D[kk];
+        if (lo) {
+          const float x2 = z2f[k];
+          const float in = (coeff[kk] * (x2 + 0.5f) + coeff[72 + kk] * (x2 * x2 - 0.25f) * 0.5f) +
+                           coeff[144 + kk] * (x2 * x2 * x2 + 0.125f) * (1.0f / 3.0f);
+          m2[k3] = k == NLEV - 1 ? mass[NLEV + 1] : mass[kk + 1] + (double)in * D[kk];
+        } else {
+          const double x2 = z2[k], x1 = -0.5;
+          const double in = (coef[kk] * (x2 - x1) + coef[72 + kk] * (x2 * x2 - x1 * x1) * 0.5) +
+                            coef[144 + kk] * (x2 * x2 * x2 - x1 * x1 * x1) * (1.0 / 3.0);
+          m2[k3] = mass[kk + 1] + in * D[kk];
+        }
       }
     }
     double below = __shfl_up_sync(FULL, m2[2], 1);
@@ -1004,8 +1068,8 @@ __global__ void __launch_bounds__(RT) k_remap(RemapArgs a) {
         const int k = l0 + k3;
         const double m1 = k3 == 0 ? below : m2[k3 - 1];
         const double out = m2[k3] - m1;
-        if (var < 2) a.v[vb + (size_t)k * 32 + var * 16] = out / t3[k3];
-        else if (var == 2) a.T[sb + (size_t)k * 16] = out / t3[k3];
+        if (var < 2) a.v[vb + (size_t)k * 32 + var * 16] = out * rt3[k3];
+        else if (var == 2) a.T[sb + (size_t)k * 16] = out * rt3[k3];
         else a.qdp[((((size_t)e * QTL + a.n0_qdp) * a.Q + (var - 3)) * NLEV + k) * 16 + p] = out;
       }
     }
@@ -1047,7 +1111,9 @@ void upload_constants(const double* dvv16, const double* hyai, const double* hyb
     ad[l] = hyai[l + 1] - hyai[l];
     bd[l] = hybi[l + 1] - hybi[l];
   }
-  (void)ps0;
+  double rdp0[NLEV];
+  for (int l = 0; l < NLEV; ++l) rdp0[l] = 1.0 / (ad[l] * ps0 + bd[l] * ps0);
+  cudaMemcpyToSymbolAsync(c_rdp0, rdp0, sizeof(double) * NLEV, 0, cudaMemcpyHostToDevice, s);
   cudaMemcpyToSymbolAsync(c_dvv, dvv16, sizeof(double) * 16, 0, cudaMemcpyHostToDevice, s);
   cudaMemcpyToSymbolAsync(c_dvvf, f, sizeof(float) * 16, 0, cudaMemcpyHostToDevice, s);
   cudaMemcpyToSymbolAsync(c_hyai, hyai, sizeof(double) * (NLEV + 1), 0, cudaMemcpyHostToDevice, s);
@@ -1159,7 +1225,7 @@ void launch_euler_step(EulerArgs<R>& a, int E, int time_avg, cudaStream_t s) {
     }
     {
       KScope k("euler_dss_qdp", s);
-      k_dss_tracers<R><<<nblk((long long)E * a.Q * NLEV * 16, 256), 256, 0, s>>>(a, E, time_avg);
+      k_dss_tracers<R><<<dim3(E * a.Q, NLEV / EQ_LEVELS), EQ_THREADS, 0, s>>>(a, time_avg);
     }
   }
   {
@@ -1170,29 +1236,29 @@ void launch_euler_step(EulerArgs<R>& a, int E, int time_avg, cudaStream_t s) {
 
 template <typename R>
 void launch_remap(const RemapArgs& a, cudaStream_t s) {
-  const size_t smem = (size_t)RCOLS * R_COL * sizeof(double);
+  const size_t smem = (size_t)RCOLS * r_col<R>() * sizeof(double);
   static bool init = false;
   if (!init) {
-    cudaFuncSetAttribute(k_remap<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(k_remap<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     init = true;
   }
   KScope k("ppm_remap", s);
-  k_remap<double><<<(a.nelem * 16 + RCOLS - 1) / RCOLS, RT, smem, s>>>(a);
+  k_remap<R><<<(a.nelem * 16 + RCOLS - 1) / RCOLS, RT, smem, s>>>(a);
 }
 
 void launch_update_q(int E, int Q, const double* qdp, double* Qc, const double* ps_v, int np1, int np1_qdp,
                      double ps0, cudaStream_t s) {
   if (Q == 0) return;
   KScope k("update_q", s);
-  k_update_q<<<nblk((long long)E * Q * NLEV * 16, 256), 256, 0, s>>>(E, Q, qdp, Qc, ps_v, np1, np1_qdp, ps0);
+  k_update_q<<<dim3(E * Q, NLEV / EQ_LEVELS), EQ_THREADS, 0, s>>>(Q, qdp, Qc, ps_v, np1, np1_qdp, ps0);
 }
 
 void launch_dss_inplace(int E, int nf, double* base, long long fs, long long es, int ls, double* scr,
                         const double* rsmp, DssTable t, cudaStream_t s) {
+  if (nf <= 0) return;
   KScope k("dss_generic", s);
-  const long long n = (long long)E * nf * NLEV * 16;
-  k_copy_fields<<<nblk(n, 256), 256, 0, s>>>(E, nf, base, fs, es, ls, scr);
-  k_dss_from_copy<<<nblk(n, 256), 256, 0, s>>>(E, nf, base, fs, es, ls, scr, rsmp, t);
+  k_copy_fields<<<dim3(E * nf, NLEV / EQ_LEVELS), EQ_THREADS, 0, s>>>(nf, base, fs, es, ls, scr);
+  k_dss_from_copy<<<dim3(E * nf, NLEV / EQ_LEVELS), EQ_THREADS, 0, s>>>(nf, base, fs, es, ls, scr, rsmp, t);
 }
 
 #define HX_INST(R)                                                                  \
