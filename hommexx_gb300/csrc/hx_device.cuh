@@ -43,10 +43,7 @@ template <typename R> constexpr bool kF32 = sizeof(R) == 4;
 // constants, and the FP32 operand then carries the horizontal variation instead of the
 // large mean (pressure, geopotential, temperature, layer thickness).  In the FP64 form the
 // value is used as is, so the arithmetic follows the reference formulas.
-template <typename R> __device__ __forceinline__ R rel(double x) {
-  if constexpr (kF32<R>) return (R)(x - sh16(x, 0));
-  else return x;
-}
+template <typename R> __device__ __forceinline__ R rel(double x);
 
 // Per-thread GLL point data: index, dvv rows/columns for the four contractions.
 template <typename R>
@@ -278,6 +275,57 @@ __device__ __forceinline__ double dkey_value(long long k) {
 }
 __device__ __forceinline__ long long kmin(long long a, long long b) { return b < a ? b : a; }
 __device__ __forceinline__ long long kmax(long long a, long long b) { return b > a ? b : a; }
+
+// ---- double <-> float conversions on the integer pipe --------------------------------
+// F2F conversions also issue to the FP64 pipe; the mixed form converts at every load
+// and store of a double field.  These restate the IEEE 754 binary64 <-> binary32
+// conversions (round to nearest, ties to even) as integer field manipulation; zeros are
+// handled inline and the rare subnormal, overflowing, infinite and NaN cases fall back to
+// the hardware conversion, so the results equal the hardware's for every input.
+__device__ __forceinline__ float d2f_rn(double x) {
+  const unsigned hi = (unsigned)__double2hiint(x);
+  const unsigned lo = (unsigned)__double2loint(x);
+  const int e = (int)((hi >> 20) & 0x7FFu) - 896;  // binary32 biased exponent
+  if (e <= 0 || e >= 255) {
+    if (((hi & 0x7FFFFFFFu) | lo) == 0u) return __uint_as_float(hi & 0x80000000u);
+    return __double2float_rn(x);
+  }
+  const unsigned m = ((hi & 0xFFFFFu) << 3) | (lo >> 29);  // top 23 of the 52 mantissa bits
+  const unsigned rest = lo & 0x1FFFFFFFu;                   // the 29 dropped bits
+  unsigned r = (hi & 0x80000000u) | ((unsigned)e << 23) | m;
+  r += (rest > 0x10000000u || (rest == 0x10000000u && (m & 1u))) ? 1u : 0u;  // carry is exact
+  return __uint_as_float(r);
+}
+__device__ __forceinline__ double f2d(float x) {
+  const unsigned u = __float_as_uint(x);
+  const unsigned e = (u >> 23) & 0xFFu;
+  if (e == 0u || e == 255u) {
+    if ((u << 1) == 0u) return __hiloint2double((int)(u & 0x80000000u), 0);
+    return (double)x;
+  }
+  return __hiloint2double((int)((u & 0x80000000u) | ((e + 896u) << 20) | ((u & 0x7FFFFFu) >> 3)),
+                          (int)(u << 29));
+}
+// double -> R and R -> double (identities in the FP64 form)
+template <typename R> __device__ __forceinline__ R cvt(double x);
+template <> __device__ __forceinline__ double cvt<double>(double x) { return x; }
+template <> __device__ __forceinline__ float cvt<float>(double x) { return d2f_rn(x); }
+__device__ __forceinline__ double dbl(double x) { return x; }
+__device__ __forceinline__ double dbl(float x) { return f2d(x); }
+
+template <typename R> __device__ __forceinline__ R rel(double x) {
+  if constexpr (kF32<R>) return d2f_rn(x - sh16(x, 0));
+  else return x;
+}
+// The same conversions on the hardware path, for kernels whose instruction issue (not
+// the FP64 pipe) limits them.
+template <typename R> __device__ __forceinline__ R cvt_hw(double x) { return (R)x; }
+__device__ __forceinline__ double dbl_hw(double x) { return x; }
+__device__ __forceinline__ double dbl_hw(float x) { return (double)x; }
+template <typename R> __device__ __forceinline__ R rel_hw(double x) {
+  if constexpr (kF32<R>) return (R)(x - sh16(x, 0));
+  else return x;
+}
 
 // Brackets one launch for the per-kernel timing hooks.
 struct KScope {

@@ -48,14 +48,14 @@ __global__ void __launch_bounds__(LG * 16) k_caar(CaarArgs<R> a) {
 #pragma unroll 1
   for (int k = 0; k < NL; ++k) {
     const int l = lg + LG * k;
-    const R u = (R)a.v[vN0 + l * 32 + p], w = (R)a.v[vN0 + l * 32 + 16 + p];
+    const R u = cvt_hw<R>(a.v[vN0 + l * 32 + p]), w = cvt_hw<R>(a.v[vN0 + l * 32 + 16 + p]);
     const double td = a.T[sN0 + l * 16 + p], dd = a.dp[sN0 + l * 16 + p];
-    const R d = (R)dd;
+    const R d = cvt_hw<R>(dd);
     const R vd0 = u * d, vd1 = w * d;
     if (a.eta_ave_w != 0.0) {  // stages 2-4 accumulate nothing (eta_ave_w = 0)
       const size_t iv = ((size_t)e * NLEV + l) * 32 + p;
-      a.vn0[iv] += (double)(eta * vd0);
-      a.vn0[iv + 16] += (double)(eta * vd1);
+      a.vn0[iv] += dbl_hw(eta * vd0);
+      a.vn0[iv + 16] += dbl_hw(eta * vd1);
     }
     const R div = divergence_sphere(t, m, vd0, vd1);
     double tv = td;
@@ -67,7 +67,7 @@ __global__ void __launch_bounds__(LG * 16) k_caar(CaarArgs<R> a) {
     }
     s_dp[l * SROW + p] = dd;
     s_tv[l * SROW + p] = tv;
-    s_div[l * SROW + p] = (double)div;
+    s_div[l * SROW + p] = dbl_hw(div);
   }
   __syncthreads();
   // ---- phase B: pressure, geopotential, omega integral (double) ----
@@ -100,7 +100,7 @@ __global__ void __launch_bounds__(LG * 16) k_caar(CaarArgs<R> a) {
 #pragma unroll
     for (int k = 0; k < 9; ++k) rt += r[k];
     double integ = seg_excl_suffix(rt, seg);
-    const double phis = (double)a.m.phis[(size_t)e * 16 + col];
+    const double phis = dbl_hw(a.m.phis[(size_t)e * 16 + col]);
     double* phig = a.phi + (size_t)e * NLEV * 16;
 #pragma unroll
     for (int k = 8; k >= 0; --k) {
@@ -134,15 +134,15 @@ __global__ void __launch_bounds__(LG * 16) k_caar(CaarArgs<R> a) {
   for (int k = 0; k < NL; ++k) {
     const int l = lg + LG * k;
     const double pd = s_p[l * SROW + p];
-    const R rp = (R)s_rp[l * SROW + p];
+    const R rp = cvt_hw<R>(s_rp[l * SROW + p]);
     R gp0, gp1;
-    gradient_sphere(t, m, rel<R>(pd), gp0, gp1);
-    const R u = (R)a.v[vN0 + l * 32 + p], w = (R)a.v[vN0 + l * 32 + 16 + p];
+    gradient_sphere(t, m, rel_hw<R>(pd), gp0, gp1);
+    const R u = cvt_hw<R>(a.v[vN0 + l * 32 + p]), w = cvt_hw<R>(a.v[vN0 + l * 32 + 16 + p]);
     const double td = a.T[sN0 + l * 16 + p];
-    const R div = (R)s_div[l * SROW + p];
+    const R div = cvt_hw<R>(s_div[l * SROW + p]);
     const R vgp = u * gp0 + w * gp1;
-    const R omega = (vgp - ((R)s_om[l * SROW + p] + R(0.5) * div)) * rp;
-    if (a.eta_ave_w != 0.0) a.omega_p[((size_t)e * NLEV + l) * 16 + p] += (double)(eta * omega);
+    const R omega = (vgp - (cvt_hw<R>(s_om[l * SROW + p]) + R(0.5) * div)) * rp;
+    if (a.eta_ave_w != 0.0) a.omega_p[((size_t)e * NLEV + l) * 16 + p] += dbl_hw(eta * omega);
     // time level "nm1" (RK combine of stage 5 fused here), in double
     double tm = a.T[sM + l * 16 + p], dm = a.dp[sM + l * 16 + p];
     double vm0 = a.v[vM + l * 32 + p], vm1 = a.v[vM + l * 32 + 16 + p];
@@ -158,15 +158,15 @@ __global__ void __launch_bounds__(LG * 16) k_caar(CaarArgs<R> a) {
     }
     // temperature (compute_temperature_np1)
     R gt0, gt1;
-    gradient_sphere(t, m, rel<R>(td), gt0, gt1);
-    const R tv = (R)s_tv[l * SROW + p];
+    gradient_sphere(t, m, rel_hw<R>(td), gt0, gt1);
+    const R tv = cvt_hw<R>(s_tv[l * SROW + p]);
     const R vgt = u * gt0 + w * gt1;
     const R ttens = -vgt + R(kKappa) * tv * omega;
-    const double tnew = spd * ((double)(ttens * dt) + tm);
+    const double tnew = spd * (dbl_hw(ttens * dt) + tm);
     // velocity (compute_velocity_np1 with compute_energy_grad)
     const R rr = R(kRgas) * (tv * rp);
     R eg0 = rr * gp0, eg1 = rr * gp1;
-    const R ephi = R(0.5) * (u * u + w * w) + rel<R>(s_dp[l * SROW + p]);
+    const R ephi = R(0.5) * (u * u + w * w) + rel_hw<R>(s_dp[l * SROW + p]);
     R ge0, ge1;
     gradient_sphere(t, m, ephi, ge0, ge1);
     eg0 += ge0;
@@ -174,10 +174,10 @@ __global__ void __launch_bounds__(LG * 16) k_caar(CaarArgs<R> a) {
     const R vort = vorticity_sphere(t, m, u, w) + fcor;
     eg0 = -eg0 + w * vort;
     eg1 = -eg1 - u * vort;
-    const double vn0_ = spd * ((double)(eg0 * dt) + vm0);
-    const double vn1_ = spd * ((double)(eg1 * dt) + vm1);
+    const double vn0_ = spd * (dbl_hw(eg0 * dt) + vm0);
+    const double vn1_ = spd * (dbl_hw(eg1 * dt) + vm1);
     // dp3d (compute_dp3d_np1, eta_dot_dpdn = 0 for rsplit > 0)
-    const double dnew = spd * (dm - (double)(div * dt));
+    const double dnew = spd * (dm - dbl_hw(div * dt));
     out[l * 64 + p] = vn0_;
     out[l * 64 + 16 + p] = vn1_;
     out[l * 64 + 32 + p] = tnew;
@@ -224,14 +224,14 @@ __global__ void __launch_bounds__(LG * 16) k_hv_lap1(HvArgs<R> a) {
 #pragma unroll 1
   for (int k = 0; k < NL; ++k) {
     const int l = lg + LG * k;
-    const R lt = laplace_simple(t, m, rel<R>(a.T[sb + l * 16 + p]));
-    const R ld = laplace_simple(t, m, rel<R>(a.dp[sb + l * 16 + p]));
+    const R lt = laplace_simple(t, m, rel_hw<R>(a.T[sb + l * 16 + p]));
+    const R ld = laplace_simple(t, m, rel_hw<R>(a.dp[sb + l * 16 + p]));
     R l0, l1;
-    vlaplace_contra(t, m, nr, (R)a.v[vb + l * 32 + p], (R)a.v[vb + l * 32 + 16 + p], l0, l1);
-    out[l * 64 + p] = (double)l0;
-    out[l * 64 + 16 + p] = (double)l1;
-    out[l * 64 + 32 + p] = (double)lt;
-    out[l * 64 + 48 + p] = (double)ld;
+    vlaplace_contra(t, m, nr, cvt_hw<R>(a.v[vb + l * 32 + p]), cvt_hw<R>(a.v[vb + l * 32 + 16 + p]), l0, l1);
+    out[l * 64 + p] = dbl_hw(l0);
+    out[l * 64 + 16 + p] = dbl_hw(l1);
+    out[l * 64 + 32 + p] = dbl_hw(lt);
+    out[l * 64 + 48 + p] = dbl_hw(ld);
   }
 }
 
@@ -262,10 +262,10 @@ __global__ void __launch_bounds__(LG * 16) k_hv_lap2(HvArgs<R> a) {
 #pragma unroll 1
   for (int k = 0; k < NL; ++k) {
     const int l = lg + LG * k;
-    const R v0 = (R)(dss_gather(a.bufA, NLEV * 64, 64, e, l, p, a.dss) * rs);
-    const R v1 = (R)(dss_gather(a.bufA + 16, NLEV * 64, 64, e, l, p, a.dss) * rs);
-    const R t1 = (R)(dss_gather(a.bufA + 32, NLEV * 64, 64, e, l, p, a.dss) * rs);
-    const R d1 = (R)(dss_gather(a.bufA + 48, NLEV * 64, 64, e, l, p, a.dss) * rs);
+    const R v0 = cvt<R>(dss_gather(a.bufA, NLEV * 64, 64, e, l, p, a.dss) * rs);
+    const R v1 = cvt<R>(dss_gather(a.bufA + 16, NLEV * 64, 64, e, l, p, a.dss) * rs);
+    const R t1 = cvt<R>(dss_gather(a.bufA + 32, NLEV * 64, 64, e, l, p, a.dss) * rs);
+    const R d1 = cvt<R>(dss_gather(a.bufA + 48, NLEV * 64, 64, e, l, p, a.dss) * rs);
     R lt, ld, l0, l1;
     if (a.consthv) {
       lt = laplace_simple(t, m, t1);
@@ -279,12 +279,12 @@ __global__ void __launch_bounds__(LG * 16) k_hv_lap2(HvArgs<R> a) {
     const size_t i3 = ((size_t)e * NLEV + l) * 16 + p;
     const double dpn = a.dp[sb + l * 16 + p];
     a.dpdiss_ave[i3] += wh * dpn;
-    a.dpdiss_bih[i3] += (double)(whr * ld);
+    a.dpdiss_bih[i3] += dbl(whr * ld);
     R vt0 = l0 * R(-a.nu), vt1 = l1 * R(-a.nu);
     R ttn = lt * R(-a.nu_s), dpt = ld * R(-a.nu_p);
     if (a.nu_top > 0 && __any_sync(FULL, l < 3)) {
       // nu_top sponge on the top three levels, applied to the np1 state
-      const R un = (R)a.v[vb + l * 32 + p], wn = (R)a.v[vb + l * 32 + 16 + p];
+      const R un = cvt<R>(a.v[vb + l * 32 + p]), wn = cvt<R>(a.v[vb + l * 32 + 16 + p]);
       R lv0, lv1;
       vlaplace_contra(t, m, R(1), un, wn, lv0, lv1);
       const R ltt = laplace_simple(t, m, rel<R>(a.T[sb + l * 16 + p]));
@@ -297,10 +297,10 @@ __global__ void __launch_bounds__(LG * 16) k_hv_lap2(HvArgs<R> a) {
         dpt += sc * ldd;
       }
     }
-    out[l * 64 + p] = (double)vt0;
-    out[l * 64 + 16 + p] = (double)vt1;
-    out[l * 64 + 32 + p] = (double)ttn;
-    out[l * 64 + 48 + p] = (double)(dpt * dt) + dpn * spd;
+    out[l * 64 + p] = dbl(vt0);
+    out[l * 64 + 16 + p] = dbl(vt1);
+    out[l * 64 + 32 + p] = dbl(ttn);
+    out[l * 64 + 48 + p] = dbl(dpt * dt) + dpn * spd;
   }
 }
 
@@ -311,23 +311,23 @@ __global__ void k_hv_update(HvArgs<R> a, int E) {
   if (idx >= E * NLEV * 16) return;
   const int e = idx / (NLEV * 16), l = (idx / 16) % NLEV, p = idx & 15;
   const double rsd = a.m.rspheremp_d[e * 16 + p];
-  const R rs = (R)rsd;
+  const R rs = cvt<R>(rsd);
   const R dt = R(a.dt);
-  R vt0 = (R)dss_gather(a.bufB, NLEV * 64, 64, e, l, p, a.dss);
-  R vt1 = (R)dss_gather(a.bufB + 16, NLEV * 64, 64, e, l, p, a.dss);
-  R tt = (R)dss_gather(a.bufB + 32, NLEV * 64, 64, e, l, p, a.dss);
+  R vt0 = cvt<R>(dss_gather(a.bufB, NLEV * 64, 64, e, l, p, a.dss));
+  R vt1 = cvt<R>(dss_gather(a.bufB + 16, NLEV * 64, 64, e, l, p, a.dss));
+  R tt = cvt<R>(dss_gather(a.bufB + 32, NLEV * 64, 64, e, l, p, a.dss));
   const double dpt = dss_gather(a.bufB + 48, NLEV * 64, 64, e, l, p, a.dss);
   const size_t vb = (((size_t)e * NTL + a.np1) * NLEV + l) * 32 + p;
   const size_t sb = (((size_t)e * NTL + a.np1) * NLEV + l) * 16 + p;
   vt0 = dt * vt0 * rs;
   vt1 = dt * vt1 * rs;
-  const double v0 = a.v[vb] + (double)vt0, v1 = a.v[vb + 16] + (double)vt1;
+  const double v0 = a.v[vb] + dbl(vt0), v1 = a.v[vb + 16] + dbl(vt1);
   a.v[vb] = v0;
   a.v[vb + 16] = v1;
   tt = dt * tt * rs;
-  const R heating = vt0 * (R)v0 + vt1 * (R)v1;
+  const R heating = vt0 * cvt<R>(v0) + vt1 * cvt<R>(v1);
   constexpr R rcp = R(1.0 / kCp);
-  if constexpr (kF32<R>) a.T[sb] = a.T[sb] + (double)(tt - heating * rcp);
+  if constexpr (kF32<R>) a.T[sb] = a.T[sb] + dbl(tt - heating * rcp);
   else a.T[sb] = a.T[sb] + tt - heating * rcp;
   a.dp[sb] = dpt * rsd;
 }
@@ -400,10 +400,10 @@ __global__ void __launch_bounds__(LG * 16) k_precompute_divdp(EulerArgs<R> a) {
   for (int k = 0; k < NL; ++k) {
     const int l = lg + LG * k;
     const size_t iv = ((size_t)e * NLEV + l) * 32 + p;
-    const R d = divergence_sphere(t, m, (R)a.vn0[iv], (R)a.vn0[iv + 16]);
+    const R d = divergence_sphere(t, m, cvt<R>(a.vn0[iv]), cvt<R>(a.vn0[iv + 16]));
     const size_t i3 = ((size_t)e * NLEV + l) * 16 + p;
-    a.divdp[i3] = (double)d;
-    a.divdp_proj[i3] = (double)d;
+    a.divdp[i3] = dbl(d);
+    a.divdp_proj[i3] = dbl(d);
   }
 }
 
@@ -422,7 +422,7 @@ __global__ void __launch_bounds__(LG * 16) k_qminmax(EulerArgs<R> a, double* qli
 #pragma unroll
   for (int k = 0; k < NL; ++k) {
     const size_t i3 = ((size_t)e * NLEV + lg + LG * k) * 16 + p;
-    rdp[k] = R(1) / ((R)a.derived_dp[i3] - rhsdt * (R)a.divdp_proj[i3]);
+    rdp[k] = R(1) / (cvt<R>(a.derived_dp[i3]) - rhsdt * cvt<R>(a.divdp_proj[i3]));
   }
 #pragma unroll 1
   for (int q = 0; q < a.Q; ++q) {
@@ -433,8 +433,8 @@ __global__ void __launch_bounds__(LG * 16) k_qminmax(EulerArgs<R> a, double* qli
 #pragma unroll
     for (int k = 0; k < NL; ++k) {
       const int l = lg + LG * k;
-      const R val = (R)qsrc[l * 16 + p] * rdp[k];
-      if (store_q) qt[l * 16 + p] = (double)val;
+      const R val = cvt<R>(qsrc[l * 16 + p]) * rdp[k];
+      if (store_q) qt[l * 16 + p] = dbl(val);
       double dmn, dmx;
       if constexpr (kF32<R>) {
         R mn = val, mx = val;
@@ -443,8 +443,8 @@ __global__ void __launch_bounds__(LG * 16) k_qminmax(EulerArgs<R> a, double* qli
           mn = fminf(mn, __shfl_xor_sync(FULL, mn, off, 16));
           mx = fmaxf(mx, __shfl_xor_sync(FULL, mx, off, 16));
         }
-        dmn = (double)mn;
-        dmx = (double)mx;
+        dmn = dbl(mn);
+        dmx = dbl(mx);
       } else {  // exact min/max on the integer pipe
         long long mn = dkey(val), mx = mn;
 #pragma unroll
@@ -499,9 +499,9 @@ __global__ void __launch_bounds__(LG * 16) k_bih_pre(EulerArgs<R> a) {
 #pragma unroll 1
   for (int k = 0; k < NL; ++k) {
     const int l = lg + LG * k;
-    R s = (R)a.qtens[qb + l * 16 + p];
-    if (a.nu_p > 0) s = s * (R)a.dpdiss_ave[((size_t)e * NLEV + l) * 16 + p] * R(c_rdp0[l]);
-    a.qscr[qb + l * 16 + p] = (double)laplace_simple(t, m, s);
+    R s = cvt<R>(a.qtens[qb + l * 16 + p]);
+    if (a.nu_p > 0) s = s * cvt<R>(a.dpdiss_ave[((size_t)e * NLEV + l) * 16 + p]) * cvt<R>(c_rdp0[l]);
+    a.qscr[qb + l * 16 + p] = dbl(laplace_simple(t, m, s));
   }
 }
 
@@ -528,9 +528,9 @@ __global__ void __launch_bounds__(LG * 16) k_bih_post(EulerArgs<R> a) {
 #pragma unroll 1
   for (int k = 0; k < NL; ++k) {
     const int l = lg + LG * k;
-    const R s = (R)(dss_gather(fbase, (long long)a.Q * NLEV * 16, 16, e, l, p, a.dss) * rs);
+    const R s = cvt<R>(dss_gather(fbase, (long long)a.Q * NLEV * 16, 16, e, l, p, a.dss) * rs);
     const R lap = a.consthv ? laplace_simple(t, m, s) : laplace_tensor(t, m, tv, s);
-    a.qtens[qb + l * 16 + p] = (double)(fac * R(a.dp0[l]) * lap * rsp_local);
+    a.qtens[qb + l * 16 + p] = dbl(fac * cvt<R>(a.dp0[l]) * lap * rsp_local);
   }
 }
 
@@ -541,33 +541,51 @@ __global__ void k_aal_setup(EulerArgs<R> a, int E) {
   if (idx >= E * NLEV * 16) return;
   const int e = idx / (NLEV * 16), l = (idx / 16) % NLEV, p = idx & 15;
   const R rhsdt = R(a.rhs_multiplier * a.dt);
-  const R dpt = (R)a.derived_dp[idx] - rhsdt * (R)a.divdp_proj[idx];
+  const R dpt = cvt<R>(a.derived_dp[idx]) - rhsdt * cvt<R>(a.divdp_proj[idx]);
   const size_t iv = ((size_t)e * NLEV + l) * 32 + p;
   const R rdpt = R(1) / dpt;
-  a.vstar[iv] = (double)((R)a.vn0[iv] * rdpt);
-  a.vstar[iv + 16] = (double)((R)a.vn0[iv + 16] * rdpt);
-  R dk = dpt - R(a.dt) * (R)a.divdp[idx];
+  a.vstar[iv] = dbl(cvt<R>(a.vn0[iv]) * rdpt);
+  a.vstar[iv + 16] = dbl(cvt<R>(a.vn0[iv + 16]) * rdpt);
+  R dk = dpt - R(a.dt) * cvt<R>(a.divdp[idx]);
   if (a.nu_p > 0 && a.rhs_viss != 0.0)
-    dk += R(-a.rhs_viss * a.dt * a.nu_q) * (R)a.dpdiss_bih[idx] / a.m.spheremp[e * 16 + p];
-  a.dpdissk[idx] = (double)dk;
+    dk += R(-a.rhs_viss * a.dt * a.nu_q) * cvt<R>(a.dpdiss_bih[idx]) / a.m.spheremp[e * 16 + p];
+  a.dpdissk[idx] = dbl(dk);
   a.fscr[idx] = a.f_dss[idx] * a.m.spheremp_d[e * 16 + p];
 }
 
-// The quasi-monotone limiters of with_limiter_shell (EulerStepFunctorImpl.hpp:693-884)
-// on one level of 16 points, one thread, sums in point order.
+// Is any point outside [minp, maxp]?  In FP64 on the integer pipe (exact).
 template <typename R>
-__device__ void limiter_level(int option, R* x, const R* c, double& minp_io, double& maxp_io) {
-  R s0 = 0, s1 = 0;
+__device__ __forceinline__ bool any_outside(const R* x, R minp, R maxp) {
+  bool out = false;
+  if constexpr (kF32<R>) {
 #pragma unroll
-  for (int k = 0; k < 16; ++k) {
-    s0 += x[k] * c[k];
-    s1 += c[k];
+    for (int k = 0; k < 16; ++k) out |= (x[k] > maxp) | (x[k] < minp);
+  } else {
+    const long long kmn = dkey(minp), kmx = dkey(maxp);
+#pragma unroll
+    for (int k = 0; k < 16; ++k) {
+      const long long kx = dkey(x[k]);
+      out |= (kx > kmx) | (kx < kmn);
+    }
   }
-  if (s1 <= R(0)) return;
-  R minp = (R)minp_io, maxp = (R)maxp_io;
+  return out;
+}
+
+// The quasi-monotone limiters of with_limiter_shell (EulerStepFunctorImpl.hpp:693-884)
+// on one level of 16 points, one thread, sums in point order; s1 = sum of c.  Returns
+// false when the level needs no limiting (x unchanged); the bounds are relaxed to the
+// level mean first, as in the reference.
+template <typename R>
+__device__ bool limiter_level(int option, R* x, const R* c, R s1, double& minp_io, double& maxp_io) {
+  R s0 = 0;
+#pragma unroll
+  for (int k = 0; k < 16; ++k) s0 += x[k] * c[k];
+  if (s1 <= R(0)) return false;
+  R minp = cvt<R>(minp_io), maxp = cvt<R>(maxp_io);
   if (minp < R(0)) { minp = R(0); minp_io = 0.0; }
-  if (s0 < minp * s1) { minp = s0 / s1; minp_io = (double)minp; }
-  if (s0 > maxp * s1) { maxp = s0 / s1; maxp_io = (double)maxp; }
+  if (s0 < minp * s1) { minp = s0 / s1; minp_io = dbl(minp); }
+  if (s0 > maxp * s1) { maxp = s0 / s1; maxp_io = dbl(maxp); }
+  if (!any_outside(x, minp, maxp)) return false;  // no clipping: addmass = 0
   const R mass = s0;
   if (option == 8) {
     const R tol = R(5e-14);
@@ -607,7 +625,7 @@ __device__ void limiter_level(int option, R* x, const R* c, double& minp_io, dou
       else if (x[k] < minp) { delta = x[k] - minp; x[k] = minp; }
       addmass += delta * c[k];
     }
-    if (addmass == R(0)) return;
+    if (addmass == R(0)) return true;
     R fac = 0;
     if (addmass > R(0)) {
 #pragma unroll
@@ -627,6 +645,7 @@ __device__ void limiter_level(int option, R* x, const R* c, double& minp_io, dou
       }
     }
   }
+  return true;
 }
 
 // AALTracerPhase: qtens = Qdp - dt div(vstar Qdp) [+ qtens_biharmonic], limiter,
@@ -656,10 +675,10 @@ __global__ void __launch_bounds__(LG * 16) k_aal_tracer(EulerArgs<R> a) {
   for (int k = 0; k < NL; ++k) {
     const int l = lg + LG * k;
     const size_t iv = ((size_t)e * NLEV + l) * 32 + p;
-    const R vs0 = (R)a.vstar[iv], vs1 = (R)a.vstar[iv + 16];
+    const R vs0 = cvt<R>(a.vstar[iv]), vs1 = cvt<R>(a.vstar[iv + 16]);
     w0[k] = (m.di00 * vs0 + m.di10 * vs1) * m.md;
     w1[k] = (m.di01 * vs0 + m.di11 * vs1) * m.md;
-    const R dm = (R)a.dpdissk[((size_t)e * NLEV + l) * 16 + p];
+    const R dm = cvt<R>(a.dpdissk[((size_t)e * NLEV + l) * 16 + p]);
     s_dm[l * SROW + p] = dm;
     s_rdm[l * SROW + p] = R(1) / dm;
     s_c[l * SROW + p] = m.sp * dm;
@@ -681,10 +700,10 @@ __global__ void __launch_bounds__(LG * 16) k_aal_tracer(EulerArgs<R> a) {
     for (int k = 0; k < NL; ++k) {
       const int l = lg + LG * k;
       const double qdd = a.qdp[qn0 + l * 16 + p];
-      const R qd = (R)qdd;
+      const R qd = cvt<R>(qdd);
       const R dv = (t.ddx(w0[k] * qd) + t.ddy(w1[k] * qd)) * m.fdiv;
       const double q0 = add_hv ? a.qtens[qb + l * 16 + p] : 0.0;
-      if constexpr (kF32<R>) s_q[l * SROW + p] = qdd + (double)(mdt * dv) + q0;
+      if constexpr (kF32<R>) s_q[l * SROW + p] = qdd + dbl(mdt * dv) + q0;
       else s_q[l * SROW + p] = (qdd + mdt * dv + q0);
     }
     __syncthreads();
@@ -694,15 +713,17 @@ __global__ void __launch_bounds__(LG * 16) k_aal_tracer(EulerArgs<R> a) {
 #pragma unroll
         for (int k = 0; k < 16; ++k) {
           c[k] = s_c[l * SROW + k];
-          x[k] = (R)s_q[l * SROW + k] * s_rdm[l * SROW + k];
+          x[k] = cvt<R>(s_q[l * SROW + k]) * s_rdm[l * SROW + k];
         }
         double* ql = a.qlim + ((size_t)e * a.Q + q) * 2 * NLEV;
         double mn = ql[l], mx = ql[NLEV + l];
-        limiter_level<R>(a.limiter_option, x, c, mn, mx);
+        const bool lim = limiter_level<R>(a.limiter_option, x, c, s_c1[l], mn, mx);
         ql[l] = mn;
         ql[NLEV + l] = mx;
+        if (lim) {
 #pragma unroll
-        for (int k = 0; k < 16; ++k) s_q[l * SROW + k] = (double)(x[k] * s_dm[l * SROW + k]);
+          for (int k = 0; k < 16; ++k) s_q[l * SROW + k] = dbl(x[k] * s_dm[l * SROW + k]);
+        }
       }
     }
     __syncthreads();
@@ -1051,7 +1072,7 @@ __global__ void __launch_bounds__(RT) k_remap(RemapArgs a) {
           const float x2 = z2f[k];
           const float in = (coeff[kk] * (x2 + 0.5f) + coeff[72 + kk] * (x2 * x2 - 0.25f) * 0.5f) +
                            coeff[144 + kk] * (x2 * x2 * x2 + 0.125f) * (1.0f / 3.0f);
-          m2[k3] = k == NLEV - 1 ? mass[NLEV + 1] : mass[kk + 1] + (double)in * D[kk];
+          m2[k3] = k == NLEV - 1 ? mass[NLEV + 1] : mass[kk + 1] + dbl(in) * D[kk];
         } else {
           const double x2 = z2[k], x1 = -0.5;
           const double in = (coef[kk] * (x2 - x1) + coef[72 + kk] * (x2 * x2 - x1 * x1) * 0.5) +
