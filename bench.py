@@ -52,6 +52,28 @@ MEASURED_PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
 FALLBACK_HBM_GBS = 6800.0
 
 
+# DRAM bytes (read + write) per launch and FP64-pipe active fraction measured by ncu at
+# ne16 L72 q10 (1536 elements, profiles/kernels_ne16_fp64_mixed_adjoint.md), per form.
+# Traffic is scaled to the run's size by the element count (levels and tracers fixed).
+NCU_NE16 = {
+    "fp64": {"euler_aal_tracer": (473.8e6, 0.836), "caar_stage": (153.8e6, 0.857),
+             "hv_laplace2": (158.0e6, 0.820), "ppm_remap": (328.0e6, 0.851),
+             "euler_bih_post": (278.0e6, 0.870), "hv_laplace1": (73.6e6, 0.886),
+             "euler_bih_pre": (258.5e6, 0.883), "euler_dss_qdp": (402.1e6, 0.820),
+             "euler_qminmax": (283.8e6, 0.558)},
+    "mixed": {"euler_aal_tracer": (473.9e6, 0.368), "caar_stage": (153.2e6, 0.816),
+              "hv_laplace2": (156.0e6, 0.583), "ppm_remap": (328.8e6, 0.835),
+              "euler_dss_qdp": (402.2e6, 0.820)},
+}
+
+
+def ncu_traffic(form: str, kernel: str, E: int, Q: int):
+    v = NCU_NE16.get(form, {}).get(kernel)
+    if v is None or Q != 10:
+        return None, None
+    return v[0] * E / 1536.0, v[1]
+
+
 def sypd(steps: int, seconds: float) -> float:
     return steps * SIM_SECONDS_PER_STEP / (365.0 * seconds)
 
@@ -447,6 +469,8 @@ def main():
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint leg")
     ap.add_argument("--no-dot-check", action="store_true",
                     help="skip the oracle tangent-linear dot-product check of the adjoint leg")
+    ap.add_argument("--only-adjoint", action="store_true",
+                    help="run the adjoint leg alone and print its JSON (profiling runs)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     NE, QSIZE = args.ne, args.qsize
@@ -491,6 +515,11 @@ def main():
         print(json.dumps(line))
         return
 
+    if args.only_adjoint:
+        if rank == 0:
+            from hommexx_gb300 import build as B
+            print(json.dumps(run_adjoint(B.build(), dot_check=not args.no_dot_check)))
+        return
     out, mesh = run_gpu(args, rank, world)
     if rank != 0:
         return
@@ -506,6 +535,7 @@ def main():
     peak, peak_kind = _peaks()
     top = rows[0]
     achieved = top["gbs"] or 0.0
+    traffic, pipe_frac = ncu_traffic("fp64", top["kernel"], E, QSIZE)
     value = sypd(args.steps, f["t"]) * world
     line = {
         "metric": "ne30L72 SYPD (FP64 preqx step)", "value": value, "unit": "SYPD",
@@ -518,8 +548,12 @@ def main():
         "gpu_launches": f["launches"],
         "clocks": f["clocks"],
         "roofline": {"bound": "hbm", "kernel": top["kernel"], "achieved": achieved, "peak": peak,
-                     "unit": "GB/s", "frac": achieved / peak, "traffic": None,
-                     "peak_source": peak_kind},
+                     "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
+                     "peak_source": peak_kind,
+                     "traffic_source": "ncu DRAM bytes per launch at ne16, scaled by elements",
+                     "fp64_pipe_active_ncu": pipe_frac,
+                     "note": "the FP64-form kernels are bound by the GB300 FP64 pipe "
+                             "(2 thread-instructions/SM/cycle), not by HBM"},
         "kernels": [{k: (round(v, 4) if isinstance(v, float) else v) for k, v in r.items()} for r in rows],
     }
     if "mixed" in out:
