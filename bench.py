@@ -270,6 +270,65 @@ def run_gpu(args, rank, world):
 
 
 ADJ_NE, ADJ_STEPS, ADJ_QSIZE = 16, 24, 4
+LARGE_NE, LARGE_Q, LARGE_DT, LARGE_NU, LARGE_STEPS = 120, 40, 75.0, 1e13, 12
+TRACER_KERNELS = ("precompute_divdp", "euler_qminmax", "euler_bih_pre", "euler_bih_post",
+                  "euler_minmax_nbr", "euler_aal_setup", "euler_aal_tracer", "euler_dss_qdp",
+                  "euler_dss_fvar")
+
+
+def run_large(lib_path):
+    """Large-mesh leg: ne120 L72 q40, dt 75 s, nu 1e13, 12 steps (4 remap intervals) in
+    the mixed form against the FP64 form at the same size; SYPD of both, tracer-advection
+    GB/s (field-pass bytes of the tracer kernels over their CUDA-event time), the mixed
+    form's error after the 12 steps and the mass drift."""
+    from hommexx_gb300 import abi, mesh as M, state as S
+    t0 = time.perf_counter()
+    mesh = M.build_mesh(LARGE_NE)
+    hv = S.hybrid_coordinate()
+    st = S.initial_state(mesh, LARGE_Q, hv)
+    t_gen = time.perf_counter() - t0
+    E = mesh.nelem
+    nint = LARGE_STEPS // RSPLIT
+    params = abi.SimParams(qsize=LARGE_Q, nu=LARGE_NU, rsplit=RSPLIT, hypervis_subcycle=HSUB,
+                           nu_top=2.5e5, limiter_option=8, remap_alg=1)
+    res, finals = {}, {}
+    for precision, tag in ((0, "fp64"), (1, "mixed")):
+        L = abi.HxLibrary(lib_path)
+        L.init(mesh, hv, params, st, precision=precision, abort_on_error=True)
+        L.lib.hx_enable_timing(1)
+        import ctypes
+        L.lib.hx_timer_start()
+        for _ in range(nint):
+            L.run_subcycle(LARGE_DT)
+        ms = ctypes.c_double(0)
+        L.lib.hx_timer_stop(ctypes.byref(ms))
+        L.lib.hx_enable_timing(0)
+        t = ms.value / 1e3
+        stats = L.kernel_stats()
+        model = kernel_bytes(E, LARGE_Q, 8)
+        tr_ms = sum(r[2] for r in stats if r[0] in TRACER_KERNELS)
+        tr_bytes = sum(model[r[0]][1] / model[r[0]][0] * r[1] for r in stats
+                       if r[0] in TRACER_KERNELS and r[0] in model)
+        n0 = L.tl[1]
+        i_temp = (L.tl[3] - 1) // params.qsplit  # tracer level the last remap wrote
+        q_tl = 1 if i_temp % 2 == 0 else 0
+        finals[tag] = {"T": L.get("T", n0), "dp3d": L.get("dp3d", n0), "v": L.get("v", n0),
+                       "ps_v": L.get("ps_v", n0), "Qdp": L.get("Qdp", q_tl)}
+        res[tag] = {"sypd": nint * RSPLIT * LARGE_DT / (365.0 * t), "ms_per_interval": t / nint * 1e3,
+                    "tracer_advection_gbs": tr_bytes / (tr_ms * 1e-3) / 1e9 if tr_ms else None,
+                    "tracer_share": tr_ms / (sum(r[2] for r in stats) or 1.0)}
+        L.finalize()
+    a, b = finals["mixed"], finals["fp64"]
+    res["mixed_rel_err"] = {k: float(np.max(np.abs(a[k] - b[k])) / np.max(np.abs(b[k])))
+                            for k in ("v", "T", "dp3d", "Qdp", "ps_v")}
+    sm = mesh.spheremp
+    m0 = float(np.sum(st["ps_v"][:, 1] * sm))
+    res["mass_drift"] = {tag: float(np.sum(finals[tag]["ps_v"] * sm) / m0 - 1.0) for tag in finals}
+    res["speedup_mixed_vs_fp64"] = res["mixed"]["sypd"] / res["fp64"]["sypd"]
+    res["workload"] = (f"ne{LARGE_NE} L72 ({E} elements) q{LARGE_Q}, dt {LARGE_DT:.0f} s, hv nu "
+                       f"{LARGE_NU:g} x{HSUB} subcycles, remap every {RSPLIT} steps, "
+                       f"{LARGE_STEPS} steps; input generation {t_gen:.0f} s on the host")
+    return res
 
 
 def _traj_call(fn, ins, outs, *mid):
@@ -471,6 +530,9 @@ def main():
                     help="skip the oracle tangent-linear dot-product check of the adjoint leg")
     ap.add_argument("--only-adjoint", action="store_true",
                     help="run the adjoint leg alone and print its JSON (profiling runs)")
+    ap.add_argument("--large", action="store_true",
+                    help="run the ne120 q40 mixed-vs-FP64 leg alone and print its JSON "
+                         "(needs ~200 GB of device and ~150 GB of host memory)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     NE, QSIZE = args.ne, args.qsize
@@ -515,6 +577,11 @@ def main():
         print(json.dumps(line))
         return
 
+    if args.large:
+        if rank == 0:
+            from hommexx_gb300 import build as B
+            print(json.dumps(run_large(B.build())))
+        return
     if args.only_adjoint:
         if rank == 0:
             from hommexx_gb300 import build as B

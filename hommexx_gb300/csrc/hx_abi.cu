@@ -263,7 +263,7 @@ struct BackendT : Backend {
     qtens = dalloc<double>(n3 * Q); qscr = dalloc<double>(n3 * Q);
     qlim = dalloc<double>((size_t)E * Q * 2 * NLEV); qlim_tmp = dalloc<double>((size_t)E * Q * 2 * NLEV);
     dp0 = dalloc<double>(NLEV);
-    gen_scr = dalloc<double>(n3 * (Q > 2 ? Q : 2));
+    gen_scr = dalloc<double>(n3 * 2);  // generic DSS of v / T / dp3d / omega_p (Qdp uses qscr)
     invalid = dalloc<int>(1);
     ck(cudaMallocHost(&h_invalid, sizeof(int)), "cudaMallocHost");
     wk = Work{v, T, dp, phi, dpdiss_ave, dpdiss_bih, ps_v};

@@ -80,12 +80,18 @@ def _sph_basis(lat: np.ndarray, lon: np.ndarray, lmax: int = LMAX) -> np.ndarray
     return np.array(rows)
 
 
-def _smooth_fields(basis: np.ndarray, nfields: int, seed: int) -> np.ndarray:
-    rng = np.random.default_rng(seed)
-    coef = rng.standard_normal((nfields, basis.shape[0]))
+def _smooth_coefficients(basis: np.ndarray, nfields: int, seed: int) -> np.ndarray:
+    return np.random.default_rng(seed).standard_normal((nfields, basis.shape[0]))
+
+
+def _smooth_rows(coef: np.ndarray, basis: np.ndarray) -> np.ndarray:
     f = coef @ basis
     f /= np.max(np.abs(f), axis=1, keepdims=True)
     return f
+
+
+def _smooth_fields(basis: np.ndarray, nfields: int, seed: int) -> np.ndarray:
+    return _smooth_rows(_smooth_coefficients(basis, nfields, seed), basis)
 
 
 def dynamics_direction(mesh, seed: int, hv: HVCoord | None = None, lmax: int = LMAX):
@@ -121,18 +127,18 @@ def initial_state(mesh, qsize: int, hv: HVCoord | None = None):
     s_t = _smooth_fields(basis, NLEV, 1004).reshape(NLEV, *shp).transpose(1, 0, 2, 3)
     T = 300.0 - 60.0 * (1.0 - pmid / hv.ps0) + 2.0 * s_t
     vel = np.stack([20.0 * s_u, 20.0 * s_v], axis=2)          # (E,72,2,4,4)
-    q = None
-    if qsize > 0:
-        s_q = _smooth_fields(basis, qsize * NLEV, 1005).reshape(qsize, NLEV, *shp)
-        q = 0.005 * (1.0 + s_q.transpose(2, 0, 1, 3, 4))       # (E,Q,72,4,4)
     ntl = 3
     v_all = np.ascontiguousarray(np.broadcast_to(vel[:, None], (E, ntl) + vel.shape[1:]))
     t_all = np.ascontiguousarray(np.broadcast_to(T[:, None], (E, ntl) + T.shape[1:]))
     dp_all = np.ascontiguousarray(np.broadcast_to(dp[:, None], (E, ntl) + dp.shape[1:]))
     ps_all = np.ascontiguousarray(np.broadcast_to(ps[:, None], (E, ntl, 4, 4)))
+    # tracers one at a time straight into both tracer time levels (large meshes)
+    qdp_all = np.empty((E, 2, qsize, NLEV, 4, 4))
     if qsize > 0:
-        qdp = q * dp[:, None]
-        qdp_all = np.ascontiguousarray(np.broadcast_to(qdp[:, None], (E, 2) + qdp.shape[1:]))
-    else:
-        qdp_all = np.zeros((E, 2, 0, NLEV, 4, 4))
+        coef = _smooth_coefficients(basis, qsize * NLEV, 1005)
+        for i in range(qsize):
+            s_q = _smooth_rows(coef[i * NLEV:(i + 1) * NLEV], basis).reshape(NLEV, *shp)
+            qdp = 0.005 * (1.0 + s_q.transpose(1, 0, 2, 3)) * dp   # (E,72,4,4)
+            qdp_all[:, 0, i] = qdp
+            qdp_all[:, 1, i] = qdp
     return dict(v=v_all, T=t_all, dp3d=dp_all, Qdp=qdp_all, ps_v=ps_all)
