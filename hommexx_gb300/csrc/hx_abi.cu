@@ -220,6 +220,7 @@ struct BackendT : Backend {
   double *caar_out = 0, *bufA = 0, *bufB = 0, *vstar = 0, *dpdissk = 0, *fscr = 0, *qtens = 0, *qscr = 0;
   double *qlim = 0, *qlim_tmp = 0, *dp0 = 0, *staging = 0, *rsp_d = 0, *rsp_noalloc = 0;
   double* gen_scr = 0;
+  double* lapm = 0;  // FP64 form: dense weak Laplacian per element
   int *tab_cnt = 0, *tab_src = 0, *nbr = 0, *invalid = 0;
   int* h_invalid = nullptr;
   size_t staging_n = 0;
@@ -233,7 +234,7 @@ struct BackendT : Backend {
     void* ptrs[] = {D, Dinv, metinv, metdet, spheremp, rspheremp, mp, fcor, phis, tensorvisc, vec_sph2cart,
                     v, T, dp, ps_v, qdp, Qc, phi, omega_p, eta, derived_dp, divdp, divdp_proj, dpdiss_ave,
                     dpdiss_bih, vn0, caar_out, bufA, bufB, vstar, dpdissk, fscr, qtens, qscr, qlim, qlim_tmp,
-                    dp0, staging, rsp_d, rsp_noalloc, gen_scr, tab_cnt, tab_src, nbr, invalid, sp_d};
+                    dp0, staging, rsp_d, rsp_noalloc, gen_scr, tab_cnt, tab_src, nbr, invalid, sp_d, lapm};
     for (void* p : ptrs)
       if (p) cudaFree(p);
     if (h_invalid) cudaFreeHost(h_invalid);
@@ -331,7 +332,7 @@ struct BackendT : Backend {
     m.D = D; m.Dinv = Dinv; m.metinv = metinv; m.metdet = metdet; m.spheremp = spheremp;
     m.rspheremp = rspheremp; m.mp = mp; m.fcor = fcor; m.phis = phis;
     m.tensorvisc = tensorvisc; m.vec_sph2cart = vec_sph2cart;
-    m.spheremp_d = sp_d; m.rspheremp_d = rsp_d;
+    m.spheremp_d = sp_d; m.rspheremp_d = rsp_d; m.lapm = lapm;
     return m;
   }
   DssTable table() const { return DssTable{tab_cnt, tab_src}; }
@@ -340,6 +341,17 @@ struct BackendT : Backend {
     *sr = tab_src;
     *r = rsp_noalloc;
     return tab_cnt != nullptr && rsp_noalloc != nullptr;
+  }
+
+  // Operators built from the metric and the derivative matrix, once both are on the
+  // device (the constants are uploaded by init_boundary_exchanges_c).
+  void build_operators() {
+    if constexpr (std::is_same<R, double>::value) {
+      if (!lapm) lapm = dalloc<double>((size_t)E * 256);
+      launch_lap_matrix(metric(), E, lapm, g_stream);
+      post("lap_matrix");
+      ck(cudaStreamSynchronize(g_stream), "lap_matrix");
+    }
   }
 
   void set_tables(const std::vector<int>& cnt, const std::vector<int>& src, const std::vector<int>& nb) {
@@ -1011,8 +1023,13 @@ void init_boundary_exchanges_c(void) {
     std::vector<int> cnt, src, nb;
     build_tables(s.conn, s.E, cnt, src, nb);
     upload_constants(s.dvv, s.hyai, s.hybi, s.ps0, g_stream);
-    if (s.precision == 0) static_cast<BackendT<double>&>(B()).set_tables(cnt, src, nb);
-    else static_cast<BackendT<float>&>(B()).set_tables(cnt, src, nb);
+    if (s.precision == 0) {
+      auto& b = static_cast<BackendT<double>&>(B());
+      b.set_tables(cnt, src, nb);
+      b.build_operators();
+    } else {
+      static_cast<BackendT<float>&>(B()).set_tables(cnt, src, nb);
+    }
   });
 }
 

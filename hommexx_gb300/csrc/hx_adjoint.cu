@@ -7,7 +7,8 @@
 // parabolas) and then propagates the cotangents backwards through them:
 //   * transposed sphere operators are the forward half-warp contractions with the
 //     roles swapped (d/dx <-> weak row contraction, d/dy <-> weak column contraction);
-//     the weak Laplacian is symmetric and is its own transpose;
+//     the weak Laplacian applies the transposed element matrix (FP64 form) or the
+//     contraction form, which is symmetric (mixed form);
 //   * the DSS with rspheremp, R S with S the symmetric gather-sum, is transposed as
 //     S R: a gather of rspheremp-weighted cotangents, fused into the consumer's load;
 //   * the vertical scans reverse into scans in the opposite direction (segmented
@@ -351,6 +352,8 @@ __global__ void __launch_bounds__(LG * 16) k_hvb_second(HvVjpArgs<R> a) {
   double* bd = a.xb.dp + (size_t)e * a.xb.es;
   double* mo = a.mid + (size_t)e * NLEV * 64;
   const R r2 = R(a.nu_ratio2);
+  LapOp<R> lap;
+  lap.load(a.m, e, p, true);
 #pragma unroll 1
   for (int k = 0; k < NL; ++k) {
     const int l = lg + LG * k;
@@ -362,8 +365,8 @@ __global__ void __launch_bounds__(LG * 16) k_hvb_second(HvVjpArgs<R> a) {
     const double xdt = gd * a.dt;
     R m0, m1;
     vlaplace_contra_T(t, m, r2, (R)(-a.nu * g0), (R)(-a.nu * g1), m0, m1);
-    const R mT = laplace_simple(t, m, (R)(-a.nu_s * gT));
-    const R md = laplace_simple(t, m, (R)(-a.nu_p * xdt));
+    const R mT = lap(t, m, (R)(-a.nu_s * gT));
+    const R md = lap(t, m, (R)(-a.nu_p * xdt));
     mo[l * 64 + p] = (double)m0;
     mo[l * 64 + 16 + p] = (double)m1;
     mo[l * 64 + 32 + p] = (double)mT;
@@ -373,8 +376,8 @@ __global__ void __launch_bounds__(LG * 16) k_hvb_second(HvVjpArgs<R> a) {
       const double sc = l == 0 ? 4.0 * a.nu_top : l == 1 ? 2.0 * a.nu_top : l == 2 ? a.nu_top : 0.0;
       R s0, s1;
       vlaplace_contra_T(t, m, R(1), (R)(sc * g0), (R)(sc * g1), s0, s1);
-      const R sT = laplace_simple(t, m, (R)(sc * gT));
-      const R sd = laplace_simple(t, m, (R)(sc * xdt));
+      const R sT = lap(t, m, (R)(sc * gT));
+      const R sd = lap(t, m, (R)(sc * xdt));
       if (l < 3) {
         bv[l * 32 + p] += (double)s0;
         bv[l * 32 + 16 + p] += (double)s1;
@@ -399,6 +402,8 @@ __global__ void __launch_bounds__(LG * 16) k_hvb_first(HvVjpArgs<R> a) {
   double* bT = a.xb.T + (size_t)e * a.xb.es;
   double* bd = a.xb.dp + (size_t)e * a.xb.es;
   const R r1 = R(a.nu_ratio1);
+  LapOp<R> lap;
+  lap.load(a.m, e, p, true);
 #pragma unroll 1
   for (int k = 0; k < NL; ++k) {
     const int l = lg + LG * k;
@@ -408,8 +413,8 @@ __global__ void __launch_bounds__(LG * 16) k_hvb_first(HvVjpArgs<R> a) {
     const double gd = dss_gather_w(a.mid + 48, NLEV * 64, 64, e, l, p, a.dss, rsw);
     R v0, v1;
     vlaplace_contra_T(t, m, r1, (R)g0, (R)g1, v0, v1);
-    const R lT = laplace_simple(t, m, (R)gT);
-    const R ld = laplace_simple(t, m, (R)gd);
+    const R lT = lap(t, m, (R)gT);
+    const R ld = lap(t, m, (R)gd);
     bv[l * 32 + p] += (double)v0;
     bv[l * 32 + 16 + p] += (double)v1;
     bT[l * 16 + p] += (double)lT;

@@ -41,6 +41,7 @@ struct MetricP {
   const R* vec_sph2cart;   // [E][2][3][16] or null
   const double* spheremp_d;   // double copies for the state updates and the DSS
   const double* rspheremp_d;
+  const double* lapm;  // FP64 form: weak Laplacian per element, [E][16 rows][16 cols]
 };
 
 // DSS gather table: for (e, p) the ordered sources src[(e*16+p)*3 + k] = se*16 + sp,

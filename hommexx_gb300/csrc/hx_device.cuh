@@ -160,6 +160,33 @@ __device__ __forceinline__ R laplace_simple(const Pt<R>& t, const PM<R>& m, R s)
   return -(t.wrow(w0) + t.wcol(w1)) * rre<R>();
 }
 
+// The weak Laplacian of the thread's point on one level.  FP64 form: the element's dense
+// 16x16 matrix (laplace_simple applied to the unit vectors once at initialisation), row p
+// in registers, the level's 16 inputs by shuffles: 16 DFMA instead of the contractions'
+// 22 FP64 instructions.  transpose = true loads column p (the adjoint's L^T).  Mixed
+// form: the contractions in FP32.
+template <typename R>
+struct LapOp {
+  double w[kF32<R> ? 1 : 16];
+  __device__ __forceinline__ void load(const MetricP<R>& mp, int e, int p, bool transpose = false) {
+    if constexpr (!kF32<R>) {
+      const double* L = mp.lapm + (size_t)e * 256;
+#pragma unroll
+      for (int q = 0; q < 16; ++q) w[q] = transpose ? L[q * 16 + p] : L[p * 16 + q];
+    }
+  }
+  __device__ __forceinline__ R operator()(const Pt<R>& t, const PM<R>& m, R s) const {
+    if constexpr (kF32<R>) {
+      return laplace_simple(t, m, s);
+    } else {
+      double a = 0.0;
+#pragma unroll
+      for (int q = 0; q < 16; ++q) a = fma(w[q], sh16(s, q), a);
+      return a;
+    }
+  }
+};
+
 template <typename R>
 __device__ __forceinline__ R laplace_tensor(const Pt<R>& t, const PM<R>& m, const R* tv, R s) {
   R g0, g1;
@@ -275,6 +302,28 @@ __device__ __forceinline__ double dkey_value(long long k) {
 }
 __device__ __forceinline__ long long kmin(long long a, long long b) { return b < a ? b : a; }
 __device__ __forceinline__ long long kmax(long long a, long long b) { return b > a ? b : a; }
+
+// Exact sign tests and orderings of T values: FP32 as is, FP64 on the integer pipe.
+template <typename T> __device__ __forceinline__ bool pos(T x) { return x > T(0); }
+template <> __device__ __forceinline__ bool pos<double>(double x) {
+  return __double_as_longlong(x) > 0;  // > +0 (non-NaN)
+}
+template <typename T> __device__ __forceinline__ bool less(T a, T b) { return a < b; }
+template <> __device__ __forceinline__ bool less<double>(double a, double b) {
+  return dkey(a) < dkey(b);  // exact for non-NaN except that -0 < +0
+}
+// min(|a|, |b|, |c|) with the sign of s.
+template <typename T> __device__ __forceinline__ T min3abs_signed(T a, T b, T c, T s) {
+  return fmin(fmin(fabs(a), fabs(b)), fabs(c)) * copysign(T(1), s);
+}
+template <> __device__ __forceinline__ double min3abs_signed<double>(double a, double b, double c,
+                                                                    double s) {
+  const long long m = 0x7fffffffffffffffLL;
+  long long k = __double_as_longlong(a) & m;
+  k = kmin(k, __double_as_longlong(b) & m);
+  k = kmin(k, __double_as_longlong(c) & m);
+  return __longlong_as_double(k | (__double_as_longlong(s) & ~m));
+}
 
 // ---- double <-> float conversions on the integer pipe --------------------------------
 // F2F conversions also issue to the FP64 pipe; the mixed form converts at every load

@@ -221,11 +221,13 @@ __global__ void __launch_bounds__(LG * 16) k_hv_lap1(HvArgs<R> a) {
   const size_t sb = ((size_t)e * NTL + a.np1) * NLEV * 16;
   double* out = a.bufA + (size_t)e * NLEV * 64;
   const R nr = R(a.nu_ratio1);
+  LapOp<R> lap;
+  lap.load(a.m, e, p);
 #pragma unroll 1
   for (int k = 0; k < NL; ++k) {
     const int l = lg + LG * k;
-    const R lt = laplace_simple(t, m, rel_hw<R>(a.T[sb + l * 16 + p]));
-    const R ld = laplace_simple(t, m, rel_hw<R>(a.dp[sb + l * 16 + p]));
+    const R lt = lap(t, m, rel_hw<R>(a.T[sb + l * 16 + p]));
+    const R ld = lap(t, m, rel_hw<R>(a.dp[sb + l * 16 + p]));
     R l0, l1;
     vlaplace_contra(t, m, nr, cvt_hw<R>(a.v[vb + l * 32 + p]), cvt_hw<R>(a.v[vb + l * 32 + 16 + p]), l0, l1);
     out[l * 64 + p] = dbl_hw(l0);
@@ -259,6 +261,8 @@ __global__ void __launch_bounds__(LG * 16) k_hv_lap2(HvArgs<R> a) {
   const double wh = a.eta_ave_w / a.hsub;  // eta_ave_w / hypervis_subcycle
   const R whr = R(wh);
   const R dt = R(a.dt);
+  LapOp<R> lap;
+  lap.load(a.m, e, p);
 #pragma unroll 1
   for (int k = 0; k < NL; ++k) {
     const int l = lg + LG * k;
@@ -268,8 +272,8 @@ __global__ void __launch_bounds__(LG * 16) k_hv_lap2(HvArgs<R> a) {
     const R d1 = cvt<R>(dss_gather(a.bufA + 48, NLEV * 64, 64, e, l, p, a.dss) * rs);
     R lt, ld, l0, l1;
     if (a.consthv) {
-      lt = laplace_simple(t, m, t1);
-      ld = laplace_simple(t, m, d1);
+      lt = lap(t, m, t1);
+      ld = lap(t, m, d1);
       vlaplace_contra(t, m, R(a.nu_ratio2), v0, v1, l0, l1);
     } else {
       lt = laplace_tensor(t, m, tv, t1);
@@ -287,8 +291,8 @@ __global__ void __launch_bounds__(LG * 16) k_hv_lap2(HvArgs<R> a) {
       const R un = cvt<R>(a.v[vb + l * 32 + p]), wn = cvt<R>(a.v[vb + l * 32 + 16 + p]);
       R lv0, lv1;
       vlaplace_contra(t, m, R(1), un, wn, lv0, lv1);
-      const R ltt = laplace_simple(t, m, rel<R>(a.T[sb + l * 16 + p]));
-      const R ldd = laplace_simple(t, m, rel<R>(dpn));
+      const R ltt = lap(t, m, rel<R>(a.T[sb + l * 16 + p]));
+      const R ldd = lap(t, m, rel<R>(dpn));
       if (l < 3) {
         const R sc = R((l == 0 ? 4.0 : l == 1 ? 2.0 : 1.0) * a.nu_top);
         vt0 += sc * lv0;
@@ -496,12 +500,14 @@ __global__ void __launch_bounds__(LG * 16) k_bih_pre(EulerArgs<R> a) {
   PM<R> m;
   m.load(a.m, e, p);
   const size_t qb = ((size_t)e * a.Q + q) * NLEV * 16;
+  LapOp<R> lap;
+  lap.load(a.m, e, p);
 #pragma unroll 1
   for (int k = 0; k < NL; ++k) {
     const int l = lg + LG * k;
     R s = cvt<R>(a.qtens[qb + l * 16 + p]);
     if (a.nu_p > 0) s = s * cvt<R>(a.dpdiss_ave[((size_t)e * NLEV + l) * 16 + p]) * cvt<R>(c_rdp0[l]);
-    a.qscr[qb + l * 16 + p] = dbl(laplace_simple(t, m, s));
+    a.qscr[qb + l * 16 + p] = dbl(lap(t, m, s));
   }
 }
 
@@ -525,11 +531,13 @@ __global__ void __launch_bounds__(LG * 16) k_bih_post(EulerArgs<R> a) {
   const R fac = R(-a.rhs_viss * a.dt * a.nu_q);
   const double rs = a.m.rspheremp_d[(size_t)e * 16 + p];
   const R rsp_local = R(1) / m.sp;
+  LapOp<R> lapo;
+  if (a.consthv) lapo.load(a.m, e, p);
 #pragma unroll 1
   for (int k = 0; k < NL; ++k) {
     const int l = lg + LG * k;
     const R s = cvt<R>(dss_gather(fbase, (long long)a.Q * NLEV * 16, 16, e, l, p, a.dss) * rs);
-    const R lap = a.consthv ? laplace_simple(t, m, s) : laplace_tensor(t, m, tv, s);
+    const R lap = a.consthv ? lapo(t, m, s) : laplace_tensor(t, m, tv, s);
     a.qtens[qb + l * 16 + p] = dbl(fac * cvt<R>(a.dp0[l]) * lap * rsp_local);
   }
 }
@@ -820,9 +828,9 @@ __device__ __forceinline__ void ppm_coefs(int lane, bool own, int l0, int remap_
       if (j < NLEV + 2) {
         const T a0 = A[j], am1 = A[j - 1], am2 = A[j - 2];
         T r = T(0);
-        if ((a0 - am1) * (am1 - am2) > T(0)) {
+        if (pos((a0 - am1) * (am1 - am2))) {
           const T da = g[0 * 74 + j] * (g[1 * 74 + j] * (a0 - am1) + g[2 * 74 + j] * (am1 - am2));
-          r = fmin(fmin(fabs(da), T(2) * fabs(am1 - am2)), T(2) * fabs(a0 - am1)) * copysign(T(1), da);
+          r = min3abs_signed(da, T(2) * (am1 - am2), T(2) * (a0 - am1), da);
         }
         dma[j] = r;
       }
@@ -848,10 +856,10 @@ __device__ __forceinline__ void ppm_coefs(int lane, bool own, int l0, int remap_
       const int jp = l0 + k3;
       T al = ai[jp], ar = ai[jp + 1];
       const T cm = A[jp];
-      if ((ar - cm) * (cm - al) <= T(0)) { al = cm; ar = cm; }
+      if (!pos((ar - cm) * (cm - al))) { al = cm; ar = cm; }
       constexpr T sixth = T(1.0 / 6.0);
-      if ((ar - al) * (cm - (al + ar) * T(0.5)) > (ar - al) * (ar - al) * sixth) al = T(3) * cm - T(2) * ar;
-      if ((ar - al) * (cm - (al + ar) * T(0.5)) < -(ar - al) * (ar - al) * sixth) ar = T(3) * cm - T(2) * al;
+      if (less((ar - al) * (ar - al) * sixth, (ar - al) * (cm - (al + ar) * T(0.5)))) al = T(3) * cm - T(2) * ar;
+      if (less((ar - al) * (cm - (al + ar) * T(0.5)), -(ar - al) * (ar - al) * sixth)) ar = T(3) * cm - T(2) * al;
       T c0 = T(1.5) * cm - (al + ar) / T(4), c1 = ar - al, c2 = T(3) * (T(-2) * cm + (al + ar));
       if (remap_alg == 2 && (jp < 2 || jp >= NLEV - 2)) {  // PpmFixedParabola
         c0 = cm;
@@ -1098,6 +1106,17 @@ __global__ void __launch_bounds__(RT) k_remap(RemapArgs a) {
   }
 }
 
+// Dense weak Laplacian per element: column c is laplace_simple of the unit vector e_c
+// (one half-warp per column), stored as out[e][row p][col c].
+__global__ void __launch_bounds__(256) k_lap_matrix(MetricP<double> mp, double* out) {
+  const int e = blockIdx.x, col = threadIdx.x >> 4, p = threadIdx.x & 15;
+  Pt<double> t;
+  t.init(p);
+  PM<double> m;
+  m.load(mp, e, p);
+  out[((size_t)e * 16 + p) * 16 + col] = laplace_simple(t, m, p == col ? 1.0 : 0.0);
+}
+
 template <typename R> constexpr int LG_CAAR() { return 8; }
 template <typename R> constexpr int LG_HV() { return 8; }
 template <typename R> constexpr int LG_TR() { return 8; }
@@ -1280,6 +1299,11 @@ void launch_dss_inplace(int E, int nf, double* base, long long fs, long long es,
   KScope k("dss_generic", s);
   k_copy_fields<<<dim3(E * nf, NLEV / EQ_LEVELS), EQ_THREADS, 0, s>>>(nf, base, fs, es, ls, scr);
   k_dss_from_copy<<<dim3(E * nf, NLEV / EQ_LEVELS), EQ_THREADS, 0, s>>>(nf, base, fs, es, ls, scr, rsmp, t);
+}
+
+void launch_lap_matrix(const MetricP<double>& m, int E, double* out, cudaStream_t s) {
+  KScope k("lap_matrix", s);
+  k_lap_matrix<<<E, 256, 0, s>>>(m, out);
 }
 
 #define HX_INST(R)                                                                  \

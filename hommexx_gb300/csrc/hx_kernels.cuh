@@ -86,6 +86,8 @@ struct RemapArgs {
   int* invalid;   // set to 1 on a negative or NaN source thickness
 };
 
+// Dense weak Laplacian per element ([E][16][16]) from the FP64 metric.
+void launch_lap_matrix(const MetricP<double>& m, int E, double* out, cudaStream_t s);
 void launch_prim_step_init(int E, double* eta, double* vn0, double* omega_p, double* dpa,
                            double* dpb, double* derived_dp, const double* dp, int n0, int zero_diss,
                            cudaStream_t s);
