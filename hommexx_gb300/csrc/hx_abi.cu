@@ -382,6 +382,7 @@ struct BackendT : Backend {
     a.out = caar_out; a.nm1 = nm1; a.n0 = n0;
     a.dt = dt; a.eta_ave_w = w; a.p_top = s.hyai[0] * s.ps0;
     a.rk_combine = combine; a.n0orig = n0orig;
+    a.rsplit = s.prm.rsplit; a.eta_acc = eta;
     launch_caar<R>(a, E, g_stream);
     post("caar");
     launch_dss_state(E, caar_out, wk.v, wk.T, wk.dp, np1, rsp_d, table(), g_stream);
@@ -454,9 +455,11 @@ struct BackendT : Backend {
     euler_step(s.tl.np1_qdp, s.tl.np1_qdp, dt / 2.0, 2.0, 1, s.tl.n0_qdp);
   }
 
-  // reset = false keeps an invalid-thickness flag raised by an earlier remap.
-  void launch_remap(int np1, int np1_qdp, bool reset = true) {
+  // reset = false keeps an invalid-thickness flag raised by an earlier remap; dt is the
+  // remap interval (used by the vertically Eulerian source thickness).
+  void launch_remap(int np1, int np1_qdp, bool reset = true, double dt = 0.0) {
     RemapArgs a;
+    a.rsplit = s.prm.rsplit; a.eta = eta; a.dt = dt;
     a.v = wk.v; a.T = wk.T; a.dp = wk.dp; a.qdp = qdp; a.ps_v = wk.ps_v;
     a.np1 = np1; a.n0_qdp = np1_qdp; a.Q = wk.v == v ? Q : 0; a.remap_alg = s.prm.remap_alg; a.nelem = E;
     a.ps0 = s.ps0; a.hyai0 = s.hyai[0]; a.invalid = invalid;
@@ -469,8 +472,8 @@ struct BackendT : Backend {
     ck(cudaStreamSynchronize(g_stream), "remap sync");
     return *h_invalid ? 101 : 0;
   }
-  int remap(int np1, int np1_qdp, double) override {
-    launch_remap(np1, np1_qdp);
+  int remap(int np1, int np1_qdp, double dt) override {
+    launch_remap(np1, np1_qdp, true, dt);
     return remap_status();
   }
 
@@ -495,6 +498,7 @@ struct BackendT : Backend {
 
   void run_subcycle(double dt) override {
     const Params& p = s.prm;
+    const double dt_remap = p.rsplit > 0 ? dt * p.qsplit * p.rsplit : dt * p.qsplit;
     s.tl.update_tracers_levels(p.qsplit);
     launch_dp_from_ps(E, dp, ps_v, s.tl.n0, s.ps0, g_stream);
     post("dp3d_from_ps");
@@ -504,7 +508,7 @@ struct BackendT : Backend {
       prim_step(dt);
     }
     s.tl.update_tracers_levels(p.qsplit);
-    launch_remap(s.tl.np1, s.tl.np1_qdp);
+    launch_remap(s.tl.np1, s.tl.np1_qdp, true, dt_remap);
     launch_update_q(E, Q, qdp, Qc, ps_v, s.tl.np1, s.tl.np1_qdp, s.ps0, g_stream);
     post("update_q");
     const int st = remap_status();
@@ -685,6 +689,7 @@ struct BackendT : Backend {
   void traj_forward(const double* hv, const double* hT, const double* hdp, int nsteps, double dt,
                     double* ov, double* oT, double* odp) override {
     if (!s.consthv) fail(12, "trajectory: tensor hyperviscosity (hypervis_scaling != 0) has no adjoint");
+    if (s.prm.rsplit == 0) fail(12, "trajectory: rsplit=0 (vertically Eulerian) has no adjoint");
     if (nsteps < 0 || !(dt > 0)) fail(HX_ERR_STATE, "hx_traj_forward: nsteps must be >= 0 and dt > 0");
     tj.have = false;
     traj_alloc_work();
@@ -952,7 +957,6 @@ void init_simulation_params_c(const int* remap_alg, const int* limiter_option, c
     if (!(*nu > 0)) bad("nu");
     if (!(*nu_div > 0)) bad("nu_div");
     if (*ftype != -1) fail(12, "CAM forcing (ftype 0/2) is not part of this build");
-    if (*rsplit == 0) fail(12, "rsplit=0 (vertically Eulerian step) is not part of this build");
     if (*qsplit < 1 || *hypervis_subcycle < 1 || *qsize < 0) fail(13, "invalid qsplit/hypervis_subcycle/qsize");
     Params& p = S().prm;
     p.remap_alg = *remap_alg; p.limiter_option = *limiter_option; p.rsplit = *rsplit; p.qsplit = *qsplit;

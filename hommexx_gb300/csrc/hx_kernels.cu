@@ -36,6 +36,7 @@ __global__ void __launch_bounds__(LG * 16) k_caar(CaarArgs<R> a) {
   double* s_p = sm + 3 * NLEV * SROW;   // pressure
   double* s_om = sm + 4 * NLEV * SROW;  // sum_{j<k} div_vdp_j
   double* s_rp = sm + 5 * NLEV * SROW;  // 1 / pressure
+  double* s_tot = sm + 6 * NLEV * SROW; // column sum of div(v dp) (rsplit == 0)
   const int e = blockIdx.x, tid = threadIdx.x, p = tid & 15, lg = tid >> 4;
   Pt<R> t;
   t.init(p);
@@ -119,6 +120,7 @@ __global__ void __launch_bounds__(LG * 16) k_caar(CaarArgs<R> a) {
       s_om[(l0 + k) * SROW + col] = acc;
       acc = acc + s_div[(l0 + k) * SROW + col];
     }
+    if (seg == 7) s_tot[col] = acc;
   }
   __syncthreads();
   // ---- phase C: omega_p, T, v, dp3d at np1 ----
@@ -156,12 +158,38 @@ __global__ void __launch_bounds__(LG * 16) k_caar(CaarArgs<R> a) {
       a.v[vM + l * 32 + p] = vm0;
       a.v[vM + l * 32 + 16 + p] = vm1;
     }
+    // vertically Eulerian (rsplit == 0): eta_dot_dpdn on interfaces l and l+1 from the
+    // div(v dp) scan (CaarFunctorImpl.hpp:262-300), vertical advection of T and v from
+    // the neighbouring levels (:496-597), accumulation (:236-248)
+    R tva = R(0), vva0 = R(0), vva1 = R(0), etl = R(0), etu = R(0);
+    if (a.rsplit == 0) {
+      const double tot = s_tot[p];
+      const double el = l == 0 ? 0.0 : c_hybi[l] * tot - s_om[l * SROW + p];
+      const double eu = l + 1 == NLEV ? 0.0 : c_hybi[l + 1] * tot - s_om[(l + 1) * SROW + p];
+      etl = cvt_hw<R>(el);
+      etu = cvt_hw<R>(eu);
+      const R rdp = R(0.5) * (R(1) / cvt_hw<R>(a.dp[sN0 + l * 16 + p]));
+      const R facp = rdp * etu, facm = rdp * etl;
+      const double* Tc = a.T + sN0 + l * 16 + p;
+      const double* vc = a.v + vN0 + l * 32 + p;
+      if (l + 1 < NLEV) {
+        tva += facp * (cvt_hw<R>(Tc[16]) - cvt_hw<R>(Tc[0]));
+        vva0 += facp * (cvt_hw<R>(vc[32]) - u);
+        vva1 += facp * (cvt_hw<R>(vc[48]) - w);
+      }
+      if (l > 0) {
+        tva += facm * (cvt_hw<R>(Tc[0]) - cvt_hw<R>(Tc[-16]));
+        vva0 += facm * (u - cvt_hw<R>(vc[-32]));
+        vva1 += facm * (w - cvt_hw<R>(vc[-16]));
+      }
+      if (a.eta_ave_w != 0.0) a.eta_acc[((size_t)e * NLEV + l) * 16 + p] += a.eta_ave_w * el;
+    }
     // temperature (compute_temperature_np1)
     R gt0, gt1;
     gradient_sphere(t, m, rel_hw<R>(td), gt0, gt1);
     const R tv = cvt_hw<R>(s_tv[l * SROW + p]);
     const R vgt = u * gt0 + w * gt1;
-    const R ttens = -vgt + R(kKappa) * tv * omega;
+    const R ttens = (-tva - vgt) + R(kKappa) * tv * omega;
     const double tnew = spd * (dbl_hw(ttens * dt) + tm);
     // velocity (compute_velocity_np1 with compute_energy_grad)
     const R rr = R(kRgas) * (tv * rp);
@@ -172,12 +200,12 @@ __global__ void __launch_bounds__(LG * 16) k_caar(CaarArgs<R> a) {
     eg0 += ge0;
     eg1 += ge1;
     const R vort = vorticity_sphere(t, m, u, w) + fcor;
-    eg0 = -eg0 + w * vort;
-    eg1 = -eg1 - u * vort;
+    eg0 = -eg0 + (-vva0 + w * vort);
+    eg1 = -eg1 + (-vva1 - u * vort);
     const double vn0_ = spd * (dbl_hw(eg0 * dt) + vm0);
     const double vn1_ = spd * (dbl_hw(eg1 * dt) + vm1);
     // dp3d (compute_dp3d_np1, eta_dot_dpdn = 0 for rsplit > 0)
-    const double dnew = spd * (dm - dbl_hw(div * dt));
+    const double dnew = spd * (dm - dbl_hw(((etu + div) - etl) * dt));
     out[l * 64 + p] = vn0_;
     out[l * 64 + 16 + p] = vn1_;
     out[l * 64 + 32 + p] = tnew;
@@ -908,12 +936,7 @@ __global__ void __launch_bounds__(RT) k_remap(RemapArgs a) {
   double s3[3] = {0.0, 0.0, 0.0};
   if (own) {
 #pragma unroll
-    for (int k = 0; k < 3; ++k) {
-      s3[k] = a.dp[sb + (size_t)(l0 + k) * 16];
-      D[l0 + k] = s3[k];
-      rD[l0 + k] = 1.0 / s3[k];
-      if (isnan(s3[k]) || s3[k] < 0.0) atomicExch(a.invalid, 1);
-    }
+    for (int k = 0; k < 3; ++k) s3[k] = a.dp[sb + (size_t)(l0 + k) * 16];
   }
   const double ps = warp_sum(s3[0] + s3[1] + s3[2]) + a.hyai0 * a.ps0;
   if (lane == 0) a.ps_v[((size_t)e * NTL + a.np1) * 16 + p] = ps;
@@ -925,6 +948,14 @@ __global__ void __launch_bounds__(RT) k_remap(RemapArgs a) {
       t3[k] = (c_hyai[l + 1] - c_hyai[l]) * a.ps0 + (c_hybi[l + 1] - c_hybi[l]) * ps;
       tgt[l] = t3[k];
       rt3[k] = 1.0 / t3[k];
+      if (a.rsplit == 0) {  // vertically Eulerian source thickness (RemapFunctor.hpp:42-100)
+        const size_t ie = ((size_t)e * NLEV + l) * 16 + p;
+        const double en = l + 1 < NLEV ? a.eta[ie + 16] : 0.0;
+        s3[k] = t3[k] + a.dt * (en - a.eta[ie]);
+      }
+      D[l] = s3[k];
+      rD[l] = 1.0 / s3[k];
+      if (isnan(s3[k]) || s3[k] < 0.0) atomicExch(a.invalid, 1);
     }
   }
   // compute_partitions: pio, pin cumulative thickness
@@ -1023,7 +1054,7 @@ __global__ void __launch_bounds__(RT) k_remap(RemapArgs a) {
   }
   const int nvar = 3 + a.Q;
 #pragma unroll 1
-  for (int var = 0; var < nvar; ++var) {
+  for (int var = a.rsplit == 0 ? 3 : 0; var < nvar; ++var) {
     const bool lo = kF32<R> && var >= 3;
     // extrinsic values (v dp, T dp for the states; Qdp as is), cell means, masses
     double x3[3] = {0.0, 0.0, 0.0};
@@ -1179,7 +1210,7 @@ void launch_dp_from_ps(int E, double* dp, const double* ps_v, int n0, double ps0
 template <typename R>
 void launch_caar(const CaarArgs<R>& a, int E, cudaStream_t s) {
   constexpr int LG = LG_CAAR<R>();
-  const size_t smem = 6 * NLEV * SROW * sizeof(double);
+  const size_t smem = (6 * NLEV * SROW + 16) * sizeof(double);
   static bool init = false;
   if (!init) {
     cudaFuncSetAttribute(k_caar<R, LG>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);

@@ -31,6 +31,8 @@ struct CaarArgs {
   int nm1, n0;
   double dt, eta_ave_w, p_top;  // p_top = hyai(0)*ps0
   int rk_combine, n0orig;       // stage 5: nm1 := (5 nm1 - n0orig)/4 first
+  int rsplit;                   // 0: vertically Eulerian (eta_dot_dpdn, vertical advection)
+  double* eta_acc;              // [E][72][16] eta_dot_dpdn accumulation (rsplit == 0)
 };
 
 template <typename R>
@@ -84,6 +86,9 @@ struct RemapArgs {
   int np1, n0_qdp, Q, remap_alg, nelem;
   double ps0, hyai0;
   int* invalid;   // set to 1 on a negative or NaN source thickness
+  int rsplit;     // 0: tracers only, from the source thickness tgt + dt d(eta_dot_dpdn)
+  const double* eta;  // [E][72][16] eta_dot_dpdn (rsplit == 0)
+  double dt;
 };
 
 // Dense weak Laplacian per element ([E][16][16]) from the FP64 metric.

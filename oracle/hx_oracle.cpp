@@ -548,7 +548,7 @@ void dss_minmax() {
 }
 
 // ----------------------------------------------------------------------------------
-// Caar (src/share/cxx/CaarFunctorImpl.hpp), rsplit > 0 path, one element.
+// Caar (src/share/cxx/CaarFunctorImpl.hpp), one element.
 // ----------------------------------------------------------------------------------
 // Element constants the caar tendency reads.
 struct CaarElem {
@@ -557,26 +557,31 @@ struct CaarElem {
   const double* fcor;      // [16]
   const double* spheremp;  // [16]
   double p_top;            // hyai(0) * ps0
+  int rsplit;              // 0: vertically Eulerian
+  const double* hybi;      // [NLEV + 1]
 };
 
 CaarElem caar_elem(const EM& m, int e) {
   Ctx& c = C();
   return {&m, &c.phis[(size_t)e * 16], &c.fcor[(size_t)e * 16], &c.spheremp[(size_t)e * 16],
-          c.hyai0 * c.ps0};
+          c.hyai0 * c.ps0, c.prm.rsplit, c.hybi};
 }
 
-// One caar stage of one element, rsplit > 0 (CaarFunctorImpl.hpp:97-493):
+// One caar stage of one element (CaarFunctorImpl.hpp:97-597):
 // new = spheremp * (state(nm1) + dt * tendency(state(n0))), before the DSS.  TV is the
 // virtual temperature (T itself when dry).  The outputs must not alias the inputs; vn0,
-// omega_p and phi_out (diagnostics) may be null.
+// omega_p, phi_out and eta_acc (diagnostics) may be null.  With rsplit == 0 the vertical
+// velocity eta_dot_dpdn and the vertical advection of T and v enter the tendencies and
+// eta_dot_dpdn accumulates into eta_acc.
 template <class S>
 void caar_core(const CaarElem& ce, const S* V0, const S* T0, const S* DP0, const S* TV,
                const S* Vm, const S* Tm, const S* DPm, double dt, S* v_new, S* t_new,
-               S* dp_new, double eta_ave_w, S* vn0, S* omega_p, S* phi_out) {
+               S* dp_new, double eta_ave_w, S* vn0, S* omega_p, S* phi_out, S* eta_acc = nullptr) {
   const EM& m = *ce.m;
   const size_t N3 = NP2 * NLEV;
   std::vector<S> vdp(2 * N3), div_vdp(N3), pressure(N3), gradp(2 * N3), omega(N3),
-      gradt(2 * N3), eg(2 * N3), ephi(N3), vort(N3), phi(N3);
+      gradt(2 * N3), eg(2 * N3), ephi(N3), vort(N3), phi(N3), eta(N3, S(0.0)), t_vadv(N3, S(0.0)),
+      v_vadv(2 * N3, S(0.0));
   // compute_temperature_div_vdp: CaarFunctorImpl.hpp:330-409
   for (int p = 0; p < NP2; ++p)
     for (int l = 0; l < NLEV; ++l) {
@@ -621,7 +626,42 @@ void caar_core(const CaarElem& ce, const S* V0, const S* T0, const S* DP0, const
       integration = integration + dv;
     }
   }
-  // compute_phase_3 (:136-148): omega_p, T, v, dp3d
+  // compute_phase_3 (:136-148): with rsplit == 0 first eta_dot_dpdn
+  // (compute_eta_dot_dpdn_vertadv_euler, :262-300), preq_vertadv (:496-597) and
+  // accumulate_eta_dot_dpdn (:236-248); then omega_p, T, v, dp3d
+  if (ce.rsplit == 0) {
+    for (int p = 0; p < NP2; ++p) {
+      S sdot = 0.0;
+      for (int k = 0; k < NLEV - 1; ++k) {
+        sdot += F(div_vdp.data(), p, k);
+        F(eta.data(), p, k + 1) = sdot;
+      }
+      sdot += F(div_vdp.data(), p, NLEV - 1);
+      for (int k = 1; k < NLEV; ++k) F(eta.data(), p, k) = ce.hybi[k] * sdot - F(eta.data(), p, k);
+      F(eta.data(), p, 0) = 0.0;
+      // first level
+      S facp = (0.5 * 1 / F(DP0, p, 0)) * F(eta.data(), p, 1);
+      F(t_vadv.data(), p, 0) = facp * (F(T0, p, 1) - F(T0, p, 0));
+      for (int c2 = 0; c2 < 2; ++c2)
+        FV(v_vadv.data(), c2, p, 0) = facp * (FV(V0, c2, p, 1) - FV(V0, c2, p, 0));
+      for (int k = 1; k < NLEV - 1; ++k) {
+        facp = 0.5 * (1 / F(DP0, p, k)) * F(eta.data(), p, k + 1);
+        const S facm = 0.5 * (1 / F(DP0, p, k)) * F(eta.data(), p, k);
+        F(t_vadv.data(), p, k) = facp * (F(T0, p, k + 1) - F(T0, p, k)) +
+                                 facm * (F(T0, p, k) - F(T0, p, k - 1));
+        for (int c2 = 0; c2 < 2; ++c2)
+          FV(v_vadv.data(), c2, p, k) = facp * (FV(V0, c2, p, k + 1) - FV(V0, c2, p, k)) +
+                                        facm * (FV(V0, c2, p, k) - FV(V0, c2, p, k - 1));
+      }
+      const int kl = NLEV - 1;
+      const S facm = (0.5 * (1 / F(DP0, p, kl))) * F(eta.data(), p, kl);
+      F(t_vadv.data(), p, kl) = facm * (F(T0, p, kl) - F(T0, p, kl - 1));
+      for (int c2 = 0; c2 < 2; ++c2)
+        FV(v_vadv.data(), c2, p, kl) = facm * (FV(V0, c2, p, kl) - FV(V0, c2, p, kl - 1));
+      if (eta_acc)
+        for (int k = 0; k < NLEV; ++k) F(eta_acc, p, k) += eta_ave_w * F(eta.data(), p, k);
+    }
+  }
   if (omega_p)
     for (int p = 0; p < NP2; ++p)
       for (int l = 0; l < NLEV; ++l) F(omega_p, p, l) += eta_ave_w * F(omega.data(), p, l);
@@ -631,7 +671,8 @@ void caar_core(const CaarElem& ce, const S* V0, const S* T0, const S* DP0, const
     for (int l = 0; l < NLEV; ++l) {
       const S vgrad_t = FV(V0, 0, p, l) * FV(gradt.data(), 0, p, l) +
                         FV(V0, 1, p, l) * FV(gradt.data(), 1, p, l);
-      const S ttens = (0.0 - vgrad_t) + kappa * F(TV, p, l) * F(omega.data(), p, l);
+      const S lead = ce.rsplit == 0 ? -F(t_vadv.data(), p, l) : S(0.0);
+      const S ttens = (lead - vgrad_t) + kappa * F(TV, p, l) * F(omega.data(), p, l);
       S temp_np1 = ttens * dt + F(Tm, p, l);
       temp_np1 *= ce.spheremp[p];
       F(t_new, p, l) = temp_np1;
@@ -652,10 +693,12 @@ void caar_core(const CaarElem& ce, const S* V0, const S* T0, const S* DP0, const
       F(vort.data(), p, l) += ce.fcor[p];
       S e0 = FV(eg.data(), 0, p, l), e1 = FV(eg.data(), 1, p, l);
       const S vo = F(vort.data(), p, l);
+      const S va0 = ce.rsplit == 0 ? -FV(v_vadv.data(), 0, p, l) : S(0.0);
+      const S va1 = ce.rsplit == 0 ? -FV(v_vadv.data(), 1, p, l) : S(0.0);
       e0 *= -1.0;
-      e0 += 0.0 + FV(V0, 1, p, l) * vo;
+      e0 += va0 + FV(V0, 1, p, l) * vo;
       e1 *= -1.0;
-      e1 += 0.0 - FV(V0, 0, p, l) * vo;
+      e1 += va1 - FV(V0, 0, p, l) * vo;
       e0 *= dt;
       e0 += FV(Vm, 0, p, l);
       e1 *= dt;
@@ -664,12 +707,12 @@ void caar_core(const CaarElem& ce, const S* V0, const S* T0, const S* DP0, const
       FV(v_new, 0, p, l) = smp * e0;
       FV(v_new, 1, p, l) = smp * e1;
     }
-  // compute_dp3d_np1 (:462-493), eta_dot_dpdn buffer is zero when rsplit > 0
+  // compute_dp3d_np1 (:462-493); eta_dot_dpdn is zero when rsplit > 0
   for (int p = 0; p < NP2; ++p)
     for (int l = 0; l < NLEV; ++l) {
-      S tmp = 0.0;
+      S tmp = l + 1 < NLEV ? F(eta.data(), p, l + 1) : S(0.0);
       tmp += F(div_vdp.data(), p, l);
-      tmp -= 0.0;
+      tmp -= F(eta.data(), p, l);
       tmp = F(DPm, p, l) - tmp * dt;
       F(dp_new, p, l) = ce.spheremp[p] * tmp;
     }
@@ -697,7 +740,8 @@ void caar_element(int e, int nm1, int n0, int np1, double dt, double eta_ave_w, 
   caar_core<double>(caar_elem(m, e), &c.v[IV(e, n0, 0, 0, 0)], T0, DP0, tv.data(),
                     &c.v[IV(e, nm1, 0, 0, 0)], &c.t[IS(e, nm1, 0, 0)], &c.dp3d[IS(e, nm1, 0, 0)],
                     dt, v_new.data(), t_new.data(), dp_new.data(), eta_ave_w,
-                    &c.vn0[I3V(e, 0, 0, 0)], &c.omega_p[I3(e, 0, 0)], &c.phi[I3(e, 0, 0)]);
+                    &c.vn0[I3V(e, 0, 0, 0)], &c.omega_p[I3(e, 0, 0)], &c.phi[I3(e, 0, 0)],
+                    &c.eta_dot_dpdn[I3(e, 0, 0)]);
   std::memcpy(&c.t[IS(e, np1, 0, 0)], t_new.data(), sizeof(double) * N3);
   std::memcpy(&c.v[IV(e, np1, 0, 0, 0)], v_new.data(), sizeof(double) * 2 * N3);
   std::memcpy(&c.dp3d[IS(e, np1, 0, 0)], dp_new.data(), sizeof(double) * N3);
@@ -1279,24 +1323,39 @@ void remap_state_var(const ColumnGridT<S>& G, int remap_alg, const S* src, const
   for (int l = 0; l < NLEV; ++l) x[l] = col[l] / tgt[l];
 }
 
-void remap_run(int np1, int n0_qdp, double dt) {  // RemapFunctor::run_remap, rsplit > 0
+void remap_run(int np1, int n0_qdp, double dt) {  // RemapFunctor::run_remap
   Ctx& c = C();
-  (void)dt;
   const int E = c.E, Q = c.Q;
   int valid = 1;
 #pragma omp parallel for reduction(& : valid)
   for (int e = 0; e < E; ++e) {
     for (int p = 0; p < NP2; ++p) {
       double src[NLEV], tgt[NLEV];
-      for (int l = 0; l < NLEV; ++l) {
-        src[l] = c.dp3d[IS(e, np1, p, l)];
-        if (std::isnan(src[l]) || src[l] < 0.0) valid = 0;
-      }
       ColumnGrid G;
-      c.ps_v[((size_t)e * NTL + np1) * NP2 + p] = remap_target(src, tgt, G);
-      remap_state_var(G, c.prm.remap_alg, src, tgt, &c.v[IV(e, np1, 0, p, 0)]);
-      remap_state_var(G, c.prm.remap_alg, src, tgt, &c.v[IV(e, np1, 1, p, 0)]);
-      remap_state_var(G, c.prm.remap_alg, src, tgt, &c.t[IS(e, np1, p, 0)]);
+      if (c.prm.rsplit > 0) {
+        for (int l = 0; l < NLEV; ++l) {
+          src[l] = c.dp3d[IS(e, np1, p, l)];
+          if (std::isnan(src[l]) || src[l] < 0.0) valid = 0;
+        }
+        c.ps_v[((size_t)e * NTL + np1) * NP2 + p] = remap_target(src, tgt, G);
+        remap_state_var(G, c.prm.remap_alg, src, tgt, &c.v[IV(e, np1, 0, p, 0)]);
+        remap_state_var(G, c.prm.remap_alg, src, tgt, &c.v[IV(e, np1, 1, p, 0)]);
+        remap_state_var(G, c.prm.remap_alg, src, tgt, &c.t[IS(e, np1, p, 0)]);
+      } else {
+        // vertically Eulerian: ps from dp3d(np1), tracers only, from the source
+        // thickness tgt + dt (eta_dot_dpdn(k+1) - eta_dot_dpdn(k)) (RemapFunctor.hpp:42-100)
+        double ps = 0.0;
+        for (int l = 0; l < NLEV; ++l) ps += c.dp3d[IS(e, np1, p, l)];
+        ps += c.hyai0 * c.ps0;
+        c.ps_v[((size_t)e * NTL + np1) * NP2 + p] = ps;
+        for (int l = 0; l < NLEV; ++l) {
+          tgt[l] = (c.hyai[l + 1] - c.hyai[l]) * c.ps0 + (c.hybi[l + 1] - c.hybi[l]) * ps;
+          const double en = l + 1 < NLEV ? c.eta_dot_dpdn[I3(e, p, l + 1)] : 0.0;
+          src[l] = tgt[l] + dt * (en - c.eta_dot_dpdn[I3(e, p, l)]);
+          if (std::isnan(src[l]) || src[l] < 0.0) valid = 0;
+        }
+        ppm_grids(src, tgt, G);
+      }
       double col[NLEV];
       for (int q = 0; q < Q; ++q) {
         double* base = &c.qdp[IQ(e, n0_qdp, q, p, 0, Q)];
@@ -1463,10 +1522,6 @@ void init_simulation_params_c(const int* remap_alg, const int* limiter_option, c
   if (!(*nu_div > 0)) return bad("nu_div");
   if (*ftype != -1) {
     set_error(12, "CAM forcing (ftype 0/2) is not part of this build.");
-    return;
-  }
-  if (*rsplit == 0) {
-    set_error(12, "rsplit=0 (vertically Eulerian) is not part of this build.");
     return;
   }
   Params& p = c.prm;

@@ -68,6 +68,17 @@ def test_caar_stage(pair):
     _assert_close(errs)
 
 
+def test_caar_stage_vertically_eulerian(pair):
+    """rsplit = 0: eta_dot_dpdn from the div(v dp) scan, vertical advection of T and v,
+    eta_dot_dpdn accumulation (CaarFunctorImpl.hpp:137-143, 236-300, 496-597)."""
+    g, o = pair(rsplit=0)
+    for L in (g, o):
+        L.call("hx_run_caar_stage", 0, 1, 2, DT / 5.0, 0.25)
+    errs = H.compare(g, o, ("v", "T", "dp3d"), tl=2)
+    errs.update(H.compare(g, o, ("vn0", "omega_p", "phi", "eta_dot_dpdn")))
+    _assert_close(errs)
+
+
 def test_caar_stage_in_place(pair):
     """n0 == np1 (stages 3-5 of the RK5 scheme read and write the same level)."""
     g, o = pair()
@@ -142,9 +153,11 @@ def test_remap(pair, remap_alg):
     _assert_close(errs)
 
 
-@pytest.mark.parametrize("rsplit,nsub", [(1, 1), (3, 2)])
+@pytest.mark.parametrize("rsplit,nsub", [(1, 1), (3, 2), (0, 2)])
 def test_subcycle(pair, rsplit, nsub):
-    """prim_run_subcycle_c end to end, results pushed through cxx_push_results_to_f90."""
+    """prim_run_subcycle_c end to end, results pushed through cxx_push_results_to_f90;
+    rsplit = 0 is the vertically Eulerian step (tracers alone are remapped, from the
+    thickness the accumulated eta_dot_dpdn gives)."""
     g, o = pair(rsplit=rsplit)
     for _ in range(nsub):
         tg = g.run_subcycle(DT)
@@ -152,6 +165,7 @@ def test_subcycle(pair, rsplit, nsub):
         assert tg == to
     rg, ro = g.push_results(), o.push_results()
     errs = {k: H.rel_err(rg[k], ro[k]) for k in rg}
+    errs.update(H.compare(g, o, ("eta_dot_dpdn",)))
     _assert_close(errs)
 
 

@@ -176,7 +176,7 @@ def test_solid_body_rotation(oracle_path):
     assert np.abs(vort - exact[:, None]).max() < 1e-2 * scale
 
 
-@pytest.mark.parametrize("rsplit", [1, 3])
+@pytest.mark.parametrize("rsplit", [0, 1, 3])
 def test_subcycle_conserves_mass(oracle_path, rsplit):
     L = _setup(oracle_path, ne=4, Q=3, rsplit=rsplit)
     m = H.mesh(4)
@@ -215,7 +215,7 @@ def test_constant_mixing_ratio_survives_remap(oracle_path):
 
 @pytest.mark.parametrize("field,value,code", [
     ("limiter_option", 4, 11), ("remap_alg", 3, 11), ("time_step_type", 1, 11),
-    ("hypervis_order", 1, 11), ("ftype", 2, 12), ("rsplit", 0, 12),
+    ("hypervis_order", 1, 11), ("ftype", 2, 12),
 ])
 def test_option_checks(oracle_path, gpu_lib_cpu, field, value, code):
     """cxx_f90_interface.cpp:43-52 option checks; the same codes from both libraries."""
