@@ -233,6 +233,23 @@ class HxLibrary:
             out.append((nm, int(la[i]), float(ms[i])))
         return out
 
+    # -- CAM forcing (the calls the Fortran prim_run_subcycle makes around each step) ----
+    def push_forcing(self, FM: np.ndarray, FT: np.ndarray, FQ: np.ndarray, Qdp: np.ndarray):
+        """f90_push_forcing_to_cxx: FM (E,72,2,4,4), FT (E,72,4,4), FQ (E,Q,72,4,4),
+        Qdp (E,2,Q,72,4,4)."""
+        arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (FM, FT, FQ, Qdp)]
+        self.lib.f90_push_forcing_to_cxx(*[C.c_void_p(a.ctypes.data) for a in arrs])
+        self.check("f90_push_forcing_to_cxx")
+
+    def pull_forcing(self):
+        """cxx_push_forcing_to_f90 -> dict(FM, FT, FQ)."""
+        E, Q = self.nelem, self.qsize
+        out = dict(FM=np.zeros((E, NLEV, 2, NP, NP)), FT=np.zeros((E, NLEV, NP, NP)),
+                   FQ=np.zeros((E, Q, NLEV, NP, NP)))
+        self.lib.cxx_push_forcing_to_f90(*[C.c_void_p(out[k].ctypes.data) for k in ("FM", "FT", "FQ")])
+        self.check("cxx_push_forcing_to_f90")
+        return out
+
     # -- dry-dynamics trajectory and its adjoint -----------------------------------------
     def _dyn_arrays(self, st=None):
         E = self.nelem

@@ -132,6 +132,8 @@ struct Backend {
   virtual void prim_step(double dt) = 0;
   virtual int field(const std::string& name, int tl, double* host, bool get) = 0;
   virtual int dss_field(const std::string& name, int tl, bool rsmp) = 0;
+  virtual void push_forcing(const double* FM, const double* FT, const double* FQ, const double* Qdp) = 0;
+  virtual void pull_forcing(double* FM, double* FT, double* FQ) = 0;
   virtual void traj_forward(const double* v, const double* T, const double* dp, int nsteps, double dt,
                             double* vo, double* To, double* dpo) = 0;
   virtual void traj_vjp(const double* vb, const double* Tb, const double* dpb, double* vg, double* Tg,
@@ -221,6 +223,7 @@ struct BackendT : Backend {
   double *qlim = 0, *qlim_tmp = 0, *dp0 = 0, *staging = 0, *rsp_d = 0, *rsp_noalloc = 0;
   double* gen_scr = 0;
   double* lapm = 0;  // FP64 form: dense weak Laplacian per element
+  double *fm = 0, *ft = 0, *fq = 0;  // CAM forcing, Fortran layouts (allocated on first push)
   int *tab_cnt = 0, *tab_src = 0, *nbr = 0, *invalid = 0;
   int* h_invalid = nullptr;
   size_t staging_n = 0;
@@ -234,7 +237,8 @@ struct BackendT : Backend {
     void* ptrs[] = {D, Dinv, metinv, metdet, spheremp, rspheremp, mp, fcor, phis, tensorvisc, vec_sph2cart,
                     v, T, dp, ps_v, qdp, Qc, phi, omega_p, eta, derived_dp, divdp, divdp_proj, dpdiss_ave,
                     dpdiss_bih, vn0, caar_out, bufA, bufB, vstar, dpdissk, fscr, qtens, qscr, qlim, qlim_tmp,
-                    dp0, staging, rsp_d, rsp_noalloc, gen_scr, tab_cnt, tab_src, nbr, invalid, sp_d, lapm};
+                    dp0, staging, rsp_d, rsp_noalloc, gen_scr, tab_cnt, tab_src, nbr, invalid, sp_d, lapm,
+                    fm, ft, fq};
     for (void* p : ptrs)
       if (p) cudaFree(p);
     if (h_invalid) cudaFreeHost(h_invalid);
@@ -496,10 +500,50 @@ struct BackendT : Backend {
     if (p.qsize > 0) tracers_rk2(dt * p.qsplit);
   }
 
+  // cxx_f90_interface.cpp:180-205
+  void push_forcing(const double* FM, const double* FT, const double* FQ, const double* hq) override {
+    const size_t n3 = N3();
+    if (!ft) {
+      ft = dalloc<double>(n3);
+      fm = dalloc<double>(2 * n3);
+    }
+    to_dev(fm, FM, 2 * n3);
+    to_dev(ft, FT, n3);
+    if (s.prm.ftype == 0) {
+      if (!fq) fq = dalloc<double>(n3 * (Q > 0 ? Q : 1));
+      if (Q > 0) to_dev(fq, FQ, n3 * Q);
+    }
+    if (Q > 0) to_dev(qdp, hq, n3 * QTL * Q);
+    ck(cudaStreamSynchronize(g_stream), "push_forcing");
+  }
+  // cxx_f90_interface.cpp:157-178
+  void pull_forcing(double* FM, double* FT, double* FQ) override {
+    const size_t n3 = N3();
+    if (!ft) {
+      std::memset(FM, 0, 2 * n3 * sizeof(double));
+      std::memset(FT, 0, n3 * sizeof(double));
+      if (s.prm.ftype == 0 && Q > 0) std::memset(FQ, 0, n3 * Q * sizeof(double));
+      return;
+    }
+    to_host(FM, fm, 2 * n3);
+    to_host(FT, ft, n3);
+    if (s.prm.ftype == 0 && Q > 0) {
+      if (fq) to_host(FQ, fq, n3 * Q);
+      else std::memset(FQ, 0, n3 * Q * sizeof(double));
+    }
+    ck(cudaStreamSynchronize(g_stream), "pull_forcing");
+  }
+
   void run_subcycle(double dt) override {
     const Params& p = s.prm;
     const double dt_remap = p.rsplit > 0 ? dt * p.qsplit * p.rsplit : dt * p.qsplit;
     s.tl.update_tracers_levels(p.qsplit);
+    // apply_cam_forcing (ftype 0) / apply_cam_forcing_dynamics (ftype 2), prim_driver.cpp:70-81
+    if ((p.ftype == 0 || p.ftype == 2) && ft) {
+      launch_cam_forcing(E, Q, T, v, ft, fm, p.ftype == 0 ? fq : nullptr, qdp, ps_v, Qc, s.tl.n0,
+                         s.tl.n0_qdp, p.moist ? 1 : 0, dt_remap, s.ps0, g_stream);
+      post("cam_forcing");
+    }
     launch_dp_from_ps(E, dp, ps_v, s.tl.n0, s.ps0, g_stream);
     post("dp3d_from_ps");
     prim_step(dt);
@@ -956,7 +1000,6 @@ void init_simulation_params_c(const int* remap_alg, const int* limiter_option, c
     if (!(*nu_p > 0)) bad("nu_p");
     if (!(*nu > 0)) bad("nu");
     if (!(*nu_div > 0)) bad("nu_div");
-    if (*ftype != -1) fail(12, "CAM forcing (ftype 0/2) is not part of this build");
     if (*qsplit < 1 || *hypervis_subcycle < 1 || *qsize < 0) fail(13, "invalid qsplit/hypervis_subcycle/qsize");
     Params& p = S().prm;
     p.remap_alg = *remap_alg; p.limiter_option = *limiter_option; p.rsplit = *rsplit; p.qsplit = *qsplit;
@@ -1175,6 +1218,14 @@ int hx_timer_stop(double* ms) {
     ck(cudaEventElapsedTime(&f, g_t0, g_t1), "cudaEventElapsedTime");
     *ms = f;
   });
+}
+
+void f90_push_forcing_to_cxx(const double* FM, const double* FT, const double* FQ, const double* Qdp) {
+  run([&] { B().push_forcing(FM, FT, FQ, Qdp); });
+}
+
+void cxx_push_forcing_to_f90(double* FM, double* FT, double* FQ) {
+  run([&] { B().pull_forcing(FM, FT, FQ); });
 }
 
 int hx_traj_forward(const double* v, const double* T, const double* dp3d, int nsteps, double dt,

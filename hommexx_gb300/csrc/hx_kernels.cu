@@ -416,6 +416,47 @@ __global__ void __launch_bounds__(EQ_THREADS) k_update_q(int Q, const double* qd
       qdp[((((size_t)e * QTL + np1_qdp) * Q + q) * NLEV + l) * 16 + p] / dp;
 }
 
+// CAM forcing (CamForcing.cpp:20-170).  Layouts: ft [E][72][16], fm [E][72][2][16],
+// fq [E][Q][72][16] (the Fortran layouts of the forcing arrays).
+__global__ void k_state_forcing(int E, double* T, double* v, const double* ft, const double* fm, int n0,
+                                double dt) {
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= E * NLEV * 16) return;
+  const int e = idx / (NLEV * 16), r = idx % (NLEV * 16), l = r / 16, p = r & 15;
+  T[((size_t)e * NTL + n0) * NLEV * 16 + r] += dt * ft[idx];
+  const size_t vb = (((size_t)e * NTL + n0) * NLEV + l) * 32 + p;
+  const size_t fb = ((size_t)e * NLEV + l) * 32 + p;
+  v[vb] += dt * fm[fb];
+  v[vb + 16] += dt * fm[fb + 16];
+}
+
+__device__ __forceinline__ double clip_forcing(double qdp_s, double v1) {
+  if (qdp_s + v1 < 0.0 && v1 < 0.0) v1 = qdp_s < 0.0 ? 0.0 : -qdp_s;
+  return v1;
+}
+
+// ps_v(n0) += sum over levels of tracer 0's clipped increments (moist), one thread per
+// column, levels in order; runs before the tracer forcing changes Qdp.
+__global__ void k_ps_forcing(int E, int Q, const double* fq, const double* qdp, double* ps_v, int n0,
+                             int n0_qdp, double dt) {
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= E * 16) return;
+  const int e = idx / 16, p = idx & 15;
+  const double* q0 = qdp + (((size_t)e * QTL + n0_qdp) * Q) * NLEV * 16 + p;
+  const double* f0 = fq + ((size_t)e * Q) * NLEV * 16 + p;
+  double acc = 0.0;
+  for (int l = 0; l < NLEV; ++l) acc += clip_forcing(q0[l * 16], dt * f0[l * 16]);
+  ps_v[((size_t)e * NTL + n0) * 16 + p] += acc;
+}
+
+__global__ void __launch_bounds__(EQ_THREADS) k_tracer_forcing(int Q, const double* fq, double* qdp,
+                                                               int n0_qdp, double dt) {
+  int e, q, l, p;
+  eq_index(Q, e, q, l, p);
+  double& qd = qdp[((((size_t)e * QTL + n0_qdp) * Q + q) * NLEV + l) * 16 + p];
+  qd += clip_forcing(qd, dt * fq[(((size_t)e * Q + q) * NLEV + l) * 16 + p]);
+}
+
 // ======================================================================================
 // Tracers (EulerStepFunctorImpl)
 // ======================================================================================
@@ -1330,6 +1371,20 @@ void launch_dss_inplace(int E, int nf, double* base, long long fs, long long es,
   KScope k("dss_generic", s);
   k_copy_fields<<<dim3(E * nf, NLEV / EQ_LEVELS), EQ_THREADS, 0, s>>>(nf, base, fs, es, ls, scr);
   k_dss_from_copy<<<dim3(E * nf, NLEV / EQ_LEVELS), EQ_THREADS, 0, s>>>(nf, base, fs, es, ls, scr, rsmp, t);
+}
+
+void launch_cam_forcing(int E, int Q, double* T, double* v, const double* ft, const double* fm,
+                        const double* fq, double* qdp, double* ps_v, double* Qc, int n0, int n0_qdp,
+                        int moist, double dt, double ps0, cudaStream_t s) {
+  {
+    KScope k("cam_forcing_state", s);
+    k_state_forcing<<<nblk((long long)E * NLEV * 16, 256), 256, 0, s>>>(E, T, v, ft, fm, n0, dt);
+  }
+  if (fq == nullptr || Q == 0) return;
+  KScope k("cam_forcing_tracers", s);
+  if (moist) k_ps_forcing<<<nblk((long long)E * 16, 128), 128, 0, s>>>(E, Q, fq, qdp, ps_v, n0, n0_qdp, dt);
+  k_tracer_forcing<<<dim3(E * Q, NLEV / EQ_LEVELS), EQ_THREADS, 0, s>>>(Q, fq, qdp, n0_qdp, dt);
+  k_update_q<<<dim3(E * Q, NLEV / EQ_LEVELS), EQ_THREADS, 0, s>>>(Q, qdp, Qc, ps_v, n0, n0_qdp, ps0);
 }
 
 void launch_lap_matrix(const MetricP<double>& m, int E, double* out, cudaStream_t s) {

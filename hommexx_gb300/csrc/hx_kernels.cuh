@@ -91,6 +91,12 @@ struct RemapArgs {
   double dt;
 };
 
+// CAM forcing (CamForcing.cpp:20-170): T, v at level n0 += dt FT, dt FM; with fq,
+// Qdp at n0_qdp += dt FQ clipped at zero, ps_v(n0) moved by tracer 0's clipped increments
+// when moist, Q = Qdp / dp.
+void launch_cam_forcing(int E, int Q, double* T, double* v, const double* ft, const double* fm,
+                        const double* fq, double* qdp, double* ps_v, double* Qc, int n0, int n0_qdp,
+                        int moist, double dt, double ps0, cudaStream_t s);
 // Dense weak Laplacian per element ([E][16][16]) from the FP64 metric.
 void launch_lap_matrix(const MetricP<double>& m, int E, double* out, cudaStream_t s);
 void launch_prim_step_init(int E, double* eta, double* vn0, double* omega_p, double* dpa,

@@ -112,6 +112,19 @@ void cxx_push_results_to_f90(double* const* v, double* const* T, double* const* 
                              double* const* Qdp, double* const* Q, double* const* ps_v,
                              double* const* omega_p);
 
+/* These two take the arrays themselves (the Fortran interface declares them as
+ * real(c_double) arrays, prim_driver_mod.F90:1328-1343), not c_ptr by reference.
+ * src/share/cxx/cxx_f90_interface.cpp:180-205 — CAM forcing in: FM (np,np,2,nlev,nelemd),
+ * FT (np,np,nlev,nelemd), FQ (np,np,nlev,qsize_d,nelemd; read for ftype 0 only) and the
+ * tracer mass Qdp (np,np,nlev,qsize_d,2,nelemd).  The Fortran prim_run_subcycle calls it
+ * before every prim_run_subcycle_c (src/share/prim_driver_mod.F90:1380).  The forcing is
+ * applied at the start of each remap interval: ftype 0 forces T, v and the tracers
+ * (CamForcing.cpp apply_cam_forcing), ftype 2 T and v (apply_cam_forcing_dynamics). */
+void f90_push_forcing_to_cxx(const double* FM, const double* FT, const double* FQ,
+                             const double* Qdp);
+/* src/share/cxx/cxx_f90_interface.cpp:157-178 — the forcing back (FQ for ftype 0 only). */
+void cxx_push_forcing_to_f90(double* FM, double* FT, double* FQ);
+
 /* ---- Additions (no counterpart in the reference) ------------------------------------ */
 
 /* Status of the last call: 0 on success, else the reference's error code

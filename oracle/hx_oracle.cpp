@@ -121,6 +121,7 @@ struct Ctx {
   std::vector<double> fcor, mp, spheremp, rspheremp, metdet, phis;
   // state
   std::vector<double> v, t, dp3d, ps_v, qdp, Qc;
+  std::vector<double> fm, ft, fq;  // CAM forcing: FM [E][2][16][NLEV], FT/FQ level-contiguous
   std::vector<double> phi, omega_p, eta_dot_dpdn, derived_dp, divdp, divdp_proj,
       dpdiss_ave, dpdiss_bih, vn0;
   // buffers
@@ -1400,6 +1401,57 @@ void prim_step(double dt) {
   if (pr.qsize > 0) tracers_rk2(dt * pr.qsplit);
 }
 
+// CAM forcing (CamForcing.cpp:20-170): state_forcing adds dt FT, dt FM to T, v at n0;
+// with tracers (ftype 0) tracer_forcing adds dt FQ to Qdp at n0_qdp, clipped so that no
+// forcing makes Qdp negative, moves ps_v by the clipped increments of tracer 0 when
+// moist, and recomputes Q.
+void apply_cam_forcing(double dt, bool tracers) {
+  Ctx& c = C();
+  if (c.ft.empty()) return;  // no forcing pushed
+  const int n0 = c.tl.n0, nq = c.tl.n0_qdp, Q = c.Q;
+#pragma omp parallel for
+  for (int e = 0; e < c.E; ++e)
+    for (int p = 0; p < NP2; ++p)
+      for (int l = 0; l < NLEV; ++l) {
+        c.t[IS(e, n0, p, l)] += dt * c.ft[I3(e, p, l)];
+        c.v[IV(e, n0, 0, p, l)] += dt * c.fm[I3V(e, 0, p, l)];
+        c.v[IV(e, n0, 1, p, l)] += dt * c.fm[I3V(e, 1, p, l)];
+      }
+  if (!tracers || Q == 0) return;
+  auto clip = [](double qdp_s, double v1) {
+    if (qdp_s + v1 < 0.0 && v1 < 0.0) v1 = qdp_s < 0.0 ? 0.0 : -qdp_s;
+    return v1;
+  };
+  auto FQ = [&](int e, int q, int p, int l) -> double& {
+    return c.fq[(((size_t)e * Q + q) * NP2 + p) * NLEV + l];
+  };
+  if (c.prm.moist) {
+#pragma omp parallel for
+    for (int e = 0; e < c.E; ++e)
+      for (int p = 0; p < NP2; ++p) {
+        double acc = 0.0;
+        for (int l = 0; l < NLEV; ++l) acc += clip(c.qdp[IQ(e, nq, 0, p, l, Q)], dt * FQ(e, 0, p, l));
+        c.ps_v[((size_t)e * NTL + n0) * NP2 + p] += acc;
+      }
+  }
+#pragma omp parallel for
+  for (int e = 0; e < c.E; ++e)
+    for (int q = 0; q < Q; ++q)
+      for (int p = 0; p < NP2; ++p)
+        for (int l = 0; l < NLEV; ++l) {
+          double& qd = c.qdp[IQ(e, nq, q, p, l, Q)];
+          qd += clip(qd, dt * FQ(e, q, p, l));
+        }
+#pragma omp parallel for
+  for (int e = 0; e < c.E; ++e)
+    for (int q = 0; q < Q; ++q)
+      for (int p = 0; p < NP2; ++p)
+        for (int l = 0; l < NLEV; ++l) {
+          const double dp = c.ai_delta[l] * c.ps0 + c.bi_delta[l] * c.ps_v[((size_t)e * NTL + n0) * NP2 + p];
+          c.Qc[(((size_t)e * Q + q) * NP2 + p) * NLEV + l] = c.qdp[IQ(e, nq, q, p, l, Q)] / dp;
+        }
+}
+
 void prim_run_subcycle(double dt, int& nstep, int& nm1, int& n0, int& np1) {  // prim_driver.cpp:31-156
   Ctx& c = C();
   const Params& pr = c.prm;
@@ -1407,6 +1459,8 @@ void prim_run_subcycle(double dt, int& nstep, int& nm1, int& n0, int& np1) {  //
   double dt_remap = dt_q;
   if (pr.rsplit > 0) dt_remap = dt_q * pr.rsplit;
   c.tl.update_tracers_levels(pr.qsplit);
+  if (pr.ftype == 0) apply_cam_forcing(dt_remap, true);
+  else if (pr.ftype == 2) apply_cam_forcing(dt_remap, false);
   // dp3d from ps_v
   const int tn0 = c.tl.n0;
 #pragma omp parallel for
@@ -1520,10 +1574,6 @@ void init_simulation_params_c(const int* remap_alg, const int* limiter_option, c
   if (!(*nu_p > 0)) return bad("nu_p");
   if (!(*nu > 0)) return bad("nu");
   if (!(*nu_div > 0)) return bad("nu_div");
-  if (*ftype != -1) {
-    set_error(12, "CAM forcing (ftype 0/2) is not part of this build.");
-    return;
-  }
   Params& p = c.prm;
   p.remap_alg = *remap_alg;
   p.limiter_option = *limiter_option;
@@ -1678,6 +1728,50 @@ void cxx_push_results_to_f90(double* const* v, double* const* T, double* const* 
     push_block(&c.omega_p[I3(e, 0, 0)], *omega_p + (size_t)e * B, 1);
   }
   std::memcpy(*ps_v, c.ps_v.data(), sizeof(double) * c.E * NTL * NP2);
+}
+
+// cxx_f90_interface.cpp:180-205: forcing in (FQ only for ftype 0) and the tracer mass.
+void f90_push_forcing_to_cxx(const double* FM, const double* FT, const double* FQ,
+                             const double* Qdp) {
+  Ctx& c = C();
+  const size_t B = (size_t)NP2 * NLEV;
+  c.fm.resize((size_t)c.E * 2 * B);
+  c.ft.resize((size_t)c.E * B);
+  for (int e = 0; e < c.E; ++e) {
+    pull_block(FM + (size_t)e * 2 * B, &c.fm[I3V(e, 0, 0, 0)], 2);
+    pull_block(FT + (size_t)e * B, &c.ft[I3(e, 0, 0)], 1);
+  }
+  if (c.prm.ftype == 0) {
+    c.fq.resize((size_t)c.E * c.Q * B);
+    for (int e = 0; e < c.E; ++e)
+      for (int q = 0; q < c.Q; ++q)
+        pull_block(FQ + ((size_t)e * c.Q + q) * B, &c.fq[((size_t)e * c.Q + q) * B], 1);
+  }
+  for (int e = 0; e < c.E; ++e)
+    for (int qt = 0; qt < QTL; ++qt)
+      for (int q = 0; q < c.Q; ++q)
+        pull_block(Qdp + (((size_t)e * QTL + qt) * c.Q + q) * B, &c.qdp[IQ(e, qt, q, 0, 0, c.Q)], 1);
+}
+
+// cxx_f90_interface.cpp:157-178
+void cxx_push_forcing_to_f90(double* FM, double* FT, double* FQ) {
+  Ctx& c = C();
+  const size_t B = (size_t)NP2 * NLEV;
+  if (c.ft.empty()) {  // nothing pushed: zero forcing
+    std::memset(FM, 0, sizeof(double) * c.E * 2 * B);
+    std::memset(FT, 0, sizeof(double) * c.E * B);
+  } else {
+    for (int e = 0; e < c.E; ++e) {
+      push_block(&c.fm[I3V(e, 0, 0, 0)], FM + (size_t)e * 2 * B, 2);
+      push_block(&c.ft[I3(e, 0, 0)], FT + (size_t)e * B, 1);
+    }
+  }
+  if (c.prm.ftype == 0) {
+    if (c.fq.empty()) c.fq.assign((size_t)c.E * c.Q * B, 0.0);
+    for (int e = 0; e < c.E; ++e)
+      for (int q = 0; q < c.Q; ++q)
+        push_block(&c.fq[((size_t)e * c.Q + q) * B], FQ + ((size_t)e * c.Q + q) * B, 1);
+  }
 }
 
 int hx_last_error(char* buf, int buflen) {

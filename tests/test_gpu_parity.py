@@ -169,6 +169,39 @@ def test_subcycle(pair, rsplit, nsub):
     _assert_close(errs)
 
 
+def _forcing(ne, Q, seed):
+    rng = np.random.default_rng(seed)
+    E = 6 * ne * ne
+    st = H.state(ne, Q)
+    FM = 1e-4 * rng.standard_normal((E, 72, 2, 4, 4))
+    FT = 1e-4 * rng.standard_normal((E, 72, 4, 4))
+    FQ = 5e-6 * rng.standard_normal((E, Q, 72, 4, 4))
+    # strong negative tracer forcing at some points so that the clipping acts
+    mask = rng.random(FQ.shape) < 0.05
+    FQ[mask] = -2.0 * st["Qdp"][:, 1][mask] / 900.0
+    return FM, FT, FQ, st["Qdp"]
+
+
+@pytest.mark.parametrize("ftype,moist", [(0, False), (0, True), (2, False)])
+def test_cam_forcing(pair, ftype, moist):
+    """f90_push_forcing_to_cxx / cxx_push_forcing_to_f90 around two remap intervals with
+    forcing applied at their start (CamForcing.cpp: state, clipped tracer and, when
+    moist, surface-pressure forcing)."""
+    g, o = pair(rsplit=3, ftype=ftype, moisture=moist)
+    FM, FT, FQ, Qdp = _forcing(4, 4, 7 + ftype)
+    for _ in range(2):
+        for L in (g, o):
+            L.push_forcing(FM, FT, FQ, Qdp if _ == 0 else L.push_results()["Qdp"])
+            L.run_subcycle(DT)
+    rg, ro = g.push_results(), o.push_results()
+    errs = {k: H.rel_err(rg[k], ro[k]) for k in rg}
+    _assert_close(errs)
+    fg, fo = g.pull_forcing(), o.pull_forcing()
+    for k in fg:
+        assert np.array_equal(fg[k], fo[k]), k
+    assert np.array_equal(fg["FT"], FT)
+
+
 def test_mass_conservation_gpu(pair):
     g, _ = pair(rsplit=3)
     m = H.mesh(4)

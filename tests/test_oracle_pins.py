@@ -215,7 +215,7 @@ def test_constant_mixing_ratio_survives_remap(oracle_path):
 
 @pytest.mark.parametrize("field,value,code", [
     ("limiter_option", 4, 11), ("remap_alg", 3, 11), ("time_step_type", 1, 11),
-    ("hypervis_order", 1, 11), ("ftype", 2, 12),
+    ("hypervis_order", 1, 11), ("ftype", 1, 11),
 ])
 def test_option_checks(oracle_path, gpu_lib_cpu, field, value, code):
     """cxx_f90_interface.cpp:43-52 option checks; the same codes from both libraries."""
