@@ -112,7 +112,7 @@ class HxLibrary:
 
     # -- initialisation (prim_init1 / prim_init2 order) --------------------------------
     def init(self, mesh, hv, params: SimParams, state: dict, precision: int = 0,
-             abort_on_error: bool = False, time_levels=(1, 2, 3)):
+             abort_on_error: bool = False, time_levels=(1, 2, 3), diagnostics: bool = False):
         L = self.lib
         p = params.resolved()
         L.hx_set_abort_on_error(0 if not abort_on_error else 1)
@@ -147,6 +147,8 @@ class HxLibrary:
         self.nelem = mesh.nelem
         self.qsize = p.qsize
         self.set_state(state)
+        if diagnostics:
+            self.init_diagnostics()
         hyam = np.ascontiguousarray(hv.hyam)
         hyai = np.ascontiguousarray(hv.hyai)
         hybm = np.ascontiguousarray(hv.hybm)
@@ -159,6 +161,22 @@ class HxLibrary:
         L.init_time_level_c(_i(nm1), _i(n0), _i(np1), _i(0), _i(0))
         self.tl = [nm1 - 1, n0 - 1, np1 - 1, 0]
         return self
+
+    DIAG_NAMES = ("Q", "Qvar", "Qmass", "Q1mass", "IEner", "IEner_wet", "KEner", "PEner")
+
+    def init_diagnostics(self, fill: float = np.nan):
+        """init_diagnostics_c with host arrays in the Fortran layouts of elem%state%Q and
+        elem%accum (np,np,nlev,qsize) / (np,np,qsize,4) / (np,np,qsize) / (np,np,4) /
+        (np,np), filled with ``fill``; the library writes them whenever a remap interval
+        computes diagnostics.  Returns the dict of arrays."""
+        E, Q = self.nelem, self.qsize
+        shapes = dict(Q=(E, Q, NLEV, NP, NP), Qvar=(E, 4, Q, NP, NP), Qmass=(E, 4, Q, NP, NP),
+                      Q1mass=(E, Q, NP, NP), IEner=(E, 4, NP, NP), IEner_wet=(E, NP, NP),
+                      KEner=(E, 4, NP, NP), PEner=(E, 4, NP, NP))
+        self.diag = {k: np.full(shapes[k], fill) for k in self.DIAG_NAMES}
+        self.lib.init_diagnostics_c(*[_pp(self.diag[k]) for k in self.DIAG_NAMES])
+        self.check("init_diagnostics_c")
+        return self.diag
 
     def set_state(self, state: dict):
         arrs = [np.ascontiguousarray(state[k], dtype=np.float64)

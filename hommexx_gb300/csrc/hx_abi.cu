@@ -17,6 +17,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <climits>
 #include <map>
 #include <memory>
 #include <string>
@@ -34,7 +35,7 @@ struct Params {
   int state_frequency = 1, hypervis_order = 2, hypervis_subcycle = 1, ftype = -1;
   double nu = 0, nu_p = 0, nu_q = 0, nu_s = 0, nu_div = 0, nu_top = 0, hypervis_scaling = 0;
   double nu_ratio1 = 1, nu_ratio2 = 1;
-  bool moist = false, set = false;
+  bool moist = false, disable_diagnostics = true, use_cpstar = false, set = false;
 };
 
 struct TimeLevel {
@@ -120,7 +121,7 @@ struct Backend {
                           const double* ps_v) = 0;
   virtual void push(double* v, double* T, double* dp, double* qdp, double* Q, double* ps_v,
                     double* omega_p) = 0;
-  virtual void run_subcycle(double dt) = 0;
+  virtual void run_subcycle(double dt, int last_time_step) = 0;
   virtual void caar_stage(int nm1, int n0, int np1, double dt, double w, int n0_qdp, int combine,
                           int n0orig) = 0;
   virtual void rk5(int nm1, int n0, int np1, int n0_qdp, double dt, double w) = 0;
@@ -158,6 +159,8 @@ struct Session {
   std::string last_msg;
   bool abort_on_error = true;
   int traj_mode = 0;  // checkpointing of the dry trajectory (hx_traj_set_checkpointing)
+  // init_diagnostics_c host arrays: Q, Qvar, Qmass, Q1mass, IEner, IEner_wet, KEner, PEner
+  double* diag[8] = {};
   ~Session() {}
 };
 
@@ -224,6 +227,7 @@ struct BackendT : Backend {
   double* gen_scr = 0;
   double* lapm = 0;  // FP64 form: dense weak Laplacian per element
   double *fm = 0, *ft = 0, *fq = 0;  // CAM forcing, Fortran layouts (allocated on first push)
+  double *phis_d = 0, *diag_d = 0;   // FP64 phis; diagnostics scratch (allocated on first use)
   int *tab_cnt = 0, *tab_src = 0, *nbr = 0, *invalid = 0;
   int* h_invalid = nullptr;
   size_t staging_n = 0;
@@ -238,7 +242,7 @@ struct BackendT : Backend {
                     v, T, dp, ps_v, qdp, Qc, phi, omega_p, eta, derived_dp, divdp, divdp_proj, dpdiss_ave,
                     dpdiss_bih, vn0, caar_out, bufA, bufB, vstar, dpdissk, fscr, qtens, qscr, qlim, qlim_tmp,
                     dp0, staging, rsp_d, rsp_noalloc, gen_scr, tab_cnt, tab_src, nbr, invalid, sp_d, lapm,
-                    fm, ft, fq};
+                    fm, ft, fq, phis_d, diag_d};
     for (void* p : ptrs)
       if (p) cudaFree(p);
     if (h_invalid) cudaFreeHost(h_invalid);
@@ -257,6 +261,7 @@ struct BackendT : Backend {
     rspheremp = dalloc<R>((size_t)E * 16); mp = dalloc<R>((size_t)E * 16);
     fcor = dalloc<R>((size_t)E * 16); phis = dalloc<R>((size_t)E * 16);
     sp_d = dalloc<double>((size_t)E * 16); rsp_d = dalloc<double>((size_t)E * 16);
+    phis_d = dalloc<double>((size_t)E * 16);
     v = dalloc<double>(n3 * NTL * 2); T = dalloc<double>(n3 * NTL); dp = dalloc<double>(n3 * NTL);
     ps_v = dalloc<double>((size_t)E * NTL * 16);
     qdp = dalloc<double>(n3 * QTL * Q); Qc = dalloc<double>(n3 * Q);
@@ -297,6 +302,7 @@ struct BackendT : Backend {
     to_dev_R(metinv, a[7], (size_t)E * 64);
     to_dev_R(phis, a[8], (size_t)E * 16);
     to_dev(sp_d, a[4], (size_t)E * 16);
+    to_dev(phis_d, a[8], (size_t)E * 16);
     to_dev(rsp_d, a[5], (size_t)E * 16);
     if (!rsp_noalloc) rsp_noalloc = dalloc<double>((size_t)E * 16);
     ck(cudaMemcpyAsync(rsp_noalloc, a[5], (size_t)E * 16 * sizeof(double), cudaMemcpyHostToDevice, g_stream), "H2D");
@@ -534,15 +540,75 @@ struct BackendT : Backend {
     ck(cudaStreamSynchronize(g_stream), "pull_forcing");
   }
 
-  void run_subcycle(double dt) override {
+  // Tracer mass diagnostics (Diagnostics.cpp:37-84): Q is copied into the host array
+  // Q, and the column sums of Qdp*Q and Qdp at the call's tracer level into
+  // Qvar(:,:,:,ivar), Qmass(:,:,:,ivar) and Q1mass.
+  void diag_scalars(bool before_advance, int ivar) {
+    s.tl.update_tracers_levels(s.prm.qsplit);
+    const int t2 = before_advance ? s.tl.n0_qdp : s.tl.np1_qdp;
+    if (s.prm.time_step_type <= 0 || Q == 0) return;
+    diag_alloc();
+    double* qv = diag_d + (size_t)E * 64;
+    double* qm = qv + (size_t)E * Q * 16;
+    launch_diag_scalars(E, Q, qdp, Qc, t2, qv, qm, g_stream);
+    post("diag_scalars");
+    const size_t w = (size_t)Q * 16 * sizeof(double);
+    ck(cudaMemcpyAsync(s.diag[0], Qc, N3() * Q * sizeof(double), cudaMemcpyDeviceToHost, g_stream), "D2H Q");
+    ck(cudaMemcpy2DAsync(s.diag[1] + (size_t)ivar * Q * 16, 4 * w, qv, w, w, E, cudaMemcpyDeviceToHost, g_stream),
+       "D2H Qvar");
+    ck(cudaMemcpy2DAsync(s.diag[2] + (size_t)ivar * Q * 16, 4 * w, qm, w, w, E, cudaMemcpyDeviceToHost, g_stream),
+       "D2H Qmass");
+    ck(cudaMemcpyAsync(s.diag[3], qm, w * E, cudaMemcpyDeviceToHost, g_stream), "D2H Q1mass");
+    ck(cudaStreamSynchronize(g_stream), "diag_scalars");
+  }
+
+  // Column energies (Diagnostics.cpp:86-185) into IEner/KEner/PEner(:,:,ivar) and IEner_wet.
+  void energy_halftimes(bool before_advance, int ivar) {
+    s.tl.update_tracers_levels(s.prm.qsplit);
+    const int t1 = before_advance ? s.tl.n0 : s.tl.np1;
+    const int t1q = before_advance ? s.tl.n0_qdp : s.tl.np1_qdp;
+    diag_alloc();
+    launch_diag_energy(E, Q, T, v, ps_v, phis_d, qdp, t1, t1q, s.prm.use_cpstar ? 1 : 0, s.ps0, diag_d,
+                       g_stream);
+    post("diag_energy");
+    const size_t w = 16 * sizeof(double), n = (size_t)E * 16;
+    ck(cudaMemcpy2DAsync(s.diag[4] + (size_t)ivar * 16, 4 * w, diag_d, w, w, E, cudaMemcpyDeviceToHost, g_stream),
+       "D2H IEner");
+    ck(cudaMemcpyAsync(s.diag[5], diag_d + n, w * E, cudaMemcpyDeviceToHost, g_stream), "D2H IEner_wet");
+    ck(cudaMemcpy2DAsync(s.diag[6] + (size_t)ivar * 16, 4 * w, diag_d + 2 * n, w, w, E, cudaMemcpyDeviceToHost,
+                         g_stream), "D2H KEner");
+    ck(cudaMemcpy2DAsync(s.diag[7] + (size_t)ivar * 16, 4 * w, diag_d + 3 * n, w, w, E, cudaMemcpyDeviceToHost,
+                         g_stream), "D2H PEner");
+    ck(cudaStreamSynchronize(g_stream), "energy_halftimes");
+  }
+
+  // energies [4][E][16] then Qvar and Qmass [E][Q][16]
+  void diag_alloc() {
+    if (!diag_d) diag_d = dalloc<double>((size_t)E * 64 + (size_t)E * Q * 32);
+  }
+
+  void run_subcycle(double dt, int last_time_step) override {
     const Params& p = s.prm;
     const double dt_remap = p.rsplit > 0 ? dt * p.qsplit * p.rsplit : dt * p.qsplit;
+    // prim_driver.cpp:37-58; the arrays of init_diagnostics_c must be set
+    const int nstep_end = s.tl.nstep + (p.rsplit > 0 ? p.qsplit * p.rsplit : p.qsplit);
+    bool diag = (p.state_frequency > 0 && nstep_end % p.state_frequency == 0) || nstep_end == s.tl.nstep0 ||
+                nstep_end >= last_time_step;
+    if (p.disable_diagnostics || !s.diag[0]) diag = false;
+    if (diag) {
+      diag_scalars(true, 3);
+      energy_halftimes(true, 2);
+    }
     s.tl.update_tracers_levels(p.qsplit);
     // apply_cam_forcing (ftype 0) / apply_cam_forcing_dynamics (ftype 2), prim_driver.cpp:70-81
     if ((p.ftype == 0 || p.ftype == 2) && ft) {
       launch_cam_forcing(E, Q, T, v, ft, fm, p.ftype == 0 ? fq : nullptr, qdp, ps_v, Qc, s.tl.n0,
                          s.tl.n0_qdp, p.moist ? 1 : 0, dt_remap, s.ps0, g_stream);
       post("cam_forcing");
+    }
+    if (diag) {
+      energy_halftimes(true, 0);
+      diag_scalars(true, 0);
     }
     launch_dp_from_ps(E, dp, ps_v, s.tl.n0, s.ps0, g_stream);
     post("dp3d_from_ps");
@@ -556,8 +622,15 @@ struct BackendT : Backend {
     launch_update_q(E, Q, qdp, Qc, ps_v, s.tl.np1, s.tl.np1_qdp, s.ps0, g_stream);
     post("update_q");
     const int st = remap_status();
+    if (st) {
+      s.tl.update_dynamics_levels();
+      fail(101, "Negative (or nan) layer thickness detected, aborting!");
+    }
+    if (diag) {
+      diag_scalars(false, 1);
+      energy_halftimes(false, 1);
+    }
     s.tl.update_dynamics_levels();
-    if (st) fail(101, "Negative (or nan) layer thickness detected, aborting!");
   }
 
   // Field access in the Fortran layout of one time level.
@@ -983,7 +1056,7 @@ void init_simulation_params_c(const int* remap_alg, const int* limiter_option, c
                               const double* nu_q, const double* nu_s, const double* nu_div,
                               const double* nu_top, const int* hypervis_order, const int* hypervis_subcycle,
                               const double* hypervis_scaling, const int* ftype, const bool* prescribed_wind,
-                              const bool* moisture, const bool*, const bool*,
+                              const bool* moisture, const bool* disable_diagnostics, const bool* use_cpstar,
                               const bool* use_semi_lagrangian_transport) {
   run([&] {
     auto bad = [](const char* opt) {
@@ -1007,6 +1080,7 @@ void init_simulation_params_c(const int* remap_alg, const int* limiter_option, c
     p.nu = *nu; p.nu_p = *nu_p; p.nu_q = *nu_q; p.nu_s = *nu_s; p.nu_div = *nu_div; p.nu_top = *nu_top;
     p.hypervis_order = *hypervis_order; p.hypervis_subcycle = *hypervis_subcycle;
     p.hypervis_scaling = *hypervis_scaling; p.ftype = *ftype; p.moist = *moisture;
+    p.disable_diagnostics = *disable_diagnostics; p.use_cpstar = *use_cpstar;
     if (p.nu != p.nu_div) {
       const double ratio = p.nu_div / p.nu;
       if (p.hypervis_scaling != 0.0) { p.nu_ratio1 = ratio * ratio; p.nu_ratio2 = 1.0; }
@@ -1059,8 +1133,14 @@ void init_elements_states_c(const double* const* v, const double* const* T, cons
   });
 }
 
-void init_diagnostics_c(double* const*, double* const*, double* const*, double* const*, double* const*,
-                        double* const*, double* const*, double* const*) {}
+void init_diagnostics_c(double* const* q, double* const* qvar, double* const* qmass, double* const* q1mass,
+                        double* const* iener, double* const* iener_wet, double* const* kener,
+                        double* const* pener) {
+  run([&] {
+    double* const* a[8] = {q, qvar, qmass, q1mass, iener, iener_wet, kener, pener};
+    for (int i = 0; i < 8; ++i) S().diag[i] = *a[i];
+  });
+}
 
 void init_boundary_exchanges_c(void) {
   run([] {
@@ -1087,9 +1167,10 @@ void init_time_level_c(const int* nm1, const int* n0, const int* np1, const int*
   });
 }
 
-void prim_run_subcycle_c(const double* dt, int* nstep, int* nm1, int* n0, int* np1, const int*) {
+void prim_run_subcycle_c(const double* dt, int* nstep, int* nm1, int* n0, int* np1,
+                         const int* last_time_step) {
   run([&] {
-    B().run_subcycle(*dt);
+    B().run_subcycle(*dt, last_time_step ? *last_time_step : INT_MAX);
     const TimeLevel& t = S().tl;
     *nstep = t.nstep; *nm1 = t.nm1; *n0 = t.n0; *np1 = t.np1;
   });

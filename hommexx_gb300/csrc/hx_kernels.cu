@@ -416,6 +416,61 @@ __global__ void __launch_bounds__(EQ_THREADS) k_update_q(int Q, const double* qd
       qdp[((((size_t)e * QTL + np1_qdp) * Q + q) * NLEV + l) * 16 + p] / dp;
 }
 
+// Tracer mass diagnostics (Diagnostics.cpp:37-84): one thread per (element, tracer, GLL
+// point) sums its column of Qdp*Q and of Qdp at tracer level tq, level by level and
+// without fused multiply-adds, as the reference's host loop does.  Outputs [E][Q][16].
+__global__ void k_diag_scalars(int EQ, int Q, const double* __restrict__ qdp, const double* __restrict__ Qc,
+                               int tq, double* __restrict__ qvar, double* __restrict__ qmass) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= EQ * 16) return;
+  const int eq = i >> 4, p = i & 15, e = eq / Q, q = eq - e * Q;
+  const double* a = qdp + (((size_t)e * QTL + tq) * Q + q) * NLEV * 16 + p;
+  const double* b = Qc + (size_t)eq * NLEV * 16 + p;
+  double sqq = 0.0, sq = 0.0;
+#pragma unroll 8
+  for (int l = 0; l < NLEV; ++l) {
+    const double x = a[l * 16];
+    sqq = __dadd_rn(sqq, __dmul_rn(x, b[l * 16]));
+    sq = __dadd_rn(sq, x);
+  }
+  qvar[i] = sqq;
+  qmass[i] = sq;
+}
+
+// Column energies (Diagnostics.cpp:86-185): one thread per (element, GLL point) at
+// dynamics level t1, with dp = dA ps0 + dB ps_v and cp* = cp (1 + kq Qdp(tracer 1)/dp)
+// when cpstar, else cp.  Sums in level order without fused multiply-adds.
+// out: IEner, IEner_wet, KEner, PEner, each [E][16].
+__global__ void k_diag_energy(int E, int Q, const double* __restrict__ T, const double* __restrict__ v,
+                              const double* __restrict__ ps_v, const double* __restrict__ phis,
+                              const double* __restrict__ qdp, int t1, int t1q, int cpstar, double ps0,
+                              double cp, double kq, double* __restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= E * 16) return;
+  const int e = i >> 4, p = i & 15;
+  const double ps = ps_v[((size_t)e * NTL + t1) * 16 + p], ph = phis[i];
+  const double* tc = T + ((size_t)e * NTL + t1) * NLEV * 16 + p;
+  const double* vc = v + ((size_t)e * NTL + t1) * NLEV * 32 + p;
+  const double* qc = qdp + ((size_t)e * QTL + t1q) * Q * NLEV * 16 + p;  // tracer 1
+  double ie = 0.0, iew = 0.0, ke = 0.0, pe = 0.0;
+#pragma unroll 4
+  for (int l = 0; l < NLEV; ++l) {
+    const double dp = __dadd_rn(__dmul_rn(c_ai_delta[l], ps0), __dmul_rn(c_bi_delta[l], ps));
+    double cps = cp;
+    if (cpstar) cps = __dmul_rn(cp, __dadd_rn(1.0, __dmul_rn(kq, __ddiv_rn(qc[l * 16], dp))));
+    const double t = tc[l * 16], u = vc[l * 32], w = vc[l * 32 + 16];
+    ie = __dadd_rn(ie, __dmul_rn(__dmul_rn(cps, t), dp));
+    iew = __dadd_rn(iew, __dmul_rn(__dmul_rn(__dsub_rn(cps, cp), t), dp));
+    ke = __dadd_rn(ke, __dmul_rn(__dmul_rn(__dadd_rn(__dmul_rn(u, u), __dmul_rn(w, w)), 0.5), dp));
+    pe = __dadd_rn(pe, __dmul_rn(ph, dp));
+  }
+  const size_t n = (size_t)E * 16;
+  out[i] = ie;
+  out[n + i] = iew;
+  out[2 * n + i] = ke;
+  out[3 * n + i] = pe;
+}
+
 // CAM forcing (CamForcing.cpp:20-170).  Layouts: ft [E][72][16], fm [E][72][2][16],
 // fq [E][Q][72][16] (the Fortran layouts of the forcing arrays).
 __global__ void k_state_forcing(int E, double* T, double* v, const double* ft, const double* fm, int n0,
@@ -1385,6 +1440,24 @@ void launch_cam_forcing(int E, int Q, double* T, double* v, const double* ft, co
   if (moist) k_ps_forcing<<<nblk((long long)E * 16, 128), 128, 0, s>>>(E, Q, fq, qdp, ps_v, n0, n0_qdp, dt);
   k_tracer_forcing<<<dim3(E * Q, NLEV / EQ_LEVELS), EQ_THREADS, 0, s>>>(Q, fq, qdp, n0_qdp, dt);
   k_update_q<<<dim3(E * Q, NLEV / EQ_LEVELS), EQ_THREADS, 0, s>>>(Q, qdp, Qc, ps_v, n0, n0_qdp, ps0);
+}
+
+void launch_diag_scalars(int E, int Q, const double* qdp, const double* Qc, int tq, double* qvar,
+                         double* qmass, cudaStream_t s) {
+  if (Q == 0) return;
+  KScope k("diag_scalars", s);
+  k_diag_scalars<<<nblk((long long)E * Q * 16, 128), 128, 0, s>>>(E * Q, Q, qdp, Qc, tq, qvar, qmass);
+}
+
+void launch_diag_energy(int E, int Q, const double* T, const double* v, const double* ps_v, const double* phis,
+                        const double* qdp, int t1, int t1q, int cpstar, double ps0, double* out,
+                        cudaStream_t s) {
+  // PhysicalConstants.hpp:18-20
+  const double cp = 1005.0, cpwv = 1870.0;
+  const double kq = cpwv / cp - 1.0;
+  KScope k("diag_energy", s);
+  k_diag_energy<<<nblk((long long)E * 16, 128), 128, 0, s>>>(E, Q, T, v, ps_v, phis, qdp, t1, t1q,
+                                                               cpstar && Q > 0, ps0, cp, kq, out);
 }
 
 void launch_lap_matrix(const MetricP<double>& m, int E, double* out, cudaStream_t s) {

@@ -112,6 +112,13 @@ template <typename R> void launch_euler_step(EulerArgs<R>& a, int E, int time_av
 template <typename R> void launch_remap(const RemapArgs& a, cudaStream_t s);
 void launch_update_q(int E, int Q, const double* qdp, double* Qc, const double* ps_v, int np1,
                      int np1_qdp, double ps0, cudaStream_t s);
+// Energy and tracer mass diagnostics (Diagnostics.cpp): qvar/qmass [E][Q][16] at tracer
+// level tq; out = IEner, IEner_wet, KEner, PEner, each [E][16], at dynamics level t1.
+void launch_diag_scalars(int E, int Q, const double* qdp, const double* Qc, int tq, double* qvar,
+                         double* qmass, cudaStream_t s);
+void launch_diag_energy(int E, int Q, const double* T, const double* v, const double* ps_v, const double* phis,
+                        const double* qdp, int t1, int t1q, int cpstar, double ps0, double* out,
+                        cudaStream_t s);
 // Generic DSS of nf fields (field f at base + f*fs, element stride es, level stride ls).
 void launch_dss_inplace(int E, int nf, double* base, long long fs, long long es, int ls,
                         double* scratch, const double* rsmp, DssTable t, cudaStream_t s);

@@ -87,8 +87,15 @@ void init_elements_states_c(const double* const* v, const double* const* T,
                             const double* const* dp3d, const double* const* Qdp,
                             const double* const* ps_v);
 
-/* src/share/cxx/cxx_f90_interface.cpp:253-262 — diagnostics are off on the timed
- * step; the pointers are recorded only. */
+/* src/share/cxx/cxx_f90_interface.cpp:253-262 — host arrays elem%state%Q
+ * (np,np,nlev,qsize_d,nelemd) and elem%accum Qvar, Qmass (np,np,qsize_d,4,nelemd), Q1mass
+ * (np,np,qsize_d,nelemd), IEner, KEner, PEner (np,np,4,nelemd), IEner_wet (np,np,nelemd);
+ * qsize_d is qsize, as for Qdp.  A remap interval that computes diagnostics
+ * (prim_driver.cpp:49-58: nstep_end a multiple of state_frequency, equal to nstep0, or
+ * >= last_time_step; never with disable_diagnostics) writes them as Diagnostics.cpp does:
+ * Q and Qvar/Qmass slots 4, 1, 2 and IEner/KEner/PEner slots 3, 1, 2 (1-based), before
+ * forcing, after forcing and after the remap.  Until this is called, no interval computes
+ * diagnostics. */
 void init_diagnostics_c(double* const* q, double* const* qvar, double* const* qmass,
                         double* const* q1mass, double* const* iener,
                         double* const* iener_wet, double* const* kener,

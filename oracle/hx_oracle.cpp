@@ -22,6 +22,7 @@
 // jgp = Fortran i).
 
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -88,7 +89,7 @@ struct Params {
   int qsize = 0, state_frequency = 1, hypervis_order = 2, hypervis_subcycle = 1, ftype = -1;
   double nu = 0, nu_p = 0, nu_q = 0, nu_s = 0, nu_div = 0, nu_top = 0, hypervis_scaling = 0;
   double nu_ratio1 = 1, nu_ratio2 = 1;
-  bool moist = false, disable_diagnostics = true, set = false;
+  bool moist = false, disable_diagnostics = true, use_cpstar = false, set = false;
 };
 
 struct TimeLevel {
@@ -122,6 +123,8 @@ struct Ctx {
   // state
   std::vector<double> v, t, dp3d, ps_v, qdp, Qc;
   std::vector<double> fm, ft, fq;  // CAM forcing: FM [E][2][16][NLEV], FT/FQ level-contiguous
+  // init_diagnostics_c host arrays: Q, Qvar, Qmass, Q1mass, IEner, IEner_wet, KEner, PEner
+  double* diag[8] = {};
   std::vector<double> phi, omega_p, eta_dot_dpdn, derived_dp, divdp, divdp_proj,
       dpdiss_ave, dpdiss_bih, vn0;
   // buffers
@@ -1452,15 +1455,101 @@ void apply_cam_forcing(double dt, bool tracers) {
         }
 }
 
-void prim_run_subcycle(double dt, int& nstep, int& nm1, int& n0, int& np1) {  // prim_driver.cpp:31-156
+void push_block(const double* in, double* f, int ncomp);
+
+// Tracer mass diagnostics (Diagnostics.cpp:37-84): the mixing ratio is copied into the
+// host array Q (np,np,nlev,qsize,nelemd); per tracer and GLL point the column sums of
+// Qdp*Q and of Qdp at the call's tracer level go to Qvar(:,:,q,ivar), Qmass(:,:,q,ivar)
+// and Q1mass(:,:,q).
+void diag_scalars(bool before_advance, int ivar) {
+  Ctx& c = C();
+  c.tl.update_tracers_levels(c.prm.qsplit);
+  const int t2 = before_advance ? c.tl.n0_qdp : c.tl.np1_qdp;
+  if (c.prm.time_step_type <= 0) return;
+  const int Q = c.Q;
+  const size_t B = (size_t)NP2 * NLEV;
+  for (int e = 0; e < c.E; ++e)
+    for (int q = 0; q < Q; ++q)
+      push_block(&c.Qc[((size_t)e * Q + q) * B], c.diag[0] + ((size_t)e * Q + q) * B, 1);
+#pragma omp parallel for
+  for (int e = 0; e < c.E; ++e)
+    for (int q = 0; q < Q; ++q)
+      for (int p = 0; p < NP2; ++p) {
+        double sqq = 0.0, sq = 0.0;
+        for (int l = 0; l < NLEV; ++l) {
+          const double qd = c.qdp[IQ(e, t2, q, p, l, Q)];
+          sqq += qd * c.Qc[(((size_t)e * Q + q) * NP2 + p) * NLEV + l];
+          sq += qd;
+        }
+        const size_t k = (((size_t)e * 4 + ivar) * Q + q) * NP2 + p;
+        c.diag[1][k] = sqq;
+        c.diag[2][k] = sq;
+        c.diag[3][((size_t)e * Q + q) * NP2 + p] = sq;
+      }
+}
+
+// Column energies (Diagnostics.cpp:86-185) at the call's dynamics level, with the layer
+// thickness taken from ps_v: IEner = sum cp* T dp, IEner_wet = sum (cp* - cp) T dp,
+// KEner = sum (u^2 + v^2)/2 dp, PEner = sum phis dp; cp* = cp (1 + (cpv/cp - 1) q0) with
+// q0 = Qdp(tracer 1)/dp when use_cpstar, else cp.  cp = 1005, cpv = 1870
+// (PhysicalConstants.hpp:18-20).
+void energy_halftimes(bool before_advance, int ivar) {
+  Ctx& c = C();
+  c.tl.update_tracers_levels(c.prm.qsplit);
+  const int t1 = before_advance ? c.tl.n0 : c.tl.np1;
+  const int t1q = before_advance ? c.tl.n0_qdp : c.tl.np1_qdp;
+  const double cp = 1005.0, cpwv = 1870.0;
+  const bool cpstar = c.prm.use_cpstar && c.Q > 0;
+#pragma omp parallel for
+  for (int e = 0; e < c.E; ++e)
+    for (int p = 0; p < NP2; ++p) {
+      double ie = 0.0, iew = 0.0, ke = 0.0, pe = 0.0;
+      const double ps = c.ps_v[((size_t)e * NTL + t1) * NP2 + p], phis = c.phis[(size_t)e * NP2 + p];
+      for (int l = 0; l < NLEV; ++l) {
+        const double dp = c.ai_delta[l] * c.ps0 + c.bi_delta[l] * ps;
+        double cps = cp;
+        if (cpstar) cps = cp * (1.0 + (cpwv / cp - 1.0) * (c.qdp[IQ(e, t1q, 0, p, l, c.Q)] / dp));
+        const double T = c.t[IS(e, t1, p, l)];
+        const double u = c.v[IV(e, t1, 0, p, l)], v = c.v[IV(e, t1, 1, p, l)];
+        ie += cps * T * dp;
+        iew += (cps - cp) * T * dp;
+        ke += (u * u + v * v) * 0.5 * dp;
+        pe += phis * dp;
+      }
+      const size_t k = ((size_t)e * 4 + ivar) * NP2 + p;
+      c.diag[4][k] = ie;
+      c.diag[5][(size_t)e * NP2 + p] = iew;
+      c.diag[6][k] = ke;
+      c.diag[7][k] = pe;
+    }
+}
+
+void prim_run_subcycle(double dt, int& nstep, int& nm1, int& n0, int& np1,
+                       int last_time_step) {  // prim_driver.cpp:31-156
   Ctx& c = C();
   const Params& pr = c.prm;
   const double dt_q = dt * pr.qsplit;
   double dt_remap = dt_q;
-  if (pr.rsplit > 0) dt_remap = dt_q * pr.rsplit;
+  int nstep_end = c.tl.nstep + pr.qsplit;
+  if (pr.rsplit > 0) {
+    dt_remap = dt_q * pr.rsplit;
+    nstep_end = c.tl.nstep + pr.qsplit * pr.rsplit;
+  }
+  // prim_driver.cpp:49-58; the arrays of init_diagnostics_c must be set
+  bool diag = (pr.state_frequency > 0 && nstep_end % pr.state_frequency == 0) ||
+              nstep_end == c.tl.nstep0 || nstep_end >= last_time_step;
+  if (pr.disable_diagnostics || !c.diag[0]) diag = false;
+  if (diag) {
+    diag_scalars(true, 3);
+    energy_halftimes(true, 2);
+  }
   c.tl.update_tracers_levels(pr.qsplit);
   if (pr.ftype == 0) apply_cam_forcing(dt_remap, true);
   else if (pr.ftype == 2) apply_cam_forcing(dt_remap, false);
+  if (diag) {
+    energy_halftimes(true, 0);
+    diag_scalars(true, 0);
+  }
   // dp3d from ps_v
   const int tn0 = c.tl.n0;
 #pragma omp parallel for
@@ -1490,6 +1579,10 @@ void prim_run_subcycle(double dt, int& nstep, int& nm1, int& n0, int& np1) {  //
           const double dp = c.ai_delta[l] * c.ps0 + c.bi_delta[l] * c.ps_v[((size_t)e * NTL + tnp1) * NP2 + p];
           c.Qc[(((size_t)e * c.Q + q) * NP2 + p) * NLEV + l] = c.qdp[IQ(e, np1_qdp, q, p, l, c.Q)] / dp;
         }
+  if (diag) {
+    diag_scalars(false, 1);
+    energy_halftimes(false, 1);
+  }
   c.tl.update_dynamics_levels();
   nstep = c.tl.nstep;
   nm1 = c.tl.nm1;
@@ -1557,7 +1650,7 @@ void init_simulation_params_c(const int* remap_alg, const int* limiter_option, c
                               const int* hypervis_order, const int* hypervis_subcycle,
                               const double* hypervis_scaling, const int* ftype,
                               const bool* prescribed_wind, const bool* moisture,
-                              const bool* disable_diagnostics, const bool*,
+                              const bool* disable_diagnostics, const bool* use_cpstar,
                               const bool* use_semi_lagrangian_transport) {
   Ctx& c = C();
   c.last_err = 0;
@@ -1594,6 +1687,7 @@ void init_simulation_params_c(const int* remap_alg, const int* limiter_option, c
   p.ftype = *ftype;
   p.moist = *moisture;
   p.disable_diagnostics = *disable_diagnostics;
+  p.use_cpstar = *use_cpstar;
   if (p.nu != p.nu_div) {
     const double ratio = p.nu_div / p.nu;
     if (p.hypervis_scaling != 0.0) {
@@ -1687,8 +1781,12 @@ void init_elements_states_c(const double* const* v, const double* const* T,
   std::memcpy(c.ps_v.data(), *ps_v, sizeof(double) * c.E * NTL * NP2);
 }
 
-void init_diagnostics_c(double* const*, double* const*, double* const*, double* const*,
-                        double* const*, double* const*, double* const*, double* const*) {}
+void init_diagnostics_c(double* const* q, double* const* qvar, double* const* qmass,
+                        double* const* q1mass, double* const* iener, double* const* iener_wet,
+                        double* const* kener, double* const* pener) {
+  double* const* a[8] = {q, qvar, qmass, q1mass, iener, iener_wet, kener, pener};
+  for (int i = 0; i < 8; ++i) C().diag[i] = *a[i];
+}
 
 void init_boundary_exchanges_c(void) { build_tables(); }
 
@@ -1702,9 +1800,10 @@ void init_time_level_c(const int* nm1, const int* n0, const int* np1, const int*
   c.tl.nstep0 = *nstep0;
 }
 
-void prim_run_subcycle_c(const double* dt, int* nstep, int* nm1, int* n0, int* np1, const int*) {
+void prim_run_subcycle_c(const double* dt, int* nstep, int* nm1, int* n0, int* np1,
+                         const int* last_time_step) {
   C().last_err = 0;
-  prim_run_subcycle(*dt, *nstep, *nm1, *n0, *np1);
+  prim_run_subcycle(*dt, *nstep, *nm1, *n0, *np1, last_time_step ? *last_time_step : INT_MAX);
 }
 
 void cxx_push_results_to_f90(double* const* v, double* const* T, double* const* dp3d,

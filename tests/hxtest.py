@@ -57,13 +57,15 @@ def lib(path: str) -> abi.HxLibrary:
     return _LIBS[path]
 
 
-def setup(path: str, ne: int = 4, Q: int = 4, precision: int = 0, **kw) -> abi.HxLibrary:
-    """(Re)initialise the library at ``path`` with the seeded state."""
+def setup(path: str, ne: int = 4, Q: int = 4, precision: int = 0, diagnostics: bool = False,
+          **kw) -> abi.HxLibrary:
+    """(Re)initialise the library at ``path`` with the seeded state; with ``diagnostics``
+    the host arrays of init_diagnostics_c are set up too (``L.diag``)."""
     L = lib(path)
     if L.nelem:
         L.finalize()
     p = abi.SimParams(qsize=Q, **kw)
-    L.init(mesh(ne), hvc(), p, state(ne, Q), precision=precision)
+    L.init(mesh(ne), hvc(), p, state(ne, Q), precision=precision, diagnostics=diagnostics)
     return L
 
 

@@ -202,6 +202,36 @@ def test_cam_forcing(pair, ftype, moist):
     assert np.array_equal(fg["FT"], FT)
 
 
+@pytest.mark.parametrize("cpstar,ftype", [(False, -1), (True, 0)])
+def test_diagnostics(pair, cpstar, ftype):
+    """Energy and tracer mass diagnostics (Diagnostics.cpp) written into the
+    init_diagnostics_c host arrays over two remap intervals (CAM forcing between the
+    before-forcing and after-forcing slots when ftype is 0).  The slots computed before the
+    first step, from identical inputs, agree bit for bit; the rest within 1e-12; the
+    untouched slots stay untouched on both sides."""
+    g, o = pair(rsplit=3, ftype=ftype, moisture=cpstar, use_cpstar=cpstar, disable_diagnostics=False,
+                state_frequency=1, diagnostics=True)
+    FM, FT, FQ, Qdp = _forcing(4, 4, 21)
+    for it in range(2):
+        for L in (g, o):
+            if ftype == 0:
+                L.push_forcing(FM, FT, FQ, Qdp if it == 0 else L.push_results()["Qdp"])
+            L.run_subcycle(DT)
+        if it == 0:
+            for k in ("IEner", "KEner", "PEner"):
+                assert np.array_equal(g.diag[k][:, 2], o.diag[k][:, 2]), k
+            for k in ("Qvar", "Qmass"):
+                assert np.array_equal(g.diag[k][:, 3], o.diag[k][:, 3]), k
+        errs = {}
+        for k in g.diag:
+            a, b = g.diag[k], o.diag[k]
+            assert np.array_equal(np.isnan(a), np.isnan(b)), k
+            ok = ~np.isnan(b)
+            errs[k] = H.rel_err(a[ok], b[ok])
+        _assert_close(errs)
+    assert np.isnan(g.diag["IEner"][:, 3]).all() and np.isnan(g.diag["Qvar"][:, 2]).all()
+
+
 def test_mass_conservation_gpu(pair):
     g, _ = pair(rsplit=3)
     m = H.mesh(4)
