@@ -9,6 +9,7 @@ the boundary as a plain pointer.
 from __future__ import annotations
 
 import ctypes as C
+import struct
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -93,6 +94,8 @@ class HxLibrary:
         L.hx_run_remap.argtypes = [C.c_int, C.c_int, C.c_double]
         L.hx_run_prim_step.argtypes = [C.c_double]
         L.hx_run_dss.argtypes = [C.c_char_p, C.c_int, C.c_int]
+        L.hx_write_restart.argtypes = [C.c_char_p]
+        L.hx_read_restart.argtypes = [C.c_char_p]
         L.hx_launch_count.restype = C.c_longlong
         L.hx_kernel_stats.argtypes = [C.c_char_p, C.c_int, C.POINTER(C.c_longlong),
                                       C.POINTER(C.c_double), C.c_int]
@@ -193,6 +196,32 @@ class HxLibrary:
         self.check("prim_run_subcycle_c")
         self.tl = [nm1.value, n0.value, np1.value, nstep.value]
         return self.tl
+
+    # -- restart files (format of include/hxgpu.h) -------------------------------------
+    RESTART_HEADER = struct.Struct("<8sII6i5iiQQ48s")
+
+    def write_restart(self, path) -> None:
+        rc = self.lib.hx_write_restart(str(path).encode())
+        if rc:
+            self.check(f"hx_write_restart({path})")
+
+    def read_restart(self, path) -> None:
+        """Replace the session's state and time levels with the file's."""
+        rc = self.lib.hx_read_restart(str(path).encode())
+        if rc:
+            self.check(f"hx_read_restart({path})")
+        h = self.read_restart_header(path)
+        self.tl = [h["nm1"] - 1, h["n0"] - 1, h["np1"] - 1, h["nstep"]]
+
+    @classmethod
+    def read_restart_header(cls, path) -> dict:
+        with open(path, "rb") as f:
+            raw = f.read(cls.RESTART_HEADER.size)
+        v = cls.RESTART_HEADER.unpack(raw)
+        keys = ("magic", "version", "header_bytes", "nelem", "np", "nlev", "qsize", "timelevels",
+                "qsize_timelevels", "nm1", "n0", "np1", "nstep", "nstep0", "reserved0",
+                "record_bytes", "checksum", "reserved")
+        return dict(zip(keys, v))
 
     def push_results(self, out: dict | None = None):
         E, Q = self.nelem, self.qsize

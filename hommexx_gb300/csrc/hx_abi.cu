@@ -13,6 +13,7 @@
 // once from the add_connection calls (src/share/cxx/mpi/Connectivity.cpp:77-170).
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -139,6 +140,8 @@ struct Backend {
                             double* vo, double* To, double* dpo) = 0;
   virtual void traj_vjp(const double* vb, const double* Tb, const double* dpb, double* vg, double* Tg,
                         double* dpg) = 0;
+  virtual void write_restart(const std::string& path) = 0;
+  virtual void read_restart(const std::string& path) = 0;
 };
 
 struct Session;
@@ -631,6 +634,164 @@ struct BackendT : Backend {
       energy_halftimes(false, 1);
     }
     s.tl.update_dynamics_levels();
+  }
+
+  // ---- restart files (format in include/hxgpu.h) ----------------------------------------
+  // The element record's segments: each is one element's block of a device array, the
+  // device arrays being element-major in the Fortran layout the record uses.
+  struct Seg {
+    double* dev;
+    size_t words;
+  };
+  std::vector<Seg> restart_segments() {
+    return {{v, (size_t)NTL * NLEV * 32}, {T, (size_t)NTL * NLEV * 16}, {dp, (size_t)NTL * NLEV * 16},
+            {ps_v, (size_t)NTL * 16},     {phis_d, 16},                 {Qc, (size_t)Q * NLEV * 16},
+            {qdp, (size_t)QTL * Q * NLEV * 16}};
+  }
+  static size_t record_words(const std::vector<Seg>& segs) {
+    size_t n = 0;
+    for (const Seg& g : segs) n += g.words;
+    return n;
+  }
+  unsigned long long restart_checksum(const std::vector<Seg>& segs) {
+    const size_t rw = record_words(segs);
+    unsigned long long* d = dalloc<unsigned long long>(1);
+    size_t off = 0;
+    for (const Seg& g : segs) {
+      launch_restart_checksum(g.dev, E, (int)g.words, (long long)rw, (long long)off, d, g_stream);
+      off += g.words;
+    }
+    unsigned long long h = 0;
+    cudaError_t e1 = cudaGetLastError();
+    cudaError_t e2 = cudaMemcpyAsync(&h, d, sizeof(h), cudaMemcpyDeviceToHost, g_stream);
+    cudaError_t e3 = cudaStreamSynchronize(g_stream);
+    cudaFree(d);
+    ck(e1, "restart checksum");
+    ck(e2, "restart checksum D2H");
+    ck(e3, "restart checksum");
+    return h;
+  }
+  // Two pinned host buffers of up to 256 MiB of whole element records, and the events
+  // that say when the copies from/into each have finished.
+  struct Staging {
+    char* buf[2] = {nullptr, nullptr};
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+    int per = 1;  // element records per buffer
+    void init(size_t rec_bytes, int E) {
+      const size_t cap = (size_t)256 << 20;
+      per = (int)std::max<size_t>(1, std::min<size_t>((size_t)E, cap / rec_bytes));
+      for (int b = 0; b < 2; ++b) {
+        ck(cudaMallocHost(&buf[b], rec_bytes * per), "cudaMallocHost restart staging");
+        ck(cudaEventCreateWithFlags(&ev[b], cudaEventDisableTiming), "cudaEventCreate");
+      }
+    }
+    ~Staging() {
+      cudaStreamSynchronize(g_stream);
+      for (int b = 0; b < 2; ++b) {
+        if (buf[b]) cudaFreeHost(buf[b]);
+        if (ev[b]) cudaEventDestroy(ev[b]);
+      }
+    }
+  };
+  struct File {
+    FILE* f;
+    ~File() {
+      if (f) fclose(f);
+    }
+  };
+
+  void write_restart(const std::string& path) override {
+    const std::vector<Seg> segs = restart_segments();
+    const size_t rw = record_words(segs), rb = rw * 8;
+    hx_restart_header h;
+    std::memset(&h, 0, sizeof(h));
+    std::memcpy(h.magic, HX_RESTART_MAGIC, 8);
+    h.version = HX_RESTART_VERSION;
+    h.header_bytes = sizeof(h);
+    h.nelem = E; h.np = 4; h.nlev = NLEV; h.qsize = Q; h.timelevels = NTL; h.qsize_timelevels = QTL;
+    h.nm1 = s.tl.nm1 + 1; h.n0 = s.tl.n0 + 1; h.np1 = s.tl.np1 + 1; h.nstep = s.tl.nstep; h.nstep0 = s.tl.nstep0;
+    h.record_bytes = rb;
+    h.checksum = restart_checksum(segs);
+    File f{std::fopen(path.c_str(), "wb")};
+    if (!f.f) fail(HX_ERR_IO, "cannot open restart file '" + path + "' for writing");
+    if (std::fwrite(&h, sizeof(h), 1, f.f) != 1) fail(HX_ERR_IO, "write error on '" + path + "'");
+    Staging st;
+    st.init(rb, E);
+    const int nchunk = (E + st.per - 1) / st.per;
+    auto put = [&](int k) {  // write chunk k once its copies have landed
+      const int b = k & 1, e0 = k * st.per, n = std::min(st.per, E - e0);
+      ck(cudaEventSynchronize(st.ev[b]), "restart D2H");
+      if (std::fwrite(st.buf[b], rb, n, f.f) != (size_t)n) fail(HX_ERR_IO, "write error on '" + path + "'");
+    };
+    for (int k = 0; k < nchunk; ++k) {
+      const int b = k & 1, e0 = k * st.per, n = std::min(st.per, E - e0);
+      size_t off = 0;
+      for (const Seg& g : segs) {
+        if (g.words) {
+          const size_t w = g.words * 8;
+          ck(cudaMemcpy2DAsync(st.buf[b] + off, rb, g.dev + (size_t)e0 * g.words, w, w, n, cudaMemcpyDeviceToHost,
+                               g_stream), "restart D2H");
+        }
+        off += g.words * 8;
+      }
+      ck(cudaEventRecord(st.ev[b], g_stream), "cudaEventRecord");
+      if (k > 0) put(k - 1);
+    }
+    put(nchunk - 1);
+    FILE* ff = f.f;
+    f.f = nullptr;
+    if (std::fclose(ff) != 0) fail(HX_ERR_IO, "write error on '" + path + "'");
+  }
+
+  void read_restart(const std::string& path) override {
+    const std::vector<Seg> segs = restart_segments();
+    const size_t rw = record_words(segs), rb = rw * 8;
+    File f{std::fopen(path.c_str(), "rb")};
+    if (!f.f) fail(HX_ERR_IO, "cannot open restart file '" + path + "'");
+    hx_restart_header h;
+    if (std::fread(&h, sizeof(h), 1, f.f) != 1) fail(HX_ERR_IO, "'" + path + "': short header");
+    if (std::memcmp(h.magic, HX_RESTART_MAGIC, 8) != 0 || h.header_bytes != sizeof(h))
+      fail(HX_ERR_IO, "'" + path + "' is not a restart file");
+    if (h.version != HX_RESTART_VERSION) fail(HX_ERR_IO, "'" + path + "': restart version does not match");
+    if (h.nelem != E || h.np != 4 || h.nlev != NLEV || h.qsize != Q || h.timelevels != NTL ||
+        h.qsize_timelevels != QTL || h.record_bytes != rb)
+      fail(HX_ERR_IO, "'" + path + "': restart file does not match the session (nelem " + std::to_string(h.nelem) +
+                          ", qsize " + std::to_string(h.qsize) + ", np " + std::to_string(h.np) + ", nlev " +
+                          std::to_string(h.nlev) + ")");
+    for (int t : {h.nm1, h.n0, h.np1})
+      if (t < 1 || t > NTL) fail(HX_ERR_IO, "'" + path + "': bad time level in header");
+    std::vector<double> phis_h((size_t)E * 16);
+    size_t phis_off = 0;
+    for (const Seg& g : segs) {
+      if (g.dev == phis_d) break;
+      phis_off += g.words * 8;
+    }
+    {
+      Staging st;
+      st.init(rb, E);
+      const int nchunk = (E + st.per - 1) / st.per;
+      for (int k = 0; k < nchunk; ++k) {
+        const int b = k & 1, e0 = k * st.per, n = std::min(st.per, E - e0);
+        if (k >= 2) ck(cudaEventSynchronize(st.ev[b]), "restart H2D");
+        if (std::fread(st.buf[b], rb, n, f.f) != (size_t)n) fail(HX_ERR_IO, "'" + path + "': short read");
+        for (int i = 0; i < n; ++i)
+          std::memcpy(&phis_h[(size_t)(e0 + i) * 16], st.buf[b] + (size_t)i * rb + phis_off, 16 * sizeof(double));
+        size_t off = 0;
+        for (const Seg& g : segs) {
+          if (g.words) {
+            const size_t w = g.words * 8;
+            ck(cudaMemcpy2DAsync(g.dev + (size_t)e0 * g.words, w, st.buf[b] + off, rb, w, n, cudaMemcpyHostToDevice,
+                                 g_stream), "restart H2D");
+          }
+          off += g.words * 8;
+        }
+        ck(cudaEventRecord(st.ev[b], g_stream), "cudaEventRecord");
+      }
+    }
+    if (restart_checksum(segs) != h.checksum) fail(HX_ERR_IO, "'" + path + "': checksum mismatch");
+    to_dev_R(phis, phis_h.data(), phis_h.size());
+    s.tl.nm1 = h.nm1 - 1; s.tl.n0 = h.n0 - 1; s.tl.np1 = h.np1 - 1;
+    s.tl.nstep = h.nstep; s.tl.nstep0 = h.nstep0;
   }
 
   // Field access in the Fortran layout of one time level.
@@ -1329,6 +1490,20 @@ int hx_traj_set_checkpointing(int mode) {
   return run([&] {
     if (mode < 0 || mode > 2) fail(HX_ERR_STATE, "hx_traj_set_checkpointing: mode must be 0, 1 or 2");
     S().traj_mode = mode;
+  });
+}
+
+int hx_write_restart(const char* path) {
+  return run([&] {
+    if (!path) fail(HX_ERR_IO, "hx_write_restart: null path");
+    B().write_restart(path);
+  });
+}
+
+int hx_read_restart(const char* path) {
+  return run([&] {
+    if (!path) fail(HX_ERR_IO, "hx_read_restart: null path");
+    B().read_restart(path);
   });
 }
 

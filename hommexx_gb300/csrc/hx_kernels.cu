@@ -471,6 +471,34 @@ __global__ void k_diag_energy(int E, int Q, const double* __restrict__ T, const 
   out[3 * n + i] = pe;
 }
 
+// Restart-file checksum: the sum modulo 2^64 of splitmix64(w_k + (k + 1) * golden) over
+// the file's record words w_k.  Element e's segment of `words` words sits at src + e*words
+// and its word j at record index k = e*rec_words + off + j.  One block per element.
+__device__ __forceinline__ unsigned long long splitmix64(unsigned long long z) {
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+
+__global__ void __launch_bounds__(256) k_restart_checksum(const unsigned long long* __restrict__ src, int words,
+                                                          long long rec_words, long long off,
+                                                          unsigned long long* out) {
+  __shared__ unsigned long long part[8];
+  const int e = blockIdx.x;
+  const unsigned long long* p = src + (size_t)e * words;
+  const unsigned long long k0 = (unsigned long long)e * rec_words + off + 1;
+  unsigned long long acc = 0;
+  for (int j = threadIdx.x; j < words; j += blockDim.x) acc += splitmix64(p[j] + (k0 + j) * 0x9E3779B97F4A7C15ull);
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+  if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned long long t = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += part[w];
+    atomicAdd(out, t);
+  }
+}
+
 // CAM forcing (CamForcing.cpp:20-170).  Layouts: ft [E][72][16], fm [E][72][2][16],
 // fq [E][Q][72][16] (the Fortran layouts of the forcing arrays).
 __global__ void k_state_forcing(int E, double* T, double* v, const double* ft, const double* fm, int n0,
@@ -1458,6 +1486,14 @@ void launch_diag_energy(int E, int Q, const double* T, const double* v, const do
   KScope k("diag_energy", s);
   k_diag_energy<<<nblk((long long)E * 16, 128), 128, 0, s>>>(E, Q, T, v, ps_v, phis, qdp, t1, t1q,
                                                                cpstar && Q > 0, ps0, cp, kq, out);
+}
+
+void launch_restart_checksum(const double* src, int E, int words, long long rec_words, long long off,
+                             unsigned long long* out, cudaStream_t s) {
+  if (words <= 0 || E <= 0) return;
+  KScope k("restart_checksum", s);
+  k_restart_checksum<<<E, 256, 0, s>>>(reinterpret_cast<const unsigned long long*>(src), words, rec_words, off,
+                                       out);
 }
 
 void launch_lap_matrix(const MetricP<double>& m, int E, double* out, cudaStream_t s) {

@@ -99,6 +99,10 @@ void launch_cam_forcing(int E, int Q, double* T, double* v, const double* ft, co
                         int moist, double dt, double ps0, cudaStream_t s);
 // Dense weak Laplacian per element ([E][16][16]) from the FP64 metric.
 void launch_lap_matrix(const MetricP<double>& m, int E, double* out, cudaStream_t s);
+// Restart-file checksum of E element segments (segment e at src + e*words, its word j at
+// record word index e*rec_words + off + j), added to *out.
+void launch_restart_checksum(const double* src, int E, int words, long long rec_words, long long off,
+                             unsigned long long* out, cudaStream_t s);
 void launch_prim_step_init(int E, double* eta, double* vn0, double* omega_p, double* dpa,
                            double* dpb, double* derived_dp, const double* dp, int n0, int zero_diss,
                            cudaStream_t s);

@@ -135,7 +135,8 @@ void cxx_push_forcing_to_f90(double* FM, double* FT, double* FQ);
 /* ---- Additions (no counterpart in the reference) ------------------------------------ */
 
 /* Status of the last call: 0 on success, else the reference's error code
- * (11, 12, 13, 101) or HX_ERR_CUDA; the message is copied into buf. */
+ * (11, 12, 13, 101), HX_ERR_CUDA, HX_ERR_STATE or HX_ERR_IO; the message is copied into
+ * buf. */
 #define HX_ERR_CUDA 200
 #define HX_ERR_STATE 201
 int hx_last_error(char* buf, int buflen);
@@ -235,6 +236,42 @@ int hx_traj_vjp(const double* v_bar, const double* T_bar, const double* dp3d_bar
 int hx_traj_jvp(const double* dv, const double* dT, const double* ddp3d, double* v_tan,
                 double* T_tan, double* dp3d_tan);
 int hx_traj_set_checkpointing(int mode);
+
+/* ---- Restart files (no counterpart in the reference's C++ layer) ------------------
+ * A binary restart format in place of the Fortran restart_io_mod.F90 (WriteRestart /
+ * ReadRestart, src/restart_io_mod.F90:626-698): a 128-byte header, then one record per
+ * element holding the prognostic elem_state_t of src/share/element_mod.F90:103-115 in
+ * its Fortran layouts, in this order:
+ *   v (np,np,2,nlev,3)  T (np,np,nlev,3)  dp3d (np,np,nlev,3)  ps_v (np,np,3)
+ *   phis (np,np)  Q (np,np,nlev,qsize)  Qdp (np,np,nlev,qsize,2)
+ * All numbers little-endian; doubles are IEEE binary64.  The header keeps the
+ * reference's TimeLevel_t (nm1, n0, np1 1-based; nstep, nstep0) and is checked on
+ * read against the session (nelem, np, nlev, qsize), as CheckRestartHeader checks ne,
+ * np and nlev (src/restart_io_mod.F90:440-471).  checksum is the sum modulo 2^64, over
+ * the 64-bit words w_k of all records (k = 0, 1, ... from the first record), of
+ * splitmix64(w_k + (k + 1) * 0x9E3779B97F4A7C15), splitmix64 being the output
+ * function z ^= z >> 30; z *= 0xBF58476D1CE4E5B9; z ^= z >> 27; z *= 0x94D049BB133111EB;
+ * z ^= z >> 31 (Steele, Lea and Flood, OOPSLA 2014).
+ * hx_write_restart writes the session's state and time levels; hx_read_restart
+ * replaces them (phis included).  Both stream the records through host buffers of at
+ * most 256 MiB, so device memory use does not grow.  Errors: HX_ERR_IO (open, read,
+ * write, bad magic or version, size mismatch, checksum), HX_ERR_STATE (no session). */
+#define HX_ERR_IO 202
+#define HX_RESTART_MAGIC "HXRESTRT"
+#define HX_RESTART_VERSION 1
+typedef struct hx_restart_header {
+  char magic[8];         /* HX_RESTART_MAGIC, not NUL-terminated */
+  unsigned int version;  /* HX_RESTART_VERSION */
+  unsigned int header_bytes;  /* 128 */
+  int nelem, np, nlev, qsize, timelevels, qsize_timelevels;  /* -, 4, 72, -, 3, 2 */
+  int nm1, n0, np1, nstep, nstep0;  /* TimeLevel_t, levels 1-based */
+  int reserved0;
+  unsigned long long record_bytes;  /* bytes of one element record */
+  unsigned long long checksum;
+  char reserved[48];
+} hx_restart_header;
+int hx_write_restart(const char* path);
+int hx_read_restart(const char* path);
 
 /* Page-lock (pin) host memory so init/push copies run at full link bandwidth. */
 int hx_host_register(void* ptr, size_t bytes);

@@ -1873,6 +1873,130 @@ void cxx_push_forcing_to_f90(double* FM, double* FT, double* FQ) {
   }
 }
 
+// Restart files (format and checksum as documented in include/hxgpu.h): records
+// restate the prognostic elem_state_t of src/share/element_mod.F90:103-115, the header
+// the TimeLevel_t and the size checks of src/restart_io_mod.F90:401-471.
+static unsigned long long splitmix64(unsigned long long z) {
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+static size_t restart_record_words(int Q) {
+  return (size_t)NTL * NLEV * 32 + 2 * (size_t)NTL * NLEV * 16 + NTL * 16 + 16 + (size_t)Q * NLEV * 16 +
+         (size_t)QTL * Q * NLEV * 16;
+}
+static unsigned long long restart_sum(const double* rec, size_t words, unsigned long long k0) {
+  unsigned long long acc = 0;
+  for (size_t j = 0; j < words; ++j) {
+    unsigned long long w;
+    std::memcpy(&w, rec + j, 8);
+    acc += splitmix64(w + (k0 + j + 1) * 0x9E3779B97F4A7C15ull);
+  }
+  return acc;
+}
+static void pack_record(int e, double* r) {
+  Ctx& c = C();
+  const size_t B = (size_t)NP2 * NLEV;
+  for (int tl = 0; tl < NTL; ++tl) push_block(&c.v[IV(e, tl, 0, 0, 0)], r + tl * 2 * B, 2);
+  r += NTL * 2 * B;
+  for (int tl = 0; tl < NTL; ++tl) push_block(&c.t[IS(e, tl, 0, 0)], r + tl * B, 1);
+  r += NTL * B;
+  for (int tl = 0; tl < NTL; ++tl) push_block(&c.dp3d[IS(e, tl, 0, 0)], r + tl * B, 1);
+  r += NTL * B;
+  std::memcpy(r, &c.ps_v[(size_t)e * NTL * NP2], sizeof(double) * NTL * NP2);
+  r += NTL * NP2;
+  std::memcpy(r, &c.phis[(size_t)e * NP2], sizeof(double) * NP2);
+  r += NP2;
+  for (int q = 0; q < c.Q; ++q) push_block(&c.Qc[((size_t)e * c.Q + q) * B], r + q * B, 1);
+  r += (size_t)c.Q * B;
+  for (int qt = 0; qt < QTL; ++qt)
+    for (int q = 0; q < c.Q; ++q) push_block(&c.qdp[IQ(e, qt, q, 0, 0, c.Q)], r + ((size_t)qt * c.Q + q) * B, 1);
+}
+static void unpack_record(int e, const double* r) {
+  Ctx& c = C();
+  const size_t B = (size_t)NP2 * NLEV;
+  for (int tl = 0; tl < NTL; ++tl) pull_block(r + tl * 2 * B, &c.v[IV(e, tl, 0, 0, 0)], 2);
+  r += NTL * 2 * B;
+  for (int tl = 0; tl < NTL; ++tl) pull_block(r + tl * B, &c.t[IS(e, tl, 0, 0)], 1);
+  r += NTL * B;
+  for (int tl = 0; tl < NTL; ++tl) pull_block(r + tl * B, &c.dp3d[IS(e, tl, 0, 0)], 1);
+  r += NTL * B;
+  std::memcpy(&c.ps_v[(size_t)e * NTL * NP2], r, sizeof(double) * NTL * NP2);
+  r += NTL * NP2;
+  std::memcpy(&c.phis[(size_t)e * NP2], r, sizeof(double) * NP2);
+  r += NP2;
+  for (int q = 0; q < c.Q; ++q) pull_block(r + q * B, &c.Qc[((size_t)e * c.Q + q) * B], 1);
+  r += (size_t)c.Q * B;
+  for (int qt = 0; qt < QTL; ++qt)
+    for (int q = 0; q < c.Q; ++q) pull_block(r + ((size_t)qt * c.Q + q) * B, &c.qdp[IQ(e, qt, q, 0, 0, c.Q)], 1);
+}
+
+int hx_write_restart(const char* path) {
+  Ctx& c = C();
+  c.last_err = 0;
+  if (c.E == 0) { set_error(HX_ERR_STATE, "library not initialised"); return HX_ERR_STATE; }
+  const size_t rw = restart_record_words(c.Q);
+  hx_restart_header h;
+  std::memset(&h, 0, sizeof(h));
+  std::memcpy(h.magic, HX_RESTART_MAGIC, 8);
+  h.version = HX_RESTART_VERSION;
+  h.header_bytes = sizeof(h);
+  h.nelem = c.E; h.np = NP; h.nlev = NLEV; h.qsize = c.Q; h.timelevels = NTL; h.qsize_timelevels = QTL;
+  h.nm1 = c.tl.nm1 + 1; h.n0 = c.tl.n0 + 1; h.np1 = c.tl.np1 + 1; h.nstep = c.tl.nstep; h.nstep0 = c.tl.nstep0;
+  h.record_bytes = rw * 8;
+  std::vector<double> all((size_t)c.E * rw);
+  unsigned long long sum = 0;
+  for (int e = 0; e < c.E; ++e) {
+    pack_record(e, &all[(size_t)e * rw]);
+    sum += restart_sum(&all[(size_t)e * rw], rw, (unsigned long long)e * rw);
+  }
+  h.checksum = sum;
+  FILE* f = path ? std::fopen(path, "wb") : nullptr;
+  if (!f) { set_error(HX_ERR_IO, "cannot open restart file for writing"); return HX_ERR_IO; }
+  bool ok = std::fwrite(&h, sizeof(h), 1, f) == 1 && std::fwrite(all.data(), 8, all.size(), f) == all.size();
+  ok = (std::fclose(f) == 0) && ok;
+  if (!ok) { set_error(HX_ERR_IO, "write error on restart file"); return HX_ERR_IO; }
+  return 0;
+}
+
+int hx_read_restart(const char* path) {
+  Ctx& c = C();
+  c.last_err = 0;
+  if (c.E == 0) { set_error(HX_ERR_STATE, "library not initialised"); return HX_ERR_STATE; }
+  auto err = [&](const std::string& m) { set_error(HX_ERR_IO, m); return HX_ERR_IO; };
+  FILE* f = path ? std::fopen(path, "rb") : nullptr;
+  if (!f) return err("cannot open restart file");
+  const size_t rw = restart_record_words(c.Q);
+  hx_restart_header h;
+  std::vector<double> all;
+  bool ok = std::fread(&h, sizeof(h), 1, f) == 1;
+  if (ok && (std::memcmp(h.magic, HX_RESTART_MAGIC, 8) != 0 || h.header_bytes != sizeof(h))) {
+    std::fclose(f);
+    return err("not a restart file");
+  }
+  if (ok && h.version != HX_RESTART_VERSION) { std::fclose(f); return err("restart version does not match"); }
+  if (ok && (h.nelem != c.E || h.np != NP || h.nlev != NLEV || h.qsize != c.Q || h.timelevels != NTL ||
+             h.qsize_timelevels != QTL || h.record_bytes != rw * 8)) {
+    std::fclose(f);
+    return err("restart file does not match the session");
+  }
+  if (ok) {
+    all.resize((size_t)c.E * rw);
+    ok = std::fread(all.data(), 8, all.size(), f) == all.size();
+  }
+  std::fclose(f);
+  if (!ok) return err("short read on restart file");
+  for (int t : {h.nm1, h.n0, h.np1})
+    if (t < 1 || t > NTL) return err("bad time level in restart header");
+  unsigned long long sum = 0;
+  for (int e = 0; e < c.E; ++e) sum += restart_sum(&all[(size_t)e * rw], rw, (unsigned long long)e * rw);
+  for (int e = 0; e < c.E; ++e) unpack_record(e, &all[(size_t)e * rw]);
+  c.tl.nm1 = h.nm1 - 1; c.tl.n0 = h.n0 - 1; c.tl.np1 = h.np1 - 1;
+  c.tl.nstep = h.nstep; c.tl.nstep0 = h.nstep0;
+  if (sum != h.checksum) return err("checksum mismatch");
+  return 0;
+}
+
 int hx_last_error(char* buf, int buflen) {
   Ctx& c = C();
   if (buf && buflen > 0) {
