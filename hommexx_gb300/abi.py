@@ -197,6 +197,40 @@ class HxLibrary:
         self.tl = [nm1.value, n0.value, np1.value, nstep.value]
         return self.tl
 
+    # -- cubed-sphere mesh generated by the library (hx_cube_mesh) ----------------------
+    def cube_mesh(self, ne: int, hypervis_scaling: float = 0.0):
+        """The mesh of ``mesh.build_mesh(ne)`` computed by hx_cube_mesh (metric on the
+        GPU), as a ``mesh.Mesh``."""
+        from . import mesh as M
+        E = 6 * ne * ne
+        a = dict(dvv=np.empty((NP, NP)), D=np.empty((E, 2, 2, NP, NP)), Dinv=np.empty((E, 2, 2, NP, NP)),
+                 fcor=np.empty((E, NP, NP)), mp=np.empty((E, NP, NP)), spheremp=np.empty((E, NP, NP)),
+                 rspheremp=np.empty((E, NP, NP)), metdet=np.empty((E, NP, NP)),
+                 metinv=np.empty((E, 2, 2, NP, NP)), tensorvisc=np.empty((E, 2, 2, NP, NP)),
+                 vec_sph2cart=np.empty((E, 2, 3, NP, NP)), lat=np.empty((E, NP, NP)),
+                 lon=np.empty((E, NP, NP)))
+        conn_f = np.empty((E, 8, 2), dtype=np.int32)
+        order = ("dvv", "D", "Dinv", "fcor", "mp", "spheremp", "rspheremp", "metdet", "metinv",
+                 "tensorvisc", "vec_sph2cart", "lat", "lon")
+        rc = self.lib.hx_cube_mesh(C.c_int(ne), C.c_double(hypervis_scaling),
+                                   *[C.c_void_p(a[k].ctypes.data) for k in order],
+                                   C.c_void_p(conn_f.ctypes.data))
+        if rc:
+            self.check("hx_cube_mesh")
+        # (remote element, remote add_connection position), 1-based, by position ->
+        # the Mesh's [e][C slot] = (remote element, remote C slot), 0-based
+        slot_of_pos = np.array([2, 3, 0, 1, 4, 5, 6, 7])
+        conn = -np.ones((E, 8, 2), dtype=np.int64)
+        for s in range(8):
+            col = conn_f[:, M.F90_POS_OF_SLOT[s] - 1]
+            ok = col[:, 0] > 0
+            conn[ok, s, 0] = col[ok, 0] - 1
+            conn[ok, s, 1] = slot_of_pos[col[ok, 1] - 1]
+        return M.Mesh(ne=ne, nelem=E, dvv=a["dvv"], D=a["D"], Dinv=a["Dinv"], metinv=a["metinv"],
+                      metdet=a["metdet"], mp=a["mp"], spheremp=a["spheremp"], rspheremp=a["rspheremp"],
+                      fcor=a["fcor"], phis=np.zeros((E, NP, NP)), lat=a["lat"], lon=a["lon"],
+                      vec_sph2cart=a["vec_sph2cart"], tensorvisc=a["tensorvisc"], connections=conn)
+
     # -- restart files (format of include/hxgpu.h) -------------------------------------
     RESTART_HEADER = struct.Struct("<8sII6i5iiQQ48s")
 

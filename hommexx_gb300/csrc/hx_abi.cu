@@ -1493,6 +1493,90 @@ int hx_traj_set_checkpointing(int mode) {
   });
 }
 
+int hx_cube_mesh(int ne, double hypervis_scaling, double* dvv, double* D, double* Dinv, double* fcor, double* mp,
+                 double* spheremp, double* rspheremp, double* metdet, double* metinv, double* tensorvisc,
+                 double* vec_sph2cart, double* lat, double* lon, int* connections) {
+  return run([&] {
+    if (ne < 1 || ne > 1024) fail(13, "hx_cube_mesh: ne must be in [1, 1024]");
+    const int E = 6 * ne * ne;
+    const size_t n16 = (size_t)E * 16;
+    cudaStream_t st = g_stream ? g_stream : cudaStreamPerThread;
+    // device outputs, one allocation
+    double* buf = nullptr;
+    const size_t total = n16 * (4 * 4 + 7) + n16 * 6;
+    ck(cudaMalloc(&buf, total * sizeof(double)), "cudaMalloc cube mesh");
+    struct Free {
+      double* p;
+      ~Free() { cudaFree(p); }
+    } fr{buf};
+    double* q = buf;
+    auto take = [&](size_t n) { double* r = q; q += n; return r; };
+    CubeMeshDev d{};
+    d.D = take(n16 * 4); d.Dinv = take(n16 * 4); d.metinv = take(n16 * 4); d.tens = take(n16 * 4);
+    d.metdet = take(n16); d.mp = take(n16); d.spheremp = take(n16); d.fcor = take(n16); d.lat = take(n16);
+    d.lon = take(n16); d.vec = take(n16 * 6);
+    const CubeMeshStatus cs = cube_metric(ne, hypervis_scaling, d, st);
+    ck(cs.err, "cube mesh kernels");
+    auto get = [&](double* host, const double* dev, size_t n) {
+      if (host) ck(cudaMemcpy(host, dev, n * sizeof(double), cudaMemcpyDeviceToHost), "D2H cube mesh");
+    };
+    get(D, d.D, n16 * 4); get(Dinv, d.Dinv, n16 * 4); get(metinv, d.metinv, n16 * 4);
+    get(tensorvisc, d.tens, n16 * 4); get(metdet, d.metdet, n16); get(mp, d.mp, n16);
+    get(fcor, d.fcor, n16); get(lat, d.lat, n16); get(lon, d.lon, n16); get(vec_sph2cart, d.vec, n16 * 6);
+    const std::vector<int> conn = cube_connectivity(ne);
+    // rspheremp = 1 / DSS(spheremp), the DSS in the library's own accumulation order
+    std::vector<double> sp(n16);
+    get(sp.data(), d.spheremp, n16);
+    if (spheremp) std::memcpy(spheremp, sp.data(), n16 * sizeof(double));
+    if (rspheremp) {
+      std::vector<int> cnt, src, nb;
+      build_tables(conn, E, cnt, src, nb);
+      for (size_t ep = 0; ep < n16; ++ep) {
+        double acc = sp[ep];
+        for (int k = 0; k < cnt[ep]; ++k) {
+          const int s2 = src[ep * MAXSRC + k];
+          acc += sp[(size_t)(s2 >> 4) * 16 + (s2 & 15)];
+        }
+        rspheremp[ep] = 1.0 / acc;
+      }
+    }
+    if (connections) {
+      // C slot S N W E SW SE NW NE -> add_connection position W=1 E=2 S=3 N=4 SW=5 SE=6 NW=7 NE=8
+      const int pos[8] = {3, 4, 1, 2, 5, 6, 7, 8};
+      for (int e = 0; e < E; ++e)
+        for (int sl = 0; sl < 8; ++sl) {
+          const int r = conn[((size_t)e * 8 + sl) * 2], rs = conn[((size_t)e * 8 + sl) * 2 + 1];
+          int* o = connections + ((size_t)e * 8 + pos[sl] - 1) * 2;
+          o[0] = r < 0 ? 0 : r + 1;
+          o[1] = r < 0 ? 0 : pos[rs];
+        }
+    }
+    if (dvv) {
+      // dvv(a,b) = L'_a(x_b) of the GLL points (derivative_mod_base.F90:437-475), in the
+      // memory order init_derivative_c takes: dvv[b][a]
+      const double x[4] = {-1.0, -1.0 / std::sqrt(5.0), 1.0 / std::sqrt(5.0), 1.0};
+      double leg[4];
+      for (int i = 0; i < 4; ++i) {
+        double p0 = 1.0, p1 = x[i];
+        for (int k = 1; k < 3; ++k) {
+          const double p2 = ((2 * k + 1) * x[i] * p1 - k * p0) / (k + 1);
+          p0 = p1;
+          p1 = p2;
+        }
+        leg[i] = p1;
+      }
+      for (int a = 0; a < 4; ++a)
+        for (int b = 0; b < 4; ++b) {
+          double v = 0.0;
+          if (a != b) v = (1.0 / (x[b] - x[a])) * leg[b] / leg[a];
+          if (a == 3 && b == 3) v = 4.0 * 3.0 / 4.0;
+          if (a == 0 && b == 0) v = -4.0 * 3.0 / 4.0;
+          dvv[b * 4 + a] = v;
+        }
+    }
+  });
+}
+
 int hx_write_restart(const char* path) {
   return run([&] {
     if (!path) fail(HX_ERR_IO, "hx_write_restart: null path");

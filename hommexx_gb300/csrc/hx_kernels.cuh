@@ -8,6 +8,8 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <vector>
+
 #include "hx_common.h"
 
 namespace hx {
@@ -99,6 +101,18 @@ void launch_cam_forcing(int E, int Q, double* T, double* v, const double* ft, co
                         int moist, double dt, double ps0, cudaStream_t s);
 // Dense weak Laplacian per element ([E][16][16]) from the FP64 metric.
 void launch_lap_matrix(const MetricP<double>& m, int E, double* out, cudaStream_t s);
+// Cubed-sphere mesh generation (hx_mesh.cu).  Device outputs in the init_elements_2d_c
+// layouts (any may be null); status carries the CUDA error and the area correction.
+struct CubeMeshDev {
+  double *D, *Dinv, *metinv, *metdet, *mp, *spheremp, *fcor, *vec, *tens, *lat, *lon;
+};
+struct CubeMeshStatus {
+  cudaError_t err;
+  double alpha_c;
+};
+CubeMeshStatus cube_metric(int ne, double hypervis_scaling, const CubeMeshDev& out, cudaStream_t s);
+// [E][8][2] (remote element, remote slot), 0-based slots S N W E SW SE NW NE, -1 if none.
+std::vector<int> cube_connectivity(int ne);
 // Restart-file checksum of E element segments (segment e at src + e*words, its word j at
 // record word index e*rec_words + off + j), added to *out.
 void launch_restart_checksum(const double* src, int E, int words, long long rec_words, long long off,

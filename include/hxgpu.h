@@ -237,6 +237,30 @@ int hx_traj_jvp(const double* dv, const double* dT, const double* ddp3d, double*
                 double* T_tan, double* dp3d_tan);
 int hx_traj_set_checkpointing(int mode);
 
+/* ---- Cubed-sphere mesh generated on the GPU (no counterpart in the reference's C++
+ * layer) ----
+ * The inputs the Fortran driver builds before it calls init_derivative_c,
+ * init_elements_2d_c and add_connection, for an equiangular gnomonic cubed sphere of
+ * 6 ne^2 elements with np = 4 GLL points: dvv (derivative_mod_base.F90:437-475), the
+ * metric of metric_atomic (cube_mod.F90:215-454) rescaled to a total area of 4 pi as
+ * prim_driver_mod.F90:403-418 does, mp and spheremp = mp metdet, rspheremp = 1/DSS
+ * (spheremp) (mass_matrix_mod.F90:98-115), fcor = 2 Omega sin(lat), vec_sphere2cart and,
+ * when hypervis_scaling != 0, tensorVisc (cube_mod.F90:310-440); Omega = 7.292e-5,
+ * rearth = 6.376e6.  Host outputs in the layouts init_elements_2d_c takes: D, Dinv,
+ * metinv, tensorvisc (np,np,2,2,nelemd); vec_sph2cart (np,np,3,2,nelemd); fcor, mp,
+ * spheremp, rspheremp, metdet, lat, lon (np,np,nelemd); dvv (np,np).  connections
+ * (2,8,nelemd): for element e and add_connection position k (W=1 E=2 S=3 N=4 SW=5 SE=6
+ * NW=7 NE=8) the 1-based remote element and its position, or 0 0 where there is no
+ * neighbour (the missing corner of the elements at the eight cube corners).  Elements
+ * are ordered face by face, then row by row.  Any output may be null.  The metric is
+ * computed on the GPU, one thread per GLL point; the connectivity on the host from exact
+ * integer corner positions.  Needs no session.  Returns 0, 13 (ne outside [1, 1024]) or
+ * HX_ERR_CUDA. */
+int hx_cube_mesh(int ne, double hypervis_scaling, double* dvv, double* D, double* Dinv,
+                 double* fcor, double* mp, double* spheremp, double* rspheremp,
+                 double* metdet, double* metinv, double* tensorvisc, double* vec_sph2cart,
+                 double* lat, double* lon, int* connections);
+
 /* ---- Restart files (no counterpart in the reference's C++ layer) ------------------
  * A binary restart format in place of the Fortran restart_io_mod.F90 (WriteRestart /
  * ReadRestart, src/restart_io_mod.F90:626-698): a 128-byte header, then one record per
