@@ -247,6 +247,21 @@ __device__ __forceinline__ double dss_gather(const T* base, long long es, int ls
   return acc;
 }
 
+// Thread -> (level in a group of 8, point) for a 128-thread block of a standalone DSS:
+// each warp holds one class of points over the 8 levels -- interior {5,6,9,10} (no
+// contribution from other elements), edge {1,2,4,7} and {8,11,13,14} (one), corner
+// {0,3,12,15} (two or three) -- so the gather loop has one trip count per warp instead
+// of every warp running the longest.  Each point still sums in its own fixed order.
+__device__ __forceinline__ void dss_thread_point(int& lo, int& p) {
+  constexpr unsigned long long kPerm = 0x5ull | 0x6ull << 4 | 0x9ull << 8 | 0xAull << 12 | 0x1ull << 16 |
+                                       0x2ull << 20 | 0x4ull << 24 | 0x7ull << 28 | 0x8ull << 32 |
+                                       0xBull << 36 | 0xDull << 40 | 0xEull << 44 | 0x0ull << 48 |
+                                       0x3ull << 52 | 0xCull << 56 | 0xFull << 60;
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  lo = lane >> 2;
+  p = (int)((kPerm >> (4 * (w * 4 + (lane & 3)))) & 15);
+}
+
 // ---- segmented column scans (128 threads: 16 columns x 8 segments of 9 levels) ------
 // Exclusive prefix of the per-segment totals within an 8-lane group.
 __device__ __forceinline__ double seg_excl_prefix(double tot, int seg) {

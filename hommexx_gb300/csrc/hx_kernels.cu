@@ -215,11 +215,13 @@ __global__ void __launch_bounds__(LG * 16) k_caar(CaarArgs<R> a) {
 
 // DSS of the Caar output into the state of time level np1, times rspheremp
 // (BoundaryExchange::exchange(rspheremp) on v, T, dp3d: CaarFunctor.cpp:114).
-__global__ void k_dss_state(int E, const double* __restrict__ src, double* v, double* T, double* dp,
-                            int np1, const double* __restrict__ rsmp, DssTable tab) {
-  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= E * NLEV * 16) return;
-  const int e = idx / (NLEV * 16), l = (idx / 16) % NLEV, p = idx & 15;
+// Grid (E, 9), 128 threads: 8 levels per block, warps by point class.
+__global__ void __launch_bounds__(128) k_dss_state(const double* __restrict__ src, double* v, double* T,
+                                                   double* dp, int np1, const double* __restrict__ rsmp,
+                                                   DssTable tab) {
+  int lo, p;
+  dss_thread_point(lo, p);
+  const int e = blockIdx.x, l = blockIdx.y * 8 + lo;
   const double r = rsmp[e * 16 + p];
   const double a0 = dss_gather(src, NLEV * 64, 64, e, l, p, tab) * r;
   const double a1 = dss_gather(src + 16, NLEV * 64, 64, e, l, p, tab) * r;
@@ -337,11 +339,12 @@ __global__ void __launch_bounds__(LG * 16) k_hv_lap2(HvArgs<R> a) {
 }
 
 // DSS of bufB and TagUpdateStates.
+// Grid (E, 9), 128 threads: 8 levels per block, warps by point class.
 template <typename R>
-__global__ void k_hv_update(HvArgs<R> a, int E) {
-  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= E * NLEV * 16) return;
-  const int e = idx / (NLEV * 16), l = (idx / 16) % NLEV, p = idx & 15;
+__global__ void __launch_bounds__(128) k_hv_update(HvArgs<R> a) {
+  int lo, p;
+  dss_thread_point(lo, p);
+  const int e = blockIdx.x, l = blockIdx.y * 8 + lo;
   const double rsd = a.m.rspheremp_d[e * 16 + p];
   const R rs = cvt<R>(rsd);
   const R dt = R(a.dt);
@@ -404,6 +407,16 @@ __device__ __forceinline__ void eq_index(int nq, int& e, int& q, int& l, int& p)
   q = eq - e * nq;
   l = blockIdx.y * EQ_LEVELS + (threadIdx.x >> 4);
   p = threadIdx.x & 15;
+}
+// The same grid for the DSS kernels, with the warps grouped by point class.
+__device__ __forceinline__ void eq_index_dss(int nq, int& e, int& q, int& l, int& p) {
+  static_assert(EQ_LEVELS == 8 && EQ_THREADS == 128, "dss_thread_point covers 8 levels x 16 points");
+  const int eq = blockIdx.x;
+  e = eq / nq;
+  q = eq - e * nq;
+  int lo;
+  dss_thread_point(lo, p);
+  l = blockIdx.y * EQ_LEVELS + lo;
 }
 
 __global__ void __launch_bounds__(EQ_THREADS) k_update_q(int Q, const double* qdp, double* Qc,
@@ -905,7 +918,7 @@ template <typename R> constexpr size_t aal_smem() {
 template <typename R>
 __global__ void __launch_bounds__(EQ_THREADS) k_dss_tracers(EulerArgs<R> a, int time_avg) {
   int e, q, l, p;
-  eq_index(a.Q, e, q, l, p);
+  eq_index_dss(a.Q, e, q, l, p);
   const double rs = a.m.rspheremp_d[e * 16 + p];
   const double v = dss_gather(a.qscr + (size_t)q * NLEV * 16, (long long)a.Q * NLEV * 16, 16, e, l, p, a.dss) * rs;
   const size_t d = ((((size_t)e * QTL + a.np1_qdp) * a.Q + q) * NLEV + l) * 16 + p;
@@ -917,14 +930,15 @@ __global__ void __launch_bounds__(EQ_THREADS) k_dss_tracers(EulerArgs<R> a, int 
   }
 }
 
-__global__ void k_dss_field(int E, const double* __restrict__ src, double* dst,
-                            const double* __restrict__ rsmp, DssTable tab) {
-  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= E * NLEV * 16) return;
-  const int e = idx / (NLEV * 16), l = (idx / 16) % NLEV, p = idx & 15;
+// Grid (E, 9), 128 threads: 8 levels per block, warps by point class.
+__global__ void __launch_bounds__(128) k_dss_field(const double* __restrict__ src, double* dst,
+                                                   const double* __restrict__ rsmp, DssTable tab) {
+  int lo, p;
+  dss_thread_point(lo, p);
+  const int e = blockIdx.x, l = blockIdx.y * 8 + lo;
   double v = dss_gather(src, NLEV * 16, 16, e, l, p, tab);
   if (rsmp) v *= rsmp[e * 16 + p];
-  dst[idx] = v;
+  dst[((size_t)e * NLEV + l) * 16 + p] = v;
 }
 
 // Generic in-place DSS through a scratch copy.
@@ -938,7 +952,7 @@ __global__ void __launch_bounds__(EQ_THREADS) k_dss_from_copy(int nf, double* ba
                                                                long long es, int ls, const double* scr,
                                                                const double* rsmp, DssTable tab) {
   int e, f, l, p;
-  eq_index(nf, e, f, l, p);
+  eq_index_dss(nf, e, f, l, p);
   double v = dss_gather(scr + (size_t)f * NLEV * 16, (long long)nf * NLEV * 16, 16, e, l, p, tab);
   if (rsmp) v *= rsmp[e * 16 + p];
   base[(size_t)f * fs + (size_t)e * es + (size_t)l * ls + p] = v;
@@ -1347,7 +1361,7 @@ void launch_caar(const CaarArgs<R>& a, int E, cudaStream_t s) {
 void launch_dss_state(int E, const double* src, double* v, double* T, double* dp, int np1,
                       const double* rsmp, DssTable t, cudaStream_t s) {
   KScope k("dss_caar", s);
-  k_dss_state<<<nblk((long long)E * NLEV * 16, 256), 256, 0, s>>>(E, src, v, T, dp, np1, rsmp, t);
+  k_dss_state<<<dim3(E, NLEV / 8), 128, 0, s>>>(src, v, T, dp, np1, rsmp, t);
 }
 
 template <typename R>
@@ -1364,7 +1378,7 @@ void launch_hv(const HvArgs<R>& a, int E, cudaStream_t s) {
     }
     {
       KScope k("hv_dss_update", s);
-      k_hv_update<R><<<nblk((long long)E * NLEV * 16, 256), 256, 0, s>>>(a, E);
+      k_hv_update<R><<<dim3(E, NLEV / 8), 128, 0, s>>>(a);
     }
   }
 }
@@ -1425,7 +1439,7 @@ void launch_euler_step(EulerArgs<R>& a, int E, int time_avg, cudaStream_t s) {
   }
   {
     KScope k("euler_dss_fvar", s);
-    k_dss_field<<<nblk((long long)E * NLEV * 16, 256), 256, 0, s>>>(E, a.fscr, a.f_dss, a.m.rspheremp_d, a.dss);
+    k_dss_field<<<dim3(E, NLEV / 8), 128, 0, s>>>(a.fscr, a.f_dss, a.m.rspheremp_d, a.dss);
   }
 }
 
