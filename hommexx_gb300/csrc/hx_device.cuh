@@ -391,6 +391,17 @@ template <typename R> __device__ __forceinline__ R rel_hw(double x) {
   else return x;
 }
 
+// 1/x in FP64 from the FP32 reciprocal of x refined by two Newton-Raphson steps
+// r <- r + r (1 - x r), each of which squares the relative error (about 2^-23 -> 2^-46
+// -> below one ulp of the result); rf returns the FP32 reciprocal.  For positive normal
+// x within the FP32 exponent range (2^-126 .. 2^127); within one ulp of 1.0 / x.
+__device__ __forceinline__ double rcp_newton(double x, float& rf) {
+  rf = 1.0f / (float)x;
+  double r = (double)rf;
+  r = fma(r, fma(-x, r, 1.0), r);
+  return fma(r, fma(-x, r, 1.0), r);
+}
+
 // Brackets one launch for the per-kernel timing hooks.
 struct KScope {
   const char* n;

@@ -14,6 +14,7 @@
 //   HyperviscosityFunctorImpl.{hpp:72-257,cpp:56-112}, EulerStepFunctorImpl.hpp:118-884,
 //   RemapFunctor.hpp:299-463, PpmRemap.hpp:174-689, BoundaryExchange.cpp:285-849,
 //   prim_driver.cpp:90-206, prim_step.cpp:42-66, prim_advance_exp.cpp:138-156.
+#include <algorithm>
 #include <cstdio>
 
 #include "hx_device.cuh"
@@ -35,8 +36,14 @@ __global__ void __launch_bounds__(LG * 16) k_caar(CaarArgs<R> a) {
   double* s_div = sm + 2 * NLEV * SROW; // div(v dp)
   double* s_p = sm + 3 * NLEV * SROW;   // pressure
   double* s_om = sm + 4 * NLEV * SROW;  // sum_{j<k} div_vdp_j
-  double* s_rp = sm + 5 * NLEV * SROW;  // 1 / pressure
+  double* s_rp = sm + 5 * NLEV * SROW;  // 1 / pressure (FP64 form)
   double* s_tot = sm + 6 * NLEV * SROW; // column sum of div(v dp) (rsplit == 0)
+  // Mixed form: 1/p in FP32 in place of s_rp, and the FP32 u, v, div(v dp) of phase A
+  // kept for phase C ([72][16] floats each) so that it neither reloads nor re-converts.
+  float* f_rp = reinterpret_cast<float*>(s_rp);
+  float* f_u = reinterpret_cast<float*>(s_tot + 16);
+  float* f_w = f_u + NLEV * 16;
+  float* f_div = f_w + NLEV * 16;
   const int e = blockIdx.x, tid = threadIdx.x, p = tid & 15, lg = tid >> 4;
   Pt<R> t;
   t.init(p);
@@ -69,6 +76,11 @@ __global__ void __launch_bounds__(LG * 16) k_caar(CaarArgs<R> a) {
     s_dp[l * SROW + p] = dd;
     s_tv[l * SROW + p] = tv;
     s_div[l * SROW + p] = dbl_hw(div);
+    if constexpr (kF32<R>) {
+      f_u[l * 16 + p] = u;
+      f_w[l * 16 + p] = w;
+      f_div[l * 16 + p] = div;
+    }
   }
   __syncthreads();
   // ---- phase B: pressure, geopotential, omega integral (double) ----
@@ -91,9 +103,16 @@ __global__ void __launch_bounds__(LG * 16) k_caar(CaarArgs<R> a) {
       const double d = s_dp[(l0 + k) * SROW + col];
       pr = pr + 0.5 * (prev + d);
       prev = d;
-      const double rp = 1.0 / pr;
+      double rp;
+      if constexpr (kF32<R>) {  // the FP32 reciprocal serves phase C
+        float rf;
+        rp = rcp_newton(pr, rf);
+        f_rp[(l0 + k) * SROW + col] = rf;
+      } else {
+        rp = 1.0 / pr;
+        s_rp[(l0 + k) * SROW + col] = rp;
+      }
       s_p[(l0 + k) * SROW + col] = pr;
-      s_rp[(l0 + k) * SROW + col] = rp;
       r[k] = kRgas * s_tv[(l0 + k) * SROW + col] * (d * 0.5 * rp);
     }
     // geopotential: phi_k = phis + 2 sum_{j>k} r_j + r_k
@@ -136,12 +155,21 @@ __global__ void __launch_bounds__(LG * 16) k_caar(CaarArgs<R> a) {
   for (int k = 0; k < NL; ++k) {
     const int l = lg + LG * k;
     const double pd = s_p[l * SROW + p];
-    const R rp = cvt_hw<R>(s_rp[l * SROW + p]);
+    R rp, u, w, div;
+    if constexpr (kF32<R>) {
+      rp = f_rp[l * SROW + p];
+      u = f_u[l * 16 + p];
+      w = f_w[l * 16 + p];
+      div = f_div[l * 16 + p];
+    } else {
+      rp = s_rp[l * SROW + p];
+      u = a.v[vN0 + l * 32 + p];
+      w = a.v[vN0 + l * 32 + 16 + p];
+      div = s_div[l * SROW + p];
+    }
     R gp0, gp1;
     gradient_sphere(t, m, rel_hw<R>(pd), gp0, gp1);
-    const R u = cvt_hw<R>(a.v[vN0 + l * 32 + p]), w = cvt_hw<R>(a.v[vN0 + l * 32 + 16 + p]);
     const double td = a.T[sN0 + l * 16 + p];
-    const R div = cvt_hw<R>(s_div[l * SROW + p]);
     const R vgp = u * gp0 + w * gp1;
     const R omega = (vgp - (cvt_hw<R>(s_om[l * SROW + p]) + R(0.5) * div)) * rp;
     if (a.eta_ave_w != 0.0) a.omega_p[((size_t)e * NLEV + l) * 16 + p] += dbl_hw(eta * omega);
@@ -1348,7 +1376,8 @@ void launch_dp_from_ps(int E, double* dp, const double* ps_v, int n0, double ps0
 template <typename R>
 void launch_caar(const CaarArgs<R>& a, int E, cudaStream_t s) {
   constexpr int LG = LG_CAAR<R>();
-  const size_t smem = (6 * NLEV * SROW + 16) * sizeof(double);
+  // mixed form: + u, v, div(v dp) in FP32 ([72][16] each)
+  const size_t smem = (6 * NLEV * SROW + 16) * sizeof(double) + (kF32<R> ? 3 * NLEV * 16 * sizeof(float) : 0);
   static bool init = false;
   if (!init) {
     cudaFuncSetAttribute(k_caar<R, LG>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);

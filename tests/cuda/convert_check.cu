@@ -1,7 +1,8 @@
 // Checks the integer-pipe double<->float conversions of hx_device.cuh against the
 // hardware conversions, bit for bit: random bit patterns over every exponent, ties,
-// zeros, subnormals, overflow, infinities and NaN.  Prints the mismatch count; exit
-// status 0 when there is none.
+// zeros, subnormals, overflow, infinities and NaN; and the Newton-Raphson reciprocal
+// rcp_newton against IEEE division (within one ulp, over positive x of exponents
+// -120 .. 120).  Prints the mismatch counts; exit status 0 when there are none.
 #include <cstdio>
 #include <cstdlib>
 
@@ -33,19 +34,29 @@ __global__ void check(unsigned long long n, unsigned long long* bad) {
   const double d1 = hx::f2d(g), d2 = (double)g;
   const bool nan2 = (d1 != d1) && (d2 != d2);
   if (__double_as_longlong(d1) != __double_as_longlong(d2) && !nan2) atomicAdd(bad + 1, 1ULL);
+  // reciprocal: positive x, exponent in [-120, 120]
+  const unsigned long long m2 = mix(i ^ 0xABCDEFULL);
+  const double x2 = __longlong_as_double((long long)((m2 & 0x000FFFFFFFFFFFFFULL) |
+                                                     ((unsigned long long)(1023 - 120 + (int)((m2 >> 52) % 241)) << 52)));
+  float rf;
+  const long long r1 = __double_as_longlong(hx::rcp_newton(x2, rf)), r2 = __double_as_longlong(1.0 / x2);
+  const long long du = r1 > r2 ? r1 - r2 : r2 - r1;
+  if (du > 1) atomicAdd(bad + 2, 1ULL);
+  if (du == 1) atomicAdd(bad + 3, 1ULL);
 }
 
 }  // namespace
 
 int main() {
   unsigned long long* bad = nullptr;
-  if (cudaMalloc(&bad, 2 * sizeof(unsigned long long)) != cudaSuccess) return 2;
-  cudaMemset(bad, 0, 2 * sizeof(unsigned long long));
+  if (cudaMalloc(&bad, 4 * sizeof(unsigned long long)) != cudaSuccess) return 2;
+  cudaMemset(bad, 0, 4 * sizeof(unsigned long long));
   const unsigned long long n = 1ULL << 26;
   check<<<(unsigned)((n + 255) / 256), 256>>>(n, bad);
-  unsigned long long h[2] = {0, 0};
+  unsigned long long h[4] = {0, 0, 0, 0};
   if (cudaMemcpy(h, bad, sizeof(h), cudaMemcpyDeviceToHost) != cudaSuccess) return 2;
-  std::printf("d2f mismatches %llu, f2d mismatches %llu, of %llu each\n", h[0], h[1], n);
+  std::printf("d2f mismatches %llu, f2d mismatches %llu, rcp beyond 1 ulp %llu (1 ulp: %llu), of %llu each\n",
+              h[0], h[1], h[2], h[3], n);
   cudaFree(bad);
-  return (h[0] == 0 && h[1] == 0) ? 0 : 1;
+  return (h[0] == 0 && h[1] == 0 && h[2] == 0) ? 0 : 1;
 }
