@@ -1195,9 +1195,12 @@ __global__ void __launch_bounds__(RT) k_remap(RemapArgs a) {
     }
   }
   __syncwarp();
-  // Mixed form: the tracers' reconstructions run in FP32 from float copies of the grid
-  // weights, z2 and 1/D; their cell integrals and the mass below each interface stay in
-  // FP64, and the bottom interface carries the exact column mass (mass fixer).
+  // Mixed form: the reconstructions run in FP32 from float copies of the grid weights,
+  // z2 and 1/D; the cell integrals and the mass below each interface stay in FP64, and
+  // the bottom interface carries the exact column mass (mass fixer).  v and T are
+  // reconstructed relative to their column mean Aref (PPM is shift-equivariant: the
+  // parabolas of A - Aref are those of A less Aref), so FP32 carries the deviations, and
+  // Aref's share of each integral, Aref (x2 + 1/2), is added back in FP64.
   float* gf = reinterpret_cast<float*>(sm + R_GF);  // [10][74]
   float* z2f = gf + 740;
   float* rDf = z2f + 72;
@@ -1206,7 +1209,7 @@ __global__ void __launch_bounds__(RT) k_remap(RemapArgs a) {
   float* aif = reinterpret_cast<float*>(sm + R_AI);
   float* coeff = reinterpret_cast<float*>(sm + R_COEF);
   if constexpr (kF32<R>) {
-    if (a.Q > 0) {
+    {
       for (int i = lane; i < 740; i += 32) gf[i] = (float)g[i];
       if (own) {
 #pragma unroll
@@ -1221,7 +1224,7 @@ __global__ void __launch_bounds__(RT) k_remap(RemapArgs a) {
   const int nvar = 3 + a.Q;
 #pragma unroll 1
   for (int var = a.rsplit == 0 ? 3 : 0; var < nvar; ++var) {
-    const bool lo = kF32<R> && var >= 3;
+    constexpr bool lo = kF32<R>;
     // extrinsic values (v dp, T dp for the states; Qdp as is), cell means, masses
     double x3[3] = {0.0, 0.0, 0.0};
     if (own) {
@@ -1231,10 +1234,11 @@ __global__ void __launch_bounds__(RT) k_remap(RemapArgs a) {
         if (var < 2) x3[k] = a.v[vb + (size_t)l * 32 + var * 16] * s3[k];
         else if (var == 2) x3[k] = a.T[sb + (size_t)l * 16] * s3[k];
         else x3[k] = a.qdp[((((size_t)e * QTL + a.n0_qdp) * a.Q + (var - 3)) * NLEV + l) * 16 + p];
-        if (lo) Af[l] = (float)x3[k] * rDf[l];
-        else A[l] = x3[k] * rD[l];
+        if (!lo) A[l] = x3[k] * rD[l];
+        else if (var >= 3) Af[l] = (float)x3[k] * rDf[l];
       }
     }
+    double aref = 0.0;  // mixed form, v and T: column mean
     {
       double ex = warp_excl_scan(x3[0] + x3[1] + x3[2], lane);
       if (own) {
@@ -1246,6 +1250,13 @@ __global__ void __launch_bounds__(RT) k_remap(RemapArgs a) {
       }
       if (lane == 23) mass[NLEV + 1] = ex;  // mass[NLEV] + x[NLEV-1]
       if (lane == 0) mass[0] = 0.0;
+      if (lo && var < 3) {
+        aref = __shfl_sync(FULL, ex, 23) / pio[NLEV];
+        if (own) {
+#pragma unroll
+          for (int k = 0; k < 3; ++k) Af[l0 + k] = (float)fma(x3[k], rD[l0 + k], -aref);
+        }
+      }
     }
     __syncwarp();
     if (lane == 0) {  // ghost cells: mirrored (remap_alg 1, 2) or constant (3)
@@ -1277,7 +1288,8 @@ __global__ void __launch_bounds__(RT) k_remap(RemapArgs a) {
           const float x2 = z2f[k];
           const float in = (coeff[kk] * (x2 + 0.5f) + coeff[72 + kk] * (x2 * x2 - 0.25f) * 0.5f) +
                            coeff[144 + kk] * (x2 * x2 * x2 + 0.125f) * (1.0f / 3.0f);
-          m2[k3] = k == NLEV - 1 ? mass[NLEV + 1] : mass[kk + 1] + dbl(in) * D[kk];
+          const double ind = var < 3 ? fma(aref, z2[k] + 0.5, dbl(in)) : dbl(in);
+          m2[k3] = k == NLEV - 1 ? mass[NLEV + 1] : mass[kk + 1] + ind * D[kk];
         } else {
           const double x2 = z2[k], x1 = -0.5;
           const double in = (coef[kk] * (x2 - x1) + coef[72 + kk] * (x2 * x2 - x1 * x1) * 0.5) +
