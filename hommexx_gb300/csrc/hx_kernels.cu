@@ -314,20 +314,47 @@ __global__ void __launch_bounds__(LG * 16) k_hv_lap2(HvArgs<R> a) {
   const size_t vb = ((size_t)e * NTL + a.np1) * NLEV * 32;
   const size_t sb = ((size_t)e * NTL + a.np1) * NLEV * 16;
   double* out = a.bufB + (size_t)e * NLEV * 64;
-  const double rs = a.m.rspheremp_d[(size_t)e * 16 + p];
   const double spd = a.m.spheremp_d[(size_t)e * 16 + p];
   const double wh = a.eta_ave_w / a.hsub;  // eta_ave_w / hypervis_subcycle
   const R whr = R(wh);
   const R dt = R(a.dt);
   LapOp<R> lap;
   lap.load(a.m, e, p);
+  // Mixed form: DSS(rspheremp) of the first laplacians into shared memory [4][72][16],
+  // with the warps grouped by point class (dss_thread_point) so that each gather loop
+  // runs one trip count per warp; every point sums in its own fixed order.  The FP64 form
+  // gathers inside the level loop, where the gathers' memory latency overlaps the FP64
+  // operator work of the other levels.
+  extern __shared__ double hsm[];
+  R* s_in = reinterpret_cast<R*>(hsm);
+  const double rs = a.m.rspheremp_d[(size_t)e * 16 + p];
+  if constexpr (kF32<R>) {
+    static_assert(LG * 16 == 128, "dss_thread_point maps 128 threads");
+    int lo, pg;
+    dss_thread_point(lo, pg);
+    const double rsg = a.m.rspheremp_d[(size_t)e * 16 + pg];
+#pragma unroll 1
+    for (int l = lo; l < NLEV; l += 8)
+#pragma unroll
+      for (int f = 0; f < 4; ++f)
+        s_in[(f * NLEV + l) * 16 + pg] = cvt<R>(dss_gather(a.bufA + f * 16, NLEV * 64, 64, e, l, pg, a.dss) * rsg);
+    __syncthreads();
+  }
 #pragma unroll 1
   for (int k = 0; k < NL; ++k) {
     const int l = lg + LG * k;
-    const R v0 = cvt<R>(dss_gather(a.bufA, NLEV * 64, 64, e, l, p, a.dss) * rs);
-    const R v1 = cvt<R>(dss_gather(a.bufA + 16, NLEV * 64, 64, e, l, p, a.dss) * rs);
-    const R t1 = cvt<R>(dss_gather(a.bufA + 32, NLEV * 64, 64, e, l, p, a.dss) * rs);
-    const R d1 = cvt<R>(dss_gather(a.bufA + 48, NLEV * 64, 64, e, l, p, a.dss) * rs);
+    R v0, v1, t1, d1;
+    if constexpr (kF32<R>) {
+      v0 = s_in[(0 * NLEV + l) * 16 + p];
+      v1 = s_in[(1 * NLEV + l) * 16 + p];
+      t1 = s_in[(2 * NLEV + l) * 16 + p];
+      d1 = s_in[(3 * NLEV + l) * 16 + p];
+    } else {
+      v0 = dss_gather(a.bufA, NLEV * 64, 64, e, l, p, a.dss) * rs;
+      v1 = dss_gather(a.bufA + 16, NLEV * 64, 64, e, l, p, a.dss) * rs;
+      t1 = dss_gather(a.bufA + 32, NLEV * 64, 64, e, l, p, a.dss) * rs;
+      d1 = dss_gather(a.bufA + 48, NLEV * 64, 64, e, l, p, a.dss) * rs;
+    }
     R lt, ld, l0, l1;
     if (a.consthv) {
       lt = lap(t, m, t1);
@@ -722,14 +749,25 @@ __global__ void __launch_bounds__(LG * 16) k_bih_post(EulerArgs<R> a) {
   const size_t qb = ((size_t)e * a.Q + q) * NLEV * 16;
   const double* fbase = a.qscr + (size_t)q * NLEV * 16;
   const R fac = R(-a.rhs_viss * a.dt * a.nu_q);
-  const double rs = a.m.rspheremp_d[(size_t)e * 16 + p];
   const R rsp_local = R(1) / m.sp;
   LapOp<R> lapo;
   if (a.consthv) lapo.load(a.m, e, p);
+  // DSS(rspheremp) into shared memory [72][16] with warps grouped by point class
+  __shared__ R s_in[NLEV * 16];
+  {
+    static_assert(LG * 16 == 128, "dss_thread_point maps 128 threads");
+    int lo, pg;
+    dss_thread_point(lo, pg);
+    const double rsg = a.m.rspheremp_d[(size_t)e * 16 + pg];
+#pragma unroll 1
+    for (int l = lo; l < NLEV; l += 8)
+      s_in[l * 16 + pg] = cvt<R>(dss_gather(fbase, (long long)a.Q * NLEV * 16, 16, e, l, pg, a.dss) * rsg);
+  }
+  __syncthreads();
 #pragma unroll 1
   for (int k = 0; k < NL; ++k) {
     const int l = lg + LG * k;
-    const R s = cvt<R>(dss_gather(fbase, (long long)a.Q * NLEV * 16, 16, e, l, p, a.dss) * rs);
+    const R s = s_in[l * 16 + p];
     const R lap = a.consthv ? lapo(t, m, s) : laplace_tensor(t, m, tv, s);
     a.qtens[qb + l * 16 + p] = dbl(fac * cvt<R>(a.dp0[l]) * lap * rsp_local);
   }
@@ -1415,7 +1453,7 @@ void launch_hv(const HvArgs<R>& a, int E, cudaStream_t s) {
     }
     {
       KScope k("hv_laplace2", s);
-      k_hv_lap2<R, LG><<<E, LG * 16, 0, s>>>(a);
+      k_hv_lap2<R, LG><<<E, LG * 16, kF32<R> ? 4 * NLEV * 16 * sizeof(R) : 0, s>>>(a);
     }
     {
       KScope k("hv_dss_update", s);
