@@ -296,8 +296,9 @@ __global__ void __launch_bounds__(LG * 16) k_hv_lap1(HvArgs<R> a) {
 }
 
 // DSS(rspheremp) of bufA, second laplacian, TagHyperPreExchange -> bufB (pre-DSS).
+// Occupancy: 6 CTAs per SM in the mixed form (80 registers), 3 in the FP64 form.
 template <typename R, int LG>
-__global__ void __launch_bounds__(LG * 16) k_hv_lap2(HvArgs<R> a) {
+__global__ void __launch_bounds__(LG * 16, kF32<R> ? 6 : 3) k_hv_lap2(HvArgs<R> a) {
   constexpr int NL = NLEV / LG;
   const int e = blockIdx.x, tid = threadIdx.x, p = tid & 15, lg = tid >> 4;
   Pt<R> t;
@@ -732,8 +733,9 @@ __global__ void __launch_bounds__(LG * 16) k_bih_pre(EulerArgs<R> a) {
 }
 
 // DSS(rspheremp) of qscr, BIHPostConstHV/TensorHV laplace, rhsviss_adjustment -> qtens.
+// Occupancy: 9 CTAs per SM in the mixed form, 6 in the FP64 form (at most 85 registers).
 template <typename R, int LG>
-__global__ void __launch_bounds__(LG * 16) k_bih_post(EulerArgs<R> a) {
+__global__ void __launch_bounds__(LG * 16, kF32<R> ? 9 : 6) k_bih_post(EulerArgs<R> a) {
   constexpr int NL = NLEV / LG;
   const int eq = blockIdx.x, e = eq / a.Q, q = eq % a.Q;
   const int tid = threadIdx.x, p = tid & 15, lg = tid >> 4;
@@ -891,8 +893,11 @@ __device__ bool limiter_level(int option, R* x, const R* c, R s1, double& minp_i
 // spheremp -> qscr (pre-DSS).  One CTA per element loops over the tracers: vstar, the
 // limiter weights c = spheremp dpdissk, 1/dpdissk and sum(c) are formed once per element
 // and reused by every tracer.
+// Occupancy: 6 CTAs per SM in the mixed form (at most 80 registers; the kernel waits on
+// memory and shared-memory latency more than it issues, so occupancy pays for a 12-byte
+// spill), 3 in the FP64 form (168 registers).
 template <typename R, int LG>
-__global__ void __launch_bounds__(LG * 16) k_aal_tracer(EulerArgs<R> a) {
+__global__ void __launch_bounds__(LG * 16, kF32<R> ? 6 : 3) k_aal_tracer(EulerArgs<R> a) {
   constexpr int NL = NLEV / LG;
   extern __shared__ double tsm[];
   double* s_q = tsm;                                            // [72][17] double
