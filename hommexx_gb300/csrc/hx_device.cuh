@@ -397,7 +397,7 @@ template <typename R> __device__ __forceinline__ R rel_hw(double x) {
 // x within the FP32 exponent range (2^-126 .. 2^127); within one ulp of 1.0 / x.
 __device__ __forceinline__ double rcp_newton(double x, float& rf) {
   rf = 1.0f / (float)x;
-  double r = (double)rf;
+  double r = f2d(rf);  // exact; on the integer pipe
   r = fma(r, fma(-x, r, 1.0), r);
   return fma(r, fma(-x, r, 1.0), r);
 }

@@ -75,7 +75,7 @@ __global__ void __launch_bounds__(LG * 16) k_caar(CaarArgs<R> a) {
     }
     s_dp[l * SROW + p] = dd;
     s_tv[l * SROW + p] = tv;
-    s_div[l * SROW + p] = dbl_hw(div);
+    s_div[l * SROW + p] = dbl(div);
     if constexpr (kF32<R>) {
       f_u[l * 16 + p] = u;
       f_w[l * 16 + p] = w;
@@ -218,7 +218,10 @@ __global__ void __launch_bounds__(LG * 16) k_caar(CaarArgs<R> a) {
     const R tv = cvt_hw<R>(s_tv[l * SROW + p]);
     const R vgt = u * gt0 + w * gt1;
     const R ttens = (-tva - vgt) + R(kKappa) * tv * omega;
-    const double tnew = spd * (dbl_hw(ttens * dt) + tm);
+    // float -> double on the integer pipe (dbl: a few integer instructions) relieves the
+    // FP64 pipe this kernel is bound by; double -> float stays on the hardware path
+    // (cvt_hw), whose integer form is long enough to cost more than it saves.
+    const double tnew = spd * (dbl(ttens * dt) + tm);
     // velocity (compute_velocity_np1 with compute_energy_grad)
     const R rr = R(kRgas) * (tv * rp);
     R eg0 = rr * gp0, eg1 = rr * gp1;
@@ -230,10 +233,10 @@ __global__ void __launch_bounds__(LG * 16) k_caar(CaarArgs<R> a) {
     const R vort = vorticity_sphere(t, m, u, w) + fcor;
     eg0 = -eg0 + (-vva0 + w * vort);
     eg1 = -eg1 + (-vva1 - u * vort);
-    const double vn0_ = spd * (dbl_hw(eg0 * dt) + vm0);
-    const double vn1_ = spd * (dbl_hw(eg1 * dt) + vm1);
+    const double vn0_ = spd * (dbl(eg0 * dt) + vm0);
+    const double vn1_ = spd * (dbl(eg1 * dt) + vm1);
     // dp3d (compute_dp3d_np1, eta_dot_dpdn = 0 for rsplit > 0)
-    const double dnew = spd * (dm - dbl_hw(((etu + div) - etl) * dt));
+    const double dnew = spd * (dm - dbl(((etu + div) - etl) * dt));
     out[l * 64 + p] = vn0_;
     out[l * 64 + 16 + p] = vn1_;
     out[l * 64 + 32 + p] = tnew;
@@ -1253,12 +1256,13 @@ __global__ void __launch_bounds__(RT) k_remap(RemapArgs a) {
   float* coeff = reinterpret_cast<float*>(sm + R_COEF);
   if constexpr (kF32<R>) {
     {
-      for (int i = lane; i < 740; i += 32) gf[i] = (float)g[i];
+      // conversions on the integer pipe (d2f_rn): the FP64 pipe is this kernel's limit
+      for (int i = lane; i < 740; i += 32) gf[i] = d2f_rn(g[i]);
       if (own) {
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
-          z2f[l0 + k] = (float)z2[l0 + k];
-          rDf[l0 + k] = (float)rD[l0 + k];
+          z2f[l0 + k] = d2f_rn(z2[l0 + k]);
+          rDf[l0 + k] = d2f_rn(rD[l0 + k]);
         }
       }
       __syncwarp();
@@ -1278,7 +1282,7 @@ __global__ void __launch_bounds__(RT) k_remap(RemapArgs a) {
         else if (var == 2) x3[k] = a.T[sb + (size_t)l * 16] * s3[k];
         else x3[k] = a.qdp[((((size_t)e * QTL + a.n0_qdp) * a.Q + (var - 3)) * NLEV + l) * 16 + p];
         if (!lo) A[l] = x3[k] * rD[l];
-        else if (var >= 3) Af[l] = (float)x3[k] * rDf[l];
+        else if (var >= 3) Af[l] = d2f_rn(x3[k]) * rDf[l];
       }
     }
     double aref = 0.0;  // mixed form, v and T: column mean
@@ -1297,7 +1301,7 @@ __global__ void __launch_bounds__(RT) k_remap(RemapArgs a) {
         aref = __shfl_sync(FULL, ex, 23) / pio[NLEV];
         if (own) {
 #pragma unroll
-          for (int k = 0; k < 3; ++k) Af[l0 + k] = (float)fma(x3[k], rD[l0 + k], -aref);
+          for (int k = 0; k < 3; ++k) Af[l0 + k] = d2f_rn(fma(x3[k], rD[l0 + k], -aref));
         }
       }
     }
