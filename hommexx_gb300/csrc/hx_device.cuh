@@ -391,15 +391,23 @@ template <typename R> __device__ __forceinline__ R rel_hw(double x) {
   else return x;
 }
 
-// 1/x in FP64 from the FP32 reciprocal of x refined by two Newton-Raphson steps
-// r <- r + r (1 - x r), each of which squares the relative error (about 2^-23 -> 2^-46
-// -> below one ulp of the result); rf returns the FP32 reciprocal.  For positive normal
-// x within the FP32 exponent range (2^-126 .. 2^127); within one ulp of 1.0 / x.
+// 1/x in FP64 from the approximate FP32 reciprocal of x (__fdividef, within 2 ulp)
+// refined by two Newton-Raphson steps r <- r + r (1 - x r), each of which squares the
+// relative error (about 2^-22 -> 2^-44 -> below one ulp of the result); rf returns the
+// FP32 reciprocal.  For x of magnitude 2^-125 .. 2^125; within one ulp of 1.0 / x.
 __device__ __forceinline__ double rcp_newton(double x, float& rf) {
-  rf = 1.0f / (float)x;
+  rf = __fdividef(1.0f, (float)x);
   double r = f2d(rf);  // exact; on the integer pipe
   r = fma(r, fma(-x, r, 1.0), r);
   return fma(r, fma(-x, r, 1.0), r);
+}
+
+// a / b from r = rcp_newton(b): the product a r corrected once by its residual,
+// q + r (a - q b) (the final step of Markstein's division, IBM J. Res. Dev. 34 (1990)
+// 111-119), within one ulp of the IEEE quotient.  Same domain for b as rcp_newton.
+__device__ __forceinline__ double div_newton(double a, double b, double r) {
+  const double q = a * r;
+  return fma(fma(-q, b, a), r, q);
 }
 
 // Brackets one launch for the per-kernel timing hooks.

@@ -478,14 +478,24 @@ __device__ __forceinline__ void eq_index_dss(int nq, int& e, int& q, int& l, int
   l = blockIdx.y * EQ_LEVELS + lo;
 }
 
-__global__ void __launch_bounds__(EQ_THREADS) k_update_q(int Q, const double* qdp, double* Qc,
-                                                          const double* ps_v, int np1, int np1_qdp,
-                                                          double ps0) {
-  int e, q, l, p;
-  eq_index(Q, e, q, l, p);
+// update_q (prim_driver.cpp:171-206): Q = Qdp / dp, dp = dA ps0 + dB ps_v.  Grid (E, 9),
+// 128 threads: one thread per (element, level, point) forms 1/dp once and divides every
+// tracer by it with one corrected multiplication (div_newton, within one ulp of the IEEE
+// quotient); a thickness outside (1e-30, 1e30) takes the IEEE division.
+__global__ void __launch_bounds__(128) k_update_q(int Q, const double* __restrict__ qdp, double* __restrict__ Qc,
+                                                  const double* __restrict__ ps_v, int np1, int np1_qdp,
+                                                  double ps0) {
+  const int e = blockIdx.x, l = blockIdx.y * 8 + (threadIdx.x >> 4), p = threadIdx.x & 15;
   const double dp = c_ai_delta[l] * ps0 + c_bi_delta[l] * ps_v[((size_t)e * NTL + np1) * 16 + p];
-  Qc[(((size_t)e * Q + q) * NLEV + l) * 16 + p] =
-      qdp[((((size_t)e * QTL + np1_qdp) * Q + q) * NLEV + l) * 16 + p] / dp;
+  const double* src = qdp + ((((size_t)e * QTL + np1_qdp) * Q) * NLEV + l) * 16 + p;
+  double* dst = Qc + (((size_t)e * Q) * NLEV + l) * 16 + p;
+  if (dp > 1e-30 && dp < 1e30) {
+    float rf;
+    const double r = rcp_newton(dp, rf);
+    for (int q = 0; q < Q; ++q) dst[(size_t)q * NLEV * 16] = div_newton(src[(size_t)q * NLEV * 16], dp, r);
+  } else {
+    for (int q = 0; q < Q; ++q) dst[(size_t)q * NLEV * 16] = src[(size_t)q * NLEV * 16] / dp;
+  }
 }
 
 // Tracer mass diagnostics (Diagnostics.cpp:37-84): one thread per (element, tracer, GLL
@@ -1159,14 +1169,15 @@ __global__ void __launch_bounds__(RT) k_remap(RemapArgs a) {
       const int l = l0 + k;
       t3[k] = (c_hyai[l + 1] - c_hyai[l]) * a.ps0 + (c_hybi[l + 1] - c_hybi[l]) * ps;
       tgt[l] = t3[k];
-      rt3[k] = 1.0 / t3[k];
+      float rf;
+      rt3[k] = rcp_newton(t3[k], rf);
       if (a.rsplit == 0) {  // vertically Eulerian source thickness (RemapFunctor.hpp:42-100)
         const size_t ie = ((size_t)e * NLEV + l) * 16 + p;
         const double en = l + 1 < NLEV ? a.eta[ie + 16] : 0.0;
         s3[k] = t3[k] + a.dt * (en - a.eta[ie]);
       }
       D[l] = s3[k];
-      rD[l] = 1.0 / s3[k];
+      rD[l] = rcp_newton(s3[k], rf);
       if (isnan(s3[k]) || s3[k] < 0.0) atomicExch(a.invalid, 1);
     }
   }
@@ -1211,7 +1222,7 @@ __global__ void __launch_bounds__(RT) k_remap(RemapArgs a) {
         atomicExch(a.invalid, 1);
       }
       kid[k] = kk - 1;
-      z2[k] = (pin[k + 1] - (pio[kk - 1] + pio[kk]) * 0.5) / D[kk - 1];
+      z2[k] = (pin[k + 1] - (pio[kk - 1] + pio[kk]) * 0.5) * rD[kk - 1];
     }
   }
   // compute_grids (double)
@@ -1221,16 +1232,18 @@ __global__ void __launch_bounds__(RT) k_remap(RemapArgs a) {
       const int j = 3 * lane + k3;
       if (j < NLEV + 2) {
         const double dm2 = D[j - 2], dm1 = D[j - 1], d0 = D[j];
-        const double r10 = 1.0 / (dm1 + d0);  // shared by g1, g3, g5
-        g[0 * 74 + j] = dm1 / (dm2 + dm1 + d0);
+        // reciprocals by Newton-Raphson (rcp_newton, within one ulp)
+        float rf;
+        const double r10 = rcp_newton(dm1 + d0, rf);  // shared by g1, g3, g5
+        g[0 * 74 + j] = dm1 * rcp_newton(dm2 + dm1 + d0, rf);
         g[1 * 74 + j] = (2.0 * dm2 + dm1) * r10;
-        g[2 * 74 + j] = (dm1 + 2.0 * d0) / (dm2 + dm1);
+        g[2 * 74 + j] = (dm1 + 2.0 * d0) * rcp_newton(dm2 + dm1, rf);
         if (j < NLEV + 1) {
           const double dp1 = D[j + 1];
-          const double r6 = 1.0 / (2.0 * dm1 + d0);  // shared by g6, g8
-          const double r7 = 1.0 / (2.0 * d0 + dm1);  // shared by g7, g9
+          const double r6 = rcp_newton(2.0 * dm1 + d0, rf);  // shared by g6, g8
+          const double r7 = rcp_newton(2.0 * d0 + dm1, rf);  // shared by g7, g9
           g[3 * 74 + j] = dm1 * r10;
-          g[4 * 74 + j] = 1.0 / (dm2 + dm1 + d0 + dp1);
+          g[4 * 74 + j] = rcp_newton(dm2 + dm1 + d0 + dp1, rf);
           g[5 * 74 + j] = (2.0 * dm1 * d0) * r10;
           g[6 * 74 + j] = (dm2 + dm1) * r6;
           g[7 * 74 + j] = (dp1 + d0) * r7;
@@ -1547,7 +1560,7 @@ void launch_update_q(int E, int Q, const double* qdp, double* Qc, const double* 
                      double ps0, cudaStream_t s) {
   if (Q == 0) return;
   KScope k("update_q", s);
-  k_update_q<<<dim3(E * Q, NLEV / EQ_LEVELS), EQ_THREADS, 0, s>>>(Q, qdp, Qc, ps_v, np1, np1_qdp, ps0);
+  k_update_q<<<dim3(E, NLEV / 8), 128, 0, s>>>(Q, qdp, Qc, ps_v, np1, np1_qdp, ps0);
 }
 
 void launch_dss_inplace(int E, int nf, double* base, long long fs, long long es, int ls, double* scr,
@@ -1569,7 +1582,7 @@ void launch_cam_forcing(int E, int Q, double* T, double* v, const double* ft, co
   KScope k("cam_forcing_tracers", s);
   if (moist) k_ps_forcing<<<nblk((long long)E * 16, 128), 128, 0, s>>>(E, Q, fq, qdp, ps_v, n0, n0_qdp, dt);
   k_tracer_forcing<<<dim3(E * Q, NLEV / EQ_LEVELS), EQ_THREADS, 0, s>>>(Q, fq, qdp, n0_qdp, dt);
-  k_update_q<<<dim3(E * Q, NLEV / EQ_LEVELS), EQ_THREADS, 0, s>>>(Q, qdp, Qc, ps_v, n0, n0_qdp, ps0);
+  k_update_q<<<dim3(E, NLEV / 8), 128, 0, s>>>(Q, qdp, Qc, ps_v, n0, n0_qdp, ps0);
 }
 
 void launch_diag_scalars(int E, int Q, const double* qdp, const double* Qc, int tq, double* qvar,

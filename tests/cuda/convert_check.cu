@@ -1,8 +1,9 @@
 // Checks the integer-pipe double<->float conversions of hx_device.cuh against the
 // hardware conversions, bit for bit: random bit patterns over every exponent, ties,
-// zeros, subnormals, overflow, infinities and NaN; and the Newton-Raphson reciprocal
-// rcp_newton against IEEE division (within one ulp, over positive x of exponents
-// -120 .. 120).  Prints the mismatch counts; exit status 0 when there are none.
+// zeros, subnormals, overflow, infinities and NaN; the Newton-Raphson reciprocal
+// rcp_newton against IEEE division over positive divisors of exponents -120 .. 120, and
+// the corrected quotient div_newton over numerators of exponents -300 .. 300 (both
+// within one ulp).  Prints the mismatch counts; exit status 0 when there are none.
 #include <cstdio>
 #include <cstdlib>
 
@@ -43,20 +44,29 @@ __global__ void check(unsigned long long n, unsigned long long* bad) {
   const long long du = r1 > r2 ? r1 - r2 : r2 - r1;
   if (du > 1) atomicAdd(bad + 2, 1ULL);
   if (du == 1) atomicAdd(bad + 3, 1ULL);
+  // quotient: numerators of any sign over exponents -300 .. 300, the same divisors
+  const unsigned long long m3 = mix(i ^ 0x13579BDFULL);
+  const double a3 = __longlong_as_double((long long)((m3 & 0x800FFFFFFFFFFFFFULL) |
+                                                     ((unsigned long long)(1023 - 300 + (int)((m3 >> 52) % 601)) << 52)));
+  const long long q1 = __double_as_longlong(hx::div_newton(a3, x2, hx::rcp_newton(x2, rf)));
+  const long long q2 = __double_as_longlong(a3 / x2);
+  const long long dq = q1 > q2 ? q1 - q2 : q2 - q1;
+  if (dq > 1) atomicAdd(bad + 4, 1ULL);
+  if (dq == 1) atomicAdd(bad + 5, 1ULL);
 }
 
 }  // namespace
 
 int main() {
   unsigned long long* bad = nullptr;
-  if (cudaMalloc(&bad, 4 * sizeof(unsigned long long)) != cudaSuccess) return 2;
-  cudaMemset(bad, 0, 4 * sizeof(unsigned long long));
+  if (cudaMalloc(&bad, 6 * sizeof(unsigned long long)) != cudaSuccess) return 2;
+  cudaMemset(bad, 0, 6 * sizeof(unsigned long long));
   const unsigned long long n = 1ULL << 26;
   check<<<(unsigned)((n + 255) / 256), 256>>>(n, bad);
-  unsigned long long h[4] = {0, 0, 0, 0};
+  unsigned long long h[6] = {0, 0, 0, 0, 0, 0};
   if (cudaMemcpy(h, bad, sizeof(h), cudaMemcpyDeviceToHost) != cudaSuccess) return 2;
-  std::printf("d2f mismatches %llu, f2d mismatches %llu, rcp beyond 1 ulp %llu (1 ulp: %llu), of %llu each\n",
-              h[0], h[1], h[2], h[3], n);
+  std::printf("d2f mismatches %llu, f2d mismatches %llu, rcp beyond 1 ulp %llu (1 ulp: %llu), "
+              "div beyond 1 ulp %llu (1 ulp: %llu), of %llu each\n", h[0], h[1], h[2], h[3], h[4], h[5], n);
   cudaFree(bad);
-  return (h[0] == 0 && h[1] == 0 && h[2] == 0) ? 0 : 1;
+  return (h[0] == 0 && h[1] == 0 && h[2] == 0 && h[4] == 0) ? 0 : 1;
 }

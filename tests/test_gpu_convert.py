@@ -1,6 +1,7 @@
 """The mixed form's integer-pipe double<->float conversions (hx_device.cuh) equal the
 hardware conversions bit for bit (2^26 random inputs each way, with ties, zeros,
-subnormal-range exponents, overflow, infinities and NaN)."""
+subnormal-range exponents, overflow, infinities and NaN); the Newton-Raphson reciprocal
+rcp_newton and the corrected quotient div_newton stay within one ulp of IEEE division."""
 import os
 import subprocess
 
