@@ -53,17 +53,19 @@ FALLBACK_HBM_GBS = 6800.0
 
 
 # DRAM bytes (read + write) per launch and FP64-pipe active fraction measured by ncu at
-# ne16 L72 q10 (1536 elements, profiles/kernels_ne16_fp64_mixed_adjoint.md), per form.
-# Traffic is scaled to the run's size by the element count (levels and tracers fixed).
+# ne16 L72 q10 (1536 elements; dram__bytes_read.sum + dram__bytes_write.sum and
+# sm__pipe_fp64_cycles_active of the third launch of each kernel), per form.  Traffic is
+# scaled to the run's size by the element count (levels and tracers fixed).
 NCU_NE16 = {
-    "fp64": {"euler_aal_tracer": (473.8e6, 0.836), "caar_stage": (153.8e6, 0.857),
-             "hv_laplace2": (158.0e6, 0.820), "ppm_remap": (328.0e6, 0.851),
-             "euler_bih_post": (278.0e6, 0.870), "hv_laplace1": (73.6e6, 0.886),
-             "euler_bih_pre": (258.5e6, 0.883), "euler_dss_qdp": (402.1e6, 0.820),
-             "euler_qminmax": (283.8e6, 0.558)},
-    "mixed": {"euler_aal_tracer": (473.9e6, 0.368), "caar_stage": (153.2e6, 0.816),
-              "hv_laplace2": (156.0e6, 0.583), "ppm_remap": (328.8e6, 0.835),
-              "euler_dss_qdp": (402.2e6, 0.820)},
+    "fp64": {"euler_aal_tracer": (473.5e6, 0.836), "caar_stage": (153.5e6, 0.857),
+             "hv_laplace2": (161.5e6, 0.814), "ppm_remap": (327.9e6, 0.849),
+             "euler_bih_post": (281.9e6, 0.870), "hv_laplace1": (77.3e6, 0.892),
+             "euler_bih_pre": (260.5e6, 0.905), "euler_dss_qdp": (400.1e6, 0.818),
+             "euler_qminmax": (283.8e6, 0.552)},
+    "mixed": {"euler_aal_tracer": (472.4e6, 0.385), "caar_stage": (151.3e6, 0.785),
+              "hv_laplace2": (151.0e6, 0.491), "ppm_remap": (328.8e6, 0.643),
+              "euler_dss_qdp": (400.0e6, 0.817), "euler_qminmax": (282.1e6, 0.325),
+              "euler_bih_post": (273.9e6, 0.482)},
 }
 
 
