@@ -169,6 +169,36 @@ def test_subcycle(pair, rsplit, nsub):
     _assert_close(errs)
 
 
+@pytest.mark.parametrize("ne,Q,kw", [
+    (1, 1, dict(rsplit=3)),                                   # 6 elements: every corner a cube corner
+    (2, 0, dict(rsplit=3)),                                   # no tracers
+    (2, 7, dict(rsplit=2, qsplit=2)),                         # odd tracer count, two dynamics steps per tracer step
+    (3, 3, dict(rsplit=1, hypervis_subcycle=1, nu_div=2.5e16)),  # nu_div != nu (nu_ratio)
+    (2, 2, dict(rsplit=3, hypervis_subcycle=4, nu_top=0.0)),  # no sponge
+])
+def test_subcycle_edge_cases(pair, ne, Q, kw):
+    """Two remap intervals through prim_run_subcycle_c on small, tracer-free and odd-sized
+    configurations, results through cxx_push_results_to_f90."""
+    g, o = pair(ne=ne, Q=Q, **kw)
+    for _ in range(2):
+        assert g.run_subcycle(DT) == o.run_subcycle(DT)
+    rg, ro = g.push_results(), o.push_results()
+    errs = {k: H.rel_err(rg[k], ro[k]) for k in rg if ro[k].size}
+    _assert_close(errs)
+    if Q == 0:
+        assert rg["Qdp"].size == 0 and rg["Q"].size == 0
+
+
+def test_subcycle_edge_mixed_ne1(pair):
+    """The mixed form on the 6-element cube stays close to the FP64 oracle."""
+    g, o = pair(ne=1, Q=2, precision=1, rsplit=3)
+    g.run_subcycle(DT)
+    o.run_subcycle(DT)
+    rg, ro = g.push_results(), o.push_results()
+    errs = {k: H.rel_err(rg[k], ro[k]) for k in ("T", "dp3d", "v", "Qdp", "ps_v")}
+    assert errs["T"] < 1e-6 and errs["dp3d"] < 1e-5 and errs["ps_v"] < 1e-7, errs
+
+
 def _forcing(ne, Q, seed):
     rng = np.random.default_rng(seed)
     E = 6 * ne * ne
