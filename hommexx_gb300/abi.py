@@ -94,6 +94,8 @@ class HxLibrary:
         L.hx_run_remap.argtypes = [C.c_int, C.c_int, C.c_double]
         L.hx_run_prim_step.argtypes = [C.c_double]
         L.hx_run_dss.argtypes = [C.c_char_p, C.c_int, C.c_int]
+        L.hx_set_async_copies.argtypes = [C.c_int]
+        L.hx_stream_results.argtypes = [C.c_void_p] * 7
         L.hx_write_restart.argtypes = [C.c_char_p]
         L.hx_read_restart.argtypes = [C.c_char_p]
         L.hx_launch_count.restype = C.c_longlong
@@ -230,6 +232,21 @@ class HxLibrary:
                       metdet=a["metdet"], mp=a["mp"], spheremp=a["spheremp"], rspheremp=a["rspheremp"],
                       fcor=a["fcor"], phis=np.zeros((E, NP, NP)), lat=a["lat"], lon=a["lon"],
                       vec_sph2cart=a["vec_sph2cart"], tensorvisc=a["tensorvisc"], connections=conn)
+
+    # -- copies that overlap the step --------------------------------------------------
+    def set_async_copies(self, on: bool = True) -> None:
+        """hx_set_async_copies: Qdp streams in while the next interval's dynamics run."""
+        if self.lib.hx_set_async_copies(C.c_int(1 if on else 0)):
+            self.check("hx_set_async_copies")
+
+    def stream_results(self, out: dict | None) -> None:
+        """hx_stream_results: every interval copies its results into ``out`` (the arrays
+        ``push_results`` fills) as they become final; None stops."""
+        keys = ("v", "T", "dp3d", "Qdp", "Q", "ps_v", "omega_p")
+        ptrs = [C.c_void_p(out[k].ctypes.data) if out is not None else C.c_void_p(None) for k in keys]
+        self._keep["stream"] = out
+        if self.lib.hx_stream_results(*ptrs):
+            self.check("hx_stream_results")
 
     # -- restart files (format of include/hxgpu.h) -------------------------------------
     RESTART_HEADER = struct.Struct("<8sII6i5iiQQ48s")

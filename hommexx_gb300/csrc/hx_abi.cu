@@ -86,6 +86,8 @@ struct Timing {
 };
 Timing g_tim;
 cudaStream_t g_stream = nullptr;
+// Copies that overlap the step (hx_set_async_copies, hx_stream_results) run on g_copy.
+cudaStream_t g_copy = nullptr;
 
 void flush_timing() {
   if (g_tim.pending.empty()) return;
@@ -141,6 +143,8 @@ struct Backend {
   virtual void traj_vjp(const double* vb, const double* Tb, const double* dpb, double* vg, double* Tg,
                         double* dpg) = 0;
   virtual void write_restart(const std::string& path) = 0;
+  // Orders the session stream after any Qdp copy still streaming in (hx_set_async_copies).
+  virtual void copies_ready() = 0;
   virtual void read_restart(const std::string& path) = 0;
 };
 
@@ -164,6 +168,10 @@ struct Session {
   int traj_mode = 0;  // checkpointing of the dry trajectory (hx_traj_set_checkpointing)
   // init_diagnostics_c host arrays: Q, Qvar, Qmass, Q1mass, IEner, IEner_wet, KEner, PEner
   double* diag[8] = {};
+  // hx_set_async_copies / hx_stream_results
+  bool async_copies = false;
+  double* stream_to[7] = {};   // v, T, dp3d, Qdp, Q, ps_v, omega_p host destinations
+  bool streamed = false;       // the destinations hold the state of the last interval
   ~Session() {}
 };
 
@@ -231,6 +239,9 @@ struct BackendT : Backend {
   double* lapm = 0;  // FP64 form: dense weak Laplacian per element
   double *fm = 0, *ft = 0, *fq = 0;  // CAM forcing, Fortran layouts (allocated on first push)
   double *phis_d = 0, *diag_d = 0;   // FP64 phis; diagnostics scratch (allocated on first use)
+  cudaEvent_t ev_qdp_in = nullptr, ev_mark = nullptr;
+  bool qdp_pending = false;   // Qdp still streaming in on g_copy
+  bool stream_last = false;   // the next prim_step is the interval's last
   int *tab_cnt = 0, *tab_src = 0, *nbr = 0, *invalid = 0;
   int* h_invalid = nullptr;
   size_t staging_n = 0;
@@ -249,6 +260,8 @@ struct BackendT : Backend {
     for (void* p : ptrs)
       if (p) cudaFree(p);
     if (h_invalid) cudaFreeHost(h_invalid);
+    if (ev_qdp_in) cudaEventDestroy(ev_qdp_in);
+    if (ev_mark) cudaEventDestroy(ev_mark);
     free_traj();
   }
 
@@ -279,6 +292,8 @@ struct BackendT : Backend {
     gen_scr = dalloc<double>(n3 * 2);  // generic DSS of v / T / dp3d / omega_p (Qdp uses qscr)
     invalid = dalloc<int>(1);
     ck(cudaMallocHost(&h_invalid, sizeof(int)), "cudaMallocHost");
+    ck(cudaEventCreateWithFlags(&ev_qdp_in, cudaEventDisableTiming), "cudaEventCreate");
+    ck(cudaEventCreateWithFlags(&ev_mark, cudaEventDisableTiming), "cudaEventCreate");
     wk = Work{v, T, dp, phi, dpdiss_ave, dpdiss_bih, ps_v};
   }
 
@@ -322,8 +337,74 @@ struct BackendT : Backend {
     to_dev(v, hv, n3 * NTL * 2);
     to_dev(T, hT, n3 * NTL);
     to_dev(dp, hdp, n3 * NTL);
-    if (Q > 0) ck(cudaMemcpyAsync(qdp, hq, n3 * QTL * Q * sizeof(double), cudaMemcpyHostToDevice, g_stream), "H2D qdp");
+    copies_ready();
+    if (Q > 0 && s.async_copies) {
+      // Qdp streams in on g_copy, after the work already queued on g_stream, while the
+      // next interval's dynamics run; its first reader waits for ev_qdp_in.
+      ck(cudaEventRecord(ev_mark, g_stream), "cudaEventRecord");
+      ck(cudaStreamWaitEvent(g_copy, ev_mark, 0), "cudaStreamWaitEvent");
+      ck(cudaMemcpyAsync(qdp, hq, n3 * QTL * Q * sizeof(double), cudaMemcpyHostToDevice, g_copy), "H2D qdp");
+      ck(cudaEventRecord(ev_qdp_in, g_copy), "cudaEventRecord");
+      qdp_pending = true;
+    } else if (Q > 0) {
+      ck(cudaMemcpyAsync(qdp, hq, n3 * QTL * Q * sizeof(double), cudaMemcpyHostToDevice, g_stream), "H2D qdp");
+    }
     ck(cudaMemcpyAsync(ps_v, hps, (size_t)E * NTL * 16 * sizeof(double), cudaMemcpyHostToDevice, g_stream), "H2D ps");
+  }
+
+  void copies_ready() override {
+    if (!qdp_pending) return;
+    ck(cudaStreamWaitEvent(g_stream, ev_qdp_in, 0), "cudaStreamWaitEvent");
+    qdp_pending = false;
+  }
+
+  // hx_stream_results: device -> host copies on g_copy, each enqueued once its data is
+  // final (after what g_stream has queued so far).  Level lvl of a field whose host and
+  // device layouts are [E][nlev][block].
+  void stream_level(int which, const double* dev, size_t block, int nlev, int lvl) {
+    double* host = s.stream_to[which];
+    if (!host || block == 0) return;
+    const size_t w = block * sizeof(double), pitch = w * nlev;
+    ck(cudaMemcpy2DAsync(host + (size_t)lvl * block, pitch, dev + (size_t)lvl * block, pitch, w, E,
+                         cudaMemcpyDeviceToHost, g_copy), "D2H stream");
+  }
+  void stream_mark() {
+    ck(cudaEventRecord(ev_mark, g_stream), "cudaEventRecord");
+    ck(cudaStreamWaitEvent(g_copy, ev_mark, 0), "cudaStreamWaitEvent");
+  }
+  bool streaming() const { return s.stream_to[0] != nullptr; }
+  // the dynamics levels other than np1 are final after the last dynamics; omega_p too
+  // when there are no tracers (the tracer step's last stage DSSes it in place)
+  void stream_dynamics(int np1) {
+    stream_mark();
+    for (int lvl = 0; lvl < NTL; ++lvl) {
+      if (lvl == np1) continue;
+      stream_level(0, v, (size_t)NLEV * 32, NTL, lvl);
+      stream_level(1, T, (size_t)NLEV * 16, NTL, lvl);
+      stream_level(2, dp, (size_t)NLEV * 16, NTL, lvl);
+    }
+    if (Q == 0) stream_level(6, omega_p, (size_t)NLEV * 16, 1, 0);
+  }
+  // the tracer level the remap does not write and omega_p are final after the last
+  // tracer step
+  void stream_tracers(int n0_qdp) {
+    if (Q == 0) return;
+    stream_mark();
+    stream_level(3, qdp, (size_t)Q * NLEV * 16, QTL, n0_qdp);
+    stream_level(6, omega_p, (size_t)NLEV * 16, 1, 0);
+  }
+  // the rest after the remap and update_q; waits for every streamed copy
+  void stream_rest(int np1, int np1_qdp) {
+    stream_mark();
+    stream_level(0, v, (size_t)NLEV * 32, NTL, np1);
+    stream_level(1, T, (size_t)NLEV * 16, NTL, np1);
+    stream_level(2, dp, (size_t)NLEV * 16, NTL, np1);
+    stream_level(5, ps_v, (size_t)NTL * 16, 1, 0);
+    if (Q > 0) {
+      stream_level(3, qdp, (size_t)Q * NLEV * 16, QTL, np1_qdp);
+      stream_level(4, Qc, (size_t)Q * NLEV * 16, 1, 0);
+    }
+    ck(cudaStreamSynchronize(g_copy), "streamed results");
   }
 
   void push(double* hv, double* hT, double* hdp, double* hq, double* hQ, double* hps, double* homega) override {
@@ -506,7 +587,12 @@ struct BackendT : Backend {
       rk5(s.tl.nm1, s.tl.n0, s.tl.np1, n0_qdp, dt, w);
       hypervis(s.tl.np1, dt, w);
     }
-    if (p.qsize > 0) tracers_rk2(dt * p.qsplit);
+    if (stream_last) stream_dynamics(s.tl.np1);
+    if (p.qsize > 0) {
+      copies_ready();
+      tracers_rk2(dt * p.qsplit);
+      if (stream_last) stream_tracers(s.tl.n0_qdp);
+    }
   }
 
   // cxx_f90_interface.cpp:180-205
@@ -598,6 +684,9 @@ struct BackendT : Backend {
     bool diag = (p.state_frequency > 0 && nstep_end % p.state_frequency == 0) || nstep_end == s.tl.nstep0 ||
                 nstep_end >= last_time_step;
     if (p.disable_diagnostics || !s.diag[0]) diag = false;
+    if (diag || p.moist || p.ftype == 0) copies_ready();
+    const bool stream = streaming();
+    s.streamed = false;
     if (diag) {
       diag_scalars(true, 3);
       energy_halftimes(true, 2);
@@ -615,23 +704,32 @@ struct BackendT : Backend {
     }
     launch_dp_from_ps(E, dp, ps_v, s.tl.n0, s.ps0, g_stream);
     post("dp3d_from_ps");
+    stream_last = stream && p.rsplit <= 1;
     prim_step(dt);
     for (int r = 1; r < p.rsplit; ++r) {
       s.tl.update_dynamics_levels();
+      stream_last = stream && r == p.rsplit - 1;
       prim_step(dt);
     }
+    stream_last = false;
+    copies_ready();
     s.tl.update_tracers_levels(p.qsplit);
     launch_remap(s.tl.np1, s.tl.np1_qdp, true, dt_remap);
     launch_update_q(E, Q, qdp, Qc, ps_v, s.tl.np1, s.tl.np1_qdp, s.ps0, g_stream);
     post("update_q");
     const int st = remap_status();
     if (st) {
+      if (stream) cudaStreamSynchronize(g_copy);  // no copy outlives the call
       s.tl.update_dynamics_levels();
       fail(101, "Negative (or nan) layer thickness detected, aborting!");
     }
     if (diag) {
       diag_scalars(false, 1);
       energy_halftimes(false, 1);
+    }
+    if (stream) {
+      stream_rest(s.tl.np1, s.tl.np1_qdp);
+      s.streamed = true;
     }
     s.tl.update_dynamics_levels();
   }
@@ -1127,9 +1225,13 @@ int run(F&& f) {
   return 0;
 }
 
+// Every entry point but prim_run_subcycle_c: any Qdp still streaming in is ordered
+// before the call's work, and the streamed results stop standing for the state.
 Backend& B() {
   Session& s = S();
   if (!s.be) fail(HX_ERR_STATE, "library not initialised (call init_elements_2d_c first)");
+  s.streamed = false;
+  s.be->copies_ready();
   return *s.be;
 }
 
@@ -1163,6 +1265,7 @@ void initialize_hommexx_session(void) {
       if (n < 1) fail(HX_ERR_CUDA, "no CUDA device");
       ck(cudaSetDevice(0), "cudaSetDevice");
       ck(cudaStreamCreateWithFlags(&g_stream, cudaStreamNonBlocking), "cudaStreamCreate");
+      ck(cudaStreamCreateWithFlags(&g_copy, cudaStreamNonBlocking), "cudaStreamCreate");
       g_tim.pool.resize(8192);
       for (auto& e : g_tim.pool) ck(cudaEventCreate(&e), "cudaEventCreate");
       set_kernel_hook(hook_before, hook_after);
@@ -1173,6 +1276,7 @@ void initialize_hommexx_session(void) {
 void finalize_hommexx_session(void) {
   run([] {
     if (g_stream) cudaStreamSynchronize(g_stream);
+    if (g_copy) cudaStreamSynchronize(g_copy);
     delete g_s;
     g_s = nullptr;
     g_tim.stats.clear();
@@ -1331,7 +1435,9 @@ void init_time_level_c(const int* nm1, const int* n0, const int* np1, const int*
 void prim_run_subcycle_c(const double* dt, int* nstep, int* nm1, int* n0, int* np1,
                          const int* last_time_step) {
   run([&] {
-    B().run_subcycle(*dt, last_time_step ? *last_time_step : INT_MAX);
+    Session& s = S();
+    if (!s.be) fail(HX_ERR_STATE, "library not initialised (call init_elements_2d_c first)");
+    s.be->run_subcycle(*dt, last_time_step ? *last_time_step : INT_MAX);
     const TimeLevel& t = S().tl;
     *nstep = t.nstep; *nm1 = t.nm1; *n0 = t.n0; *np1 = t.np1;
   });
@@ -1339,7 +1445,35 @@ void prim_run_subcycle_c(const double* dt, int* nstep, int* nm1, int* n0, int* n
 
 void cxx_push_results_to_f90(double* const* v, double* const* T, double* const* dp3d, double* const* Qdp,
                              double* const* Q, double* const* ps_v, double* const* omega_p) {
-  run([&] { B().push(*v, *T, *dp3d, *Qdp, *Q, *ps_v, *omega_p); });
+  run([&] {
+    Session& s = S();
+    double* const p[7] = {*v, *T, *dp3d, *Qdp, *Q, *ps_v, *omega_p};
+    bool same = s.streamed;
+    for (int i = 0; i < 7; ++i) same = same && p[i] == s.stream_to[i];
+    if (same) return;  // prim_run_subcycle_c already streamed this state here
+    B().push(*v, *T, *dp3d, *Qdp, *Q, *ps_v, *omega_p);
+  });
+}
+
+int hx_set_async_copies(int on) {
+  return run([&] {
+    Session& s = S();
+    if (!on && s.be) s.be->copies_ready();
+    s.async_copies = on != 0;
+  });
+}
+
+int hx_stream_results(double* v, double* T, double* dp3d, double* Qdp, double* Q, double* ps_v,
+                      double* omega_p) {
+  return run([&] {
+    Session& s = S();
+    double* const p[7] = {v, T, dp3d, Qdp, Q, ps_v, omega_p};
+    int n = 0;
+    for (int i = 0; i < 7; ++i) n += p[i] != nullptr;
+    if (n != 0 && n != 7) fail(13, "hx_stream_results: give all seven destinations or none");
+    for (int i = 0; i < 7; ++i) s.stream_to[i] = p[i];
+    s.streamed = false;
+  });
 }
 
 int hx_last_error(char* buf, int buflen) {

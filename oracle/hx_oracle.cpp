@@ -125,6 +125,8 @@ struct Ctx {
   std::vector<double> fm, ft, fq;  // CAM forcing: FM [E][2][16][NLEV], FT/FQ level-contiguous
   // init_diagnostics_c host arrays: Q, Qvar, Qmass, Q1mass, IEner, IEner_wet, KEner, PEner
   double* diag[8] = {};
+  double* stream_to[7] = {};  // hx_stream_results destinations
+  bool streamed = false;
   std::vector<double> phi, omega_p, eta_dot_dpdn, derived_dp, divdp, divdp_proj,
       dpdiss_ave, dpdiss_bih, vn0;
   // buffers
@@ -1802,14 +1804,27 @@ void init_time_level_c(const int* nm1, const int* n0, const int* np1, const int*
 
 void prim_run_subcycle_c(const double* dt, int* nstep, int* nm1, int* n0, int* np1,
                          const int* last_time_step) {
-  C().last_err = 0;
+  Ctx& c = C();
+  c.last_err = 0;
+  c.streamed = false;
   prim_run_subcycle(*dt, *nstep, *nm1, *n0, *np1, last_time_step ? *last_time_step : INT_MAX);
+  if (c.stream_to[0] && c.last_err == 0) {
+    double* const* p = c.stream_to;
+    cxx_push_results_to_f90(&p[0], &p[1], &p[2], &p[3], &p[4], &p[5], &p[6]);
+    c.streamed = true;
+  }
 }
 
 void cxx_push_results_to_f90(double* const* v, double* const* T, double* const* dp3d,
                              double* const* Qdp, double* const* Q, double* const* ps_v,
                              double* const* omega_p) {
   Ctx& c = C();
+  {
+    double* const p[7] = {*v, *T, *dp3d, *Qdp, *Q, *ps_v, *omega_p};
+    bool same = c.streamed;
+    for (int i = 0; i < 7; ++i) same = same && p[i] == c.stream_to[i];
+    if (same) return;
+  }
   const size_t B = (size_t)NP2 * NLEV;
   for (int e = 0; e < c.E; ++e)
     for (int tl = 0; tl < NTL; ++tl) {
@@ -1994,6 +2009,24 @@ int hx_read_restart(const char* path) {
   c.tl.nm1 = h.nm1 - 1; c.tl.n0 = h.n0 - 1; c.tl.np1 = h.np1 - 1;
   c.tl.nstep = h.nstep; c.tl.nstep0 = h.nstep0;
   if (sum != h.checksum) return err("checksum mismatch");
+  return 0;
+}
+
+// Copies that overlap the step: on the CPU the input is read at once (the flag has no
+// effect) and the streamed results are pushed when each interval ends.
+int hx_set_async_copies(int) { return 0; }
+int hx_stream_results(double* v, double* T, double* dp3d, double* Qdp, double* Q, double* ps_v,
+                      double* omega_p) {
+  Ctx& c = C();
+  double* const p[7] = {v, T, dp3d, Qdp, Q, ps_v, omega_p};
+  int n = 0;
+  for (int i = 0; i < 7; ++i) n += p[i] != nullptr;
+  if (n != 0 && n != 7) {
+    set_error(13, "hx_stream_results: give all seven destinations or none");
+    return 13;
+  }
+  for (int i = 0; i < 7; ++i) c.stream_to[i] = p[i];
+  c.streamed = false;
   return 0;
 }
 
