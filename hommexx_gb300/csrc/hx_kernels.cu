@@ -1061,9 +1061,9 @@ constexpr int R_DMA = R_MASS + 74;     // dma[0 .. 73]
 constexpr int R_AI = R_DMA + 74;       // ai[0 .. 72]
 constexpr int R_COEF = R_AI + 74;      // coef[3][72]
 constexpr int R_RD = R_COEF + 216;     // 1 / D[0 .. 71]
-constexpr int R_GF = R_RD + 72;        // mixed form: float g[10][74], z2[72], 1/D[72]
+constexpr int R_GF = R_RD + 72;        // mixed form: float g[10][74], z2[72], 1/D[72], delta[-1 .. 73]
 // doubles per column
-template <typename R> constexpr int r_col() { return kF32<R> ? R_GF + (740 + 72 + 72) / 2 : R_GF; }
+template <typename R> constexpr int r_col() { return kF32<R> ? R_GF + (740 + 72 + 72 + 76) / 2 : R_GF; }
 
 // compute_ppm and the monotone parabola coefficients (PpmRemap.hpp:202-353) for one
 // variable of one column in T: slopes dma (j in 0 .. 73), edge values ai (j in 0 .. 72),
@@ -1117,6 +1117,68 @@ __device__ __forceinline__ void ppm_coefs(int lane, bool own, int l0, int remap_
         c2 = T(0);
       }
       coef[0 * 72 + jp] = c0;
+      coef[1 * 72 + jp] = c1;
+      coef[2 * 72 + jp] = c2;
+    }
+  }
+}
+
+// The same reconstruction from the neighbour differences df[j] = A[j] - A[j-1]
+// (j = -1 .. 73, ghosts included) alone, for the mixed form's v and T: slopes dma from
+// df; edge offsets e[j] = ai[j] - A[j-1]; for cell k the parabola's offsets
+// dl = al - A[k] = e[k] - df[k] and dr = ar - A[k] = e[k+1], limited as above, give
+// coef = (c0 - A[k], c1, c2) = (-(dl + dr) / 4, dr - dl, 3 (dl + dr)).  FP32 carries only
+// differences; A[k]'s share of a cell integral is added in FP64 by the caller.
+__device__ __forceinline__ void ppm_coefs_delta(int lane, bool own, int l0, int remap_alg, const float* df,
+                                                const float* g, float* dma, float* e, float* coef) {
+  if (lane < 25) {
+#pragma unroll
+    for (int k3 = 0; k3 < 3; ++k3) {
+      const int j = 3 * lane + k3;
+      if (j < NLEV + 2) {
+        const float d1 = df[j], d2 = df[j - 1];
+        float r = 0.0f;
+        if (d1 * d2 > 0.0f) {
+          const float da = g[0 * 74 + j] * (g[1 * 74 + j] * d1 + g[2 * 74 + j] * d2);
+          r = min3abs_signed(da, 2.0f * d2, 2.0f * d1, da);
+        }
+        dma[j] = r;
+      }
+    }
+  }
+  __syncwarp();
+  if (lane < 25) {
+#pragma unroll
+    for (int k3 = 0; k3 < 3; ++k3) {
+      const int j = 3 * lane + k3;
+      if (j < NLEV + 1) {
+        const float d1 = df[j];
+        e[j] = g[3 * 74 + j] * d1 +
+               g[4 * 74 + j] * (g[5 * 74 + j] * (g[6 * 74 + j] - g[7 * 74 + j]) * d1 - g[8 * 74 + j] * dma[j + 1] +
+                                g[9 * 74 + j] * dma[j]);
+      }
+    }
+  }
+  __syncwarp();
+  if (own) {
+#pragma unroll
+    for (int k3 = 0; k3 < 3; ++k3) {
+      const int jp = l0 + k3;
+      float dl = e[jp] - df[jp], dr = e[jp + 1];
+      if (!(dr * -dl > 0.0f)) { dl = 0.0f; dr = 0.0f; }
+      constexpr float sixth = 1.0f / 6.0f;
+      float c1 = dr - dl;
+      if (c1 * c1 * sixth < c1 * (-(dl + dr) * 0.5f)) dl = -2.0f * dr;
+      c1 = dr - dl;
+      if (c1 * (-(dl + dr) * 0.5f) < -c1 * c1 * sixth) dr = -2.0f * dl;
+      float d0 = -(dl + dr) * 0.25f, c2 = 3.0f * (dl + dr);
+      c1 = dr - dl;
+      if (remap_alg == 2 && (jp < 2 || jp >= NLEV - 2)) {  // PpmFixedParabola
+        d0 = 0.0f;
+        c1 = 0.0f;
+        c2 = 0.0f;
+      }
+      coef[0 * 72 + jp] = d0;
       coef[1 * 72 + jp] = c1;
       coef[2 * 72 + jp] = c2;
     }
@@ -1257,12 +1319,14 @@ __global__ void __launch_bounds__(RT) k_remap(RemapArgs a) {
   // Mixed form: the reconstructions run in FP32 from float copies of the grid weights,
   // z2 and 1/D; the cell integrals and the mass below each interface stay in FP64, and
   // the bottom interface carries the exact column mass (mass fixer).  v and T are
-  // reconstructed relative to their column mean Aref (PPM is shift-equivariant: the
-  // parabolas of A - Aref are those of A less Aref), so FP32 carries the deviations, and
-  // Aref's share of each integral, Aref (x2 + 1/2), is added back in FP64.
+  // reconstructed from their neighbour differences (ppm_coefs_delta), so FP32 carries
+  // only differences and parabola offsets, and the cell mean's share of each partial
+  // integral, A[kk] (x2 + 1/2), is added in FP64; the tracers (non-negative, of their own
+  // scale) are reconstructed from their FP32 cell means.
   float* gf = reinterpret_cast<float*>(sm + R_GF);  // [10][74]
   float* z2f = gf + 740;
   float* rDf = z2f + 72;
+  float* dlf = rDf + 72 + 1;  // df[-1 .. 73]
   float* Af = reinterpret_cast<float*>(sm + R_A) + 2;
   float* dmaf = reinterpret_cast<float*>(sm + R_DMA);
   float* aif = reinterpret_cast<float*>(sm + R_AI);
@@ -1294,11 +1358,10 @@ __global__ void __launch_bounds__(RT) k_remap(RemapArgs a) {
         if (var < 2) x3[k] = a.v[vb + (size_t)l * 32 + var * 16] * s3[k];
         else if (var == 2) x3[k] = a.T[sb + (size_t)l * 16] * s3[k];
         else x3[k] = a.qdp[((((size_t)e * QTL + a.n0_qdp) * a.Q + (var - 3)) * NLEV + l) * 16 + p];
-        if (!lo) A[l] = x3[k] * rD[l];
-        else if (var >= 3) Af[l] = d2f_rn(x3[k]) * rDf[l];
+        if (!lo || var < 3) A[l] = x3[k] * rD[l];
+        else Af[l] = d2f_rn(x3[k]) * rDf[l];
       }
     }
-    double aref = 0.0;  // mixed form, v and T: column mean
     {
       double ex = warp_excl_scan(x3[0] + x3[1] + x3[2], lane);
       if (own) {
@@ -1310,16 +1373,26 @@ __global__ void __launch_bounds__(RT) k_remap(RemapArgs a) {
       }
       if (lane == 23) mass[NLEV + 1] = ex;  // mass[NLEV] + x[NLEV-1]
       if (lane == 0) mass[0] = 0.0;
-      if (lo && var < 3) {
-        aref = __shfl_sync(FULL, ex, 23) / pio[NLEV];
-        if (own) {
-#pragma unroll
-          for (int k = 0; k < 3; ++k) Af[l0 + k] = d2f_rn(fma(x3[k], rD[l0 + k], -aref));
-        }
-      }
     }
     __syncwarp();
-    if (lane == 0) {  // ghost cells: mirrored (remap_alg 1, 2) or constant (3)
+    const bool dlt = lo && var < 3;  // mixed form, v and T: reconstruction from differences
+    if (dlt) {
+      // df[j] = A[j] - A[j-1]; ghosts: mirrored (remap_alg 1, 2) or constant (3) cells
+      if (own) {
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+          const int j = l0 + k;
+          if (j >= 1) dlf[j] = d2f_rn(A[j] - A[j - 1]);
+        }
+      }
+      __syncwarp();
+      if (lane == 0) {
+        dlf[0] = 0.0f;
+        dlf[-1] = a.remap_alg == 3 ? 0.0f : -dlf[1];
+        dlf[NLEV] = 0.0f;
+        dlf[NLEV + 1] = a.remap_alg == 3 ? 0.0f : -dlf[NLEV - 1];
+      }
+    } else if (lane == 0) {  // ghost cells: mirrored (remap_alg 1, 2) or constant (3)
       if (lo) {
         Af[-1] = Af[0];
         Af[-2] = a.remap_alg == 3 ? Af[0] : Af[1];
@@ -1333,7 +1406,8 @@ __global__ void __launch_bounds__(RT) k_remap(RemapArgs a) {
       }
     }
     __syncwarp();
-    if (lo) ppm_coefs<float>(lane, own, l0, a.remap_alg, Af, gf, dmaf, aif, coeff);
+    if (dlt) ppm_coefs_delta(lane, own, l0, a.remap_alg, dlf, gf, dmaf, aif, coeff);
+    else if (lo) ppm_coefs<float>(lane, own, l0, a.remap_alg, Af, gf, dmaf, aif, coeff);
     else ppm_coefs<double>(lane, own, l0, a.remap_alg, A, g, dma, ai, coef);
     __syncwarp();
     // compute_remap: mass below each new interface, in double; new cell masses are
@@ -1348,7 +1422,8 @@ __global__ void __launch_bounds__(RT) k_remap(RemapArgs a) {
           const float x2 = z2f[k];
           const float in = (coeff[kk] * (x2 + 0.5f) + coeff[72 + kk] * (x2 * x2 - 0.25f) * 0.5f) +
                            coeff[144 + kk] * (x2 * x2 * x2 + 0.125f) * (1.0f / 3.0f);
-          const double ind = var < 3 ? fma(aref, z2[k] + 0.5, dbl(in)) : dbl(in);
+          // v and T: the coefficients are offsets from the cell mean A[kk]
+          const double ind = dlt ? fma(A[kk], z2[k] + 0.5, dbl(in)) : dbl(in);
           m2[k3] = k == NLEV - 1 ? mass[NLEV + 1] : mass[kk + 1] + ind * D[kk];
         } else {
           const double x2 = z2[k], x1 = -0.5;
