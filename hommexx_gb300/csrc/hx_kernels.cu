@@ -104,9 +104,9 @@ __global__ void __launch_bounds__(LG * 16) k_caar(CaarArgs<R> a) {
       pr = pr + 0.5 * (prev + d);
       prev = d;
       double rp;
-      if constexpr (kF32<R>) {  // the FP32 reciprocal serves phase C
+      if constexpr (kF32<R>) {  // one Newton step (2^-42); the FP32 reciprocal serves phase C
         float rf;
-        rp = rcp_newton(pr, rf);
+        rp = rcp_newton1(pr, rf);
         f_rp[(l0 + k) * SROW + col] = rf;
       } else {
         rp = 1.0 / pr;

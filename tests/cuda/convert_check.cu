@@ -3,7 +3,8 @@
 // zeros, subnormals, overflow, infinities and NaN; the Newton-Raphson reciprocal
 // rcp_newton against IEEE division over positive divisors of exponents -120 .. 120, and
 // the corrected quotient div_newton over numerators of exponents -300 .. 300 (both
-// within one ulp).  Prints the mismatch counts; exit status 0 when there are none.
+// within one ulp), and the one-step rcp_newton1 (relative error below 2^-42).  Prints
+// the mismatch counts; exit status 0 when there are none.
 #include <cstdio>
 #include <cstdlib>
 
@@ -53,20 +54,24 @@ __global__ void check(unsigned long long n, unsigned long long* bad) {
   const long long dq = q1 > q2 ? q1 - q2 : q2 - q1;
   if (dq > 1) atomicAdd(bad + 4, 1ULL);
   if (dq == 1) atomicAdd(bad + 5, 1ULL);
+  // one Newton step: relative error below 2^-42
+  const double r1s = hx::rcp_newton1(x2, rf), r1e = 1.0 / x2;
+  if (fabs(r1s - r1e) > 0x1p-42 * fabs(r1e)) atomicAdd(bad + 6, 1ULL);
 }
 
 }  // namespace
 
 int main() {
   unsigned long long* bad = nullptr;
-  if (cudaMalloc(&bad, 6 * sizeof(unsigned long long)) != cudaSuccess) return 2;
-  cudaMemset(bad, 0, 6 * sizeof(unsigned long long));
+  if (cudaMalloc(&bad, 7 * sizeof(unsigned long long)) != cudaSuccess) return 2;
+  cudaMemset(bad, 0, 7 * sizeof(unsigned long long));
   const unsigned long long n = 1ULL << 26;
   check<<<(unsigned)((n + 255) / 256), 256>>>(n, bad);
-  unsigned long long h[6] = {0, 0, 0, 0, 0, 0};
+  unsigned long long h[7] = {0, 0, 0, 0, 0, 0, 0};
   if (cudaMemcpy(h, bad, sizeof(h), cudaMemcpyDeviceToHost) != cudaSuccess) return 2;
   std::printf("d2f mismatches %llu, f2d mismatches %llu, rcp beyond 1 ulp %llu (1 ulp: %llu), "
-              "div beyond 1 ulp %llu (1 ulp: %llu), of %llu each\n", h[0], h[1], h[2], h[3], h[4], h[5], n);
+              "div beyond 1 ulp %llu (1 ulp: %llu), one-step rcp beyond 2^-42 %llu, of %llu each\n", h[0], h[1],
+              h[2], h[3], h[4], h[5], h[6], n);
   cudaFree(bad);
-  return (h[0] == 0 && h[1] == 0 && h[2] == 0 && h[4] == 0) ? 0 : 1;
+  return (h[0] == 0 && h[1] == 0 && h[2] == 0 && h[4] == 0 && h[6] == 0) ? 0 : 1;
 }
