@@ -88,21 +88,20 @@ __global__ void __launch_bounds__(LG * 16) k_caar(CaarArgs<R> a) {
     const int col = tid >> 3, seg = tid & 7, l0 = seg * 9;
     // pressure: p_k = p_{k-1} + (dp_{k-1} + dp_k)/2, p_{-1} = hyai0 ps0, dp_{-1} = 0
     double prev = seg == 0 ? 0.0 : s_dp[(l0 - 1) * SROW + col];
-    double tot = 0.0;
+    double tot = 0.0, tp[9];  // the segment's terms, summed again below in the same order
 #pragma unroll
     for (int k = 0; k < 9; ++k) {
       const double d = s_dp[(l0 + k) * SROW + col];
-      tot += 0.5 * (prev + d);
+      tp[k] = 0.5 * (prev + d);
+      tot += tp[k];
       prev = d;
     }
     double pr = a.p_top + seg_excl_prefix(tot, seg);
-    prev = seg == 0 ? 0.0 : s_dp[(l0 - 1) * SROW + col];
     double r[9];
 #pragma unroll
     for (int k = 0; k < 9; ++k) {
       const double d = s_dp[(l0 + k) * SROW + col];
-      pr = pr + 0.5 * (prev + d);
-      prev = d;
+      pr = pr + tp[k];
       double rp;
       if constexpr (kF32<R>) {  // one Newton step (2^-42); the FP32 reciprocal serves phase C
         float rf;
