@@ -96,12 +96,14 @@ struct Pt {
 template <typename R>
 struct PM {
   R di00, di01, di10, di11, d00, d01, d10, d11, md, fdiv, sp, mp, a00, a01, a10, a11, rsp;
+  R gr00, gr01, gr10, gr11;  // Dinv * rrearth, for gradient_sphere
   R l00, l01, l10, l11;  // spheremp * (Dinv Dinv^T) * rrearth, for laplace_simple
   __device__ __forceinline__ void load(const MetricP<R>& m, int e, int p) {
     const R* Di = m.Dinv + (size_t)e * 64;
     const R* D = m.D + (size_t)e * 64;
     const R* Mi = m.metinv + (size_t)e * 64;
     di00 = Di[p]; di01 = Di[16 + p]; di10 = Di[32 + p]; di11 = Di[48 + p];
+    gr00 = di00 * rre<R>(); gr01 = di01 * rre<R>(); gr10 = di10 * rre<R>(); gr11 = di11 * rre<R>();
     d00 = D[p]; d01 = D[16 + p]; d10 = D[32 + p]; d11 = D[48 + p];
     md = m.metdet[(size_t)e * 16 + p];
     fdiv = R(1.0) / md * rre<R>();
@@ -119,12 +121,12 @@ struct PM {
 };
 
 // ---- sphere operators on one point-level (SphereOperators.hpp) ------------------------
+// The 1/rearth of the derivatives is folded into the metric factors (m.gr = Dinv / a).
 template <typename R>
 __device__ __forceinline__ void gradient_sphere(const Pt<R>& t, const PM<R>& m, R s, R& g0, R& g1) {
-  const R v0 = t.ddx(s) * rre<R>();
-  const R v1 = t.ddy(s) * rre<R>();
-  g0 = m.di00 * v0 + m.di01 * v1;
-  g1 = m.di10 * v0 + m.di11 * v1;
+  const R v0 = t.ddx(s), v1 = t.ddy(s);
+  g0 = m.gr00 * v0 + m.gr01 * v1;
+  g1 = m.gr10 * v0 + m.gr11 * v1;
 }
 
 template <typename R>
