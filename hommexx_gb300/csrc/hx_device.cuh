@@ -97,6 +97,7 @@ template <typename R>
 struct PM {
   R di00, di01, di10, di11, d00, d01, d10, d11, md, fdiv, sp, mp, a00, a01, a10, a11, rsp;
   R gr00, gr01, gr10, gr11;  // Dinv * rrearth, for gradient_sphere
+  R dm00, dm01, dm10, dm11;  // Dinv * metdet, for divergence_sphere
   R l00, l01, l10, l11;  // spheremp * (Dinv Dinv^T) * rrearth, for laplace_simple
   __device__ __forceinline__ void load(const MetricP<R>& m, int e, int p) {
     const R* Di = m.Dinv + (size_t)e * 64;
@@ -110,6 +111,7 @@ struct PM {
     sp = m.spheremp[(size_t)e * 16 + p];
     rsp = m.rspheremp[(size_t)e * 16 + p];
     mp = m.mp[(size_t)e * 16 + p];
+    dm00 = di00 * md; dm01 = di01 * md; dm10 = di10 * md; dm11 = di11 * md;
     a00 = Mi[p] * md; a01 = Mi[16 + p] * md; a10 = Mi[32 + p] * md; a11 = Mi[48 + p] * md;
     // c = (Dinv^T-contraction of the Dinv-contraction): c_a = sum_b K_ab v_b with
     // K_ab = sum_c Dinv(c,a) Dinv(c,b) in the reference's C++ indices.
@@ -129,10 +131,11 @@ __device__ __forceinline__ void gradient_sphere(const Pt<R>& t, const PM<R>& m, 
   g1 = m.gr10 * v0 + m.gr11 * v1;
 }
 
+// metdet folded into the metric factors (m.dm = Dinv metdet)
 template <typename R>
 __device__ __forceinline__ R divergence_sphere(const Pt<R>& t, const PM<R>& m, R v0, R v1) {
-  const R gv0 = (m.di00 * v0 + m.di10 * v1) * m.md;
-  const R gv1 = (m.di01 * v0 + m.di11 * v1) * m.md;
+  const R gv0 = m.dm00 * v0 + m.dm10 * v1;
+  const R gv1 = m.dm01 * v0 + m.dm11 * v1;
   return (t.ddx(gv0) + t.ddy(gv1)) * m.fdiv;
 }
 
