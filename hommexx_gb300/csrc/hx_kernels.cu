@@ -947,7 +947,7 @@ __global__ void __launch_bounds__(LG * 16, kF32<R> ? 6 : 3) k_aal_tracer(EulerAr
     s_c1[l] = s1;
   }
   const bool add_hv = a.rhs_viss != 0.0;
-  const R mdt = R(-a.dt);
+  const R mdf = R(-a.dt) * m.fdiv;  // -dt times divergence_sphere's scale
 #pragma unroll 1
   for (int q = 0; q < a.Q; ++q) {
     const size_t qn0 = (((size_t)e * QTL + a.n0_qdp) * a.Q + q) * NLEV * 16;
@@ -957,10 +957,10 @@ __global__ void __launch_bounds__(LG * 16, kF32<R> ? 6 : 3) k_aal_tracer(EulerAr
       const int l = lg + LG * k;
       const double qdd = a.qdp[qn0 + l * 16 + p];
       const R qd = cvt<R>(qdd);
-      const R dv = (t.ddx(w0[k] * qd) + t.ddy(w1[k] * qd)) * m.fdiv;
+      const R dvs = t.ddx(w0[k] * qd) + t.ddy(w1[k] * qd);  // div(vstar Qdp) / fdiv
       const double q0 = add_hv ? a.qtens[qb + l * 16 + p] : 0.0;
-      if constexpr (kF32<R>) s_q[l * SROW + p] = qdd + dbl(mdt * dv) + q0;
-      else s_q[l * SROW + p] = (qdd + mdt * dv + q0);
+      if constexpr (kF32<R>) s_q[l * SROW + p] = qdd + dbl(mdf * dvs) + q0;
+      else s_q[l * SROW + p] = (qdd + mdf * dvs + q0);
     }
     __syncthreads();
     for (int l = tid; l < NLEV; l += blockDim.x) {
