@@ -723,6 +723,14 @@ __global__ void k_minmax_nbr(int E, int Q, const double* __restrict__ pre, doubl
 }
 
 // BIHPre: qtens (Q) [* dpdiss_ave / dp0] -> laplace -> qscr (pre-DSS).
+// The tracer-independent weight of the biharmonic's first Laplacian, dpdiss_ave / dp0,
+// once per point and level (into the dpdissk scratch, which aal_setup writes later).
+__global__ void k_bih_weight(int E, const double* __restrict__ dpa, double* __restrict__ w) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= E * NLEV * 16) return;
+  w[i] = dpa[i] * c_rdp0[(i >> 4) % NLEV];
+}
+
 template <typename R, int LG>
 __global__ void __launch_bounds__(LG * 16) k_bih_pre(EulerArgs<R> a) {
   constexpr int NL = NLEV / LG;
@@ -739,7 +747,7 @@ __global__ void __launch_bounds__(LG * 16) k_bih_pre(EulerArgs<R> a) {
   for (int k = 0; k < NL; ++k) {
     const int l = lg + LG * k;
     R s = cvt<R>(a.qtens[qb + l * 16 + p]);
-    if (a.nu_p > 0) s = s * cvt<R>(a.dpdiss_ave[((size_t)e * NLEV + l) * 16 + p]) * cvt<R>(c_rdp0[l]);
+    if (a.nu_p > 0) s = s * cvt<R>(a.dpdissk[((size_t)e * NLEV + l) * 16 + p]);  // dpdiss_ave / dp0
     a.qscr[qb + l * 16 + p] = dbl(lap(t, m, s));
   }
 }
@@ -763,7 +771,7 @@ __global__ void __launch_bounds__(LG * 16, kF32<R> ? 9 : 6) k_bih_post(EulerArgs
   const size_t qb = ((size_t)e * a.Q + q) * NLEV * 16;
   const double* fbase = a.qscr + (size_t)q * NLEV * 16;
   const R fac = R(-a.rhs_viss * a.dt * a.nu_q);
-  const R rsp_local = R(1) / m.sp;
+  const R cf = fac * (R(1) / m.sp);  // the factor and 1/spheremp of this point
   LapOp<R> lapo;
   if (a.consthv) lapo.load(a.m, e, p);
   // DSS(rspheremp) into shared memory [72][16] with warps grouped by point class
@@ -783,7 +791,7 @@ __global__ void __launch_bounds__(LG * 16, kF32<R> ? 9 : 6) k_bih_post(EulerArgs
     const int l = lg + LG * k;
     const R s = s_in[l * 16 + p];
     const R lap = a.consthv ? lapo(t, m, s) : laplace_tensor(t, m, tv, s);
-    a.qtens[qb + l * 16 + p] = dbl(fac * cvt<R>(a.dp0[l]) * lap * rsp_local);
+    a.qtens[qb + l * 16 + p] = dbl(cf * cvt<R>(a.dp0[l]) * lap);
   }
 }
 
@@ -1578,6 +1586,10 @@ void launch_euler_step(EulerArgs<R>& a, int E, int time_avg, cudaStream_t s) {
     }
     if (a.rhs_multiplier == 2.0) {
       a.rhs_viss = 3.0;
+      if (a.nu_p > 0) {
+        KScope k("euler_bih_weight", s);
+        k_bih_weight<<<nblk((long long)E * NLEV * 16, 256), 256, 0, s>>>(E, a.dpdiss_ave, a.dpdissk);
+      }
       {
         KScope k("euler_bih_pre", s);
         k_bih_pre<R, LG><<<EQ, LG * 16, 0, s>>>(a);
