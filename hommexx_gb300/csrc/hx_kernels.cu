@@ -235,7 +235,7 @@ __global__ void __launch_bounds__(LG * 16) k_caar(CaarArgs<R> a) {
     const double vn0_ = spd * (dbl(eg0 * dt) + vm0);
     const double vn1_ = spd * (dbl(eg1 * dt) + vm1);
     // dp3d (compute_dp3d_np1, eta_dot_dpdn = 0 for rsplit > 0)
-    const double dnew = spd * (dm - dbl(((etu + div) - etl) * dt));
+    const double dnew = a.rsplit == 0 ? spd * (dm - dbl(((etu + div) - etl) * dt)) : spd * (dm - dbl(div * dt));
     out[l * 64 + p] = vn0_;
     out[l * 64 + 16 + p] = vn1_;
     out[l * 64 + 32 + p] = tnew;
@@ -290,10 +290,10 @@ __global__ void __launch_bounds__(LG * 16) k_hv_lap1(HvArgs<R> a) {
     const R ld = lap(t, m, rel_hw<R>(a.dp[sb + l * 16 + p]));
     R l0, l1;
     vlaplace_contra(t, m, nr, cvt_hw<R>(a.v[vb + l * 32 + p]), cvt_hw<R>(a.v[vb + l * 32 + 16 + p]), l0, l1);
-    out[l * 64 + p] = dbl_hw(l0);
-    out[l * 64 + 16 + p] = dbl_hw(l1);
-    out[l * 64 + 32 + p] = dbl_hw(lt);
-    out[l * 64 + 48 + p] = dbl_hw(ld);
+    out[l * 64 + p] = dbl(l0);  // float -> double on the integer pipe in the mixed form
+    out[l * 64 + 16 + p] = dbl(l1);
+    out[l * 64 + 32 + p] = dbl(lt);
+    out[l * 64 + 48 + p] = dbl(ld);
   }
 }
 
