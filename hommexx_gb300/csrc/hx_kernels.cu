@@ -731,6 +731,8 @@ __global__ void k_bih_weight(int E, const double* __restrict__ dpa, double* __re
   w[i] = dpa[i] * c_rdp0[(i >> 4) % NLEV];
 }
 
+// (The mixed form converts its two inputs per point on the hardware path: this kernel's
+// FP64 pipe has room, its instruction issue less.)
 template <typename R, int LG>
 __global__ void __launch_bounds__(LG * 16) k_bih_pre(EulerArgs<R> a) {
   constexpr int NL = NLEV / LG;
@@ -746,8 +748,8 @@ __global__ void __launch_bounds__(LG * 16) k_bih_pre(EulerArgs<R> a) {
 #pragma unroll 1
   for (int k = 0; k < NL; ++k) {
     const int l = lg + LG * k;
-    R s = cvt<R>(a.qtens[qb + l * 16 + p]);
-    if (a.nu_p > 0) s = s * cvt<R>(a.dpdissk[((size_t)e * NLEV + l) * 16 + p]);  // dpdiss_ave / dp0
+    R s = cvt_hw<R>(a.qtens[qb + l * 16 + p]);
+    if (a.nu_p > 0) s = s * cvt_hw<R>(a.dpdissk[((size_t)e * NLEV + l) * 16 + p]);  // dpdiss_ave / dp0
     a.qscr[qb + l * 16 + p] = dbl(lap(t, m, s));
   }
 }
