@@ -1354,6 +1354,23 @@ __global__ void __launch_bounds__(RT) k_remap(RemapArgs a) {
       __syncwarp();
     }
   }
+  // The partial-cell integral's weights depend on the target level only: this lane's
+  // three levels' x2 + 1/2, (x2^2 - 1/4) / 2, (x2^3 + 1/8) / 3, once for all variables.
+  double wz[3][3];
+  float wzf[3][3];
+#pragma unroll
+  for (int k3 = 0; k3 < 3; ++k3) {
+    const double x2 = own ? z2[l0 + k3] : 0.0;
+    wz[k3][0] = x2 + 0.5;
+    wz[k3][1] = (x2 * x2 - 0.25) * 0.5;
+    wz[k3][2] = (x2 * x2 * x2 + 0.125) * (1.0 / 3.0);
+    if constexpr (kF32<R>) {
+      const float xf = own ? z2f[l0 + k3] : 0.0f;
+      wzf[k3][0] = xf + 0.5f;
+      wzf[k3][1] = (xf * xf - 0.25f) * 0.5f;
+      wzf[k3][2] = (xf * xf * xf + 0.125f) * (1.0f / 3.0f);
+    }
+  }
   const int nvar = 3 + a.Q;
 #pragma unroll 1
   for (int var = a.rsplit == 0 ? 3 : 0; var < nvar; ++var) {
@@ -1428,16 +1445,12 @@ __global__ void __launch_bounds__(RT) k_remap(RemapArgs a) {
         const int k = l0 + k3;
         const int kk = kid[k];
         if (lo) {
-          const float x2 = z2f[k];
-          const float in = (coeff[kk] * (x2 + 0.5f) + coeff[72 + kk] * (x2 * x2 - 0.25f) * 0.5f) +
-                           coeff[144 + kk] * (x2 * x2 * x2 + 0.125f) * (1.0f / 3.0f);
+          const float in = (coeff[kk] * wzf[k3][0] + coeff[72 + kk] * wzf[k3][1]) + coeff[144 + kk] * wzf[k3][2];
           // v and T: the coefficients are offsets from the cell mean A[kk]
-          const double ind = dlt ? fma(A[kk], z2[k] + 0.5, dbl(in)) : dbl(in);
+          const double ind = dlt ? fma(A[kk], wz[k3][0], dbl(in)) : dbl(in);
           m2[k3] = k == NLEV - 1 ? mass[NLEV + 1] : mass[kk + 1] + ind * D[kk];
         } else {
-          const double x2 = z2[k], x1 = -0.5;
-          const double in = (coef[kk] * (x2 - x1) + coef[72 + kk] * (x2 * x2 - x1 * x1) * 0.5) +
-                            coef[144 + kk] * (x2 * x2 * x2 - x1 * x1 * x1) * (1.0 / 3.0);
+          const double in = (coef[kk] * wz[k3][0] + coef[72 + kk] * wz[k3][1]) + coef[144 + kk] * wz[k3][2];
           m2[k3] = mass[kk + 1] + in * D[kk];
         }
       }
