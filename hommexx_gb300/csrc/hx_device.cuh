@@ -328,6 +328,13 @@ template <typename T> __device__ __forceinline__ bool pos(T x) { return x > T(0)
 template <> __device__ __forceinline__ bool pos<double>(double x) {
   return __double_as_longlong(x) > 0;  // > +0 (non-NaN)
 }
+// a b > 0 for non-NaN a, b: FP32 as is; FP64 on the integer pipe as "the same sign and
+// neither zero" (differs from the product's test only where a b would underflow to 0).
+template <typename T> __device__ __forceinline__ bool pos_prod(T a, T b) { return a * b > T(0); }
+template <> __device__ __forceinline__ bool pos_prod<double>(double a, double b) {
+  const long long x = __double_as_longlong(a), y = __double_as_longlong(b);
+  return (x ^ y) >= 0 && (x << 1) != 0 && (y << 1) != 0;
+}
 template <typename T> __device__ __forceinline__ bool less(T a, T b) { return a < b; }
 template <> __device__ __forceinline__ bool less<double>(double a, double b) {
   return dkey(a) < dkey(b);  // exact for non-NaN except that -0 < +0

@@ -1087,7 +1087,7 @@ __device__ __forceinline__ void ppm_coefs(int lane, bool own, int l0, int remap_
       if (j < NLEV + 2) {
         const T a0 = A[j], am1 = A[j - 1], am2 = A[j - 2];
         T r = T(0);
-        if (pos((a0 - am1) * (am1 - am2))) {
+        if (pos_prod(a0 - am1, am1 - am2)) {
           const T da = g[0 * 74 + j] * (g[1 * 74 + j] * (a0 - am1) + g[2 * 74 + j] * (am1 - am2));
           r = min3abs_signed(da, T(2) * (am1 - am2), T(2) * (a0 - am1), da);
         }
@@ -1103,7 +1103,7 @@ __device__ __forceinline__ void ppm_coefs(int lane, bool own, int l0, int remap_
       if (j < NLEV + 1) {
         const T a0 = A[j], am1 = A[j - 1];
         ai[j] = am1 + g[3 * 74 + j] * (a0 - am1) +
-                g[4 * 74 + j] * (g[5 * 74 + j] * (g[6 * 74 + j] - g[7 * 74 + j]) * (a0 - am1) -
+                g[4 * 74 + j] * (g[5 * 74 + j] * (a0 - am1) -
                                  g[8 * 74 + j] * dma[j + 1] + g[9 * 74 + j] * dma[j]);
       }
     }
@@ -1115,7 +1115,7 @@ __device__ __forceinline__ void ppm_coefs(int lane, bool own, int l0, int remap_
       const int jp = l0 + k3;
       T al = ai[jp], ar = ai[jp + 1];
       const T cm = A[jp];
-      if (!pos((ar - cm) * (cm - al))) { al = cm; ar = cm; }
+      if (!pos_prod(ar - cm, cm - al)) { al = cm; ar = cm; }
       constexpr T sixth = T(1.0 / 6.0);
       if (less((ar - al) * (ar - al) * sixth, (ar - al) * (cm - (al + ar) * T(0.5)))) al = T(3) * cm - T(2) * ar;
       if (less((ar - al) * (cm - (al + ar) * T(0.5)), -(ar - al) * (ar - al) * sixth)) ar = T(3) * cm - T(2) * al;
@@ -1163,7 +1163,7 @@ __device__ __forceinline__ void ppm_coefs_delta(int lane, bool own, int l0, int 
       if (j < NLEV + 1) {
         const float d1 = df[j];
         e[j] = g[3 * 74 + j] * d1 +
-               g[4 * 74 + j] * (g[5 * 74 + j] * (g[6 * 74 + j] - g[7 * 74 + j]) * d1 - g[8 * 74 + j] * dma[j + 1] +
+               g[4 * 74 + j] * (g[5 * 74 + j] * d1 - g[8 * 74 + j] * dma[j + 1] +
                                 g[9 * 74 + j] * dma[j]);
       }
     }
@@ -1315,9 +1315,8 @@ __global__ void __launch_bounds__(RT) k_remap(RemapArgs a) {
           const double r7 = rcp_newton(2.0 * d0 + dm1, rf);  // shared by g7, g9
           g[3 * 74 + j] = dm1 * r10;
           g[4 * 74 + j] = rcp_newton(dm2 + dm1 + d0 + dp1, rf);
-          g[5 * 74 + j] = (2.0 * dm1 * d0) * r10;
-          g[6 * 74 + j] = (dm2 + dm1) * r6;
-          g[7 * 74 + j] = (dp1 + d0) * r7;
+          // row 5 holds g5 (g6 - g7), the only form the edge values use
+          g[5 * 74 + j] = ((2.0 * dm1 * d0) * r10) * ((dm2 + dm1) * r6 - (dp1 + d0) * r7);
           g[8 * 74 + j] = dm1 * (dm2 + dm1) * r6;
           g[9 * 74 + j] = d0 * (d0 + dp1) * r7;
         }
