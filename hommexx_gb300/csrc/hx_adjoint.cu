@@ -28,9 +28,9 @@ namespace {
 // gradient_sphere^T: (g0, g1) -> scalar
 template <typename R>
 __device__ __forceinline__ R gradient_sphere_T(const Pt<R>& t, const PM<R>& m, R g0, R g1) {
-  const R x = m.di00 * g0 + m.di10 * g1;
-  const R y = m.di01 * g0 + m.di11 * g1;
-  return (t.wrow(x) + t.wcol(y)) * rre<R>();
+  const R x = m.gr00 * g0 + m.gr10 * g1;  // gr = Dinv / rearth
+  const R y = m.gr01 * g0 + m.gr11 * g1;
+  return t.wrow(x) + t.wcol(y);
 }
 
 // divergence_sphere^T: scalar -> (v0, v1)
@@ -39,8 +39,8 @@ __device__ __forceinline__ void divergence_sphere_T(const Pt<R>& t, const PM<R>&
                                                     R& v1) {
   const R s = db * m.fdiv;
   const R g0 = t.wrow(s), g1 = t.wcol(s);
-  v0 = m.md * (m.di00 * g0 + m.di01 * g1);
-  v1 = m.md * (m.di10 * g0 + m.di11 * g1);
+  v0 = m.dm00 * g0 + m.dm01 * g1;  // dm = Dinv metdet
+  v1 = m.dm10 * g0 + m.dm11 * g1;
 }
 
 // vorticity_sphere^T: scalar -> (v0, v1)
@@ -64,10 +64,8 @@ __device__ __forceinline__ void vlaplace_contra_T(const Pt<R>& t, const PM<R>& m
   const R Yb = -(m.a01 * b0 + m.a11 * b1);
   R divb = m.mp * (t.ddx(Xb) + t.ddy(Yb));
   if (nu_ratio > R(0) && nu_ratio != R(1)) divb *= nu_ratio;
-  // curl_sphere_wk_testcov (factor -1) reversed
-  const R sb0 = -(m.d00 * l0 + m.d01 * l1) * rre<R>();
-  const R sb1 = -(m.d10 * l0 + m.d11 * l1) * rre<R>();
-  const R vortb = m.mp * (t.ddx(sb1) - t.ddy(sb0));
+  // curl_sphere_wk_testcov (factor -1) reversed: its covariant terms are -(b0, b1)
+  const R vortb = m.mp * (t.ddy(b0) - t.ddx(b1));
   R a0, a1, c0, c1;
   vorticity_sphere_T(t, m, vortb, a0, a1);
   divergence_sphere_T(t, m, divb, c0, c1);
