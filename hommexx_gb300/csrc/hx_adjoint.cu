@@ -95,15 +95,15 @@ template <typename R, int LG>
 __global__ void __launch_bounds__(LG * 16) k_caar_vjp(CaarVjpArgs<R> a) {
   constexpr int NL = NLEV / LG;
   extern __shared__ double sm[];
-  double* s_dp = sm;                      // dp3d
-  double* s_T = sm + NLEV * SROW;         // T
-  double* s_div = sm + 2 * NLEV * SROW;   // div(v dp); then the omega-integral cotangent
-  double* s_p = sm + 3 * NLEV * SROW;     // pressure
-  double* s_rp = sm + 4 * NLEV * SROW;    // 1 / pressure
-  double* s_I = sm + 5 * NLEV * SROW;     // sum_{j<l} div_vdp_j
-  double* s_phib = sm + 6 * NLEV * SROW;  // cotangent of phi; then the scans' T cotangent
-  double* s_pb = sm + 7 * NLEV * SROW;    // cotangent of p; then the scans' dp3d cotangent
-  double* s_dvb = sm + 8 * NLEV * SROW;   // cotangent of div(v dp)
+  // (T and dp3d are read from the stage input, which stays in L1: seven arrays of shared
+  // memory keep three CTAs per SM)
+  double* s_div = sm;                     // div(v dp); then the omega-integral cotangent
+  double* s_p = sm + 1 * NLEV * SROW;     // pressure
+  double* s_rp = sm + 2 * NLEV * SROW;    // 1 / pressure
+  double* s_I = sm + 3 * NLEV * SROW;     // sum_{j<l} div_vdp_j
+  double* s_phib = sm + 4 * NLEV * SROW;  // cotangent of phi; then the scans' T cotangent
+  double* s_pb = sm + 5 * NLEV * SROW;    // cotangent of p; then the scans' dp3d cotangent
+  double* s_dvb = sm + 6 * NLEV * SROW;   // cotangent of div(v dp)
   const int e = blockIdx.x, tid = threadIdx.x, p = tid & 15, lg = tid >> 4;
   Pt<R> t;
   t.init(p);
@@ -120,27 +120,25 @@ __global__ void __launch_bounds__(LG * 16) k_caar_vjp(CaarVjpArgs<R> a) {
     const double dd = xd[l * 16 + p];
     const R d = (R)dd;
     const R div = divergence_sphere(t, m, u * d, w * d);
-    s_dp[l * SROW + p] = dd;
-    s_T[l * SROW + p] = xT[l * 16 + p];
     s_div[l * SROW + p] = (double)div;
   }
   __syncthreads();
   // ---- phase B: pressure, 1/p, omega integral (as the forward, in double) ----
   if (tid < 128) {
     const int col = tid >> 3, seg = tid & 7, l0 = seg * 9;
-    double prev = seg == 0 ? 0.0 : s_dp[(l0 - 1) * SROW + col];
+    double prev = seg == 0 ? 0.0 : xd[(l0 - 1) * 16 + col];
     double tot = 0.0;
 #pragma unroll
     for (int k = 0; k < 9; ++k) {
-      const double d = s_dp[(l0 + k) * SROW + col];
+      const double d = xd[(l0 + k) * 16 + col];
       tot += 0.5 * (prev + d);
       prev = d;
     }
     double pr = a.p_top + seg_excl_prefix(tot, seg);
-    prev = seg == 0 ? 0.0 : s_dp[(l0 - 1) * SROW + col];
+    prev = seg == 0 ? 0.0 : xd[(l0 - 1) * 16 + col];
 #pragma unroll
     for (int k = 0; k < 9; ++k) {
-      const double d = s_dp[(l0 + k) * SROW + col];
+      const double d = xd[(l0 + k) * 16 + col];
       pr = pr + 0.5 * (prev + d);
       prev = d;
       s_p[(l0 + k) * SROW + col] = pr;
@@ -182,7 +180,7 @@ __global__ void __launch_bounds__(LG * 16) k_caar_vjp(CaarVjpArgs<R> a) {
     const R gv0 = (R)(a.dt * spd * pv0), gv1 = (R)(a.dt * spd * pv1);
     const R gT = (R)(a.dt * spd * pT), gdp = (R)(a.dt * spd * pdp);
     // forward intermediates
-    const double td = s_T[l * SROW + p];
+    const double td = xT[l * 16 + p];
     const R u = (R)xv[l * 32 + p], w = (R)xv[l * 32 + 16 + p];
     const R T = (R)td;
     const R rp = (R)s_rp[l * SROW + p];
@@ -248,7 +246,7 @@ __global__ void __launch_bounds__(LG * 16) k_caar_vjp(CaarVjpArgs<R> a) {
       const double phb = s_phib[i];
       const double rb = phb + 2.0 * acc;
       acc += phb;
-      const double rp = s_rp[i], T = s_T[i], dp = s_dp[i];
+      const double rp = s_rp[i], T = xT[(l0 + k) * 16 + col], dp = xd[(l0 + k) * 16 + col];
       const double hr = dp * 0.5 * rp;  // r = Rgas T dp / (2 p)
       Tb2[k] = kRgas * hr * rb;
       dpb2[k] = kRgas * T * 0.5 * rp * rb;
@@ -292,7 +290,7 @@ __global__ void __launch_bounds__(LG * 16) k_caar_vjp(CaarVjpArgs<R> a) {
     R vd0, vd1;
     divergence_sphere_T(t, m, (R)s_dvb[l * SROW + p], vd0, vd1);
     const double u = xv[l * 32 + p], w = xv[l * 32 + 16 + p];
-    const double dd = s_dp[l * SROW + p];
+    const double dd = xd[l * 16 + p];
     ov[l * 32 + p] += dd * (double)vd0;
     ov[l * 32 + 16 + p] += dd * (double)vd1;
     oT[l * 16 + p] += s_phib[l * SROW + p];
@@ -1092,7 +1090,7 @@ void upload_adjoint_constants(const double* dvv16, const double* hyai, const dou
 template <typename R>
 void launch_caar_vjp(const CaarVjpArgs<R>& a, int E, cudaStream_t s) {
   constexpr int LG = LG_ADJ<R>();
-  const size_t smem = 9 * NLEV * SROW * sizeof(double);
+  const size_t smem = 7 * NLEV * SROW * sizeof(double);
   static bool init = false;
   if (!init) {
     cudaFuncSetAttribute(k_caar_vjp<R, LG>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
