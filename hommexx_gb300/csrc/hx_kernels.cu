@@ -649,17 +649,21 @@ __global__ void __launch_bounds__(LG * 16) k_precompute_divdp(EulerArgs<R> a) {
 // once per point and level and reused for every tracer; Q = Qdp / dp goes to qtens when
 // the biharmonic needs it; per-level min/max over the 16 points (in R, exact) to
 // qlim_out, combined with the previous qlim when rhs_multiplier == 1.
-template <typename R, int LG>
-__global__ void __launch_bounds__(LG * 16) k_qminmax(EulerArgs<R> a, double* qlim_out, int store_q) {
-  constexpr int NL = NLEV / LG;
-  const int e = blockIdx.x;
-  const int tid = threadIdx.x, p = tid & 15, lg = tid >> 4;
+// Grid E, 96 threads: thread (lv = tid / 4, c = tid % 4) owns points 4c .. 4c+3 of
+// levels lv, lv + 24 and lv + 48, so the min/max over a level's 16 points is three local
+// steps and two shuffles among four lanes (min and max are exact: any order gives the
+// same bounds).
+template <typename R>
+__global__ void __launch_bounds__(96) k_qminmax(EulerArgs<R> a, double* qlim_out, int store_q) {
+  const int e = blockIdx.x, tid = threadIdx.x, c = tid & 3, lv = tid >> 2;
   const R rhsdt = R(a.rhs_multiplier * a.dt);
-  R rdp[NL];
+  R rdp[3][4];
 #pragma unroll
-  for (int k = 0; k < NL; ++k) {
-    const size_t i3 = ((size_t)e * NLEV + lg + LG * k) * 16 + p;
-    rdp[k] = R(1) / (cvt<R>(a.derived_dp[i3]) - rhsdt * cvt<R>(a.divdp_proj[i3]));
+  for (int r = 0; r < 3; ++r) {
+    const size_t i3 = ((size_t)e * NLEV + lv + 24 * r) * 16 + 4 * c;
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+      rdp[r][j] = R(1) / (cvt<R>(a.derived_dp[i3 + j]) - rhsdt * cvt<R>(a.divdp_proj[i3 + j]));
   }
 #pragma unroll 1
   for (int q = 0; q < a.Q; ++q) {
@@ -668,31 +672,40 @@ __global__ void __launch_bounds__(LG * 16) k_qminmax(EulerArgs<R> a, double* qli
     double* ql = qlim_out + ((size_t)e * a.Q + q) * 2 * NLEV;
     const double* qo = a.qlim + ((size_t)e * a.Q + q) * 2 * NLEV;
 #pragma unroll
-    for (int k = 0; k < NL; ++k) {
-      const int l = lg + LG * k;
-      const R val = cvt<R>(qsrc[l * 16 + p]) * rdp[k];
-      if (store_q) qt[l * 16 + p] = dbl(val);
+    for (int r = 0; r < 3; ++r) {
+      const int l = lv + 24 * r;
+      const double2* src = reinterpret_cast<const double2*>(qsrc + l * 16 + 4 * c);
+      const double2 s01 = src[0], s23 = src[1];
+      R v[4] = {cvt<R>(s01.x) * rdp[r][0], cvt<R>(s01.y) * rdp[r][1], cvt<R>(s23.x) * rdp[r][2],
+                cvt<R>(s23.y) * rdp[r][3]};
+      if (store_q) {
+        double2* dst = reinterpret_cast<double2*>(qt + l * 16 + 4 * c);
+        dst[0] = make_double2(dbl(v[0]), dbl(v[1]));
+        dst[1] = make_double2(dbl(v[2]), dbl(v[3]));
+      }
       double dmn, dmx;
       if constexpr (kF32<R>) {
-        R mn = val, mx = val;
+        R mn = fminf(fminf(v[0], v[1]), fminf(v[2], v[3]));
+        R mx = fmaxf(fmaxf(v[0], v[1]), fmaxf(v[2], v[3]));
 #pragma unroll
-        for (int off = 8; off >= 1; off >>= 1) {
-          mn = fminf(mn, __shfl_xor_sync(FULL, mn, off, 16));
-          mx = fmaxf(mx, __shfl_xor_sync(FULL, mx, off, 16));
+        for (int off = 1; off <= 2; off <<= 1) {
+          mn = fminf(mn, __shfl_xor_sync(FULL, mn, off, 4));
+          mx = fmaxf(mx, __shfl_xor_sync(FULL, mx, off, 4));
         }
         dmn = dbl(mn);
         dmx = dbl(mx);
       } else {  // exact min/max on the integer pipe
-        long long mn = dkey(val), mx = mn;
+        const long long k0 = dkey(v[0]), k1 = dkey(v[1]), k2 = dkey(v[2]), k3 = dkey(v[3]);
+        long long mn = kmin(kmin(k0, k1), kmin(k2, k3)), mx = kmax(kmax(k0, k1), kmax(k2, k3));
 #pragma unroll
-        for (int off = 8; off >= 1; off >>= 1) {
-          mn = kmin(mn, __shfl_xor_sync(FULL, mn, off, 16));
-          mx = kmax(mx, __shfl_xor_sync(FULL, mx, off, 16));
+        for (int off = 1; off <= 2; off <<= 1) {
+          mn = kmin(mn, __shfl_xor_sync(FULL, mn, off, 4));
+          mx = kmax(mx, __shfl_xor_sync(FULL, mx, off, 4));
         }
         dmn = dkey_value(mn);
         dmx = dkey_value(mx);
       }
-      if (p == 0) {
+      if (c == 0) {
         if (a.rhs_multiplier == 1.0) {
           dmn = fmin(qo[l], dmn);
           dmx = fmax(qo[NLEV + l], dmx);
@@ -1596,7 +1609,7 @@ void launch_euler_step(EulerArgs<R>& a, int E, int time_avg, cudaStream_t s) {
     const bool nbr = (a.rhs_multiplier == 0.0 || a.rhs_multiplier == 2.0);
     {
       KScope k("euler_qminmax", s);
-      k_qminmax<R, LG><<<E, LG * 16, 0, s>>>(a, nbr ? a.qlim_tmp : a.qlim, a.rhs_multiplier == 2.0);
+      k_qminmax<R><<<E, 96, 0, s>>>(a, nbr ? a.qlim_tmp : a.qlim, a.rhs_multiplier == 2.0);
     }
     if (a.rhs_multiplier == 2.0) {
       a.rhs_viss = 3.0;
