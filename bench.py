@@ -209,7 +209,6 @@ def run_gpu(args, rank, world):
     hv = S.hybrid_coordinate()
     state = S.initial_state(mesh, QSIZE, hv)
     out = {}
-    import ctypes
     forms = [f for f in args.forms.split(",") if f]
     for precision, tag in ((0, "fp64"), (1, "mixed")):
         if tag not in forms or (tag == "mixed" and args.no_mixed):
@@ -227,11 +226,24 @@ def run_gpu(args, rank, world):
         launches = L.lib.hx_launch_count() - launches0
         stats = L.kernel_stats()
         t = _max_over_ranks(t, world)
-        # end-to-end through the C ABI with pinned host buffers
-        res = L.push_results()
-        host_in = {k: np.ascontiguousarray(state[k]) for k in ("v", "T", "dp3d", "Qdp", "ps_v")}
-        for a in list(host_in.values()) + list(res.values()):
-            L.lib.hx_host_register(ctypes.c_void_p(a.ctypes.data), ctypes.c_size_t(a.nbytes))
+        # end-to-end through the C ABI with host buffers page-locked at allocation
+        # (cudaHostAlloc through torch's pinned allocator, which raises rather than fall
+        # back to pageable memory)
+        import torch
+        keep = []
+
+        def pinned(shape, fill=None):
+            t = torch.empty(tuple(shape), dtype=torch.float64, pin_memory=True)
+            keep.append(t)
+            a = t.numpy()
+            if fill is not None:
+                a[...] = fill
+            return a
+
+        res0 = L.push_results()
+        res = {k: pinned(v.shape) for k, v in res0.items()}
+        del res0
+        host_in = {k: pinned(state[k].shape, state[k]) for k in ("v", "T", "dp3d", "Qdp", "ps_v")}
         h2d = sum(a.nbytes for a in host_in.values())
         d2h = sum(a.nbytes for a in res.values())
         L.set_async_copies(True)
@@ -240,17 +252,27 @@ def run_gpu(args, rank, world):
         L.run_subcycle(DT)
         L.push_results(res)
         _barrier(world)
+        tp = [0.0, 0.0, 0.0]
         t0 = time.perf_counter()
         for _ in range(args.steps):
+            ta = time.perf_counter()
             L.set_state(host_in)
+            tb = time.perf_counter()
             L.run_subcycle(DT)
+            tc = time.perf_counter()
             L.push_results(res)
+            td = time.perf_counter()
+            tp[0] += tb - ta
+            tp[1] += tc - tb
+            tp[2] += td - tc
         te = time.perf_counter() - t0
         te = _max_over_ranks(te, world)
         L.stream_results(None)
         L.set_async_copies(False)
-        for a in list(host_in.values()) + list(res.values()):
-            L.lib.hx_host_unregister(ctypes.c_void_p(a.ctypes.data))
+        print(f"[e2e {tag}] per interval: init_elements_states_c {1e3 * tp[0] / args.steps:.2f} ms, "
+              f"prim_run_subcycle_c {1e3 * tp[1] / args.steps:.2f} ms, cxx_push_results_to_f90 "
+              f"{1e3 * tp[2] / args.steps:.2f} ms", file=sys.stderr)
+        del keep
         out[tag] = dict(t=t, te=te, launches=launches, stats=stats, clocks=cs.summary(),
                         h2d=h2d, d2h=d2h)
         if tag == "fp64":
@@ -622,8 +644,8 @@ def main():
         "e2e": {"value": sypd(args.steps, f["te"]) * world, "unit": "SYPD",
                 "h2d_bytes_per_step": f["h2d"], "d2h_bytes_per_step": f["d2h"],
                 "copies": "init_elements_states_c / prim_run_subcycle_c / cxx_push_results_to_f90 "
-                          "from pinned host memory; Qdp in and the results out overlap the step "
-                          "(hx_set_async_copies, hx_stream_results)"},
+                          "from host memory page-locked at allocation; Qdp in and the results out "
+                          "overlap the step (hx_set_async_copies, hx_stream_results)"},
         "gpu_launches": f["launches"],
         "clocks": f["clocks"],
         "roofline": {"bound": "hbm", "kernel": top["kernel"], "achieved": achieved, "peak": peak,
