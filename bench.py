@@ -60,15 +60,15 @@ FALLBACK_HBM_GBS = 6800.0
 # sm__pipe_fp64_cycles_active of the third launch of each kernel), per form.  Traffic is
 # scaled to the run's size by the element count (levels and tracers fixed).
 NCU_NE16 = {
-    "fp64": {"euler_aal_tracer": (473.5e6, 0.836), "caar_stage": (153.5e6, 0.857),
-             "hv_laplace2": (161.5e6, 0.814), "ppm_remap": (327.9e6, 0.849),
-             "euler_bih_post": (281.9e6, 0.870), "hv_laplace1": (77.3e6, 0.892),
-             "euler_bih_pre": (260.5e6, 0.905), "euler_dss_qdp": (400.1e6, 0.818),
-             "euler_qminmax": (283.8e6, 0.552)},
-    "mixed": {"euler_aal_tracer": (472.4e6, 0.385), "caar_stage": (151.3e6, 0.785),
-              "hv_laplace2": (151.0e6, 0.491), "ppm_remap": (328.8e6, 0.643),
-              "euler_dss_qdp": (400.0e6, 0.817), "euler_qminmax": (282.1e6, 0.325),
-              "euler_bih_post": (273.9e6, 0.482)},
+    "fp64": {"euler_aal_tracer": (473.5e6, 0.839), "caar_stage": (153.3e6, 0.863),
+             "hv_laplace2": (162.0e6, 0.818), "ppm_remap": (328.5e6, 0.850),
+             "euler_bih_post": (282.0e6, 0.863), "hv_laplace1": (77.4e6, 0.894),
+             "euler_bih_pre": (260.5e6, 0.912), "euler_dss_qdp": (399.9e6, 0.817),
+             "euler_qminmax": (283.2e6, 0.649)},
+    "mixed": {"euler_aal_tracer": (472.6e6, 0.374), "caar_stage": (151.5e6, 0.782),
+              "hv_laplace2": (151.6e6, 0.504), "ppm_remap": (328.5e6, 0.645),
+              "euler_dss_qdp": (399.9e6, 0.818), "euler_qminmax": (276.9e6, 0.138),
+              "euler_bih_post": (274.1e6, 0.479)},
 }
 
 
