@@ -9,7 +9,7 @@ from hommexx_gb300 import abi, mesh as M, state as S
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("ne,hvs", [(4, 0.0), (4, 3.2), (16, 0.0), (30, 0.0)])
+@pytest.mark.parametrize("ne,hvs", [(1, 0.0), (2, 0.0), (4, 0.0), (4, 3.2), (16, 0.0), (30, 0.0)])
 def test_cube_mesh_matches_numpy_generator(gpu_path, ne, hvs):
     d = H.lib(gpu_path).cube_mesh(ne, hvs)
     m = M.build_mesh(ne, hvs)

@@ -262,6 +262,18 @@ def test_diagnostics(pair, cpstar, ftype):
     assert np.isnan(g.diag["IEner"][:, 3]).all() and np.isnan(g.diag["Qvar"][:, 2]).all()
 
 
+def test_diagnostics_mixed_form(pair):
+    """A mixed-form session fills the init_diagnostics_c arrays like the FP64 oracle, to
+    the mixed form's accuracy (diagnostics themselves are FP64 sums)."""
+    g, o = pair(precision=1, rsplit=3, disable_diagnostics=False, state_frequency=1, diagnostics=True)
+    g.run_subcycle(DT)
+    o.run_subcycle(DT)
+    for k in ("IEner", "KEner", "PEner"):
+        assert np.array_equal(g.diag[k][:, 2], o.diag[k][:, 2]), k   # before the step: same inputs
+        assert H.rel_err(g.diag[k][:, 1], o.diag[k][:, 1]) < 1e-6, k
+    assert H.rel_err(g.diag["Qmass"][:, 1], o.diag["Qmass"][:, 1]) < 1e-5
+
+
 def test_mass_conservation_gpu(pair):
     g, _ = pair(rsplit=3)
     m = H.mesh(4)

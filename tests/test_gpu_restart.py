@@ -21,14 +21,17 @@ def test_restart_file_matches_oracle_bytes(gpu_path, oracle_path, tmp_path):
     assert fg.read_bytes() == fo.read_bytes()
 
 
-def test_restart_continuation_gpu(gpu_path, tmp_path):
+@pytest.mark.parametrize("precision,rsplit", [(0, 3), (1, 3), (0, 0)])
+def test_restart_continuation_gpu(gpu_path, tmp_path, precision, rsplit):
+    """Two intervals in one run equal one interval, restart, one interval (bit for bit),
+    in the FP64 and mixed forms and with the vertically Eulerian step."""
     f = tmp_path / "r.bin"
-    L = H.setup(gpu_path, 4, 4, rsplit=3)
+    L = H.setup(gpu_path, 4, 4, precision=precision, rsplit=rsplit)
     L.run_subcycle(DT)
     L.write_restart(f)
     L.run_subcycle(DT)
     want, tl = L.push_results(), list(L.tl)
-    L = H.setup(gpu_path, 4, 4, rsplit=3)
+    L = H.setup(gpu_path, 4, 4, precision=precision, rsplit=rsplit)
     L.read_restart(f)
     L.run_subcycle(DT)
     got = L.push_results()
