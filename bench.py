@@ -12,9 +12,10 @@ mirrored remap; seeded smooth synthetic initial state (spherical harmonics of de
 * ``e2e``: the same through the C ABI with host buffers, each step copying the state in
   (``init_elements_states_c``) and the results out (``cxx_push_results_to_f90``) from
   pinned host memory, wall clock.  The copies overlap the step where their data allow
-  (``hx_set_async_copies``: Qdp streams in during the first dynamics step;
-  ``hx_stream_results``: each result field is copied out once it is final); every byte
-  still crosses the host link inside the timed region.
+  (``hx_set_async_copies``: time levels nm1 and np1 stream in during the first Caar
+  stages and Qdp during the first dynamics step; ``hx_stream_results``: each result
+  piece is copied out once it is final, the last ones chunk by chunk of the final
+  remap); every byte still crosses the host link inside the timed region.
 * ``mixed``: the mixed-precision form timed the same way, with its error against the
   FP64 form after ``--error-days`` simulated days.
 * ``roofline``: the kernel with the largest share of device time; algorithmic bytes per
@@ -644,8 +645,9 @@ def main():
         "e2e": {"value": sypd(args.steps, f["te"]) * world, "unit": "SYPD",
                 "h2d_bytes_per_step": f["h2d"], "d2h_bytes_per_step": f["d2h"],
                 "copies": "init_elements_states_c / prim_run_subcycle_c / cxx_push_results_to_f90 "
-                          "from host memory page-locked at allocation; Qdp in and the results out "
-                          "overlap the step (hx_set_async_copies, hx_stream_results)"},
+                          "from host memory page-locked at allocation; time levels nm1/np1 and Qdp in "
+                          "and the results out overlap the step (hx_set_async_copies, "
+                          "hx_stream_results)"},
         "gpu_launches": f["launches"],
         "clocks": f["clocks"],
         "roofline": {"bound": "hbm", "kernel": top["kernel"], "achieved": achieved, "peak": peak,

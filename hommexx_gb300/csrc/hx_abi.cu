@@ -143,7 +143,7 @@ struct Backend {
   virtual void traj_vjp(const double* vb, const double* Tb, const double* dpb, double* vg, double* Tg,
                         double* dpg) = 0;
   virtual void write_restart(const std::string& path) = 0;
-  // Orders the session stream after any Qdp copy still streaming in (hx_set_async_copies).
+  // Orders the session stream after any state copy still streaming in (hx_set_async_copies).
   virtual void copies_ready() = 0;
   virtual void read_restart(const std::string& path) = 0;
 };
@@ -239,8 +239,9 @@ struct BackendT : Backend {
   double* lapm = 0;  // FP64 form: dense weak Laplacian per element
   double *fm = 0, *ft = 0, *fq = 0;  // CAM forcing, Fortran layouts (allocated on first push)
   double *phis_d = 0, *diag_d = 0;   // FP64 phis; diagnostics scratch (allocated on first use)
-  cudaEvent_t ev_qdp_in = nullptr, ev_mark = nullptr;
+  cudaEvent_t ev_qdp_in = nullptr, ev_mark = nullptr, ev_lvl[NTL] = {};
   bool qdp_pending = false;   // Qdp still streaming in on g_copy
+  bool lvl_pending[NTL] = {}; // a dynamics level still streaming in on g_copy
   bool stream_last = false;   // the next prim_step is the interval's last
   int *tab_cnt = 0, *tab_src = 0, *nbr = 0, *invalid = 0;
   int* h_invalid = nullptr;
@@ -262,6 +263,8 @@ struct BackendT : Backend {
     if (h_invalid) cudaFreeHost(h_invalid);
     if (ev_qdp_in) cudaEventDestroy(ev_qdp_in);
     if (ev_mark) cudaEventDestroy(ev_mark);
+    for (cudaEvent_t ev : ev_lvl)
+      if (ev) cudaEventDestroy(ev);
     free_traj();
   }
 
@@ -294,6 +297,7 @@ struct BackendT : Backend {
     ck(cudaMallocHost(&h_invalid, sizeof(int)), "cudaMallocHost");
     ck(cudaEventCreateWithFlags(&ev_qdp_in, cudaEventDisableTiming), "cudaEventCreate");
     ck(cudaEventCreateWithFlags(&ev_mark, cudaEventDisableTiming), "cudaEventCreate");
+    for (cudaEvent_t& ev : ev_lvl) ck(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "cudaEventCreate");
     wk = Work{v, T, dp, phi, dpdiss_ave, dpdiss_bih, ps_v};
   }
 
@@ -334,77 +338,109 @@ struct BackendT : Backend {
   void set_states(const double* hv, const double* hT, const double* hdp, const double* hq,
                   const double* hps) override {
     const size_t n3 = N3();
+    copies_ready();
+    if (s.async_copies) {
+      // Everything streams in on g_copy, after the work already queued on g_stream: the
+      // dynamics level by level, n0 (with ps_v) first, which g_stream waits for at once;
+      // nm1 and np1, which the next interval writes before it reads them, are waited for
+      // just before their first writer (the DSS of the Caar stage that targets them);
+      // then Qdp, waited for by its first reader.
+      stream_mark();
+      const int order[NTL] = {s.tl.n0, s.tl.nm1, s.tl.np1};
+      for (int lvl : order) {
+        level_in(v, hv, (size_t)NLEV * 32, lvl);
+        level_in(T, hT, (size_t)NLEV * 16, lvl);
+        level_in(dp, hdp, (size_t)NLEV * 16, lvl);
+        if (lvl == s.tl.n0)
+          ck(cudaMemcpyAsync(ps_v, hps, (size_t)E * NTL * 16 * sizeof(double), cudaMemcpyHostToDevice, g_copy),
+             "H2D ps");
+        ck(cudaEventRecord(ev_lvl[lvl], g_copy), "cudaEventRecord");
+        lvl_pending[lvl] = true;
+      }
+      level_ready(s.tl.n0);
+      if (Q > 0) {
+        ck(cudaMemcpyAsync(qdp, hq, n3 * QTL * Q * sizeof(double), cudaMemcpyHostToDevice, g_copy), "H2D qdp");
+        ck(cudaEventRecord(ev_qdp_in, g_copy), "cudaEventRecord");
+        qdp_pending = true;
+      }
+      return;
+    }
     to_dev(v, hv, n3 * NTL * 2);
     to_dev(T, hT, n3 * NTL);
     to_dev(dp, hdp, n3 * NTL);
-    copies_ready();
-    if (Q > 0 && s.async_copies) {
-      // Qdp streams in on g_copy, after the work already queued on g_stream, while the
-      // next interval's dynamics run; its first reader waits for ev_qdp_in.
-      ck(cudaEventRecord(ev_mark, g_stream), "cudaEventRecord");
-      ck(cudaStreamWaitEvent(g_copy, ev_mark, 0), "cudaStreamWaitEvent");
-      ck(cudaMemcpyAsync(qdp, hq, n3 * QTL * Q * sizeof(double), cudaMemcpyHostToDevice, g_copy), "H2D qdp");
-      ck(cudaEventRecord(ev_qdp_in, g_copy), "cudaEventRecord");
-      qdp_pending = true;
-    } else if (Q > 0) {
+    if (Q > 0)
       ck(cudaMemcpyAsync(qdp, hq, n3 * QTL * Q * sizeof(double), cudaMemcpyHostToDevice, g_stream), "H2D qdp");
-    }
     ck(cudaMemcpyAsync(ps_v, hps, (size_t)E * NTL * 16 * sizeof(double), cudaMemcpyHostToDevice, g_stream), "H2D ps");
+  }
+  // host -> device copy on g_copy of level lvl of a field laid out [E][NTL][block]
+  void level_in(double* dev, const double* host, size_t block, int lvl) {
+    const size_t w = block * sizeof(double), pitch = w * NTL;
+    ck(cudaMemcpy2DAsync(dev + (size_t)lvl * block, pitch, host + (size_t)lvl * block, pitch, w, E,
+                         cudaMemcpyHostToDevice, g_copy),
+       "H2D level");
+  }
+  // orders g_stream after the copy of dynamics level lvl, if it is still streaming in
+  void level_ready(int lvl) {
+    if (lvl < 0 || lvl >= NTL || !lvl_pending[lvl]) return;
+    ck(cudaStreamWaitEvent(g_stream, ev_lvl[lvl], 0), "cudaStreamWaitEvent");
+    lvl_pending[lvl] = false;
   }
 
   void copies_ready() override {
+    for (int lvl = 0; lvl < NTL; ++lvl) level_ready(lvl);
     if (!qdp_pending) return;
     ck(cudaStreamWaitEvent(g_stream, ev_qdp_in, 0), "cudaStreamWaitEvent");
     qdp_pending = false;
   }
 
   // hx_stream_results: device -> host copies on g_copy, each enqueued once its data is
-  // final (after what g_stream has queued so far).  Level lvl of a field whose host and
-  // device layouts are [E][nlev][block].
-  void stream_level(int which, const double* dev, size_t block, int nlev, int lvl) {
+  // final (after what g_stream has queued so far).  Level lvl of elements [e0, e0 + ne)
+  // of a field whose host and device layouts are [E][nlev][block].
+  void stream_level(int which, const double* dev, size_t block, int nlev, int lvl, int e0 = 0, int ne = -1) {
     double* host = s.stream_to[which];
-    if (!host || block == 0) return;
-    const size_t w = block * sizeof(double), pitch = w * nlev;
-    ck(cudaMemcpy2DAsync(host + (size_t)lvl * block, pitch, dev + (size_t)lvl * block, pitch, w, E,
-                         cudaMemcpyDeviceToHost, g_copy), "D2H stream");
+    if (ne < 0) ne = E - e0;
+    if (!host || block == 0 || ne <= 0) return;
+    const size_t w = block * sizeof(double), pitch = w * nlev, off = ((size_t)e0 * nlev + lvl) * block;
+    ck(cudaMemcpy2DAsync(host + off, pitch, dev + off, pitch, w, ne, cudaMemcpyDeviceToHost, g_copy),
+       "D2H stream");
   }
   void stream_mark() {
     ck(cudaEventRecord(ev_mark, g_stream), "cudaEventRecord");
     ck(cudaStreamWaitEvent(g_copy, ev_mark, 0), "cudaStreamWaitEvent");
   }
   bool streaming() const { return s.stream_to[0] != nullptr; }
-  // the dynamics levels other than np1 are final after the last dynamics; omega_p too
-  // when there are no tracers (the tracer step's last stage DSSes it in place)
-  void stream_dynamics(int np1) {
-    stream_mark();
-    for (int lvl = 0; lvl < NTL; ++lvl) {
-      if (lvl == np1) continue;
-      stream_level(0, v, (size_t)NLEV * 32, NTL, lvl);
-      stream_level(1, T, (size_t)NLEV * 16, NTL, lvl);
-      stream_level(2, dp, (size_t)NLEV * 16, NTL, lvl);
+  // one dynamics level (v, T, dp3d) of elements [e0, e0 + ne)
+  void stream_dynamics_level(int lvl, int e0 = 0, int ne = -1) {
+    stream_level(0, v, (size_t)NLEV * 32, NTL, lvl, e0, ne);
+    stream_level(1, T, (size_t)NLEV * 16, NTL, lvl, e0, ne);
+    stream_level(2, dp, (size_t)NLEV * 16, NTL, lvl, e0, ne);
+  }
+  // The interval's last remap and update_q in element chunks of whole remap waves; each
+  // chunk's results (dynamics level np1, tracer level np1_qdp, Q) stream out while the
+  // next chunk computes.  The chunks write disjoint elements, and every kernel reads
+  // only its own element, so the split changes no result.
+  void remap_streamed(int np1, int np1_qdp, double dt) {
+    ck(cudaMemsetAsync(invalid, 0, sizeof(int), g_stream), "memset");
+    const int chunk = hx::remap_chunk_elements<R>(E, 8);
+    for (int e0 = 0; e0 < E; e0 += chunk) {
+      const int ne = std::min(chunk, E - e0);
+      RemapArgs a = remap_args(np1, np1_qdp, dt);
+      const size_t n3 = (size_t)e0 * NLEV * 16;
+      a.v += n3 * NTL * 2; a.T += n3 * NTL; a.dp += n3 * NTL; a.qdp += n3 * QTL * Q;
+      a.ps_v += (size_t)e0 * NTL * 16; a.eta += n3; a.nelem = ne;
+      hx::launch_remap<R>(a, g_stream);
+      launch_update_q(ne, Q, qdp + n3 * QTL * Q, Qc + n3 * Q, ps_v + (size_t)e0 * NTL * 16, np1, np1_qdp,
+                      s.ps0, g_stream);
+      post("remap");
+      stream_mark();
+      stream_dynamics_level(np1, e0, ne);
+      if (Q > 0) {
+        stream_level(3, qdp, (size_t)Q * NLEV * 16, QTL, np1_qdp, e0, ne);
+        stream_level(4, Qc, (size_t)Q * NLEV * 16, 1, 0, e0, ne);
+      }
     }
-    if (Q == 0) stream_level(6, omega_p, (size_t)NLEV * 16, 1, 0);
-  }
-  // the tracer level the remap does not write and omega_p are final after the last
-  // tracer step
-  void stream_tracers(int n0_qdp) {
-    if (Q == 0) return;
     stream_mark();
-    stream_level(3, qdp, (size_t)Q * NLEV * 16, QTL, n0_qdp);
-    stream_level(6, omega_p, (size_t)NLEV * 16, 1, 0);
-  }
-  // the rest after the remap and update_q; waits for every streamed copy
-  void stream_rest(int np1, int np1_qdp) {
-    stream_mark();
-    stream_level(0, v, (size_t)NLEV * 32, NTL, np1);
-    stream_level(1, T, (size_t)NLEV * 16, NTL, np1);
-    stream_level(2, dp, (size_t)NLEV * 16, NTL, np1);
     stream_level(5, ps_v, (size_t)NTL * 16, 1, 0);
-    if (Q > 0) {
-      stream_level(3, qdp, (size_t)Q * NLEV * 16, QTL, np1_qdp);
-      stream_level(4, Qc, (size_t)Q * NLEV * 16, 1, 0);
-    }
-    ck(cudaStreamSynchronize(g_copy), "streamed results");
   }
 
   void push(double* hv, double* hT, double* hdp, double* hq, double* hQ, double* hps, double* homega) override {
@@ -477,8 +513,12 @@ struct BackendT : Backend {
     a.dt = dt; a.eta_ave_w = w; a.p_top = s.hyai[0] * s.ps0;
     a.rk_combine = combine; a.n0orig = n0orig;
     a.rsplit = s.prm.rsplit; a.eta_acc = eta;
+    level_ready(nm1);
+    level_ready(n0);
+    level_ready(n0orig);
     launch_caar<R>(a, E, g_stream);
     post("caar");
+    level_ready(np1);
     launch_dss_state(E, caar_out, wk.v, wk.T, wk.dp, np1, rsp_d, table(), g_stream);
     post("dss_caar");
   }
@@ -492,7 +532,10 @@ struct BackendT : Backend {
     caar_stage(nm1, np1, np1, 3.0 * dt / 4.0, 3.0 * w / 4.0, n0_qdp, 1, n0);
   }
 
-  void hypervis(int np1, double dt, double w) override { hypervis_cycles(np1, dt, w, s.prm.hypervis_subcycle); }
+  void hypervis(int np1, double dt, double w) override {
+    for (int lvl = 0; lvl < NTL; ++lvl) level_ready(lvl);
+    hypervis_cycles(np1, dt, w, s.prm.hypervis_subcycle);
+  }
 
   // ncyc of the hypervis_subcycle subcycles of HyperviscosityFunctorImpl::run
   void hypervis_cycles(int np1, double dt, double w, int ncyc) {
@@ -551,14 +594,17 @@ struct BackendT : Backend {
 
   // reset = false keeps an invalid-thickness flag raised by an earlier remap; dt is the
   // remap interval (used by the vertically Eulerian source thickness).
-  void launch_remap(int np1, int np1_qdp, bool reset = true, double dt = 0.0) {
+  RemapArgs remap_args(int np1, int np1_qdp, double dt) const {
     RemapArgs a;
     a.rsplit = s.prm.rsplit; a.eta = eta; a.dt = dt;
     a.v = wk.v; a.T = wk.T; a.dp = wk.dp; a.qdp = qdp; a.ps_v = wk.ps_v;
     a.np1 = np1; a.n0_qdp = np1_qdp; a.Q = wk.v == v ? Q : 0; a.remap_alg = s.prm.remap_alg; a.nelem = E;
     a.ps0 = s.ps0; a.hyai0 = s.hyai[0]; a.invalid = invalid;
+    return a;
+  }
+  void launch_remap(int np1, int np1_qdp, bool reset = true, double dt = 0.0) {
     if (reset) ck(cudaMemsetAsync(invalid, 0, sizeof(int), g_stream), "memset");
-    hx::launch_remap<R>(a, g_stream);
+    hx::launch_remap<R>(remap_args(np1, np1_qdp, dt), g_stream);
     post("remap");
   }
   int remap_status() {
@@ -584,14 +630,33 @@ struct BackendT : Backend {
         n0_qdp = s.tl.n0_qdp;
       }
       const double w = 1.0 / p.qsplit;
+      // In the interval's last dynamics step level n0 is only read, and nm1 is final
+      // once rk5 has combined into it; both stream out while the step goes on.
+      const bool last = stream_last && n == p.qsplit - 1;
+      if (last) {
+        stream_mark();
+        stream_dynamics_level(s.tl.n0);
+      }
       rk5(s.tl.nm1, s.tl.n0, s.tl.np1, n0_qdp, dt, w);
+      if (last) {
+        stream_mark();
+        stream_dynamics_level(s.tl.nm1);
+      }
       hypervis(s.tl.np1, dt, w);
     }
-    if (stream_last) stream_dynamics(s.tl.np1);
     if (p.qsize > 0) {
       copies_ready();
+      // the last tracer step only reads level n0_qdp; omega_p is final after its DSS
+      if (stream_last) {
+        s.tl.update_tracers_levels(p.qsplit);
+        stream_mark();
+        stream_level(3, qdp, (size_t)Q * NLEV * 16, QTL, s.tl.n0_qdp);
+      }
       tracers_rk2(dt * p.qsplit);
-      if (stream_last) stream_tracers(s.tl.n0_qdp);
+    }
+    if (stream_last) {
+      stream_mark();
+      stream_level(6, omega_p, (size_t)NLEV * 16, 1, 0);
     }
   }
 
@@ -714,9 +779,13 @@ struct BackendT : Backend {
     stream_last = false;
     copies_ready();
     s.tl.update_tracers_levels(p.qsplit);
-    launch_remap(s.tl.np1, s.tl.np1_qdp, true, dt_remap);
-    launch_update_q(E, Q, qdp, Qc, ps_v, s.tl.np1, s.tl.np1_qdp, s.ps0, g_stream);
-    post("update_q");
+    if (stream) {
+      remap_streamed(s.tl.np1, s.tl.np1_qdp, dt_remap);
+    } else {
+      launch_remap(s.tl.np1, s.tl.np1_qdp, true, dt_remap);
+      launch_update_q(E, Q, qdp, Qc, ps_v, s.tl.np1, s.tl.np1_qdp, s.ps0, g_stream);
+      post("update_q");
+    }
     const int st = remap_status();
     if (st) {
       if (stream) cudaStreamSynchronize(g_copy);  // no copy outlives the call
@@ -728,7 +797,7 @@ struct BackendT : Backend {
       energy_halftimes(false, 1);
     }
     if (stream) {
-      stream_rest(s.tl.np1, s.tl.np1_qdp);
+      ck(cudaStreamSynchronize(g_copy), "streamed results");
       s.streamed = true;
     }
     s.tl.update_dynamics_levels();
@@ -1225,7 +1294,7 @@ int run(F&& f) {
   return 0;
 }
 
-// Every entry point but prim_run_subcycle_c: any Qdp still streaming in is ordered
+// Every entry point but prim_run_subcycle_c: any state copy still streaming in is ordered
 // before the call's work, and the streamed results stop standing for the state.
 Backend& B() {
   Session& s = S();

@@ -1658,15 +1658,34 @@ void launch_euler_step(EulerArgs<R>& a, int E, int time_avg, cudaStream_t s) {
 }
 
 template <typename R>
-void launch_remap(const RemapArgs& a, cudaStream_t s) {
+size_t remap_smem() {
   const size_t smem = (size_t)RCOLS * r_col<R>() * sizeof(double);
   static bool init = false;
   if (!init) {
     cudaFuncSetAttribute(k_remap<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     init = true;
   }
+  return smem;
+}
+
+template <typename R>
+void launch_remap(const RemapArgs& a, cudaStream_t s) {
+  const size_t smem = remap_smem<R>();
   KScope k("ppm_remap", s);
   k_remap<R><<<(a.nelem * 16 + RCOLS - 1) / RCOLS, RT, smem, s>>>(a);
+}
+
+template <typename R>
+int remap_chunk_elements(int E, int parts) {
+  const size_t smem = remap_smem<R>();
+  int dev = 0, sms = 0, per_sm = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_remap<R>, RT, smem) != cudaSuccess)
+    per_sm = 0;
+  const int wave = std::max(1, sms * per_sm * RCOLS / 16);
+  const int want = std::max(1, (E + parts - 1) / parts);
+  return std::max(1, want / wave) * wave;
 }
 
 void launch_update_q(int E, int Q, const double* qdp, double* Qc, const double* ps_v, int np1, int np1_qdp,
@@ -1734,7 +1753,8 @@ void launch_lap_matrix(const MetricP<double>& m, int E, double* out, cudaStream_
   template void launch_hv<R>(const HvArgs<R>&, int, cudaStream_t);                  \
   template void launch_precompute_divdp<R>(const EulerArgs<R>&, int, cudaStream_t); \
   template void launch_euler_step<R>(EulerArgs<R>&, int, int, cudaStream_t);  \
-  template void launch_remap<R>(const RemapArgs&, cudaStream_t);
+  template void launch_remap<R>(const RemapArgs&, cudaStream_t);                  \
+  template int remap_chunk_elements<R>(int, int);
 HX_INST(double)
 HX_INST(float)
 

@@ -128,6 +128,9 @@ template <typename R> void launch_hv(const HvArgs<R>& a, int E, cudaStream_t s);
 template <typename R> void launch_precompute_divdp(const EulerArgs<R>& a, int E, cudaStream_t s);
 template <typename R> void launch_euler_step(EulerArgs<R>& a, int E, int time_avg, cudaStream_t s);
 template <typename R> void launch_remap(const RemapArgs& a, cudaStream_t s);
+// Elements per launch when a remap over E elements is split into about `parts` launches:
+// a whole number of full waves (SMs x resident CTAs x 4 columns / 16 points), at least one.
+template <typename R> int remap_chunk_elements(int E, int parts);
 void launch_update_q(int E, int Q, const double* qdp, double* Qc, const double* ps_v, int np1,
                      int np1_qdp, double ps0, cudaStream_t s);
 // Energy and tracer mass diagnostics (Diagnostics.cpp): qvar/qmass [E][Q][16] at tracer

@@ -301,16 +301,20 @@ int hx_read_restart(const char* path);
  * traffic runs on the host link (about 210 GB/s in, 190 GB/s out on a GB300), so the
  * state copied in and out every interval costs as much as a third of a mixed-form
  * interval unless it overlaps the step's kernels.
- * hx_set_async_copies(1): init_elements_states_c returns once v, T, dp3d and ps_v are on
- * the device; Qdp keeps streaming in on a copy stream and the first kernel that reads
- * it waits for it.  The caller must leave the Qdp host array unchanged until the next
- * prim_run_subcycle_c (or any other call of this library) returns.  Default 0.
+ * hx_set_async_copies(1): init_elements_states_c returns once time level n0 of v, T and
+ * dp3d, and ps_v, are on the device; levels nm1 and np1 and then Qdp keep streaming in
+ * on a copy stream, and the first kernel that writes or reads each of them waits for it
+ * (levels nm1 and np1 are first written by the DSS of a Caar stage).  The caller must
+ * leave the v, T, dp3d and Qdp host arrays unchanged until the next prim_run_subcycle_c
+ * (or any other call of this library) returns.  Default 0.
  * hx_stream_results(v, T, dp3d, Qdp, Q, ps_v, omega_p): host destinations in the
  * layouts of cxx_push_results_to_f90 (all seven, or all NULL to stop).  Every following
- * prim_run_subcycle_c copies its results there before it returns, each field as soon as
- * it is final (the dynamics levels the remap does not write after the last dynamics
- * step, the tracer level it does not write and omega_p after the last tracer step, the
- * rest after update_q), so most of the copy overlaps the step's last kernels; a
+ * prim_run_subcycle_c copies its results there before it returns, each piece as soon as
+ * it is final: dynamics level n0 while the interval's last dynamics step runs (it only
+ * reads it), level nm1 once that step's RK stages are done, the tracer level the last
+ * tracer step only reads before that step, omega_p after it, and level np1, the other
+ * tracer level and Q chunk by chunk of elements from a final remap and update_q split
+ * into launches of whole waves, so most of the copy overlaps the step's kernels; a
  * cxx_push_results_to_f90 with the same seven pointers right after it returns at once.
  * The destinations should be page-locked (hx_host_register) for the copies to overlap. */
 int hx_set_async_copies(int on);
