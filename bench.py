@@ -28,8 +28,8 @@ mirrored remap; seeded smooth synthetic initial state (spherical harmonics of de
   and of the vector-Jacobian product (state on the device, CUDA events), the cost of
   a gradient relative to a forward run, and its checks: central finite differences of
   J = sum spheremp T_final^2 along 10 seeded smooth directions (eps = 1e-6), the
-  dot-product test against the oracle's tangent-linear model, and the mixed form's
-  gradient error against the FP64 one.
+  dot-product test against the CUDA tangent-linear model (``hx_traj_jvp``, also timed)
+  and against the oracle's, and the mixed form's gradient error against the FP64 one.
 
 ``--impl reference`` times that CPU implementation alone and prints its own line.
 Multi-GPU: the step does not shard here (one GPU per box), so N>1 runs N independent
@@ -424,6 +424,13 @@ def run_adjoint(lib_path, dot_check=True):
         fwd()
         t_f1 = _timed(L, fwd)
         t_b1 = _timed(L, vjp)
+        # tangent-linear model: the trajectory again with its tangent beside it
+        rng = np.random.default_rng(2025)
+        tin = dev({k: rng.standard_normal(x0[k].shape) for k in keys})
+        tout = [torch.empty_like(t) for t in xin]
+        torch.cuda.synchronize()
+        jvp = lambda: _traj_call(L.lib.hx_traj_jvp, tin, tout)
+        t_j = _timed(L, jvp)
         L.lib.hx_enable_timing(1)
         vjp()
         L.lib.hx_enable_timing(0)
@@ -435,6 +442,7 @@ def run_adjoint(lib_path, dot_check=True):
                         gradient_cost_vs_forward=(t_f1 + t_b1) / t_plain,
                         reverse_sweep_vs_forward=t_b1 / t_plain,
                         recompute_mode_cost_vs_forward=(t_plain + t_b2) / t_plain,
+                        jvp_ms=t_j, tangent_cost_vs_forward=t_j / t_plain,
                         vjp_kernels=[dict(kernel=n, launches=c, total_ms=round(ms, 3),
                                           share=round(ms / tot, 4)) for n, c, ms in stats[:6]])
         if tag == "fp64":
@@ -456,6 +464,10 @@ def run_adjoint(lib_path, dot_check=True):
                 dy = {k: rng.standard_normal(x0[k].shape) for k in keys}
                 L.traj_forward(x0, ADJ_STEPS, DT)
                 rhs = sum(float(np.vdot(dx[k], v)) for k, v in L.traj_vjp(dy).items())
+                lhs_gpu = sum(float(np.vdot(v, dy[k])) for k, v in L.traj_jvp(dx).items())
+                res["dot_product_gpu"] = dict(tlm_dot=lhs_gpu, adjoint_dot=rhs,
+                                              rel_err=abs(lhs_gpu - rhs) / abs(lhs_gpu),
+                                              tlm="CUDA tangent-linear model (hx_traj_jvp)")
                 O = abi.HxLibrary(os.path.join(ROOT, "oracle", "liboracle.so"))
                 O.init(mesh, hv, params, st, abort_on_error=True)
                 O.lib.hx_oracle_threads.restype = int

@@ -142,6 +142,8 @@ struct Backend {
                             double* vo, double* To, double* dpo) = 0;
   virtual void traj_vjp(const double* vb, const double* Tb, const double* dpb, double* vg, double* Tg,
                         double* dpg) = 0;
+  virtual void traj_jvp(const double* dv, const double* dT, const double* ddp, double* ov, double* oT,
+                        double* odp) = 0;
   virtual void write_restart(const std::string& path) = 0;
   // Orders the session stream after any state copy still streaming in (hx_set_async_copies).
   virtual void copies_ready() = 0;
@@ -1023,11 +1025,21 @@ struct BackendT : Backend {
     bool have = false;
   } tj;
 
+  // Tangent-linear model: tangent work levels [E][3][...] beside the trajectory's, the
+  // tangent of a Caar stage's pre-DSS output and of a subcycle's tendencies, ps_v, and
+  // scratch for the hyperviscosity kernels' dpdiss accumulations.
+  struct Tan {
+    double *v3 = nullptr, *T3 = nullptr, *dp3 = nullptr, *out = nullptr, *bufB = nullptr, *ps = nullptr,
+           *dpa = nullptr, *dpb = nullptr;
+  } tn;
+
   void free_traj() {
-    void* ptrs[] = {tj.v3, tj.T3, tj.dp3, tj.phi, tj.dpa, tj.dpb, tj.ps, tj.cot, tj.pool};
+    void* ptrs[] = {tj.v3, tj.T3, tj.dp3, tj.phi, tj.dpa, tj.dpb, tj.ps, tj.cot, tj.pool,
+                    tn.v3, tn.T3, tn.dp3, tn.out, tn.bufB, tn.ps, tn.dpa, tn.dpb};
     for (void* q : ptrs)
       if (q) cudaFree(q);
     tj = Traj();
+    tn = Tan();
   }
 
   size_t state_doubles() const { return 4 * N3(); }
@@ -1167,6 +1179,117 @@ struct BackendT : Backend {
 
   void zero(DynV d) {
     ck(cudaMemsetAsync(d.v, 0, state_doubles() * sizeof(double), g_stream), "memset");
+  }
+
+  // ---- tangent-linear model along the last trajectory ---------------------------------
+  DynV tan_level(int tl) const {
+    return DynV{tn.v3 + (size_t)tl * NLEV * 32, tn.T3 + (size_t)tl * NLEV * 16,
+                tn.dp3 + (size_t)tl * NLEV * 16, (long long)NTL * NLEV * 32, (long long)NTL * NLEV * 16};
+  }
+  void tan_alloc() {
+    if (tn.v3) return;
+    const size_t n3 = N3();
+    tn.v3 = dalloc<double>(n3 * NTL * 2);
+    tn.T3 = dalloc<double>(n3 * NTL);
+    tn.dp3 = dalloc<double>(n3 * NTL);
+    tn.out = dalloc<double>(4 * n3);
+    tn.bufB = dalloc<double>(4 * n3);
+    tn.ps = dalloc<double>((size_t)E * NTL * 16);
+    tn.dpa = dalloc<double>(n3);
+    tn.dpb = dalloc<double>(n3);
+  }
+  // One Caar stage: the tangent kernel reads the primal stage input before the forward
+  // stage (on the trajectory's work levels) advances it.
+  void caar_stage_tlm(int nm1, int n0, int np1, double dt, int combine, int n0orig) {
+    CaarJvpArgs<R> c;
+    c.m = metric();
+    c.v = wk.v; c.T = wk.T; c.dp = wk.dp;
+    c.tv = tn.v3; c.tT = tn.T3; c.tdp = tn.dp3; c.out = tn.out;
+    c.nm1 = nm1; c.n0 = n0; c.n0orig = n0orig; c.rk_combine = combine;
+    c.dt = dt; c.p_top = s.hyai[0] * s.ps0;
+    launch_caar_jvp<R>(c, E, g_stream);
+    post("caar_jvp");
+    launch_dss_state(E, tn.out, tn.v3, tn.T3, tn.dp3, np1, rsp_d, table(), g_stream);
+    post("dss_caar_jvp");
+    caar_stage(nm1, n0, np1, dt, 0.0, -1, combine, n0orig);
+  }
+  // One hyperviscosity subcycle: the primal Laplacians, the tangent's (the same linear
+  // kernels on the tangent levels), the tangent update, then the primal update.
+  void hv_cycle_tlm(int np1, double dt) {
+    HvArgs<R> x;
+    x.m = metric();
+    x.dss = table();
+    x.v = wk.v; x.T = wk.T; x.dp = wk.dp; x.dpdiss_ave = wk.dpdiss_ave; x.dpdiss_bih = wk.dpdiss_bih;
+    x.bufA = bufA; x.bufB = bufB;
+    x.np1 = np1; x.hsub = s.prm.hypervis_subcycle; x.ncyc = 1; x.consthv = s.consthv ? 1 : 0;
+    x.dt = dt / s.prm.hypervis_subcycle; x.eta_ave_w = 0.0;
+    x.nu = s.prm.nu; x.nu_s = s.prm.nu_s; x.nu_p = s.prm.nu_p; x.nu_top = s.prm.nu_top;
+    x.nu_ratio1 = s.prm.nu_ratio1; x.nu_ratio2 = s.prm.nu_ratio2;
+    launch_hv_laplacians<R>(x, E, g_stream);
+    HvArgs<R> d = x;
+    d.v = tn.v3; d.T = tn.T3; d.dp = tn.dp3; d.dpdiss_ave = tn.dpa; d.dpdiss_bih = tn.dpb; d.bufB = tn.bufB;
+    launch_hv_laplacians<R>(d, E, g_stream);
+    HvJvpArgs<R> u;
+    u.m = x.m; u.dss = x.dss; u.v = wk.v; u.bufB = bufB;
+    u.tv = tn.v3; u.tT = tn.T3; u.tdp = tn.dp3; u.tbufB = tn.bufB;
+    u.np1 = np1; u.dt = x.dt;
+    launch_hv_update_jvp<R>(u, E, g_stream);
+    launch_hv_update<R>(x, E, g_stream);
+    post("hypervis_jvp");
+  }
+  // One dry step of the trajectory with its tangent, both entering and leaving at
+  // level tj.cur (the order of traj_step).
+  void traj_step_tlm(double dt, bool remap) {
+    const int n0 = tj.cur, nm1 = (n0 + 2) % 3, np1 = (n0 + 1) % 3;
+    caar_stage_tlm(n0, n0, nm1, dt / 5.0, 0, n0);
+    caar_stage_tlm(n0, nm1, np1, dt / 5.0, 0, n0);
+    caar_stage_tlm(n0, np1, np1, dt / 3.0, 0, n0);
+    caar_stage_tlm(n0, np1, np1, 2.0 * dt / 3.0, 0, n0);
+    caar_stage_tlm(nm1, np1, np1, 3.0 * dt / 4.0, 1, n0);
+    for (int i = 0; i < s.prm.hypervis_subcycle; ++i) hv_cycle_tlm(np1, dt);
+    if (remap) {
+      RemapJvpArgs r;
+      r.v = wk.v; r.T = wk.T; r.dp = wk.dp;
+      r.tv = tn.v3; r.tT = tn.T3; r.tdp = tn.dp3; r.tps = tn.ps;
+      r.np1 = np1; r.remap_alg = s.prm.remap_alg; r.nelem = E; r.ps0 = s.ps0; r.hyai0 = s.hyai[0];
+      launch_remap_jvp(r, g_stream);
+      post("remap_jvp");
+      launch_remap(np1, 0, false);
+      launch_dp_from_ps(E, wk.dp, wk.ps_v, np1, s.ps0, g_stream);
+      launch_dp_from_ps(E, tn.dp3, tn.ps, np1, 0.0, g_stream);  // d(dp3d) = d(hybi) d(ps_v)
+      post("dp3d_from_ps");
+    }
+    tj.cur = np1;
+  }
+
+  // Runs the last trajectory again from its checkpointed initial state with the tangent
+  // beside it (forward mode: no checkpoints needed) and returns the final tangent.
+  void traj_jvp(const double* hdv, const double* hdT, const double* hddp, double* ov, double* oT,
+                double* odp) override {
+    if (!tj.have) fail(HX_ERR_STATE, "trajectory: run hx_traj_forward first");
+    tan_alloc();
+    const size_t n3 = N3();
+    DynV io = cot(4);
+    ck(cudaMemcpyAsync(io.v, hdv, 2 * n3 * sizeof(double), cudaMemcpyDefault, g_stream), "jvp in");
+    ck(cudaMemcpyAsync(io.T, hdT, n3 * sizeof(double), cudaMemcpyDefault, g_stream), "jvp in");
+    ck(cudaMemcpyAsync(io.dp, hddp, n3 * sizeof(double), cudaMemcpyDefault, g_stream), "jvp in");
+    if (tj.nsteps > 0) {  // (no steps: the tangent passes through unchanged)
+      const int keep_cur = tj.cur;
+      tj.cur = 1;
+      launch_copy_dyn(E, tan_level(tj.cur), io, g_stream);
+      launch_copy_dyn(E, level3(tj.cur), ckpt(0), g_stream);  // the initial state in both modes
+      ck(cudaMemsetAsync(invalid, 0, sizeof(int), g_stream), "memset");
+      {
+        WorkScope ws(*this);
+        for (int st = 0; st < tj.nsteps; ++st) traj_step_tlm(tj.dt, remaps_after(st));
+      }
+      launch_copy_dyn(E, io, tan_level(tj.cur), g_stream);
+      tj.cur = keep_cur;
+    }
+    ck(cudaMemcpyAsync(ov, io.v, 2 * n3 * sizeof(double), cudaMemcpyDefault, g_stream), "jvp out");
+    ck(cudaMemcpyAsync(oT, io.T, n3 * sizeof(double), cudaMemcpyDefault, g_stream), "jvp out");
+    ck(cudaMemcpyAsync(odp, io.dp, n3 * sizeof(double), cudaMemcpyDefault, g_stream), "jvp out");
+    if (remap_status()) fail(101, "Negative (or nan) layer thickness detected, aborting!");
   }
 
   // caar stage reversed: aout -> xm_bar (+=), x0_bar (+=)
@@ -1683,10 +1806,9 @@ int hx_traj_vjp(const double* v_bar, const double* T_bar, const double* dp3d_bar
   return run([&] { B().traj_vjp(v_bar, T_bar, dp3d_bar, v_grad, T_grad, dp3d_grad); });
 }
 
-int hx_traj_jvp(const double*, const double*, const double*, double*, double*, double*) {
-  return run([&] {
-    fail(HX_ERR_STATE, "hx_traj_jvp: the tangent-linear model is provided by the CPU oracle only");
-  });
+int hx_traj_jvp(const double* dv, const double* dT, const double* ddp3d, double* v_tan, double* T_tan,
+                double* dp3d_tan) {
+  return run([&] { B().traj_jvp(dv, dT, ddp3d, v_tan, T_tan, dp3d_tan); });
 }
 
 int hx_traj_set_checkpointing(int mode) {

@@ -1539,6 +1539,7 @@ void upload_constants(const double* dvv16, const double* hyai, const double* hyb
   cudaMemcpyToSymbolAsync(c_ai_delta, ad, sizeof(double) * NLEV, 0, cudaMemcpyHostToDevice, s);
   cudaMemcpyToSymbolAsync(c_bi_delta, bd, sizeof(double) * NLEV, 0, cudaMemcpyHostToDevice, s);
   upload_adjoint_constants(dvv16, hyai, hybi, s);
+  upload_tangent_constants(dvv16, hyai, hybi, s);
   cudaStreamSynchronize(s);
 }
 
@@ -1591,6 +1592,23 @@ void launch_hv(const HvArgs<R>& a, int E, cudaStream_t s) {
       k_hv_update<R><<<dim3(E, NLEV / 8), 128, 0, s>>>(a);
     }
   }
+}
+
+template <typename R>
+void launch_hv_laplacians(const HvArgs<R>& a, int E, cudaStream_t s) {
+  constexpr int LG = LG_HV<R>();
+  {
+    KScope k("hv_laplace1", s);
+    k_hv_lap1<R, LG><<<E, LG * 16, 0, s>>>(a);
+  }
+  KScope k("hv_laplace2", s);
+  k_hv_lap2<R, LG><<<E, LG * 16, kF32<R> ? 4 * NLEV * 16 * sizeof(R) : 0, s>>>(a);
+}
+
+template <typename R>
+void launch_hv_update(const HvArgs<R>& a, int E, cudaStream_t s) {
+  KScope k("hv_dss_update", s);
+  k_hv_update<R><<<dim3(E, NLEV / 8), 128, 0, s>>>(a);
 }
 
 template <typename R>
@@ -1754,7 +1772,9 @@ void launch_lap_matrix(const MetricP<double>& m, int E, double* out, cudaStream_
   template void launch_precompute_divdp<R>(const EulerArgs<R>&, int, cudaStream_t); \
   template void launch_euler_step<R>(EulerArgs<R>&, int, int, cudaStream_t);  \
   template void launch_remap<R>(const RemapArgs&, cudaStream_t);                  \
-  template int remap_chunk_elements<R>(int, int);
+  template int remap_chunk_elements<R>(int, int);                                  \
+  template void launch_hv_laplacians<R>(const HvArgs<R>&, int, cudaStream_t);        \
+  template void launch_hv_update<R>(const HvArgs<R>&, int, cudaStream_t);
 HX_INST(double)
 HX_INST(float)
 

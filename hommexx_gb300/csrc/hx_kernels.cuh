@@ -200,6 +200,50 @@ void launch_rk5_comb_vjp(int E, DynV by, DynV b1, DynV b0, cudaStream_t s);
 // Copy one time level (dst and src may have different element strides).
 void launch_copy_dyn(int E, DynV dst, DynV src, cudaStream_t s);
 
+// ---- tangent-linear model of the dry step (hx_tangent.cu) ----------------------------
+// Each tangent kernel reads the primal stage input, which the forward kernel launched
+// after it then advances.
+void upload_tangent_constants(const double* dvv16, const double* hyai73, const double* hybi73,
+                              cudaStream_t s);
+
+template <typename R>
+struct CaarJvpArgs {
+  MetricP<R> m;
+  const double *v, *T, *dp;  // primal state [E][3][...] (levels nm1, n0, n0orig read)
+  double *tv, *tT, *tdp;     // tangent state [E][3][...]; level nm1 rewritten when rk_combine
+  double* out;               // tangent of the pre-DSS result [E][72][4][16]
+  int nm1, n0, n0orig, rk_combine;
+  double dt, p_top;
+};
+
+template <typename R>
+struct HvJvpArgs {
+  MetricP<R> m;
+  DssTable dss;
+  const double* v;      // primal v [E][3][72][2][16] before the update
+  const double* bufB;   // primal pre-DSS tendencies of the subcycle
+  double *tv, *tT, *tdp;  // tangent state, level np1 updated
+  const double* tbufB;  // tangent pre-DSS tendencies
+  int np1;
+  double dt;            // subcycle step
+};
+
+struct RemapJvpArgs {
+  const double *v, *T, *dp;  // primal state [E][3][...], source at level np1
+  double *tv, *tT, *tdp;     // tangent state; v and T of level np1 remapped in place
+  double* tps;               // tangent ps_v [E][3][16], level np1 written
+  int np1, remap_alg, nelem;
+  double ps0, hyai0;
+};
+
+template <typename R> void launch_caar_jvp(const CaarJvpArgs<R>& a, int E, cudaStream_t s);
+template <typename R> void launch_hv_update_jvp(const HvJvpArgs<R>& a, int E, cudaStream_t s);
+void launch_remap_jvp(const RemapJvpArgs& a, cudaStream_t s);
+// The two halves of one hyperviscosity subcycle (launch_hv with ncyc = 1): the
+// Laplacians into bufB, then the DSS and state update.
+template <typename R> void launch_hv_laplacians(const HvArgs<R>& a, int E, cudaStream_t s);
+template <typename R> void launch_hv_update(const HvArgs<R>& a, int E, cudaStream_t s);
+
 // Name of the last kernel launched by the wrappers above (for per-kernel timing).
 const char* last_kernel_name();
 void set_kernel_hook(void (*before)(const char*, cudaStream_t), void (*after)(const char*, cudaStream_t));

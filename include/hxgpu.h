@@ -223,8 +223,10 @@ int hx_dss_noalloc(const double* in, double* out, int nelem, int apply_rspheremp
  * gradient with respect to the initial state (a vector-Jacobian product), reversing
  * the last forward trajectory: each caar stage, hyperviscosity subcycle and remap is
  * differentiated by hand, with its inputs checkpointed and its intermediates
- * recomputed.  hx_traj_jvp is the tangent-linear model along the same trajectory
- * (CPU oracle only; the GPU library returns HX_ERR_STATE).
+ * recomputed.  hx_traj_jvp is the tangent-linear model along the same trajectory (a
+ * Jacobian-vector product: the tangent of the final state from a tangent of the
+ * initial one), run forward from the trajectory's checkpointed initial state with
+ * hand-written tangent kernels beside the forward ones.
  * hx_traj_set_checkpointing: 0 = automatic (every RK stage and hyperviscosity
  * subcycle input of every step when that fits in device memory, else mode 2), 1 =
  * keep every stage input, 2 = keep the step inputs only and recompute each step's

@@ -10,7 +10,12 @@ central finite differences of the CUDA forward.
   bit-identical gradients;
 * the gradient of J = sum spheremp T_final^2 matches central finite differences of
   the CUDA forward (eps = 1e-6) along 10 seeded smooth directions;
-* the mixed form's gradient is close to the FP64 one.
+* the mixed form's gradient is close to the FP64 one;
+* the CUDA tangent-linear model (hx_traj_jvp) = the oracle's dual-number tangent to
+  1e-10 (remap every step and every third step, remap_alg 1 and 2, with and without
+  the nu_top sponge), passes the dot-product test against the CUDA adjoint to 1e-12,
+  matches central finite differences of the CUDA forward, leaves the adjoint of the
+  trajectory unchanged, and in the mixed form stays close to the FP64 tangent.
 """
 import numpy as np
 import pytest
@@ -118,3 +123,99 @@ def test_mixed_gradient_close_to_fp64(gpu_path):
         grads.append(g.traj_vjp(bar))
     for k in grads[0]:
         assert H.rel_err(grads[1][k], grads[0][k]) < 1e-3, (k, H.rel_err(grads[1][k], grads[0][k]))
+
+
+@pytest.mark.parametrize("nsteps,kw", [(3, dict(rsplit=1)), (3, dict(rsplit=3)),
+                                       (2, dict(rsplit=1, remap_alg=2, nu_top=0.0)),
+                                       (2, dict(rsplit=2, nu_div=3e16))])
+def test_jvp_matches_oracle(oracle_path, gpu_path, nsteps, kw):
+    o, g = _both(oracle_path, gpu_path, **kw)
+    x0 = _x0(NE)
+    o.traj_forward(x0, nsteps, DT)
+    g.traj_forward(x0, nsteps, DT)
+    dx = _rand(x0, 61)
+    to = o.traj_jvp(dx)
+    tg = g.traj_jvp(dx)
+    for k in to:
+        assert H.rel_err(tg[k], to[k]) < 1e-10, (k, H.rel_err(tg[k], to[k]))
+
+
+@pytest.mark.parametrize("rsplit", [1, 3])
+def test_gpu_dot_product(gpu_path, rsplit):
+    """<L dx, dy> = <dx, L^T dy> with both sides on the GPU."""
+    g = H.setup(gpu_path, NE, 1, rsplit=rsplit)
+    x0 = _x0(NE)
+    g.traj_forward(x0, 3, DT)
+    dx, dy = _rand(x0, 71), _rand(x0, 72)
+    lhs = _dot(g.traj_jvp(dx), dy)
+    rhs = _dot(dx, g.traj_vjp(dy))
+    assert abs(lhs - rhs) <= 1e-12 * abs(lhs), (lhs, rhs)
+
+
+def test_jvp_matches_finite_differences(gpu_path):
+    """Without a remap the step is smooth: the tangent = central FD of the CUDA forward
+    per field; with remaps (PPM limiters are only piecewise smooth, so single points
+    near a limiter switch differ) the projections on seeded random fields agree."""
+    m = H.mesh(NE)
+    x0 = _x0(NE)
+    eps = 1e-6
+    g = H.setup(gpu_path, NE, 1, rsplit=3)
+    g.traj_forward(x0, 2, DT)  # 2 steps, no remap
+    for i in range(2):
+        d = S.dynamics_direction(m, 7100 + i)
+        tl = g.traj_jvp(d)
+        fp = g.traj_forward({k: x0[k] + eps * d[k] for k in x0}, 2, DT)
+        fm = g.traj_forward({k: x0[k] - eps * d[k] for k in x0}, 2, DT)
+        for k in tl:
+            fd = (fp[k] - fm[k]) / (2 * eps)
+            assert H.rel_err(tl[k], fd) < 1e-6, (i, k, H.rel_err(tl[k], fd))
+        g.traj_forward(x0, 2, DT)
+    g = H.setup(gpu_path, NE, 1, rsplit=1)
+    g.traj_forward(x0, 3, DT)
+    w = _rand(x0, 97)
+    for i in range(3):
+        d = S.dynamics_direction(m, 7200 + i)
+        tl = g.traj_jvp(d)
+        fp = g.traj_forward({k: x0[k] + eps * d[k] for k in x0}, 3, DT)
+        fm = g.traj_forward({k: x0[k] - eps * d[k] for k in x0}, 3, DT)
+        fd = {k: (fp[k] - fm[k]) / (2 * eps) for k in tl}
+        a, b = _dot(tl, w), _dot(fd, w)
+        assert abs(a - b) <= 1e-4 * abs(b), (i, a, b)
+        g.traj_forward(x0, 3, DT)
+
+
+def test_jvp_leaves_vjp_unchanged(gpu_path):
+    g = H.setup(gpu_path, NE, 1, rsplit=1)
+    x0 = _x0(NE)
+    bar = _rand(x0, 81)
+    for mode in (1, 2):
+        g.traj_checkpointing(mode)
+        g.traj_forward(x0, 2, DT)
+        want = g.traj_vjp(bar)
+        g.traj_jvp(_rand(x0, 82))
+        got = g.traj_vjp(bar)
+        for k in want:
+            assert np.array_equal(got[k], want[k]), (mode, k)
+    g.traj_checkpointing(0)
+
+
+def test_mixed_jvp_close_to_fp64(gpu_path):
+    x0 = _x0(NE)
+    dx = _rand(x0, 91)
+    tans = []
+    for prec in (0, 1):
+        g = H.setup(gpu_path, NE, 1, precision=prec, rsplit=1)
+        g.traj_forward(x0, 3, DT)
+        tans.append(g.traj_jvp(dx))
+    for k in tans[0]:
+        assert H.rel_err(tans[1][k], tans[0][k]) < 1e-3, (k, H.rel_err(tans[1][k], tans[0][k]))
+
+
+def test_jvp_of_no_steps_is_identity(gpu_path):
+    g = H.setup(gpu_path, NE, 1, rsplit=1)
+    x0 = _x0(NE)
+    g.traj_forward(x0, 0, DT)
+    dx = _rand(x0, 95)
+    got = g.traj_jvp(dx)
+    for k in dx:
+        assert np.array_equal(got[k], dx[k]), k
