@@ -316,7 +316,7 @@ __global__ void k_hvb_update(int E, DynV x, DynV xo, DynV a, DynV xb, double* pr
   const size_t bv = (size_t)e * xb.ev + l * 32 + p, bs = (size_t)e * xb.es + l * 16 + p;
   double* pr = pre + ((size_t)e * NLEV + l) * 64 + p;
   const double tb = a.T[is];
-  const double hb = -tb / kCp;
+  const double hb = -tb * (1.0 / kCp);
 #pragma unroll
   for (int c = 0; c < 2; ++c) {
     const double vnew = xo.v[xov + c * 16];
@@ -464,8 +464,8 @@ constexpr int V_PIN = V_PIO + 74;   // pin[0 .. 72]
 constexpr int V_Z2 = V_PIN + 74;    // z2[0 .. 71]
 constexpr int V_KID = V_Z2 + 72;    // kid[0 .. 71] (int)
 constexpr int V_FIRST = V_KID + 36; // first interface of each source cell (int, -1: none)
-constexpr int V_G = V_FIRST + 36;   // g[10][74]
-constexpr int V_PINB = V_G + 740;   // cotangent of pin[0 .. 73]
+constexpr int V_G = V_FIRST + 36;   // g[11][74]; row 10 = g5 (g6 - g7) as the forward forms it
+constexpr int V_PINB = V_G + 814;   // cotangent of pin[0 .. 73]
 constexpr int V_PIOL = V_PINB + 74; // cotangent of pio[kk] from the z2 of cell kk (by kk)
 constexpr int V_A = V_PIOL + 74;    // A[-2 .. 73]
 constexpr int V_MASS = V_A + 76;    // mass[0 .. 73]
@@ -540,13 +540,14 @@ __global__ void __launch_bounds__(VC * 32) k_remap_vjp(RemapVjpArgs a) {
   double* bT = a.a.T + (size_t)e * a.a.es + p;
   double* bd = a.a.dp + (size_t)e * a.a.es + p;
   // ---- grid (as the forward kernel) ----
-  double s3[3] = {0.0, 0.0, 0.0}, t3[3] = {0.0, 0.0, 0.0};
+  double s3[3] = {0.0, 0.0, 0.0}, t3[3] = {0.0, 0.0, 0.0}, rt3[3] = {0.0, 0.0, 0.0};
   if (own) {
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
+      float rf;
       s3[k] = xd[(size_t)(l0 + k) * 16];
       D[l0 + k] = s3[k];
-      rD[l0 + k] = 1.0 / s3[k];
+      rD[l0 + k] = rcp_newton(s3[k], rf);
     }
   }
   const double ps = warp_sum(s3[0] + s3[1] + s3[2]) + a.hyai0 * a.ps0;
@@ -554,7 +555,9 @@ __global__ void __launch_bounds__(VC * 32) k_remap_vjp(RemapVjpArgs a) {
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
       const int l = l0 + k;
+      float rf;
       t3[k] = (c_hyai[l + 1] - c_hyai[l]) * a.ps0 + (c_hybi[l + 1] - c_hybi[l]) * ps;
+      rt3[k] = rcp_newton(t3[k], rf);
     }
   }
   {
@@ -599,7 +602,7 @@ __global__ void __launch_bounds__(VC * 32) k_remap_vjp(RemapVjpArgs a) {
       if (kk == NLEV + 1) kk = NLEV;
       if (kk < 1) kk = 1;
       kid[k] = kk - 1;
-      z2[k] = (pin[k + 1] - (pio[kk - 1] + pio[kk]) * 0.5) / D[kk - 1];
+      z2[k] = (pin[k + 1] - (pio[kk - 1] + pio[kk]) * 0.5) * rD[kk - 1];
     }
   }
   if (lane < 25) {
@@ -607,22 +610,25 @@ __global__ void __launch_bounds__(VC * 32) k_remap_vjp(RemapVjpArgs a) {
     for (int k3 = 0; k3 < 3; ++k3) {
       const int j = 3 * lane + k3;
       if (j < NLEV + 2) {
+        // the forward's reciprocals (rcp_newton), so the weights are the forward's
         const double dm2 = D[j - 2], dm1 = D[j - 1], d0 = D[j];
-        const double r10 = 1.0 / (dm1 + d0);
-        g[0 * 74 + j] = dm1 / (dm2 + dm1 + d0);
+        float rf;
+        const double r10 = rcp_newton(dm1 + d0, rf);
+        g[0 * 74 + j] = dm1 * rcp_newton(dm2 + dm1 + d0, rf);
         g[1 * 74 + j] = (2.0 * dm2 + dm1) * r10;
-        g[2 * 74 + j] = (dm1 + 2.0 * d0) / (dm2 + dm1);
+        g[2 * 74 + j] = (dm1 + 2.0 * d0) * rcp_newton(dm2 + dm1, rf);
         if (j < NLEV + 1) {
           const double dp1 = D[j + 1];
-          const double r6 = 1.0 / (2.0 * dm1 + d0);
-          const double r7 = 1.0 / (2.0 * d0 + dm1);
+          const double r6 = rcp_newton(2.0 * dm1 + d0, rf);
+          const double r7 = rcp_newton(2.0 * d0 + dm1, rf);
           g[3 * 74 + j] = dm1 * r10;
-          g[4 * 74 + j] = 1.0 / (dm2 + dm1 + d0 + dp1);
+          g[4 * 74 + j] = rcp_newton(dm2 + dm1 + d0 + dp1, rf);
           g[5 * 74 + j] = (2.0 * dm1 * d0) * r10;
           g[6 * 74 + j] = (dm2 + dm1) * r6;
           g[7 * 74 + j] = (dp1 + d0) * r7;
           g[8 * 74 + j] = dm1 * (dm2 + dm1) * r6;
           g[9 * 74 + j] = d0 * (d0 + dp1) * r7;
+          g[10 * 74 + j] = ((2.0 * dm1 * d0) * r10) * ((dm2 + dm1) * r6 - (dp1 + d0) * r7);
         }
       }
     }
@@ -689,15 +695,19 @@ __global__ void __launch_bounds__(VC * 32) k_remap_vjp(RemapVjpArgs a) {
         if (j < NLEV + 2) {
           const double a0 = A[j], am1 = A[j - 1], am2 = A[j - 2];
           double r = 0.0;
-          if ((a0 - am1) * (am1 - am2) > 0.0) {
+          if (pos_prod(a0 - am1, am1 - am2)) {
             const double da = g[0 * 74 + j] * (g[1 * 74 + j] * (a0 - am1) + g[2 * 74 + j] * (am1 - am2));
-            const double xa = fabs(da), ya = 2.0 * fabs(am1 - am2), za = 2.0 * fabs(a0 - am1);
-            double mv = xa;
+            // the forward's min3abs_signed; magnitudes compared as bit patterns
+            const double ya = 2.0 * (am1 - am2), za = 2.0 * (a0 - am1);
+            const long long m = 0x7fffffffffffffffLL;
+            const long long kx = __double_as_longlong(da) & m, ky = __double_as_longlong(ya) & m,
+                            kz = __double_as_longlong(za) & m;
+            long long mv = kx;
             dsel[k3] = 1;
-            if (ya < xa) { mv = ya; dsel[k3] = 2; }
-            if (za < mv) { mv = za; dsel[k3] = 3; }
+            if (ky < mv) { mv = ky; dsel[k3] = 2; }
+            if (kz < mv) dsel[k3] = 3;
             dsg[k3] = copysign(1.0, da);
-            r = mv * dsg[k3];
+            r = min3abs_signed(da, ya, za, da);
           }
           dma[j] = r;
         }
@@ -711,7 +721,7 @@ __global__ void __launch_bounds__(VC * 32) k_remap_vjp(RemapVjpArgs a) {
         if (j < NLEV + 1) {
           const double a0 = A[j], am1 = A[j - 1];
           ai[j] = am1 + g[3 * 74 + j] * (a0 - am1) +
-                  g[4 * 74 + j] * (g[5 * 74 + j] * (g[6 * 74 + j] - g[7 * 74 + j]) * (a0 - am1) -
+                  g[4 * 74 + j] * (g[10 * 74 + j] * (a0 - am1) -
                                    g[8 * 74 + j] * dma[j + 1] + g[9 * 74 + j] * dma[j]);
         }
       }
@@ -724,12 +734,12 @@ __global__ void __launch_bounds__(VC * 32) k_remap_vjp(RemapVjpArgs a) {
         const int jp = l0 + k3;
         double al = ai[jp], ar = ai[jp + 1];
         const double cm = A[jp];
-        if ((ar - cm) * (cm - al) <= 0.0) { al = cm; ar = cm; br[k3] |= 1; }
-        if ((ar - al) * (cm - (al + ar) * 0.5) > (ar - al) * (ar - al) * sixth) {
+        if (!pos_prod(ar - cm, cm - al)) { al = cm; ar = cm; br[k3] |= 1; }
+        if (less((ar - al) * (ar - al) * sixth, (ar - al) * (cm - (al + ar) * 0.5))) {
           al = 3.0 * cm - 2.0 * ar;
           br[k3] |= 2;
         }
-        if ((ar - al) * (cm - (al + ar) * 0.5) < -(ar - al) * (ar - al) * sixth) {
+        if (less((ar - al) * (cm - (al + ar) * 0.5), -(ar - al) * (ar - al) * sixth)) {
           ar = 3.0 * cm - 2.0 * al;
           br[k3] |= 4;
         }
@@ -766,10 +776,10 @@ __global__ void __launch_bounds__(VC * 32) k_remap_vjp(RemapVjpArgs a) {
       for (int k3 = 0; k3 < 3; ++k3) {
         const int k = l0 + k3;
         const double m1 = k3 == 0 ? below : m2[k3 - 1];
-        const double xn = (m2[k3] - m1) / t3[k3];
+        const double xn = (m2[k3] - m1) * rt3[k3];
         const double xb = var < 2 ? bv[(size_t)k * 32 + var * 16] : bT[(size_t)k * 16];
-        ob[k3] = xb / t3[k3];
-        tgtb[k3] -= xb * xn / t3[k3];
+        ob[k3] = xb * rt3[k3];
+        tgtb[k3] -= ob[k3] * xn;
       }
     }
     {
@@ -805,7 +815,7 @@ __global__ void __launch_bounds__(VC * 32) k_remap_vjp(RemapVjpArgs a) {
           c2b += ib * (x2 * x2 * x2 + 0.125) * (1.0 / 3.0);
           // z2 = (pin[k+1] - (pio[kk] + pio[kk+1]) / 2) / D[kk]
           const double zb = ib * (c0 + c1 * x2 + c2 * x2 * x2);
-          const double zr = zb / D[kk];
+          const double zr = zb * rD[kk];
           pinb[k + 1] += zr;
           piol[kk] -= 0.5 * zr;
           pioh[k3] -= 0.5 * zr;
@@ -946,33 +956,38 @@ __global__ void __launch_bounds__(VC * 32) k_remap_vjp(RemapVjpArgs a) {
       if (j < NLEV + 2) {
         const double a_ = D[j - 2], b_ = D[j - 1], c_ = D[j];
         double cm2 = 0.0, cm1 = 0.0, c0 = 0.0, cp1 = 0.0;
+        // the reciprocals of the forward's weight denominators
+        float rf;
+        const double r3 = rcp_newton(a_ + b_ + c_, rf), r10 = rcp_newton(b_ + c_, rf),
+                     r2 = rcp_newton(a_ + b_, rf);
         double v = gb[k3][0];  // b / (a + b + c)
         {
-          const double s = a_ + b_ + c_, sb = -v * g[0 * 74 + j] / s;
-          cm1 += v / s + sb;
+          const double sb = -v * g[0 * 74 + j] * r3;
+          cm1 += v * r3 + sb;
           cm2 += sb;
           c0 += sb;
         }
         v = gb[k3][1];  // (2a + b) / (b + c)
         {
-          const double s = b_ + c_, nb = v / s, sb = -v * g[1 * 74 + j] / s;
+          const double nb = v * r10, sb = -nb * g[1 * 74 + j];
           cm2 += 2.0 * nb;
           cm1 += nb + sb;
           c0 += sb;
         }
         v = gb[k3][2];  // (b + 2c) / (a + b)
         {
-          const double s = a_ + b_, nb = v / s, sb = -v * g[2 * 74 + j] / s;
+          const double nb = v * r2, sb = -nb * g[2 * 74 + j];
           cm1 += nb + sb;
           c0 += 2.0 * nb;
           cm2 += sb;
         }
         if (j < NLEV + 1) {
           const double d_ = D[j + 1];
+          const double r6 = rcp_newton(2.0 * b_ + c_, rf), r7 = rcp_newton(2.0 * c_ + b_, rf);
           v = gb[k3][3];  // b / (b + c)
           {
-            const double s = b_ + c_, sb = -v * g[3 * 74 + j] / s;
-            cm1 += v / s + sb;
+            const double nb = v * r10, sb = -nb * g[3 * 74 + j];
+            cm1 += nb + sb;
             c0 += sb;
           }
           v = gb[k3][4];  // 1 / (a + b + c + d)
@@ -985,34 +1000,34 @@ __global__ void __launch_bounds__(VC * 32) k_remap_vjp(RemapVjpArgs a) {
           }
           v = gb[k3][5];  // 2 b c / (b + c)
           {
-            const double s = b_ + c_, nb = v / s, sb = -v * g[5 * 74 + j] / s;
+            const double nb = v * r10, sb = -nb * g[5 * 74 + j];
             cm1 += 2.0 * c_ * nb + sb;
             c0 += 2.0 * b_ * nb + sb;
           }
           v = gb[k3][6];  // (a + b) / (2b + c)
           {
-            const double s = 2.0 * b_ + c_, nb = v / s, sb = -v * g[6 * 74 + j] / s;
+            const double nb = v * r6, sb = -nb * g[6 * 74 + j];
             cm2 += nb;
             cm1 += nb + 2.0 * sb;
             c0 += sb;
           }
           v = gb[k3][7];  // (d + c) / (2c + b)
           {
-            const double s = 2.0 * c_ + b_, nb = v / s, sb = -v * g[7 * 74 + j] / s;
+            const double nb = v * r7, sb = -nb * g[7 * 74 + j];
             cp1 += nb;
             c0 += nb + 2.0 * sb;
             cm1 += sb;
           }
           v = gb[k3][8];  // b (a + b) / (2b + c)
           {
-            const double s = 2.0 * b_ + c_, nb = v / s, sb = -v * g[8 * 74 + j] / s;
+            const double nb = v * r6, sb = -nb * g[8 * 74 + j];
             cm2 += b_ * nb;
             cm1 += (a_ + 2.0 * b_) * nb + 2.0 * sb;
             c0 += sb;
           }
           v = gb[k3][9];  // c (c + d) / (b + 2c)
           {
-            const double s = b_ + 2.0 * c_, nb = v / s, sb = -v * g[9 * 74 + j] / s;
+            const double nb = v * r7, sb = -nb * g[9 * 74 + j];
             c0 += (2.0 * c_ + d_) * nb + 2.0 * sb;
             cp1 += c_ * nb;
             cm1 += sb;
