@@ -31,19 +31,40 @@ template <typename R, int LG>
 __global__ void __launch_bounds__(LG * 16) k_caar(CaarArgs<R> a) {
   constexpr int NL = NLEV / LG;
   extern __shared__ double sm[];
-  double* s_dp = sm;                    // dp3d(n0), later phi
-  double* s_tv = sm + NLEV * SROW;      // T_v
-  double* s_div = sm + 2 * NLEV * SROW; // div(v dp)
-  double* s_p = sm + 3 * NLEV * SROW;   // pressure
-  double* s_om = sm + 4 * NLEV * SROW;  // sum_{j<k} div_vdp_j
-  double* s_rp = sm + 5 * NLEV * SROW;  // 1 / pressure (FP64 form)
-  double* s_tot = sm + 6 * NLEV * SROW; // column sum of div(v dp) (rsplit == 0)
-  // Mixed form: 1/p in FP32 in place of s_rp, and the FP32 u, v, div(v dp) of phase A
-  // kept for phase C ([72][16] floats each) so that it neither reloads nor re-converts.
-  float* f_rp = reinterpret_cast<float*>(s_rp);
-  float* f_u = reinterpret_cast<float*>(s_tot + 16);
-  float* f_w = f_u + NLEV * 16;
-  float* f_div = f_w + NLEV * 16;
+  // FP64 form: dp3d(n0) (later phi), T_v, div(v dp), pressure, omega integral
+  // sum_{j<k} div_vdp_j, 1/p and the column sum of div(v dp) (rsplit == 0), all double.
+  // Mixed form: dp3d/phi, pressure, omega integral and column sum in double; 1/p and the
+  // u, v, div(v dp) of phase A in FP32 ([72][17] and [72][16] floats), so that phase C
+  // neither reloads nor re-converts them and phase B sums div(v dp) from its exact FP64
+  // image; T_v in double only for moist runs (dry T_v is T, read from the state).  That
+  // is 48 KB instead of 73 KB: four CTAs per SM instead of three.  (The FP64 form keeps
+  // its T_v array: at four CTAs per SM, with the state reread, it measured 1 % slower.)
+  double *s_dp, *s_tv, *s_div, *s_p, *s_om, *s_rp, *s_tot;
+  float *f_rp, *f_u, *f_w, *f_div;
+  if constexpr (kF32<R>) {
+    s_dp = sm;
+    s_p = sm + NLEV * SROW;
+    s_om = sm + 2 * NLEV * SROW;
+    s_tot = sm + 3 * NLEV * SROW;
+    f_rp = reinterpret_cast<float*>(s_tot + 16);
+    f_u = f_rp + NLEV * SROW;
+    f_w = f_u + NLEV * 16;
+    f_div = f_w + NLEV * 16;
+    s_tv = reinterpret_cast<double*>(f_div + NLEV * 16);  // moist only
+    s_div = nullptr;
+    s_rp = nullptr;
+  } else {
+    s_dp = sm;
+    s_tv = sm + NLEV * SROW;
+    s_div = sm + 2 * NLEV * SROW;
+    s_p = sm + 3 * NLEV * SROW;
+    s_om = sm + 4 * NLEV * SROW;
+    s_rp = sm + 5 * NLEV * SROW;
+    s_tot = sm + 6 * NLEV * SROW;
+    f_rp = f_u = f_w = f_div = nullptr;
+  }
+  const bool moist = a.n0_qdp >= 0;
+  const bool own_tv = !kF32<R> || moist;  // T_v kept in shared memory
   const int e = blockIdx.x, tid = threadIdx.x, p = tid & 15, lg = tid >> 4;
   Pt<R> t;
   t.init(p);
@@ -74,12 +95,13 @@ __global__ void __launch_bounds__(LG * 16) k_caar(CaarArgs<R> a) {
       tv = td * Qt;
     }
     s_dp[l * SROW + p] = dd;
-    s_tv[l * SROW + p] = tv;
-    s_div[l * SROW + p] = dbl(div);
+    if (own_tv) s_tv[l * SROW + p] = tv;
     if constexpr (kF32<R>) {
       f_u[l * 16 + p] = u;
       f_w[l * 16 + p] = w;
       f_div[l * 16 + p] = div;
+    } else {
+      s_div[l * SROW + p] = div;
     }
   }
   __syncthreads();
@@ -112,7 +134,10 @@ __global__ void __launch_bounds__(LG * 16) k_caar(CaarArgs<R> a) {
         s_rp[(l0 + k) * SROW + col] = rp;
       }
       s_p[(l0 + k) * SROW + col] = pr;
-      r[k] = kRgas * s_tv[(l0 + k) * SROW + col] * (d * 0.5 * rp);
+      double tvk;
+      if (own_tv) tvk = s_tv[(l0 + k) * SROW + col];
+      else tvk = a.T[sN0 + (l0 + k) * 16 + col];
+      r[k] = kRgas * tvk * (d * 0.5 * rp);
     }
     // geopotential: phi_k = phis + 2 sum_{j>k} r_j + r_k
     double rt = 0.0;
@@ -128,15 +153,22 @@ __global__ void __launch_bounds__(LG * 16) k_caar(CaarArgs<R> a) {
       s_dp[(l0 + k) * SROW + col] = ph;  // dp no longer needed: holds phi now
       phig[(l0 + k) * 16 + col] = ph;
     }
-    // omega integral: exclusive prefix of div_vdp
+    // omega integral: exclusive prefix of div_vdp (the mixed form's FP32 div(v dp)
+    // widened exactly on the integer pipe)
+    double dv[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) {
+      if constexpr (kF32<R>) dv[k] = dbl(f_div[(l0 + k) * 16 + col]);
+      else dv[k] = s_div[(l0 + k) * SROW + col];
+    }
     double dt_ = 0.0;
 #pragma unroll
-    for (int k = 0; k < 9; ++k) dt_ += s_div[(l0 + k) * SROW + col];
+    for (int k = 0; k < 9; ++k) dt_ += dv[k];
     double acc = seg_excl_prefix(dt_, seg);
 #pragma unroll
     for (int k = 0; k < 9; ++k) {
       s_om[(l0 + k) * SROW + col] = acc;
-      acc = acc + s_div[(l0 + k) * SROW + col];
+      acc = acc + dv[k];
     }
     if (seg == 7) s_tot[col] = acc;
   }
@@ -167,10 +199,10 @@ __global__ void __launch_bounds__(LG * 16) k_caar(CaarArgs<R> a) {
       div = s_div[l * SROW + p];
     }
     R gp0, gp1;
-    gradient_sphere(t, m, rel_hw<R>(pd), gp0, gp1);
+    gradient_sphere(t, m, rel<R>(pd), gp0, gp1);
     const double td = a.T[sN0 + l * 16 + p];
     const R vgp = u * gp0 + w * gp1;
-    const R omega = (vgp - (cvt_hw<R>(s_om[l * SROW + p]) + R(0.5) * div)) * rp;
+    const R omega = (vgp - (cvt<R>(s_om[l * SROW + p]) + R(0.5) * div)) * rp;
     if (a.eta_ave_w != 0.0) a.omega_p[((size_t)e * NLEV + l) * 16 + p] += dbl_hw(eta * omega);
     // time level "nm1" (RK combine of stage 5 fused here), in double
     double tm = a.T[sM + l * 16 + p], dm = a.dp[sM + l * 16 + p];
@@ -193,38 +225,42 @@ __global__ void __launch_bounds__(LG * 16) k_caar(CaarArgs<R> a) {
       const double tot = s_tot[p];
       const double el = l == 0 ? 0.0 : c_hybi[l] * tot - s_om[l * SROW + p];
       const double eu = l + 1 == NLEV ? 0.0 : c_hybi[l + 1] * tot - s_om[(l + 1) * SROW + p];
-      etl = cvt_hw<R>(el);
-      etu = cvt_hw<R>(eu);
-      const R rdp = R(0.5) * (R(1) / cvt_hw<R>(a.dp[sN0 + l * 16 + p]));
+      etl = cvt<R>(el);
+      etu = cvt<R>(eu);
+      const R rdp = R(0.5) * (R(1) / cvt<R>(a.dp[sN0 + l * 16 + p]));
       const R facp = rdp * etu, facm = rdp * etl;
       const double* Tc = a.T + sN0 + l * 16 + p;
       const double* vc = a.v + vN0 + l * 32 + p;
       if (l + 1 < NLEV) {
-        tva += facp * (cvt_hw<R>(Tc[16]) - cvt_hw<R>(Tc[0]));
-        vva0 += facp * (cvt_hw<R>(vc[32]) - u);
-        vva1 += facp * (cvt_hw<R>(vc[48]) - w);
+        tva += facp * (cvt<R>(Tc[16]) - cvt<R>(Tc[0]));
+        vva0 += facp * (cvt<R>(vc[32]) - u);
+        vva1 += facp * (cvt<R>(vc[48]) - w);
       }
       if (l > 0) {
-        tva += facm * (cvt_hw<R>(Tc[0]) - cvt_hw<R>(Tc[-16]));
-        vva0 += facm * (u - cvt_hw<R>(vc[-32]));
-        vva1 += facm * (w - cvt_hw<R>(vc[-16]));
+        tva += facm * (cvt<R>(Tc[0]) - cvt<R>(Tc[-16]));
+        vva0 += facm * (u - cvt<R>(vc[-32]));
+        vva1 += facm * (w - cvt<R>(vc[-16]));
       }
       if (a.eta_ave_w != 0.0) a.eta_acc[((size_t)e * NLEV + l) * 16 + p] += a.eta_ave_w * el;
     }
     // temperature (compute_temperature_np1)
     R gt0, gt1;
-    gradient_sphere(t, m, rel_hw<R>(td), gt0, gt1);
-    const R tv = cvt_hw<R>(s_tv[l * SROW + p]);
+    gradient_sphere(t, m, rel<R>(td), gt0, gt1);
+    R tv;
+    if (own_tv) tv = cvt<R>(s_tv[l * SROW + p]);
+    else tv = cvt<R>(td);
     const R vgt = u * gt0 + w * gt1;
     const R ttens = (-tva - vgt) + R(kKappa) * tv * omega;
-    // float -> double on the integer pipe (dbl: a few integer instructions) relieves the
-    // FP64 pipe this kernel is bound by; double -> float stays on the hardware path
-    // (cvt_hw), whose integer form is long enough to cost more than it saves.
+    // Conversions on the integer pipe (dbl, and in phase C cvt / rel) relieve the FP64
+    // pipe this kernel is bound by (a hardware double -> float conversion takes that pipe
+    // like an FP64 add).  Phase A keeps the hardware conversions: there they follow the
+    // global loads, and the integer form measured slower (9.2 vs 8.4 ms per ne30
+    // interval), while in phase C it measured faster (8.2 vs 8.4 ms).
     const double tnew = spd * (dbl(ttens * dt) + tm);
     // velocity (compute_velocity_np1 with compute_energy_grad)
     const R rr = R(kRgas) * (tv * rp);
     R eg0 = rr * gp0, eg1 = rr * gp1;
-    const R ephi = R(0.5) * (u * u + w * w) + rel_hw<R>(s_dp[l * SROW + p]);
+    const R ephi = R(0.5) * (u * u + w * w) + rel<R>(s_dp[l * SROW + p]);
     R ge0, ge1;
     gradient_sphere(t, m, ephi, ge0, ge1);
     eg0 += ge0;
@@ -1558,11 +1594,16 @@ void launch_dp_from_ps(int E, double* dp, const double* ps_v, int n0, double ps0
 template <typename R>
 void launch_caar(const CaarArgs<R>& a, int E, cudaStream_t s) {
   constexpr int LG = LG_CAAR<R>();
-  // mixed form: + u, v, div(v dp) in FP32 ([72][16] each)
-  const size_t smem = (6 * NLEV * SROW + 16) * sizeof(double) + (kF32<R> ? 3 * NLEV * 16 * sizeof(float) : 0);
+  // shared memory layouts of k_caar: FP64 form 7 double arrays; mixed form 3 double and
+  // 4 float arrays, plus a double T_v array for moist runs
+  constexpr size_t s64 = (6 * NLEV * SROW + 16) * sizeof(double);
+  constexpr size_t s32 = (3 * NLEV * SROW + 16) * sizeof(double) + (NLEV * SROW + 3 * NLEV * 16) * sizeof(float);
+  constexpr size_t stv = NLEV * SROW * sizeof(double);
+  const size_t smem = kF32<R> ? s32 + (a.n0_qdp >= 0 ? stv : 0) : s64;
   static bool init = false;
   if (!init) {
-    cudaFuncSetAttribute(k_caar<R, LG>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(k_caar<R, LG>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)(kF32<R> ? s32 + stv : s64));
     init = true;
   }
   KScope k("caar_stage", s);

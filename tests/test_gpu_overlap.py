@@ -76,3 +76,29 @@ def test_overlapped_copies_match_plain(gpu_path, kw):
         L.set_async_copies(False)
     finally:
         _pin(L, list(host_in.values()) + list(res.values()), on=False)
+
+
+def test_async_state_visible_to_other_calls(gpu_path):
+    """With the time levels nm1 and np1 and Qdp still streaming in after
+    init_elements_states_c, any other call of the library sees the whole new state."""
+    L = H.setup(gpu_path, 4, 4, rsplit=3)
+    st = H.state(4, 4)
+    host_in = {k: np.ascontiguousarray(st[k]).copy() for k in ("v", "T", "dp3d", "Qdp", "ps_v")}
+    for k in ("T", "dp3d"):
+        host_in[k] += 1.0
+    host_in["v"] *= 1.5
+    host_in["Qdp"] *= 0.5
+    _pin(L, list(host_in.values()))
+    try:
+        L.set_async_copies(True)
+        L.set_state(host_in)
+        for tl in range(3):
+            for k in ("v", "T", "dp3d"):
+                assert np.array_equal(L.get(k, tl), host_in[k][:, tl]), (k, tl)
+        L.set_state(host_in)
+        r = L.push_results()
+        for k in ("v", "T", "dp3d", "Qdp", "ps_v"):
+            assert np.array_equal(r[k], host_in[k]), k
+        L.set_async_copies(False)
+    finally:
+        _pin(L, list(host_in.values()), on=False)

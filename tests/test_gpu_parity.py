@@ -290,10 +290,12 @@ def test_mass_conservation_gpu(pair):
     assert min(abs(x - q0) / q0 for x in qa) < 1e-12
 
 
-def test_mixed_precision_close(pair):
+@pytest.mark.parametrize("kw", [dict(rsplit=3), dict(rsplit=1, moisture=True), dict(rsplit=0)])
+def test_mixed_precision_close(pair, kw):
     """Mixed form against the FP64 oracle after one remap interval (loose bound; the
-    per-day error is reported by the benchmark)."""
-    g, o = pair(precision=1, rsplit=3)
+    per-day error is reported by the benchmark): dry, moist (virtual temperature from a
+    double shared array the dry mixed caar does not allocate) and vertically Eulerian."""
+    g, o = pair(precision=1, **kw)
     g.run_subcycle(DT)
     o.run_subcycle(DT)
     rg, ro = g.push_results(), o.push_results()
