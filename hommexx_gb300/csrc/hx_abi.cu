@@ -295,8 +295,8 @@ struct BackendT : Backend {
     qlim = dalloc<double>((size_t)E * Q * 2 * NLEV); qlim_tmp = dalloc<double>((size_t)E * Q * 2 * NLEV);
     dp0 = dalloc<double>(NLEV);
     gen_scr = dalloc<double>(n3 * 2);  // generic DSS of v / T / dp3d / omega_p (Qdp uses qscr)
-    invalid = dalloc<int>(1);
-    ck(cudaMallocHost(&h_invalid, sizeof(int)), "cudaMallocHost");
+    invalid = dalloc<int>(2);  // [0] invalid layer thickness, [1] an asynchronous-copy wait gave up
+    ck(cudaMallocHost(&h_invalid, 2 * sizeof(int)), "cudaMallocHost");
     ck(cudaEventCreateWithFlags(&ev_qdp_in, cudaEventDisableTiming), "cudaEventCreate");
     ck(cudaEventCreateWithFlags(&ev_mark, cudaEventDisableTiming), "cudaEventCreate");
     for (cudaEvent_t& ev : ev_lvl) ck(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "cudaEventCreate");
@@ -565,6 +565,7 @@ struct BackendT : Backend {
     a.Q = Q; a.n0_qdp = 0; a.np1_qdp = 1; a.limiter_option = s.prm.limiter_option;
     a.consthv = s.consthv ? 1 : 0;
     a.dt = 0; a.rhs_multiplier = 0; a.rhs_viss = 0; a.nu_p = s.prm.nu_p; a.nu_q = s.prm.nu_q;
+    a.err = invalid + 1;
     return a;
   }
 
@@ -610,9 +611,13 @@ struct BackendT : Backend {
     post("remap");
   }
   int remap_status() {
-    ck(cudaMemcpyAsync(h_invalid, invalid, sizeof(int), cudaMemcpyDeviceToHost, g_stream), "flag");
+    ck(cudaMemcpyAsync(h_invalid, invalid, 2 * sizeof(int), cudaMemcpyDeviceToHost, g_stream), "flag");
     ck(cudaStreamSynchronize(g_stream), "remap sync");
-    return *h_invalid ? 101 : 0;
+    if (h_invalid[1]) {
+      ck(cudaMemsetAsync(invalid + 1, 0, sizeof(int), g_stream), "memset");
+      fail(HX_ERR_CUDA, "tracer advection: a shared-memory bulk copy did not complete");
+    }
+    return h_invalid[0] ? 101 : 0;
   }
   int remap(int np1, int np1_qdp, double dt) override {
     launch_remap(np1, np1_qdp, true, dt);

@@ -430,6 +430,46 @@ __device__ __forceinline__ double div_newton(double a, double b, double r) {
   return fma(fma(-q, b, a), r, q);
 }
 
+// ---- bulk asynchronous copies into shared memory (the TMA engine, untiled) ---------
+// One thread arms an mbarrier with the expected byte count and issues
+// cp.async.bulk global -> shared; the copy completes the barrier's phase, which the
+// threads that read the data wait for.  Addresses 16-byte aligned, sizes multiples of
+// 16 bytes.
+__device__ __forceinline__ unsigned smem_addr(const void* p) {
+  return (unsigned)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+// Orders this thread's earlier generic-proxy accesses of shared memory before later
+// async-proxy (bulk copy) writes to it.
+__device__ __forceinline__ void fence_proxy_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, unsigned bytes, unsigned long long* bar) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+               : "memory");
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_addr(dst)),
+               "l"(src), "r"(bytes), "r"(smem_addr(bar))
+               : "memory");
+}
+// Waits for the completion of phase `parity` of the barrier; false after `tries` polls
+// (each poll may suspend the thread for a short, hardware-chosen time).
+__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned parity, int tries) {
+  for (int i = 0; i < tries; ++i) {
+    unsigned done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(done)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
 // Brackets one launch for the per-kernel timing hooks.
 struct KScope {
   const char* n;

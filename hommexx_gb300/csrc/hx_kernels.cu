@@ -963,21 +963,34 @@ __device__ bool limiter_level(int option, R* x, const R* c, R s1, double& minp_i
 // AALTracerPhase: qtens = Qdp - dt div(vstar Qdp) [+ qtens_biharmonic], limiter,
 // spheremp -> qscr (pre-DSS).  One CTA per element loops over the tracers: vstar, the
 // limiter weights c = spheremp dpdissk, 1/dpdissk and sum(c) are formed once per element
-// and reused by every tracer.
+// and reused by every tracer.  The Qdp slab of the next tracer (72 x 16 contiguous
+// doubles) streams into shared memory by a bulk asynchronous copy while the current
+// one is limited and stored, so the tracer loop does not wait on global loads.
 // Occupancy: 6 CTAs per SM in the mixed form (at most 80 registers; the kernel waits on
 // memory and shared-memory latency more than it issues, so occupancy pays for a 12-byte
 // spill), 3 in the FP64 form (168 registers).
+template <typename R> constexpr size_t aal_buf_offset() {  // bytes, 16-byte aligned
+  return (NLEV * SROW * sizeof(double) + (3 * NLEV * SROW + NLEV) * sizeof(R) + 15) / 16 * 16;
+}
 template <typename R, int LG>
 __global__ void __launch_bounds__(LG * 16, kF32<R> ? 6 : 3) k_aal_tracer(EulerArgs<R> a) {
   constexpr int NL = NLEV / LG;
-  extern __shared__ double tsm[];
+  constexpr unsigned kSlab = NLEV * 16 * sizeof(double);
+  extern __shared__ __align__(16) double tsm[];
   double* s_q = tsm;                                            // [72][17] double
   R* s_dm = reinterpret_cast<R*>(tsm + NLEV * SROW);            // dpdissk
   R* s_rdm = s_dm + NLEV * SROW;                                // 1 / dpdissk
   R* s_c = s_rdm + NLEV * SROW;                                 // spheremp * dpdissk
-  R* s_c1 = s_c + NLEV * SROW;                                  // sum of c per level
+  R* s_c1 = s_c + NLEV * SROW;                                  // sum of c per level [72]
+  double* q_buf = reinterpret_cast<double*>(reinterpret_cast<char*>(tsm) + aal_buf_offset<R>());  // [72][16]
+  unsigned long long* bar = reinterpret_cast<unsigned long long*>(q_buf + NLEV * 16);
   const int e = blockIdx.x;
   const int tid = threadIdx.x, p = tid & 15, lg = tid >> 4;
+  const double* slab0 = a.qdp + ((size_t)e * QTL + a.n0_qdp) * a.Q * NLEV * 16;
+  if (tid == 0) {
+    mbar_init(bar, 1);
+    if (a.Q > 0) bulk_load(q_buf, slab0, kSlab, bar);
+  }
   Pt<R> t;
   t.init(p);
   PM<R> m;
@@ -1007,14 +1020,25 @@ __global__ void __launch_bounds__(LG * 16, kF32<R> ? 6 : 3) k_aal_tracer(EulerAr
   }
   const bool add_hv = a.rhs_viss != 0.0;
   const R mdf = R(-a.dt) * m.fdiv;  // -dt times divergence_sphere's scale
+  unsigned parity = 0;
 #pragma unroll 1
   for (int q = 0; q < a.Q; ++q) {
-    const size_t qn0 = (((size_t)e * QTL + a.n0_qdp) * a.Q + q) * NLEV * 16;
     const size_t qb = ((size_t)e * a.Q + q) * NLEV * 16;
+    // tracer q's slab: a bounded wait, then a block-wide vote, so that a copy that never
+    // completes ends the kernel with an error flag instead of a hang
+    const bool ok = __syncthreads_and(mbar_wait(bar, parity, 1 << 20));
+    parity ^= 1u;
+    if (!ok) {
+      if (tid == 0) {
+        atomicExch(a.err, 1);
+        mbar_wait(bar, parity ^ 1u, 1 << 20);  // once more for the copy still in flight
+      }
+      return;
+    }
 #pragma unroll
     for (int k = 0; k < NL; ++k) {
       const int l = lg + LG * k;
-      const double qdd = a.qdp[qn0 + l * 16 + p];
+      const double qdd = q_buf[l * 16 + p];
       const R qd = cvt<R>(qdd);
       const R dvs = t.ddx(w0[k] * qd) + t.ddy(w1[k] * qd);  // div(vstar Qdp) / fdiv
       const double q0 = add_hv ? a.qtens[qb + l * 16 + p] : 0.0;
@@ -1022,6 +1046,10 @@ __global__ void __launch_bounds__(LG * 16, kF32<R> ? 6 : 3) k_aal_tracer(EulerAr
       else s_q[l * SROW + p] = (qdd + mdf * dvs + q0);
     }
     __syncthreads();
+    if (tid == 0 && q + 1 < a.Q) {  // the buffer is free: fetch the next tracer's slab
+      fence_proxy_async_smem();
+      bulk_load(q_buf, slab0 + (size_t)(q + 1) * NLEV * 16, kSlab, bar);
+    }
     for (int l = tid; l < NLEV; l += blockDim.x) {
       if (s_c1[l] > R(0)) {
         R x[16], c[16];
@@ -1052,7 +1080,7 @@ __global__ void __launch_bounds__(LG * 16, kF32<R> ? 6 : 3) k_aal_tracer(EulerAr
 }
 
 template <typename R> constexpr size_t aal_smem() {
-  return NLEV * SROW * sizeof(double) + (4 * NLEV * SROW) * sizeof(R);
+  return aal_buf_offset<R>() + NLEV * 16 * sizeof(double) + 16;  // + the Qdp slab and its barrier
 }
 
 // DSS(rspheremp) of the tracer scratch into Qdp(np1); with time_avg the last RK2 stage

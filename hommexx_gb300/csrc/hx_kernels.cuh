@@ -77,6 +77,7 @@ struct EulerArgs {
   int Q, n0_qdp, np1_qdp, limiter_option, consthv;
   int avg_n0_qdp;  // level averaged with np1 when the last RK2 stage fuses qdp_time_avg
   double dt, rhs_multiplier, rhs_viss, nu_p, nu_q;
+  int* err;  // set to 1 when a kernel gives up waiting for its asynchronous copies
 };
 
 struct RemapArgs {
