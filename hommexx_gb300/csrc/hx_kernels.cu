@@ -1147,9 +1147,12 @@ constexpr int R_DMA = R_MASS + 74;     // dma[0 .. 73]
 constexpr int R_AI = R_DMA + 74;       // ai[0 .. 72]
 constexpr int R_COEF = R_AI + 74;      // coef[3][72]
 constexpr int R_RD = R_COEF + 216;     // 1 / D[0 .. 71]
-constexpr int R_GF = R_RD + 72;        // mixed form: float g[10][74], z2[72], 1/D[72], delta[-1 .. 73]
+constexpr int R_END = R_RD + 72;
+// The mixed form's float g[10][74], z2[72], 1/D[72] and delta[-1 .. 73] (959 floats) use
+// the region of the double g (740 doubles), which that form does not store.
+static_assert(740 + 72 + 72 + 1 + 74 <= 2 * 740, "FP32 grid arrays exceed the double grid region");
 // doubles per column
-template <typename R> constexpr int r_col() { return kF32<R> ? R_GF + (740 + 72 + 72 + 76) / 2 : R_GF; }
+template <typename R> constexpr int r_col() { return R_END; }
 
 // compute_ppm and the monotone parabola coefficients (PpmRemap.hpp:202-353) for one
 // variable of one column in T: slopes dma (j in 0 .. 73), edge values ai (j in 0 .. 72),
@@ -1373,42 +1376,16 @@ __global__ void __launch_bounds__(RT) k_remap(RemapArgs a) {
       z2[k] = (pin[k + 1] - (pio[kk - 1] + pio[kk]) * 0.5) * rD[kk - 1];
     }
   }
-  // compute_grids (double)
-  if (lane < 25) {
-#pragma unroll
-    for (int k3 = 0; k3 < 3; ++k3) {
-      const int j = 3 * lane + k3;
-      if (j < NLEV + 2) {
-        const double dm2 = D[j - 2], dm1 = D[j - 1], d0 = D[j];
-        // reciprocals by Newton-Raphson (rcp_newton, within one ulp)
-        float rf;
-        const double r10 = rcp_newton(dm1 + d0, rf);  // shared by g1, g3, g5
-        g[0 * 74 + j] = dm1 * rcp_newton(dm2 + dm1 + d0, rf);
-        g[1 * 74 + j] = (2.0 * dm2 + dm1) * r10;
-        g[2 * 74 + j] = (dm1 + 2.0 * d0) * rcp_newton(dm2 + dm1, rf);
-        if (j < NLEV + 1) {
-          const double dp1 = D[j + 1];
-          const double r6 = rcp_newton(2.0 * dm1 + d0, rf);  // shared by g6, g8
-          const double r7 = rcp_newton(2.0 * d0 + dm1, rf);  // shared by g7, g9
-          g[3 * 74 + j] = dm1 * r10;
-          g[4 * 74 + j] = rcp_newton(dm2 + dm1 + d0 + dp1, rf);
-          // row 5 holds g5 (g6 - g7), the only form the edge values use
-          g[5 * 74 + j] = ((2.0 * dm1 * d0) * r10) * ((dm2 + dm1) * r6 - (dp1 + d0) * r7);
-          g[8 * 74 + j] = dm1 * (dm2 + dm1) * r6;
-          g[9 * 74 + j] = d0 * (d0 + dp1) * r7;
-        }
-      }
-    }
-  }
-  __syncwarp();
   // Mixed form: the reconstructions run in FP32 from float copies of the grid weights,
   // z2 and 1/D; the cell integrals and the mass below each interface stay in FP64, and
   // the bottom interface carries the exact column mass (mass fixer).  v and T are
   // reconstructed from their neighbour differences (ppm_coefs_delta), so FP32 carries
   // only differences and parabola offsets, and the cell mean's share of each partial
   // integral, A[kk] (x2 + 1/2), is added in FP64; the tracers (non-negative, of their own
-  // scale) are reconstructed from their FP32 cell means.
-  float* gf = reinterpret_cast<float*>(sm + R_GF);  // [10][74]
+  // scale) are reconstructed from their FP32 cell means.  The FP32 arrays occupy the
+  // region of the double weights, which the mixed form never stores (13.8 KB per column
+  // instead of 17.7 KB: four CTAs per SM instead of three).
+  float* gf = reinterpret_cast<float*>(sm + R_G);  // [10][74]
   float* z2f = gf + 740;
   float* rDf = z2f + 72;
   float* dlf = rDf + 72 + 1;  // df[-1 .. 73]
@@ -1416,10 +1393,41 @@ __global__ void __launch_bounds__(RT) k_remap(RemapArgs a) {
   float* dmaf = reinterpret_cast<float*>(sm + R_DMA);
   float* aif = reinterpret_cast<float*>(sm + R_AI);
   float* coeff = reinterpret_cast<float*>(sm + R_COEF);
+  // compute_grids in double; the mixed form keeps only their FP32 images, converted on
+  // the integer pipe (d2f_rn: the FP64 pipe is this kernel's limit)
+  if (lane < 25) {
+#pragma unroll
+    for (int k3 = 0; k3 < 3; ++k3) {
+      const int j = 3 * lane + k3;
+      auto put = [&](int c, double x) {
+        if constexpr (kF32<R>) gf[c * 74 + j] = d2f_rn(x);
+        else g[c * 74 + j] = x;
+      };
+      if (j < NLEV + 2) {
+        const double dm2 = D[j - 2], dm1 = D[j - 1], d0 = D[j];
+        // reciprocals by Newton-Raphson (rcp_newton, within one ulp)
+        float rf;
+        const double r10 = rcp_newton(dm1 + d0, rf);  // shared by g1, g3, g5
+        put(0, dm1 * rcp_newton(dm2 + dm1 + d0, rf));
+        put(1, (2.0 * dm2 + dm1) * r10);
+        put(2, (dm1 + 2.0 * d0) * rcp_newton(dm2 + dm1, rf));
+        if (j < NLEV + 1) {
+          const double dp1 = D[j + 1];
+          const double r6 = rcp_newton(2.0 * dm1 + d0, rf);  // shared by g6, g8
+          const double r7 = rcp_newton(2.0 * d0 + dm1, rf);  // shared by g7, g9
+          put(3, dm1 * r10);
+          put(4, rcp_newton(dm2 + dm1 + d0 + dp1, rf));
+          // row 5 holds g5 (g6 - g7), the only form the edge values use
+          put(5, ((2.0 * dm1 * d0) * r10) * ((dm2 + dm1) * r6 - (dp1 + d0) * r7));
+          put(8, dm1 * (dm2 + dm1) * r6);
+          put(9, d0 * (d0 + dp1) * r7);
+        }
+      }
+    }
+  }
+  __syncwarp();
   if constexpr (kF32<R>) {
     {
-      // conversions on the integer pipe (d2f_rn): the FP64 pipe is this kernel's limit
-      for (int i = lane; i < 740; i += 32) gf[i] = d2f_rn(g[i]);
       if (own) {
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
