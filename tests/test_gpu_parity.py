@@ -2,7 +2,7 @@
 whole remap intervals, through the C ABI, on the same seeded inputs.
 
 FP64 plain form: every field within 1e-12 relative (max |gpu - oracle| / max |oracle|),
-the bar the benchmark spec sets for the FP64 step.  The DSS sums in the reference's fixed
+the parity bar of the FP64 step.  The DSS sums in the reference's fixed
 order in double, so it is compared bit for bit.
 """
 import numpy as np
