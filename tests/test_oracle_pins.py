@@ -12,6 +12,10 @@ own property tests and to analytic identities:
   vorticity is 2 w sin(lat);
 * a remap interval conserves dry mass and tracer mass, and a constant mixing ratio
   stays constant;
+* the PPM remap (Colella and Woodward 1984, as PpmRemap.hpp:174-689 restates it) is the
+  identity when source and target grids coincide, keeps constants, and reproduces cell
+  means of a profile linear in pressure exactly away from the three cells at each end of
+  the column that the ghost cells reach;
 * option checks return the reference's error codes.
 """
 import ctypes as C
@@ -236,3 +240,70 @@ def _param_list(p):
             float(p.nu_div), float(p.nu_top), p.hypervis_order, p.hypervis_subcycle,
             float(p.hypervis_scaling), p.ftype, bool(p.prescribed_wind), bool(p.moisture),
             bool(p.disable_diagnostics), bool(p.use_cpstar), bool(p.use_semi_lagrangian_transport)]
+
+
+def _target_dp(ps):
+    """Hybrid thickness for surface pressure ps (E,4,4) -> (E,72,4,4)."""
+    hv = H.hvc()
+    da, db = np.diff(hv.hyai), np.diff(hv.hybi)
+    return da[None, :, None, None] * hv.ps0 + db[None, :, None, None] * ps[:, None]
+
+
+def _remap_case(oracle_path, alg, src_dp, v, T):
+    """Sets level 1 (v, T, dp3d) and runs the PPM remap of that level alone."""
+    L = _setup(oracle_path, ne=2, Q=1, rsplit=1, remap_alg=alg)
+    L.set("dp3d", 1, src_dp)
+    L.set("v", 1, v)
+    L.set("T", 1, T)
+    L.call("hx_run_remap", 1, 0, DT)
+    return L.get("v", 1), L.get("T", 1), L.get("dp3d", 1)
+
+
+def _columns(ne=2, seed=5):
+    rng = np.random.default_rng(seed)
+    E = 6 * ne * ne
+    ps = 1.0e5 + 800.0 * rng.standard_normal((E, 4, 4))
+    return rng, ps, _target_dp(ps)
+
+
+@pytest.mark.parametrize("alg", [1, 2])
+def test_remap_identity_on_coinciding_grids(oracle_path, alg):
+    """Source thickness = the target's: every cell is integrated over itself."""
+    rng, ps, tgt = _columns()
+    v = 20.0 * rng.standard_normal(tgt.shape[:2] + (2, 4, 4))
+    T = 250.0 + 30.0 * rng.standard_normal(tgt.shape)
+    v1, T1, dp1 = _remap_case(oracle_path, alg, tgt, v, T)
+    assert np.abs(v1 - v).max() <= 1e-12 * np.abs(v).max()
+    assert np.abs(T1 - T).max() <= 1e-12 * np.abs(T).max()
+    assert np.abs(dp1 - tgt).max() <= 1e-12 * tgt.max()
+
+
+@pytest.mark.parametrize("alg", [1, 2])
+def test_remap_keeps_constants_and_linear_profiles(oracle_path, alg):
+    """A perturbed source grid with the target's column mass: a constant stays constant
+    everywhere; cell means of a + b p stay exact in the interior (the edge values are the
+    cubic interpolant of the cumulative mass, exact for linear data, and the limiters
+    leave monotone linear data alone).  The mirrored ghost cells make the slopes of source
+    cells 0-1 and 70-71 inexact, which reaches target cells 0-2 and 69-71."""
+    rng, ps, tgt = _columns(seed=6)
+    k = np.arange(72)[None, :, None, None]
+    pert = 1.0 + 0.15 * np.sin(0.7 * k + rng.uniform(0, 6.3, (tgt.shape[0], 1, 4, 4)))
+    src = tgt * pert
+    src *= tgt.sum(axis=1, keepdims=True) / src.sum(axis=1, keepdims=True)
+    hv = H.hvc()
+    ptop = hv.hyai[0] * hv.ps0
+
+    def means(dp, a, b):  # cell means of a + b p over the cells of thickness dp
+        pi = ptop + np.concatenate([np.zeros_like(dp[:, :1]), np.cumsum(dp, axis=1)], axis=1)
+        return a + b * 0.5 * (pi[:, :-1] + pi[:, 1:])
+
+    v = np.empty(src.shape[:2] + (2, 4, 4))
+    v[:, :, 0] = 7.5                                   # constant
+    v[:, :, 1] = means(src, 3.0, 2.0e-4)               # linear in p
+    T = means(src, 200.0, 1.0e-3)
+    v1, T1, _ = _remap_case(oracle_path, alg, src, v, T)
+    assert np.abs(v1[:, :, 0] - 7.5).max() <= 1e-13 * 7.5
+    inner = slice(3, 69)
+    want_v, want_T = means(tgt, 3.0, 2.0e-4), means(tgt, 200.0, 1.0e-3)
+    assert np.abs(v1[:, inner, 1] - want_v[:, inner]).max() <= 1e-12 * np.abs(want_v).max()
+    assert np.abs(T1[:, inner] - want_T[:, inner]).max() <= 1e-12 * np.abs(want_T).max()
