@@ -9,7 +9,8 @@ own property tests and to analytic identities:
   conserves the global integral;
 * the weak Laplacian of a spherical harmonic (after DSS and the inverse mass matrix)
   approaches -l(l+1)/a^2 Y; divergence of solid-body rotation vanishes and its
-  vorticity is 2 w sin(lat);
+  vorticity is 2 w sin(lat); the curl of a gradient and the gradient of a constant
+  vanish to round-off;
 * a remap interval conserves dry mass and tracer mass, and a constant mixing ratio
   stays constant;
 * the PPM remap (Colella and Woodward 1984, as PpmRemap.hpp:174-689 restates it) is the
@@ -160,6 +161,27 @@ def test_laplacian_of_spherical_harmonic(oracle_path):
     error falling by more than 4x per doubling of resolution (ne 4 -> 8)."""
     e4, e8 = _lap_err(oracle_path, 4), _lap_err(oracle_path, 8)
     assert e8 < 1e-3 and e4 / e8 > 4.0, (e4, e8)
+
+
+def test_curl_of_gradient_vanishes(oracle_path):
+    """vorticity_sphere(gradient_sphere(f)) = 0 point by point: on each element the two
+    GLL derivative matrices act along different directions and commute, and the metric
+    (D after Dinv) cancels, so only round-off remains; the gradient of a constant is 0."""
+    ne = 4
+    L = _setup(oracle_path, ne=ne)
+    m = H.mesh(ne)
+    rng = np.random.default_rng(13)
+    lev = rng.standard_normal((72, 1))
+    y = np.sin(m.lat) * np.cos(2 * m.lon) + 0.3 * np.cos(m.lat) ** 2   # smooth, (E,4,4)
+    f = (1.0 + 0.1 * lev[None, :, :, None]) * y[:, None]
+    g = _sphere_op(L, 3, f, (m.nelem, 72, 2, 4, 4))
+    curl = _sphere_op(L, 2, g, (m.nelem, 72, 4, 4))
+    a = 6.376e6
+    gscale = np.abs(g).max()
+    assert gscale > 1e-8
+    assert np.abs(curl).max() <= 1e-12 * gscale / a, np.abs(curl).max()
+    g0 = _sphere_op(L, 3, np.full((m.nelem, 72, 4, 4), 287.0), (m.nelem, 72, 2, 4, 4))
+    assert np.abs(g0).max() <= 1e-12 * 287.0 / a
 
 
 def test_solid_body_rotation(oracle_path):
