@@ -10,7 +10,7 @@ own property tests and to analytic identities:
 * the weak Laplacian of a spherical harmonic (after DSS and the inverse mass matrix)
   approaches -l(l+1)/a^2 Y; divergence of solid-body rotation vanishes and its
   vorticity is 2 w sin(lat); the curl of a gradient and the gradient of a constant
-  vanish to round-off;
+  vanish to round-off; the weak Laplacian is symmetric and negative semi-definite;
 * a remap interval conserves dry mass and tracer mass, and a constant mixing ratio
   stays constant;
 * the PPM remap (Colella and Woodward 1984, as PpmRemap.hpp:174-689 restates it) is the
@@ -182,6 +182,23 @@ def test_curl_of_gradient_vanishes(oracle_path):
     assert np.abs(curl).max() <= 1e-12 * gscale / a, np.abs(curl).max()
     g0 = _sphere_op(L, 3, np.full((m.nelem, 72, 4, 4), 287.0), (m.nelem, 72, 2, 4, 4))
     assert np.abs(g0).max() <= 1e-12 * 287.0 / a
+
+
+def test_weak_laplacian_symmetric_negative(oracle_path):
+    """laplace_simple is the weak form -sum_q (grad phi_p . grad f) w_q: summed against a
+    second field it is symmetric, <g, L f> = <f, L g>, and <f, L f> <= 0 (the element
+    sums need no mass weights: the weak form carries them)."""
+    ne = 4
+    L = _setup(oracle_path, ne=ne)
+    m = H.mesh(ne)
+    rng = np.random.default_rng(17)
+    f = rng.standard_normal((m.nelem, 72, 4, 4))
+    g = rng.standard_normal((m.nelem, 72, 4, 4))
+    Lf = _sphere_op(L, 0, f, f.shape)
+    Lg = _sphere_op(L, 0, g, g.shape)
+    a, b = np.sum(g * Lf, axis=(0, 2, 3)), np.sum(f * Lg, axis=(0, 2, 3))  # per level
+    assert np.abs(a - b).max() <= 1e-12 * np.abs(a).max()
+    assert (np.sum(f * Lf, axis=(0, 2, 3)) < 0).all()
 
 
 def test_solid_body_rotation(oracle_path):
