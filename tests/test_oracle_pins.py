@@ -13,6 +13,8 @@ own property tests and to analytic identities:
   vanish to round-off; the weak Laplacian is symmetric and negative semi-definite;
 * a remap interval conserves dry mass and tracer mass, and a constant mixing ratio
   stays constant;
+* a resting atmosphere (v = 0, T and mixing ratios functions of the level only, ps
+  uniform) stays at rest through a whole remap interval;
 * the PPM remap (Colella and Woodward 1984, as PpmRemap.hpp:174-689 restates it) is the
   identity when source and target grids coincide, keeps constants, and reproduces cell
   means of a profile linear in pressure exactly away from the three cells at each end of
@@ -346,3 +348,38 @@ def test_remap_keeps_constants_and_linear_profiles(oracle_path, alg):
     want_v, want_T = means(tgt, 3.0, 2.0e-4), means(tgt, 200.0, 1.0e-3)
     assert np.abs(v1[:, inner, 1] - want_v[:, inner]).max() <= 1e-12 * np.abs(want_v).max()
     assert np.abs(T1[:, inner] - want_T[:, inner]).max() <= 1e-12 * np.abs(want_T).max()
+
+
+def test_resting_atmosphere_stays_at_rest(oracle_path):
+    """v = 0, T and Qdp/dp functions of the level only, ps uniform: every horizontal
+    gradient vanishes, so a whole remap interval (RK5 Caar stages, hyperviscosity,
+    tracer advection with limiter, remap) leaves the state where it was."""
+    ne, Q = 4, 2
+    m = H.mesh(ne)
+    st = {k: v.copy() for k, v in H.state(ne, Q).items()}
+    E = m.nelem
+    ps = np.full((E, 4, 4), 98000.0)
+    dp = _target_dp(ps)
+    Tl = 300.0 - 60.0 * np.linspace(1.0, 0.0, 72)
+    for tl in range(3):
+        st["v"][:, tl] = 0.0
+        st["T"][:, tl] = Tl[None, :, None, None]
+        st["dp3d"][:, tl] = dp
+        st["ps_v"][:, tl] = ps
+    for tq in range(2):
+        for q in range(Q):
+            st["Qdp"][:, tq, q] = (0.002 + 0.001 * q) * dp
+    from hommexx_gb300 import abi
+    L = H.lib(oracle_path)
+    if L.nelem:
+        L.finalize()
+    L.init(m, H.hvc(), abi.SimParams(qsize=Q, nu=1e16, rsplit=3), st)
+    L.run_subcycle(DT)
+    r = L.push_results()
+    n0 = L.tl[1]
+    assert np.abs(r["v"][:, n0]).max() < 1e-10                     # m/s (8e-13 seen)
+    assert np.abs(r["T"][:, n0] - Tl[None, :, None, None]).max() < 1e-12 * 300.0
+    assert np.abs(r["dp3d"][:, n0] - dp).max() < 1e-13 * dp.max()
+    assert np.abs(r["ps_v"][:, n0] - ps).max() < 1e-13 * 98000.0
+    for q in range(Q):
+        assert np.abs(r["Q"][:, q] - (0.002 + 0.001 * q)).max() < 1e-14
