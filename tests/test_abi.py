@@ -78,3 +78,18 @@ def test_host_side_errors_without_gpu(gpu_lib_cpu):
     assert L.hx_run_prim_step.restype is not None
     L.hx_run_prim_step.argtypes = [ctypes.c_double]
     assert L.hx_run_prim_step(300.0) == 201   # no session: state error, not a CPU run
+
+
+def test_c_driver_links_and_reports(gpu_lib_cpu, tmp_path):
+    """include/hxgpu.h compiles as C, a C driver links libhxgpu.so and gets the status
+    codes of the host-side paths (tests/c/abi_from_c.c)."""
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    exe = str(tmp_path / "abi_from_c")
+    libdir = os.path.dirname(gpu_lib_cpu)
+    subprocess.run(["gcc", "-std=c11", "-Wall", "-Werror", "-I", os.path.join(H.ROOT, "include"),
+                    os.path.join(H.ROOT, "tests", "c", "abi_from_c.c"), "-L", libdir, "-lhxgpu",
+                    f"-Wl,-rpath,{libdir}", "-o", exe], check=True, capture_output=True)
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 0, r.stdout + r.stderr
