@@ -15,6 +15,7 @@ own property tests and to analytic identities:
   stays constant;
 * a resting atmosphere (v = 0, T and mixing ratios functions of the level only, ps
   uniform) stays at rest through a whole remap interval;
+* limiters 8 and 9 keep an advected cosine bell non-negative and below its maximum;
 * the PPM remap (Colella and Woodward 1984, as PpmRemap.hpp:174-689 restates it) is the
   identity when source and target grids coincide, keeps constants, and reproduces cell
   means of a profile linear in pressure exactly away from the three cells at each end of
@@ -390,3 +391,28 @@ def test_resting_atmosphere_stays_at_rest(oracle_path):
     d = resting_deviation(oracle_path)
     assert d["v"] < 1e-10, d     # m/s (8e-13 seen)
     assert d["T"] < 1e-12 and d["dp"] < 1e-13 and d["ps"] < 1e-13 and d["Q"] < 1e-14, d
+
+
+@pytest.mark.parametrize("limiter", [8, 9])
+def test_limiters_keep_a_cosine_bell_bounded(oracle_path, limiter):
+    """A cosine bell of mixing ratio (zero outside its support) advected over three remap
+    intervals: the quasi-monotone limiters keep it non-negative to round-off and create
+    no new maximum (EulerStepFunctorImpl.hpp:693-884 with the neighbour bounds)."""
+    from hommexx_gb300 import abi
+    ne = 4
+    m = H.mesh(ne)
+    st = {k: v.copy() for k, v in H.state(ne, 1).items()}
+    d = np.arccos(np.clip(np.sin(0.3) * np.sin(m.lat) + np.cos(0.3) * np.cos(m.lat) * np.cos(m.lon - 1.0),
+                          -1.0, 1.0))
+    bell = np.where(d < 0.5, 0.5 * (1.0 + np.cos(np.pi * d / 0.5)), 0.0) * 1e-3
+    for tq in range(2):
+        st["Qdp"][:, tq, 0] = bell[:, None] * st["dp3d"][:, 1]
+    L = H.lib(oracle_path)
+    if L.nelem:
+        L.finalize()
+    L.init(m, H.hvc(), abi.SimParams(qsize=1, nu=1e16, rsplit=3, limiter_option=limiter), st)
+    for _ in range(3):
+        L.run_subcycle(DT)
+    q = L.push_results()["Q"]
+    assert q.min() >= -1e-20, q.min()          # round-off below 1e-3 mixing ratios
+    assert q.max() <= bell.max() * (1 + 1e-12), q.max()
