@@ -16,6 +16,8 @@ own property tests and to analytic identities:
 * a resting atmosphere (v = 0, T and mixing ratios functions of the level only, ps
   uniform) stays at rest through a whole remap interval;
 * limiters 8 and 9 keep an advected cosine bell non-negative and below its maximum;
+* hyperviscosity lowers the variance of T and the kinetic energy on every level and
+  keeps the layer masses;
 * the PPM remap (Colella and Woodward 1984, as PpmRemap.hpp:174-689 restates it) is the
   identity when source and target grids coincide, keeps constants, and reproduces cell
   means of a profile linear in pressure exactly away from the three cells at each end of
@@ -416,3 +418,27 @@ def test_limiters_keep_a_cosine_bell_bounded(oracle_path, limiter):
     q = L.push_results()["Q"]
     assert q.min() >= -1e-20, q.min()          # round-off below 1e-3 mixing ratios
     assert q.max() <= bell.max() * (1 + 1e-12), q.max()
+
+
+def test_hyperviscosity_dissipates_and_conserves_layer_mass(oracle_path):
+    """One hyperviscosity call (3 subcycles of the biharmonic): per level the mass-weighted
+    variance of T and the kinetic energy fall, and the layer mass sum spheremp dp3d is
+    kept to round-off (the weak Laplacian and the DSS conserve global integrals)."""
+    ne = 4
+    L = _setup(oracle_path, ne=ne, Q=1, rsplit=1, nu=1e16, nu_top=0.0)
+    w = H.mesh(ne).spheremp
+
+    def var(T):
+        mean = np.sum(T * w[:, None], axis=(0, 2, 3)) / np.sum(w)
+        return np.sum((T - mean[None, :, None, None]) ** 2 * w[:, None], axis=(0, 2, 3))
+
+    def ke(v):
+        return np.sum(v ** 2 * w[:, None, None], axis=(0, 2, 3, 4))
+
+    T0, v0, d0 = L.get("T", 2), L.get("v", 2), L.get("dp3d", 2)
+    L.call("hx_run_hypervis", 2, DT, 0.0)
+    T1, v1, d1 = L.get("T", 2), L.get("v", 2), L.get("dp3d", 2)
+    assert (var(T1) < var(T0)).all() and (ke(v1) < ke(v0)).all()
+    assert np.abs(d1 - d0).max() > 1e-9 * np.abs(d0).max()          # it did act on dp3d
+    m0, m1 = np.sum(d0 * w[:, None], axis=(0, 2, 3)), np.sum(d1 * w[:, None], axis=(0, 2, 3))
+    assert np.abs(m1 / m0 - 1).max() < 1e-14
