@@ -1,12 +1,14 @@
 """The analytic pins of the CPU oracle (tests/test_oracle_pins.py) held by the CUDA
 library directly: the PPM remap is the identity on coinciding grids and reproduces cell
-means of a profile linear in pressure in the column interior, and a resting atmosphere
-stays at rest through a whole remap interval, in the FP64 and the mixed form."""
+means of a profile linear in pressure in the column interior; a resting atmosphere
+stays at rest through a whole remap interval, in the FP64 and the mixed form; limiters
+8 and 9 keep an advected cosine bell non-negative and below its maximum; hyperviscosity
+dissipates and keeps the layer masses."""
 import numpy as np
 import pytest
 
 import hxtest as H
-from test_oracle_pins import _columns, _remap_case, resting_deviation
+from test_oracle_pins import _columns, _remap_case, bell_extremes, hyperviscosity_effect, resting_deviation
 
 pytestmark = pytest.mark.gpu
 
@@ -47,3 +49,17 @@ def test_gpu_resting_atmosphere(gpu_path, precision):
     assert d["v"] < 1e-9, d
     assert d["T"] < 1e-11 and d["dp"] < 1e-12 and d["ps"] < 1e-12, d
     assert d["Q"] < (1e-13 if precision == 0 else 2e-9), d
+
+
+@pytest.mark.parametrize("limiter", [8, 9])
+def test_gpu_limiters_keep_a_cosine_bell_bounded(gpu_path, limiter):
+    lo, hi, top = bell_extremes(gpu_path, limiter)
+    assert lo >= -1e-20, lo
+    assert hi <= top * (1 + 1e-12), hi
+
+
+def test_gpu_hyperviscosity_dissipates_and_conserves_layer_mass(gpu_path):
+    h = hyperviscosity_effect(gpu_path)
+    assert (h["var"][1] < h["var"][0]).all() and (h["ke"][1] < h["ke"][0]).all()
+    assert h["ddp"] > 1e-9
+    assert h["mass"] < 1e-14, h["mass"]
