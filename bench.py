@@ -12,10 +12,11 @@ mirrored remap; seeded smooth synthetic initial state (spherical harmonics of de
 * ``e2e``: the same through the C ABI with host buffers, each step copying the state in
   (``init_elements_states_c``) and the results out (``cxx_push_results_to_f90``) from
   pinned host memory, wall clock.  The copies overlap the step where their data allow
-  (``hx_set_async_copies``: time levels nm1 and np1 stream in during the first Caar
-  stages and Qdp during the first dynamics step; ``hx_stream_results``: each result
-  piece is copied out once it is final, the last ones chunk by chunk of the final
-  remap); every byte still crosses the host link inside the timed region.
+  (``hx_set_async_copies``: v, T, dp3d and ps_v as whole arrays before the first kernel,
+  Qdp during the first dynamics step; ``hx_stream_results``: each result piece is copied
+  out once it is final, the last ones chunk by chunk of the final remap); every byte
+  still crosses the host link inside the timed region.  The ``e2e`` block also records
+  the host link rates measured just before the loop and the wall time of each call.
 * ``mixed``: the mixed-precision form timed the same way, with its error against the
   FP64 form after ``--error-days`` simulated days.
 * ``roofline``: the kernel with the largest share of device time; algorithmic bytes per
@@ -28,8 +29,9 @@ mirrored remap; seeded smooth synthetic initial state (spherical harmonics of de
   and of the vector-Jacobian product (state on the device, CUDA events), the cost of
   a gradient relative to a forward run, and its checks: central finite differences of
   J = sum spheremp T_final^2 along 10 seeded smooth directions (eps = 1e-6), the
-  dot-product test against the CUDA tangent-linear model (``hx_traj_jvp``, also timed)
-  and against the oracle's, and the mixed form's gradient error against the FP64 one.
+  dot-product test against the CUDA tangent-linear model (``hx_traj_jvp``, also timed),
+  and the mixed form's gradient error against the FP64 one.  (The dot product against
+  the oracle's tangent-linear model is a GPU test, tests/test_gpu_adjoint.py.)
 
 ``--impl reference`` times that CPU implementation alone and prints its own line.
 Multi-GPU: the step does not shard here (one GPU per box), so N>1 runs N independent
@@ -56,28 +58,69 @@ MEASURED_PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
 FALLBACK_HBM_GBS = 6800.0
 
 
-# DRAM bytes (read + write) per launch and FP64-pipe active fraction measured by ncu at
-# ne16 L72 q10 (1536 elements; dram__bytes_read.sum + dram__bytes_write.sum and
-# sm__pipe_fp64_cycles_active of the third launch of each kernel), per form.  Traffic is
-# scaled to the run's size by the element count (levels and tracers fixed).
+# Per launch, measured by ncu at ne16 L72 q10 (1536 elements) over the launches of one
+# remap interval (profiles/launches_and_fp64_ne16.md gives the command): DRAM bytes read +
+# written (dram__bytes_read.sum + dram__bytes_write.sum) and FP64 floating-point
+# operations, DADD + DMUL + 2 DFMA thread instructions
+# (smsp__sass_thread_inst_executed_op_{dadd,dmul,dfma}_pred_on.sum), each averaged over
+# the kernel's launches in that interval.  Both are scaled to the run's size by the
+# element count (levels and tracers fixed).  A kernel that changes invalidates its row:
+# the table is re-captured with the kernels it describes.
 NCU_NE16 = {
-    "fp64": {"euler_aal_tracer": (473.5e6, 0.839), "caar_stage": (153.3e6, 0.863),
-             "hv_laplace2": (162.0e6, 0.818), "ppm_remap": (328.5e6, 0.850),
-             "euler_bih_post": (282.0e6, 0.863), "hv_laplace1": (77.4e6, 0.894),
-             "euler_bih_pre": (260.5e6, 0.912), "euler_dss_qdp": (399.9e6, 0.817),
-             "euler_qminmax": (283.2e6, 0.649)},
-    "mixed": {"euler_aal_tracer": (472.6e6, 0.374), "caar_stage": (151.5e6, 0.782),
-              "hv_laplace2": (151.6e6, 0.504), "ppm_remap": (328.5e6, 0.645),
-              "euler_dss_qdp": (399.9e6, 0.818), "euler_qminmax": (276.9e6, 0.138),
-              "euler_bih_post": (274.1e6, 0.479)},
+    "fp64": {"euler_aal_tracer": (473.5e6, None), "caar_stage": (153.3e6, None),
+             "hv_laplace2": (162.0e6, None), "ppm_remap": (328.5e6, None),
+             "euler_bih_post": (282.0e6, None), "hv_laplace1": (77.4e6, None),
+             "euler_bih_pre": (260.5e6, None), "euler_dss_qdp": (399.9e6, None),
+             "euler_qminmax": (283.2e6, None)},
+    "mixed": {"euler_aal_tracer": (472.6e6, None), "caar_stage": (151.5e6, None),
+              "hv_laplace2": (151.6e6, None), "ppm_remap": (328.5e6, None),
+              "euler_dss_qdp": (399.9e6, None), "euler_qminmax": (276.9e6, None),
+              "euler_bih_post": (274.1e6, None)},
 }
+NCU_NE16_ELEMENTS = 1536
 
 
-def ncu_traffic(form: str, kernel: str, E: int, Q: int):
+def ncu_row(form: str, kernel: str, E: int, Q: int):
+    """(DRAM bytes, FP64 FLOPs) per launch scaled to E elements, or (None, None)."""
     v = NCU_NE16.get(form, {}).get(kernel)
     if v is None or Q != 10:
         return None, None
-    return v[0] * E / 1536.0, v[1]
+    sc = E / NCU_NE16_ELEMENTS
+    return (v[0] * sc if v[0] is not None else None), (v[1] * sc if v[1] is not None else None)
+
+
+def measure_link(nbytes: int = 1 << 30, reps: int = 3):
+    """Host link rates of this machine: best of ``reps`` pinned -> device and device -> pinned
+    copies of ``nbytes`` (CUDA events on the copying stream), in GB/s."""
+    import torch
+    h = torch.empty(nbytes // 8, dtype=torch.float64, pin_memory=True)
+    d = torch.empty(nbytes // 8, dtype=torch.float64, device="cuda")
+    st = torch.cuda.Stream()
+    out = {}
+    with torch.cuda.stream(st):
+        for name, f in (("h2d_gbs", lambda: d.copy_(h, non_blocking=True)),
+                        ("d2h_gbs", lambda: h.copy_(d, non_blocking=True))):
+            best = None
+            for _ in range(reps):
+                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a.record(st)
+                f()
+                b.record(st)
+                b.synchronize()
+                ms = a.elapsed_time(b)
+                best = ms if best is None else min(best, ms)
+            out[name] = nbytes / (best * 1e-3) / 1e9
+    del h, d
+    return out
+
+
+def fp64_peak(lib_path: str):
+    """Measured FP64 FMA throughput of the device in TFLOP/s (hx_fp64_peak)."""
+    import ctypes
+    lib = ctypes.CDLL(lib_path)
+    v = ctypes.c_double(0.0)
+    rc = lib.hx_fp64_peak(ctypes.byref(v))
+    return v.value if rc == 0 else None
 
 
 def sypd(steps: int, seconds: float) -> float:
@@ -247,6 +290,7 @@ def run_gpu(args, rank, world):
         host_in = {k: pinned(state[k].shape, state[k]) for k in ("v", "T", "dp3d", "Qdp", "ps_v")}
         h2d = sum(a.nbytes for a in host_in.values())
         d2h = sum(a.nbytes for a in res.values())
+        link = measure_link()  # the host link as this run sees it, just before the e2e loop
         L.set_async_copies(True)
         L.stream_results(res)
         L.set_state(host_in)
@@ -270,12 +314,14 @@ def run_gpu(args, rank, world):
         te = _max_over_ranks(te, world)
         L.stream_results(None)
         L.set_async_copies(False)
-        print(f"[e2e {tag}] per interval: init_elements_states_c {1e3 * tp[0] / args.steps:.2f} ms, "
-              f"prim_run_subcycle_c {1e3 * tp[1] / args.steps:.2f} ms, cxx_push_results_to_f90 "
-              f"{1e3 * tp[2] / args.steps:.2f} ms", file=sys.stderr)
+        calls = {"init_elements_states_c_ms": 1e3 * tp[0] / args.steps,
+                 "prim_run_subcycle_c_ms": 1e3 * tp[1] / args.steps,
+                 "cxx_push_results_to_f90_ms": 1e3 * tp[2] / args.steps}
+        print(f"[e2e {tag}] per interval: " + ", ".join(f"{k[:-3]} {v:.2f} ms" for k, v in calls.items())
+              + f"; link h2d {link['h2d_gbs']:.1f} GB/s, d2h {link['d2h_gbs']:.1f} GB/s", file=sys.stderr)
         del keep
         out[tag] = dict(t=t, te=te, launches=launches, stats=stats, clocks=cs.summary(),
-                        h2d=h2d, d2h=d2h)
+                        h2d=h2d, d2h=d2h, link=link, calls=calls)
         if tag == "fp64":
             out["fp64_state_after"] = None
         L.finalize()
@@ -398,8 +444,6 @@ def run_adjoint(lib_path, dot_check=True):
     dev = lambda d: [torch.from_numpy(np.ascontiguousarray(d[k])).cuda() for k in keys]
     params = abi.SimParams(qsize=ADJ_QSIZE, nu=NU, rsplit=RSPLIT, hypervis_subcycle=HSUB,
                            nu_top=2.5e5)
-    if dot_check:
-        subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle")], check=True)
     res = {}
     grads = {}
     for precision, tag in ((0, "fp64"), (1, "mixed")):
@@ -468,17 +512,6 @@ def run_adjoint(lib_path, dot_check=True):
                 res["dot_product_gpu"] = dict(tlm_dot=lhs_gpu, adjoint_dot=rhs,
                                               rel_err=abs(lhs_gpu - rhs) / abs(lhs_gpu),
                                               tlm="CUDA tangent-linear model (hx_traj_jvp)")
-                O = abi.HxLibrary(os.path.join(ROOT, "oracle", "liboracle.so"))
-                O.init(mesh, hv, params, st, abort_on_error=True)
-                O.lib.hx_oracle_threads.restype = int
-                t0 = time.perf_counter()
-                O.traj_forward(x0, ADJ_STEPS, DT)
-                lhs = sum(float(np.vdot(v, dy[k])) for k, v in O.traj_jvp(dx).items())
-                res["dot_product"] = dict(tlm_dot=lhs, adjoint_dot=rhs, rel_err=abs(lhs - rhs) / abs(lhs),
-                                          tlm="CPU oracle (dual-number instantiation of its step), "
-                                              f"{O.lib.hx_oracle_threads()} threads, "
-                                              f"{time.perf_counter() - t0:.1f} s")
-                O.finalize()
         L.finalize()
     res["mixed_gradient_rel_err"] = {
         k: float(np.max(np.abs(grads["mixed"][k] - grads["fp64"][k])) / np.max(np.abs(grads["fp64"][k])))
@@ -509,18 +542,33 @@ def _max_over_ranks(x, world):
     return float(t.item())
 
 
-def roofline(stats, E, Q, rsize, steps):
+def roofline(stats, E, Q, rsize, steps, form="fp64", hbm_peak=None, fp64_peak_tflops=None):
+    """Per kernel: launches, CUDA-event time and share, algorithmic (field-pass) bytes per
+    launch and the GB/s they give with their fraction of the HBM peak; the ncu DRAM bytes
+    per launch; the FP64 FLOPs per launch (ncu instruction counts) and the TFLOP/s they
+    give with their fraction of the measured FP64 peak."""
     model = kernel_bytes(E, Q, rsize)
     total = sum(ms for _, _, ms in stats) or 1.0
     rows = []
     for name, launches, ms in stats:
         nb = model.get(name)
         per_launch = nb[1] / nb[0] if nb else None
+        t_launch = ms / launches * 1e-3 if launches else None
+        gbs = per_launch / t_launch / 1e9 if (per_launch and t_launch) else None
+        traffic, flops = ncu_row(form, name, E, Q)
+        tf = flops / t_launch / 1e12 if (flops and t_launch) else None
         rows.append(dict(kernel=name, launches=launches, total_ms=ms, share=ms / total,
-                         bytes_per_launch=per_launch,
-                         gbs=(per_launch / (ms / launches * 1e-3) / 1e9) if (nb and launches) else None))
+                         bytes_per_launch=per_launch, gbs=gbs,
+                         hbm_frac=gbs / hbm_peak if (gbs and hbm_peak) else None,
+                         dram_bytes_per_launch_ncu=traffic,
+                         fp64_flops_per_launch=flops, fp64_tflops=tf,
+                         fp64_frac=tf / fp64_peak_tflops if (tf and fp64_peak_tflops) else None))
     rows.sort(key=lambda r: -r["total_ms"])
     return rows
+
+
+def _rounded(r):
+    return {k: (round(v, 4) if isinstance(v, float) and abs(v) < 1e6 else v) for k, v in r.items()}
 
 
 def _oracle(mesh=None, state=None):
@@ -571,7 +619,7 @@ def main():
     ap.add_argument("--qsize", type=int, default=QSIZE, help="tracer count (profiling cases)")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint leg")
     ap.add_argument("--no-dot-check", action="store_true",
-                    help="skip the oracle tangent-linear dot-product check of the adjoint leg")
+                    help="skip the dot-product check of the adjoint leg")
     ap.add_argument("--only-adjoint", action="store_true",
                     help="run the adjoint leg alone and print its JSON (profiling runs)")
     ap.add_argument("--large", action="store_true",
@@ -642,45 +690,62 @@ def main():
                           "kernels": roofline(m["stats"], E, QSIZE, 8, args.steps)}))
         return
     f = out["fp64"]
-    rows = roofline(f["stats"], E, QSIZE, 8, args.steps)
     peak, peak_kind = _peaks()
+    from hommexx_gb300 import build as B
+    f64peak = fp64_peak(B.build())
+    rows = roofline(f["stats"], E, QSIZE, 8, args.steps, "fp64", peak, f64peak)
     top = rows[0]
-    achieved = top["gbs"] or 0.0
-    traffic, pipe_frac = ncu_traffic("fp64", top["kernel"], E, QSIZE)
+    # The binding roof of the top kernel: the FP64 pipe when its FP64 fraction is the
+    # larger, else HBM.
+    if top["fp64_frac"] is not None and top["fp64_frac"] > (top["hbm_frac"] or 0.0):
+        roof = {"bound": "fp64", "kernel": top["kernel"], "achieved": top["fp64_tflops"], "peak": f64peak,
+                "unit": "TFLOP/s", "frac": top["fp64_frac"],
+                "peak_source": "measured in this run (hx_fp64_peak: independent DFMA chains, full occupancy)",
+                "hbm": {"achieved": top["gbs"], "peak": peak, "unit": "GB/s", "frac": top["hbm_frac"],
+                        "peak_source": peak_kind}}
+    else:
+        roof = {"bound": "hbm", "kernel": top["kernel"], "achieved": top["gbs"], "peak": peak, "unit": "GB/s",
+                "frac": top["hbm_frac"], "peak_source": peak_kind, "fp64_peak_tflops": f64peak}
+    roof["traffic"] = top["dram_bytes_per_launch_ncu"]
+    roof["traffic_source"] = "ncu DRAM bytes per launch at ne16, scaled by elements"
+    roof["achieved_source"] = ("algorithmic bytes (field passes) or ncu FP64 FLOPs per launch over the "
+                               "kernel's CUDA-event launch time in this run")
     value = sypd(args.steps, f["t"]) * world
+    ms_dev = f["t"] / args.steps * 1e3
+    ms_e2e = f["te"] / args.steps * 1e3
     line = {
         "metric": "ne30L72 SYPD (FP64 preqx step)", "value": value, "unit": "SYPD",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": f["t"] / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+        "ms_per_step": ms_dev, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic seeded spherical-harmonic state",
         "config": config,
         "e2e": {"value": sypd(args.steps, f["te"]) * world, "unit": "SYPD",
                 "h2d_bytes_per_step": f["h2d"], "d2h_bytes_per_step": f["d2h"],
+                "ms_per_step": ms_e2e, "exposed_ms_per_step": ms_e2e - ms_dev,
+                "link": f["link"], "calls": f["calls"],
                 "copies": "init_elements_states_c / prim_run_subcycle_c / cxx_push_results_to_f90 "
                           "from host memory page-locked at allocation; time levels nm1/np1 and Qdp in "
                           "and the results out overlap the step (hx_set_async_copies, "
                           "hx_stream_results)"},
         "gpu_launches": f["launches"],
         "clocks": f["clocks"],
-        "roofline": {"bound": "hbm", "kernel": top["kernel"], "achieved": achieved, "peak": peak,
-                     "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
-                     "peak_source": peak_kind,
-                     "traffic_source": "ncu DRAM bytes per launch at ne16, scaled by elements",
-                     "fp64_pipe_active_ncu": pipe_frac,
-                     "note": "the FP64-form kernels are bound by the GB300 FP64 pipe "
-                             "(2 thread-instructions/SM/cycle), not by HBM"},
-        "kernels": [{k: (round(v, 4) if isinstance(v, float) else v) for k, v in r.items()} for r in rows],
+        "roofline": roof,
+        "kernels": [_rounded(r) for r in rows],
     }
     if "mixed" in out:
         mx = out["mixed"]
-        mrows = roofline(mx["stats"], E, QSIZE, 8, args.steps)
+        mrows = roofline(mx["stats"], E, QSIZE, 8, args.steps, "mixed", peak, f64peak)
+        ms_m = mx["t"] / args.steps * 1e3
         line["mixed"] = {"value": sypd(args.steps, mx["t"]) * world, "unit": "SYPD",
                          "speedup_vs_fp64": f["t"] / mx["t"],
                          "e2e": sypd(args.steps, mx["te"]) * world,
-                         "ms_per_step": mx["t"] / args.steps * 1e3,
-                         "top_kernel": {k: mrows[0][k] for k in ("kernel", "share", "gbs")},
-                         "kernels": [{k: (round(v, 4) if isinstance(v, float) else v)
-                                      for k, v in r.items()} for r in mrows],
+                         "e2e_ms_per_step": mx["te"] / args.steps * 1e3, "ms_per_step": ms_m,
+                         "e2e_calls": mx["calls"],
+                         "top_kernels": [{k: r[k] for k in ("kernel", "share", "gbs", "hbm_frac")}
+                                         for r in mrows[:3]],
+                         "interval_hbm_frac": (sum(v[1] for v in kernel_bytes(E, QSIZE, 8).values())
+                                               / (ms_m * 1e-3) / 1e9 / peak),
+                         "kernels": [_rounded(r) for r in mrows],
                          "clocks": mx["clocks"]}
         if "mixed_error" in out:
             line["mixed"]["error_vs_fp64"] = out["mixed_error"]

@@ -16,7 +16,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libhxgpu.so")
-SOURCES = ["hx_kernels.cu", "hx_adjoint.cu", "hx_tangent.cu", "hx_abi.cu", "hx_noalloc.cu", "hx_mesh.cu"]
+SOURCES = ["hx_kernels.cu", "hx_adjoint.cu", "hx_tangent.cu", "hx_abi.cu", "hx_noalloc.cu", "hx_mesh.cu", "hx_peak.cu"]
 
 
 def nvcc() -> str:

@@ -88,6 +88,8 @@ Timing g_tim;
 cudaStream_t g_stream = nullptr;
 // Copies that overlap the step (hx_set_async_copies, hx_stream_results) run on g_copy.
 cudaStream_t g_copy = nullptr;
+// The device the session's stream and arrays live on (set by initialize_hommexx_session).
+int g_dev = 0;
 
 void flush_timing() {
   if (g_tim.pending.empty()) return;
@@ -236,14 +238,13 @@ struct BackendT : Backend {
          *dpdiss_ave = 0, *dpdiss_bih = 0, *vn0 = 0;
   // scratch
   double *caar_out = 0, *bufA = 0, *bufB = 0, *vstar = 0, *dpdissk = 0, *fscr = 0, *qtens = 0, *qscr = 0;
-  double *qlim = 0, *qlim_tmp = 0, *dp0 = 0, *staging = 0, *rsp_d = 0, *rsp_noalloc = 0;
+  double *qlim = 0, *qlim_tmp = 0, *dp0 = 0, *staging = 0, *rsp_d = 0;
   double* gen_scr = 0;
   double* lapm = 0;  // FP64 form: dense weak Laplacian per element
   double *fm = 0, *ft = 0, *fq = 0;  // CAM forcing, Fortran layouts (allocated on first push)
   double *phis_d = 0, *diag_d = 0;   // FP64 phis; diagnostics scratch (allocated on first use)
-  cudaEvent_t ev_qdp_in = nullptr, ev_mark = nullptr, ev_lvl[NTL] = {};
+  cudaEvent_t ev_qdp_in = nullptr, ev_mark = nullptr, ev_dyn_in = nullptr;
   bool qdp_pending = false;   // Qdp still streaming in on g_copy
-  bool lvl_pending[NTL] = {}; // a dynamics level still streaming in on g_copy
   bool stream_last = false;   // the next prim_step is the interval's last
   int *tab_cnt = 0, *tab_src = 0, *nbr = 0, *invalid = 0;
   int* h_invalid = nullptr;
@@ -258,15 +259,14 @@ struct BackendT : Backend {
     void* ptrs[] = {D, Dinv, metinv, metdet, spheremp, rspheremp, mp, fcor, phis, tensorvisc, vec_sph2cart,
                     v, T, dp, ps_v, qdp, Qc, phi, omega_p, eta, derived_dp, divdp, divdp_proj, dpdiss_ave,
                     dpdiss_bih, vn0, caar_out, bufA, bufB, vstar, dpdissk, fscr, qtens, qscr, qlim, qlim_tmp,
-                    dp0, staging, rsp_d, rsp_noalloc, gen_scr, tab_cnt, tab_src, nbr, invalid, sp_d, lapm,
+                    dp0, staging, rsp_d, gen_scr, tab_cnt, tab_src, nbr, invalid, sp_d, lapm,
                     fm, ft, fq, phis_d, diag_d};
     for (void* p : ptrs)
       if (p) cudaFree(p);
     if (h_invalid) cudaFreeHost(h_invalid);
     if (ev_qdp_in) cudaEventDestroy(ev_qdp_in);
     if (ev_mark) cudaEventDestroy(ev_mark);
-    for (cudaEvent_t ev : ev_lvl)
-      if (ev) cudaEventDestroy(ev);
+    if (ev_dyn_in) cudaEventDestroy(ev_dyn_in);
     free_traj();
   }
 
@@ -299,7 +299,7 @@ struct BackendT : Backend {
     ck(cudaMallocHost(&h_invalid, 2 * sizeof(int)), "cudaMallocHost");
     ck(cudaEventCreateWithFlags(&ev_qdp_in, cudaEventDisableTiming), "cudaEventCreate");
     ck(cudaEventCreateWithFlags(&ev_mark, cudaEventDisableTiming), "cudaEventCreate");
-    for (cudaEvent_t& ev : ev_lvl) ck(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "cudaEventCreate");
+    ck(cudaEventCreateWithFlags(&ev_dyn_in, cudaEventDisableTiming), "cudaEventCreate");
     wk = Work{v, T, dp, phi, dpdiss_ave, dpdiss_bih, ps_v};
   }
 
@@ -328,8 +328,6 @@ struct BackendT : Backend {
     to_dev(sp_d, a[4], (size_t)E * 16);
     to_dev(phis_d, a[8], (size_t)E * 16);
     to_dev(rsp_d, a[5], (size_t)E * 16);
-    if (!rsp_noalloc) rsp_noalloc = dalloc<double>((size_t)E * 16);
-    ck(cudaMemcpyAsync(rsp_noalloc, a[5], (size_t)E * 16 * sizeof(double), cudaMemcpyHostToDevice, g_stream), "H2D");
     if (!consthv) {
       to_dev_R(tensorvisc, a[9], (size_t)E * 64);
       to_dev_R(vec_sph2cart, a[10], (size_t)E * 96);
@@ -342,24 +340,19 @@ struct BackendT : Backend {
     const size_t n3 = N3();
     copies_ready();
     if (s.async_copies) {
-      // Everything streams in on g_copy, after the work already queued on g_stream: the
-      // dynamics level by level, n0 (with ps_v) first, which g_stream waits for at once;
-      // nm1 and np1, which the next interval writes before it reads them, are waited for
-      // just before their first writer (the DSS of the Caar stage that targets them);
-      // then Qdp, waited for by its first reader.
+      // Everything streams in on g_copy, after the work already queued on g_stream, as
+      // whole contiguous arrays (one copy each; strided copies of single time levels ran
+      // at a fraction of the link rate on some hosts): the dynamics state and ps_v first,
+      // which g_stream waits for at once (dp3d(n0) is recomputed from ps_v, but the other
+      // time levels must land before the interval writes them), then Qdp, waited for by
+      // its first reader.
       stream_mark();
-      const int order[NTL] = {s.tl.n0, s.tl.nm1, s.tl.np1};
-      for (int lvl : order) {
-        level_in(v, hv, (size_t)NLEV * 32, lvl);
-        level_in(T, hT, (size_t)NLEV * 16, lvl);
-        level_in(dp, hdp, (size_t)NLEV * 16, lvl);
-        if (lvl == s.tl.n0)
-          ck(cudaMemcpyAsync(ps_v, hps, (size_t)E * NTL * 16 * sizeof(double), cudaMemcpyHostToDevice, g_copy),
-             "H2D ps");
-        ck(cudaEventRecord(ev_lvl[lvl], g_copy), "cudaEventRecord");
-        lvl_pending[lvl] = true;
-      }
-      level_ready(s.tl.n0);
+      ck(cudaMemcpyAsync(ps_v, hps, (size_t)E * NTL * 16 * sizeof(double), cudaMemcpyHostToDevice, g_copy), "H2D ps");
+      ck(cudaMemcpyAsync(T, hT, n3 * NTL * sizeof(double), cudaMemcpyHostToDevice, g_copy), "H2D T");
+      ck(cudaMemcpyAsync(v, hv, n3 * NTL * 2 * sizeof(double), cudaMemcpyHostToDevice, g_copy), "H2D v");
+      ck(cudaMemcpyAsync(dp, hdp, n3 * NTL * sizeof(double), cudaMemcpyHostToDevice, g_copy), "H2D dp3d");
+      ck(cudaEventRecord(ev_dyn_in, g_copy), "cudaEventRecord");
+      ck(cudaStreamWaitEvent(g_stream, ev_dyn_in, 0), "cudaStreamWaitEvent");
       if (Q > 0) {
         ck(cudaMemcpyAsync(qdp, hq, n3 * QTL * Q * sizeof(double), cudaMemcpyHostToDevice, g_copy), "H2D qdp");
         ck(cudaEventRecord(ev_qdp_in, g_copy), "cudaEventRecord");
@@ -374,22 +367,8 @@ struct BackendT : Backend {
       ck(cudaMemcpyAsync(qdp, hq, n3 * QTL * Q * sizeof(double), cudaMemcpyHostToDevice, g_stream), "H2D qdp");
     ck(cudaMemcpyAsync(ps_v, hps, (size_t)E * NTL * 16 * sizeof(double), cudaMemcpyHostToDevice, g_stream), "H2D ps");
   }
-  // host -> device copy on g_copy of level lvl of a field laid out [E][NTL][block]
-  void level_in(double* dev, const double* host, size_t block, int lvl) {
-    const size_t w = block * sizeof(double), pitch = w * NTL;
-    ck(cudaMemcpy2DAsync(dev + (size_t)lvl * block, pitch, host + (size_t)lvl * block, pitch, w, E,
-                         cudaMemcpyHostToDevice, g_copy),
-       "H2D level");
-  }
-  // orders g_stream after the copy of dynamics level lvl, if it is still streaming in
-  void level_ready(int lvl) {
-    if (lvl < 0 || lvl >= NTL || !lvl_pending[lvl]) return;
-    ck(cudaStreamWaitEvent(g_stream, ev_lvl[lvl], 0), "cudaStreamWaitEvent");
-    lvl_pending[lvl] = false;
-  }
 
   void copies_ready() override {
-    for (int lvl = 0; lvl < NTL; ++lvl) level_ready(lvl);
     if (!qdp_pending) return;
     ck(cudaStreamWaitEvent(g_stream, ev_qdp_in, 0), "cudaStreamWaitEvent");
     qdp_pending = false;
@@ -471,8 +450,8 @@ struct BackendT : Backend {
   bool dss_view(const int** c, const int** sr, const double** r) const {
     *c = tab_cnt;
     *sr = tab_src;
-    *r = rsp_noalloc;
-    return tab_cnt != nullptr && rsp_noalloc != nullptr;
+    *r = rsp_d;
+    return tab_cnt != nullptr && rsp_d != nullptr;
   }
 
   // Operators built from the metric and the derivative matrix, once both are on the
@@ -515,12 +494,8 @@ struct BackendT : Backend {
     a.dt = dt; a.eta_ave_w = w; a.p_top = s.hyai[0] * s.ps0;
     a.rk_combine = combine; a.n0orig = n0orig;
     a.rsplit = s.prm.rsplit; a.eta_acc = eta;
-    level_ready(nm1);
-    level_ready(n0);
-    level_ready(n0orig);
     launch_caar<R>(a, E, g_stream);
     post("caar");
-    level_ready(np1);
     launch_dss_state(E, caar_out, wk.v, wk.T, wk.dp, np1, rsp_d, table(), g_stream);
     post("dss_caar");
   }
@@ -535,7 +510,6 @@ struct BackendT : Backend {
   }
 
   void hypervis(int np1, double dt, double w) override {
-    for (int lvl = 0; lvl < NTL; ++lvl) level_ready(lvl);
     hypervis_cycles(np1, dt, w, s.prm.hypervis_subcycle);
   }
 
@@ -845,6 +819,19 @@ struct BackendT : Backend {
     ck(e3, "restart checksum");
     return h;
   }
+  // The same checksum on the host over n whole records (rw words each) whose first word
+  // has file word index k0 (the device kernel's sum, word for word).
+  static unsigned long long host_restart_checksum(const unsigned long long* w, int n, size_t rw, size_t k0) {
+    unsigned long long acc = 0;
+    const size_t total = (size_t)n * rw;
+    for (size_t j = 0; j < total; ++j) {
+      unsigned long long z = w[j] + (unsigned long long)(k0 + j + 1) * 0x9E3779B97F4A7C15ull;
+      z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+      z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+      acc += z ^ (z >> 31);
+    }
+    return acc;
+  }
   // Two pinned host buffers of up to 256 MiB of whole element records, and the events
   // that say when the copies from/into each have finished.
   struct Staging {
@@ -940,29 +927,39 @@ struct BackendT : Backend {
       if (g.dev == phis_d) break;
       phis_off += g.words * 8;
     }
-    {
-      Staging st;
-      st.init(rb, E);
-      const int nchunk = (E + st.per - 1) / st.per;
-      for (int k = 0; k < nchunk; ++k) {
-        const int b = k & 1, e0 = k * st.per, n = std::min(st.per, E - e0);
-        if (k >= 2) ck(cudaEventSynchronize(st.ev[b]), "restart H2D");
-        if (std::fread(st.buf[b], rb, n, f.f) != (size_t)n) fail(HX_ERR_IO, "'" + path + "': short read");
-        for (int i = 0; i < n; ++i)
-          std::memcpy(&phis_h[(size_t)(e0 + i) * 16], st.buf[b] + (size_t)i * rb + phis_off, 16 * sizeof(double));
-        size_t off = 0;
-        for (const Seg& g : segs) {
-          if (g.words) {
-            const size_t w = g.words * 8;
-            ck(cudaMemcpy2DAsync(g.dev + (size_t)e0 * g.words, w, st.buf[b] + off, rb, w, n, cudaMemcpyHostToDevice,
-                                 g_stream), "restart H2D");
-          }
-          off += g.words * 8;
-        }
-        ck(cudaEventRecord(st.ev[b], g_stream), "cudaEventRecord");
-      }
+    Staging st;
+    st.init(rb, E);
+    const int nchunk = (E + st.per - 1) / st.per;
+    // First pass: the checksum on the host, so that a damaged or truncated file leaves
+    // the session's state untouched.
+    const long data0 = std::ftell(f.f);
+    unsigned long long sum = 0;
+    for (int k = 0; k < nchunk; ++k) {
+      const int e0 = k * st.per, n = std::min(st.per, E - e0);
+      if (std::fread(st.buf[0], rb, n, f.f) != (size_t)n) fail(HX_ERR_IO, "'" + path + "': short read");
+      sum += host_restart_checksum(reinterpret_cast<const unsigned long long*>(st.buf[0]), n, rw, (size_t)e0 * rw);
     }
-    if (restart_checksum(segs) != h.checksum) fail(HX_ERR_IO, "'" + path + "': checksum mismatch");
+    if (sum != h.checksum) fail(HX_ERR_IO, "'" + path + "': checksum mismatch");
+    // Second pass: the verified records into the device state.
+    if (data0 < 0 || std::fseek(f.f, data0, SEEK_SET) != 0) fail(HX_ERR_IO, "'" + path + "': seek failed");
+    for (int k = 0; k < nchunk; ++k) {
+      const int b = k & 1, e0 = k * st.per, n = std::min(st.per, E - e0);
+      if (k >= 2) ck(cudaEventSynchronize(st.ev[b]), "restart H2D");
+      if (std::fread(st.buf[b], rb, n, f.f) != (size_t)n) fail(HX_ERR_IO, "'" + path + "': short read");
+      for (int i = 0; i < n; ++i)
+        std::memcpy(&phis_h[(size_t)(e0 + i) * 16], st.buf[b] + (size_t)i * rb + phis_off, 16 * sizeof(double));
+      size_t off = 0;
+      for (const Seg& g : segs) {
+        if (g.words) {
+          const size_t w = g.words * 8;
+          ck(cudaMemcpy2DAsync(g.dev + (size_t)e0 * g.words, w, st.buf[b] + off, rb, w, n, cudaMemcpyHostToDevice,
+                               g_stream), "restart H2D");
+        }
+        off += g.words * 8;
+      }
+      ck(cudaEventRecord(st.ev[b], g_stream), "cudaEventRecord");
+    }
+    ck(cudaStreamSynchronize(g_stream), "restart H2D");
     to_dev_R(phis, phis_h.data(), phis_h.size());
     s.tl.nm1 = h.nm1 - 1; s.tl.n0 = h.n0 - 1; s.tl.np1 = h.np1 - 1;
     s.tl.nstep = h.nstep; s.tl.nstep0 = h.nstep0;
@@ -1434,15 +1431,19 @@ Backend& B() {
 
 }  // namespace
 
+// Set-up of the no-allocation DSS on a device (hx_noalloc.cu).
+cudaError_t noalloc_setup(int dev);
+
 // Session view used by the no-allocation DSS entry point (hx_noalloc.cu).
 bool session_dss_view(int* E, const int** cnt, const int** src, const double** rsp,
-                      cudaStream_t* stream) {
+                      cudaStream_t* stream, int* dev) {
   if (!g_s || !g_s->be || !g_stream) return false;
   const bool ok = g_s->precision == 0
                       ? static_cast<BackendT<double>&>(*g_s->be).dss_view(cnt, src, rsp)
                       : static_cast<BackendT<float>&>(*g_s->be).dss_view(cnt, src, rsp);
   *E = g_s->E;
   *stream = g_stream;
+  *dev = g_dev;
   return ok;
 }
 
@@ -1461,6 +1462,7 @@ void initialize_hommexx_session(void) {
       ck(cudaGetDeviceCount(&n), "cudaGetDeviceCount");
       if (n < 1) fail(HX_ERR_CUDA, "no CUDA device");
       ck(cudaSetDevice(0), "cudaSetDevice");
+      g_dev = 0;
       ck(cudaStreamCreateWithFlags(&g_stream, cudaStreamNonBlocking), "cudaStreamCreate");
       ck(cudaStreamCreateWithFlags(&g_copy, cudaStreamNonBlocking), "cudaStreamCreate");
       g_tim.pool.resize(8192);
@@ -1619,6 +1621,8 @@ void init_boundary_exchanges_c(void) {
     } else {
       static_cast<BackendT<float>&>(B()).set_tables(cnt, src, nb);
     }
+    // hx_dss_noalloc's fixed scratch is made resident now, while allocation is allowed
+    ck(noalloc_setup(g_dev), "hx_dss_noalloc set-up");
   });
 }
 

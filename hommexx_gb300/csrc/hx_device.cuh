@@ -403,21 +403,44 @@ template <typename R> __device__ __forceinline__ R rel_hw(double x) {
   else return x;
 }
 
-// 1/x in FP64 from the approximate FP32 reciprocal of x (__fdividef, within 2 ulp)
-// refined by two Newton-Raphson steps r <- r + r (1 - x r), each of which squares the
-// relative error (about 2^-22 -> 2^-44 -> below one ulp of the result); rf returns the
-// FP32 reciprocal.  For x of magnitude 2^-125 .. 2^125; within one ulp of 1.0 / x.
+// x as a float with the mantissa truncated to 23 bits (relative error below 2^-23), on
+// the integer pipe: the exponent rebiased and the top mantissa bits moved, for |x| in
+// the float normal range, else the hardware conversion.  A seed for reciprocals, whose
+// Newton refinement removes the truncation.
+__device__ __forceinline__ float d2f_seed(double x) {
+  const unsigned hi = (unsigned)__double2hiint(x);
+  const int e = (int)((hi >> 20) & 0x7FFu) - 896;
+  if (e <= 0 || e >= 255) return __double2float_rn(x);
+  const unsigned lo = (unsigned)__double2loint(x);
+  return __uint_as_float((hi & 0x80000000u) | ((unsigned)e << 23) | ((hi & 0xFFFFFu) << 3) | (lo >> 29));
+}
+
+// 2 x, exact, on the integer pipe (the exponent field incremented) for normal x below
+// 2^1022 in magnitude; zeros, subnormals and larger values take the FP64 product.
+__device__ __forceinline__ double dtwice(double x) {
+  const long long b = __double_as_longlong(x);
+  const int e = (int)((b >> 52) & 0x7FF);
+  if (e == 0 || e >= 0x7FE) return x * 2.0;
+  return __longlong_as_double(b + (1LL << 52));
+}
+
+// 1/x in FP64 from the approximate FP32 reciprocal of x (__fdividef of the truncated
+// float image, within 3 ulp of a float) refined by two Newton-Raphson steps
+// r <- r + r (1 - x r), each of which squares the relative error (below 3 * 2^-23 ->
+// 2^-42 -> below one ulp of the result); rf returns the FP32 reciprocal.  For x of magnitude
+// 2^-125 .. 2^125; within one ulp of 1.0 / x.
 __device__ __forceinline__ double rcp_newton(double x, float& rf) {
-  rf = __fdividef(1.0f, (float)x);
+  rf = __fdividef(1.0f, d2f_seed(x));
   double r = f2d(rf);  // exact; on the integer pipe
   r = fma(r, fma(-x, r, 1.0), r);
   return fma(r, fma(-x, r, 1.0), r);
 }
 
-// One Newton-Raphson step from the same seed: relative error below 2^-42 (about
-// 2.3e-13), for the mixed form's FP64 integrands next to FP32 operators.
+// One Newton-Raphson step from the same seed: relative error below 2^-42 (the seed's
+// 3 * 2^-23 squared; about 2.3e-13), for the mixed form's FP64 integrands next to FP32
+// operators.
 __device__ __forceinline__ double rcp_newton1(double x, float& rf) {
-  rf = __fdividef(1.0f, (float)x);
+  rf = __fdividef(1.0f, d2f_seed(x));
   const double r = f2d(rf);
   return fma(r, fma(-x, r, 1.0), r);
 }

@@ -108,48 +108,46 @@ __global__ void __launch_bounds__(LG * 16) k_caar(CaarArgs<R> a) {
   // ---- phase B: pressure, geopotential, omega integral (double) ----
   if (tid < 128) {
     const int col = tid >> 3, seg = tid & 7, l0 = seg * 9;
-    // pressure: p_k = p_{k-1} + (dp_{k-1} + dp_k)/2, p_{-1} = hyai0 ps0, dp_{-1} = 0
-    double prev = seg == 0 ? 0.0 : s_dp[(l0 - 1) * SROW + col];
-    double tot = 0.0, tp[9];  // the segment's terms, summed again below in the same order
+    // pressure: p_k = p_{k-1} + (dp_{k-1} + dp_k)/2, p_{-1} = hyai0 ps0, dp_{-1} = 0, formed as
+    // p_k = c_k + dp_k / 2 with c_k = hyai0 ps0 + sum_{j<k} dp_j
+    double tot = 0.0;
 #pragma unroll
-    for (int k = 0; k < 9; ++k) {
-      const double d = s_dp[(l0 + k) * SROW + col];
-      tp[k] = 0.5 * (prev + d);
-      tot += tp[k];
-      prev = d;
-    }
-    double pr = a.p_top + seg_excl_prefix(tot, seg);
+    for (int k = 0; k < 9; ++k) tot += s_dp[(l0 + k) * SROW + col];
+    double c = a.p_top + seg_excl_prefix(tot, seg);
     double r[9];
+    constexpr double kHalfR = 0.5 * kRgas;
 #pragma unroll
     for (int k = 0; k < 9; ++k) {
       const double d = s_dp[(l0 + k) * SROW + col];
-      pr = pr + tp[k];
+      const double pr = fma(0.5, d, c);
+      c += d;
       double rp;
+      float rf;
       if constexpr (kF32<R>) {  // one Newton step (2^-42); the FP32 reciprocal serves phase C
-        float rf;
         rp = rcp_newton1(pr, rf);
         f_rp[(l0 + k) * SROW + col] = rf;
-      } else {
-        rp = 1.0 / pr;
+      } else {  // within one ulp of 1 / p
+        rp = rcp_newton(pr, rf);
         s_rp[(l0 + k) * SROW + col] = rp;
       }
       s_p[(l0 + k) * SROW + col] = pr;
       double tvk;
       if (own_tv) tvk = s_tv[(l0 + k) * SROW + col];
       else tvk = a.T[sN0 + (l0 + k) * 16 + col];
-      r[k] = kRgas * tvk * (d * 0.5 * rp);
+      r[k] = kHalfR * tvk * d * rp;  // R T_v dp / (2 p)
     }
-    // geopotential: phi_k = phis + 2 sum_{j>k} r_j + r_k
+    // geopotential: phi_k = phis + 2 sum_{j>k} r_j + r_k, with q = phis + 2 sum_{j>k} r_j
+    // carried down the segment (the doubling is exact, on the integer pipe)
     double rt = 0.0;
 #pragma unroll
     for (int k = 0; k < 9; ++k) rt += r[k];
-    double integ = seg_excl_suffix(rt, seg);
     const double phis = dbl_hw(a.m.phis[(size_t)e * 16 + col]);
+    double q = fma(2.0, seg_excl_suffix(rt, seg), phis);
     double* phig = a.phi + (size_t)e * NLEV * 16;
 #pragma unroll
     for (int k = 8; k >= 0; --k) {
-      const double ph = phis + 2.0 * integ + r[k];
-      integ = integ + r[k];
+      const double ph = q + r[k];
+      q += dtwice(r[k]);
       s_dp[(l0 + k) * SROW + col] = ph;  // dp no longer needed: holds phi now
       phig[(l0 + k) * 16 + col] = ph;
     }
@@ -198,10 +196,15 @@ __global__ void __launch_bounds__(LG * 16) k_caar(CaarArgs<R> a) {
       w = a.v[vN0 + l * 32 + 16 + p];
       div = s_div[l * SROW + p];
     }
-    R gp0, gp1;
-    gradient_sphere(t, m, rel<R>(pd), gp0, gp1);
+    // x1 and x2 derivatives of p and T; v . grad s = a0 ds/dx1 + a1 ds/dx2 with
+    // (a0, a1) = (Dinv / rearth)^T v, formed once for both
+    const R pr_ = rel<R>(pd);
+    const R p0 = t.ddx(pr_), p1 = t.ddy(pr_);
     const double td = a.T[sN0 + l * 16 + p];
-    const R vgp = u * gp0 + w * gp1;
+    const R tr_ = rel<R>(td);
+    const R T0 = t.ddx(tr_), T1 = t.ddy(tr_);
+    const R a0 = m.gr00 * u + m.gr10 * w, a1 = m.gr01 * u + m.gr11 * w;
+    const R vgp = a0 * p0 + a1 * p1;
     const R omega = (vgp - (cvt<R>(s_om[l * SROW + p]) + R(0.5) * div)) * rp;
     if (a.eta_ave_w != 0.0) a.omega_p[((size_t)e * NLEV + l) * 16 + p] += dbl_hw(eta * omega);
     // time level "nm1" (RK combine of stage 5 fused here), in double
@@ -244,30 +247,31 @@ __global__ void __launch_bounds__(LG * 16) k_caar(CaarArgs<R> a) {
       if (a.eta_ave_w != 0.0) a.eta_acc[((size_t)e * NLEV + l) * 16 + p] += a.eta_ave_w * el;
     }
     // temperature (compute_temperature_np1)
-    R gt0, gt1;
-    gradient_sphere(t, m, rel<R>(td), gt0, gt1);
     R tv;
     if (own_tv) tv = cvt<R>(s_tv[l * SROW + p]);
     else tv = cvt<R>(td);
-    const R vgt = u * gt0 + w * gt1;
-    const R ttens = (-tva - vgt) + R(kKappa) * tv * omega;
+    const R vgt = a0 * T0 + a1 * T1;
+    R ttens = R(kKappa) * tv * omega - vgt;
+    if (a.rsplit == 0) ttens -= tva;
     // Conversions on the integer pipe (dbl, and in phase C cvt / rel) relieve the FP64
     // pipe this kernel is bound by (a hardware double -> float conversion takes that pipe
     // like an FP64 add).  Phase A keeps the hardware conversions: there they follow the
     // global loads, and the integer form measured slower (9.2 vs 8.4 ms per ne30
     // interval), while in phase C it measured faster (8.2 vs 8.4 ms).
     const double tnew = spd * (dbl(ttens * dt) + tm);
-    // velocity (compute_velocity_np1 with compute_energy_grad)
+    // velocity (compute_velocity_np1 with compute_energy_grad): grad(KE + phi) +
+    // R T_v / p grad p = (Dinv / rearth) (dE/dx + rr dp/dx) with rr = R T_v / p
     const R rr = R(kRgas) * (tv * rp);
-    R eg0 = rr * gp0, eg1 = rr * gp1;
     const R ephi = R(0.5) * (u * u + w * w) + rel<R>(s_dp[l * SROW + p]);
-    R ge0, ge1;
-    gradient_sphere(t, m, ephi, ge0, ge1);
-    eg0 += ge0;
-    eg1 += ge1;
+    const R sx = rr * p0 + t.ddx(ephi), sy = rr * p1 + t.ddy(ephi);
+    R eg0 = m.gr00 * sx + m.gr01 * sy, eg1 = m.gr10 * sx + m.gr11 * sy;
     const R vort = vorticity_sphere(t, m, u, w) + fcor;
-    eg0 = -eg0 + (-vva0 + w * vort);
-    eg1 = -eg1 + (-vva1 - u * vort);
+    eg0 = w * vort - eg0;
+    eg1 = -(u * vort) - eg1;
+    if (a.rsplit == 0) {
+      eg0 -= vva0;
+      eg1 -= vva1;
+    }
     const double vn0_ = spd * (dbl(eg0 * dt) + vm0);
     const double vn1_ = spd * (dbl(eg1 * dt) + vm1);
     // dp3d (compute_dp3d_np1, eta_dot_dpdn = 0 for rsplit > 0)
@@ -1129,86 +1133,133 @@ __global__ void __launch_bounds__(EQ_THREADS) k_dss_from_copy(int nf, double* ba
 }
 
 // ======================================================================================
-// PPM vertical remap (RemapFunctor + PpmVertRemap, rsplit > 0), one CTA per column.
+// PPM vertical remap (RemapFunctor + PpmVertRemap), four columns per warp.
 // ======================================================================================
-constexpr int RCOLS = 4;            // columns (warps) per CTA
-constexpr int RT = RCOLS * 32;
-// Shared-memory slots of one column (doubles).
-constexpr int R_D = 0;                 // D[-2 .. 73]  (source thickness, ghosts)
-constexpr int R_PIO = R_D + 76;        // pio[0 .. 73]
-constexpr int R_PIN = R_PIO + 74;      // pin[0 .. 72]
-constexpr int R_Z2 = R_PIN + 74;       // z2[0 .. 71]
-constexpr int R_KID = R_Z2 + 72;       // kid[0 .. 71] (ints, 36 doubles)
-constexpr int R_TGT = R_KID + 36;      // target thickness
-constexpr int R_G = R_TGT + 72;        // ppmdx grids g[10][74]
-constexpr int R_A = R_G + 740;         // cell means A[-2 .. 73]
-constexpr int R_MASS = R_A + 76;       // mass[0 .. 73]
-constexpr int R_DMA = R_MASS + 74;     // dma[0 .. 73]
-constexpr int R_AI = R_DMA + 74;       // ai[0 .. 72]
-constexpr int R_COEF = R_AI + 74;      // coef[3][72]
-constexpr int R_RD = R_COEF + 216;     // 1 / D[0 .. 71]
-constexpr int R_END = R_RD + 72;
-// The mixed form's float g[10][74], z2[72], 1/D[72] and delta[-1 .. 73] (959 floats) use
-// the region of the double g (740 doubles), which that form does not store.
-static_assert(740 + 72 + 72 + 1 + 74 <= 2 * 740, "FP32 grid arrays exceed the double grid region");
-// doubles per column
-template <typename R> constexpr int r_col() { return R_END; }
+// A CTA is one warp holding four columns: lane (c = lane / 8, s = lane % 8) works on
+// column c, owns its levels 9s .. 9s+8 (every lane busy in the level work; the column
+// scans are 8-lane segmented shuffles) and its interfaces j = s, s+8, ..., s+72 of the
+// grid and reconstruction work (74 interfaces on 80 lane slots).  Phases are separated
+// by __syncwarp only.  Loads and stores of a level touch the four columns' consecutive
+// points, so every 32-byte sector fetched is used.
+constexpr int RCOLS = 4;  // columns per CTA
+constexpr int RT = 32;    // threads per CTA
+constexpr int RLV = 9;    // levels per lane
+constexpr int RNI = 10;   // interface slots per lane (j = s + 8 i)
+// Shared memory of one column, in doubles.  The reconstruction arrays hold R (double in
+// the FP64 form, float in the mixed form, two to a double); the mixed form adds the FP32
+// neighbour differences of v and T and FP32 reciprocals of the source thickness.
+template <typename R>
+struct RemapLayout {
+  static constexpr int RW = kF32<R> ? 2 : 1;
+  static constexpr int D = 0;                           // D[-2 .. 73], source thickness with ghosts
+  static constexpr int PIO = D + 76;                    // pio[0 .. 73]
+  static constexpr int PIN = PIO + 74;                  // pin[0 .. 72]
+  static constexpr int RDI = PIN + 74;                  // 1 / D[0 .. 71]
+  static constexpr int MASS = RDI + 72;                 // mass[0 .. 73]
+  static constexpr int A = MASS + 74;                   // cell means A[-2 .. 73], double
+  static constexpr int G = A + 76;                      // combined grid weights [5][74], R
+  static constexpr int DMA = G + 5 * 74 / RW;           // slopes dma[0 .. 73], R
+  static constexpr int AI = DMA + 74 / RW;              // edge values ai[0 .. 72], R
+  static constexpr int COEF = AI + 74 / RW;             // parabola coefficients [3][72], R
+  static constexpr int DLF = COEF + 216 / RW;           // mixed: df[-1 .. 73], float
+  static constexpr int RDF = DLF + (kF32<R> ? 38 : 0);  // mixed: 1 / D[0 .. 71], float
+  static constexpr int END = RDF + (kF32<R> ? 36 : 0);
+};
 
-// compute_ppm and the monotone parabola coefficients (PpmRemap.hpp:202-353) for one
-// variable of one column in T: slopes dma (j in 0 .. 73), edge values ai (j in 0 .. 72),
-// coefficients coef[3][72].  A has its ghost cells; g holds the grid weights [10][74].
+// (ar - cm) (cm - al) > 0, the parabola's monotonicity test: FP32 as is; FP64 as exact
+// comparisons on the integer pipe (zeros of either sign compare equal).
+__device__ __forceinline__ long long dkey0(double x) {
+  const long long k = dkey(x);
+  return k == -1 ? 0 : k;  // -0 -> +0
+}
+template <typename T> __device__ __forceinline__ bool monotone(T al, T cm, T ar) {
+  return (ar - cm) * (cm - al) > T(0);
+}
+template <> __device__ __forceinline__ bool monotone<double>(double al, double cm, double ar) {
+  const long long kl = dkey0(al), kc = dkey0(cm), kr = dkey0(ar);
+  return (kr > kc && kc > kl) || (kr < kc && kc < kl);
+}
+// The slope limiter min(|da|, |2 y|, |2 x|) with the sign of da: FP32 as is; FP64 on the
+// integer pipe, with min(|2x|, |2y|) formed as 2 min(|x|, |y|) (exact, dtwice).
+template <typename T> __device__ __forceinline__ T slope_limit(T da, T x, T y) {
+  return min3abs_signed(da, T(2) * y, T(2) * x, da);
+}
+template <> __device__ __forceinline__ double slope_limit<double>(double da, double x, double y) {
+  const long long m = 0x7fffffffffffffffLL;
+  const double t = dtwice(__longlong_as_double(kmin(__double_as_longlong(x) & m, __double_as_longlong(y) & m)));
+  const long long k = kmin(__double_as_longlong(da) & m, __double_as_longlong(t));
+  return __longlong_as_double(k | (__double_as_longlong(da) & ~m));
+}
+// A negative or NaN layer thickness (x < 0 or isnan(x)), on the integer pipe.
+__device__ __forceinline__ bool bad_thickness(double x) {
+  const long long b = __double_as_longlong(x);
+  return (b < 0 && (b << 1) != 0) || b > 0x7ff0000000000000LL;
+}
+
+// compute_ppm at this lane's interfaces (PpmRemap.hpp:202-266): slopes dma[j]
+// (j = 0 .. 73) and edge values ai[j] (j = 0 .. 72) of cell means A (ghosts included),
+// with the grid weights combined per interface (k1 = g0 g1, k2 = g0 g2, h1 = g3 + g4 g5,
+// h2 = g4 g8, h3 = g4 g9):
+//   dma_j = limit(k1 (A_j - A_j-1) + k2 (A_j-1 - A_j-2)) if A_j-1 lies between its neighbours
+//   ai_j  = A_j-1 + h1 (A_j - A_j-1) - h2 dma_j+1 + h3 dma_j.
 template <typename T>
-__device__ __forceinline__ void ppm_coefs(int lane, bool own, int l0, int remap_alg, const T* A,
-                                          const T* g, T* dma, T* ai, T* coef) {
-  if (lane < 25) {
+__device__ __forceinline__ void ppm_interfaces(int s, const T* A, const T* g, T* dma, T* ai) {
+  T d1[RNI];
 #pragma unroll
-    for (int k3 = 0; k3 < 3; ++k3) {
-      const int j = 3 * lane + k3;
-      if (j < NLEV + 2) {
-        const T a0 = A[j], am1 = A[j - 1], am2 = A[j - 2];
-        T r = T(0);
-        if (pos_prod(a0 - am1, am1 - am2)) {
-          const T da = g[0 * 74 + j] * (g[1 * 74 + j] * (a0 - am1) + g[2 * 74 + j] * (am1 - am2));
-          r = min3abs_signed(da, T(2) * (am1 - am2), T(2) * (a0 - am1), da);
-        }
-        dma[j] = r;
-      }
+  for (int i = 0; i < RNI; ++i) {
+    const int j = s + 8 * i;
+    d1[i] = T(0);
+    if (j < NLEV + 2) {
+      const T am1 = A[j - 1];
+      const T x = A[j] - am1, y = am1 - A[j - 2];
+      d1[i] = x;
+      T r = T(0);
+      if (pos_prod(x, y)) r = slope_limit(g[j] * x + g[74 + j] * y, x, y);
+      dma[j] = r;
     }
   }
   __syncwarp();
-  if (lane < 25) {
 #pragma unroll
-    for (int k3 = 0; k3 < 3; ++k3) {
-      const int j = 3 * lane + k3;
-      if (j < NLEV + 1) {
-        const T a0 = A[j], am1 = A[j - 1];
-        ai[j] = am1 + g[3 * 74 + j] * (a0 - am1) +
-                g[4 * 74 + j] * (g[5 * 74 + j] * (a0 - am1) -
-                                 g[8 * 74 + j] * dma[j + 1] + g[9 * 74 + j] * dma[j]);
-      }
-    }
+  for (int i = 0; i < RNI; ++i) {
+    const int j = s + 8 * i;
+    if (j < NLEV + 1) ai[j] = A[j - 1] + g[2 * 74 + j] * d1[i] - g[3 * 74 + j] * dma[j + 1] + g[4 * 74 + j] * dma[j];
   }
-  __syncwarp();
-  if (own) {
+}
+
+// The limited parabola of each of this lane's cells (PpmRemap.hpp:267-353):
+// coef = (c0, c1, c2) = (1.5 A - (al + ar) / 4, ar - al, 3 (al + ar - 2 A)).
+template <typename T>
+__device__ __forceinline__ void ppm_cells(int l0, int remap_alg, const T* A, const T* ai, T* coef) {
+  constexpr T sixth = T(1.0 / 6.0);
 #pragma unroll
-    for (int k3 = 0; k3 < 3; ++k3) {
-      const int jp = l0 + k3;
-      T al = ai[jp], ar = ai[jp + 1];
-      const T cm = A[jp];
-      if (!pos_prod(ar - cm, cm - al)) { al = cm; ar = cm; }
-      constexpr T sixth = T(1.0 / 6.0);
-      if (less((ar - al) * (ar - al) * sixth, (ar - al) * (cm - (al + ar) * T(0.5)))) al = T(3) * cm - T(2) * ar;
-      if (less((ar - al) * (cm - (al + ar) * T(0.5)), -(ar - al) * (ar - al) * sixth)) ar = T(3) * cm - T(2) * al;
-      T c0 = T(1.5) * cm - (al + ar) / T(4), c1 = ar - al, c2 = T(3) * (T(-2) * cm + (al + ar));
-      if (remap_alg == 2 && (jp < 2 || jp >= NLEV - 2)) {  // PpmFixedParabola
-        c0 = cm;
-        c1 = T(0);
-        c2 = T(0);
-      }
-      coef[0 * 72 + jp] = c0;
-      coef[1 * 72 + jp] = c1;
-      coef[2 * 72 + jp] = c2;
+  for (int k3 = 0; k3 < RLV; ++k3) {
+    const int jp = l0 + k3;
+    T al = ai[jp], ar = ai[jp + 1];
+    const T cm = A[jp];
+    if (!monotone(al, cm, ar)) { al = cm; ar = cm; }
+    T d = ar - al, s2 = al + ar;
+    T q = d * d * sixth, r = d * (cm - s2 * T(0.5));
+    if (less(q, r)) {
+      al = T(3) * cm - T(2) * ar;
+      d = ar - al;
+      s2 = al + ar;
+      q = d * d * sixth;
+      r = d * (cm - s2 * T(0.5));
     }
+    if (less(r, -q)) {
+      ar = T(3) * cm - T(2) * al;
+      d = ar - al;
+      s2 = al + ar;
+    }
+    T c0 = T(1.5) * cm - s2 * T(0.25), c1 = d, c2 = T(3) * (s2 - T(2) * cm);
+    if (remap_alg == 2 && (jp < 2 || jp >= NLEV - 2)) {  // PpmFixedParabola
+      c0 = cm;
+      c1 = T(0);
+      c2 = T(0);
+    }
+    coef[jp] = c0;
+    coef[72 + jp] = c1;
+    coef[144 + jp] = c2;
   }
 }
 
@@ -1218,341 +1269,297 @@ __device__ __forceinline__ void ppm_coefs(int lane, bool own, int l0, int remap_
 // dl = al - A[k] = e[k] - df[k] and dr = ar - A[k] = e[k+1], limited as above, give
 // coef = (c0 - A[k], c1, c2) = (-(dl + dr) / 4, dr - dl, 3 (dl + dr)).  FP32 carries only
 // differences; A[k]'s share of a cell integral is added in FP64 by the caller.
-__device__ __forceinline__ void ppm_coefs_delta(int lane, bool own, int l0, int remap_alg, const float* df,
-                                                const float* g, float* dma, float* e, float* coef) {
-  if (lane < 25) {
+__device__ __forceinline__ void ppm_interfaces_delta(int s, const float* df, const float* g, float* dma,
+                                                     float* e) {
 #pragma unroll
-    for (int k3 = 0; k3 < 3; ++k3) {
-      const int j = 3 * lane + k3;
-      if (j < NLEV + 2) {
-        const float d1 = df[j], d2 = df[j - 1];
-        float r = 0.0f;
-        if (d1 * d2 > 0.0f) {
-          const float da = g[0 * 74 + j] * (g[1 * 74 + j] * d1 + g[2 * 74 + j] * d2);
-          r = min3abs_signed(da, 2.0f * d2, 2.0f * d1, da);
-        }
-        dma[j] = r;
-      }
+  for (int i = 0; i < RNI; ++i) {
+    const int j = s + 8 * i;
+    if (j < NLEV + 2) {
+      const float d1 = df[j], d2 = df[j - 1];
+      float r = 0.0f;
+      if (d1 * d2 > 0.0f) r = min3abs_signed(g[j] * d1 + g[74 + j] * d2, 2.0f * d2, 2.0f * d1, g[j] * d1 + g[74 + j] * d2);
+      dma[j] = r;
     }
   }
   __syncwarp();
-  if (lane < 25) {
 #pragma unroll
-    for (int k3 = 0; k3 < 3; ++k3) {
-      const int j = 3 * lane + k3;
-      if (j < NLEV + 1) {
-        const float d1 = df[j];
-        e[j] = g[3 * 74 + j] * d1 +
-               g[4 * 74 + j] * (g[5 * 74 + j] * d1 - g[8 * 74 + j] * dma[j + 1] +
-                                g[9 * 74 + j] * dma[j]);
-      }
-    }
+  for (int i = 0; i < RNI; ++i) {
+    const int j = s + 8 * i;
+    if (j < NLEV + 1) e[j] = g[2 * 74 + j] * df[j] - g[3 * 74 + j] * dma[j + 1] + g[4 * 74 + j] * dma[j];
   }
-  __syncwarp();
-  if (own) {
+}
+__device__ __forceinline__ void ppm_cells_delta(int l0, int remap_alg, const float* df, const float* e,
+                                                float* coef) {
+  constexpr float sixth = 1.0f / 6.0f;
 #pragma unroll
-    for (int k3 = 0; k3 < 3; ++k3) {
-      const int jp = l0 + k3;
-      float dl = e[jp] - df[jp], dr = e[jp + 1];
-      if (!(dr * -dl > 0.0f)) { dl = 0.0f; dr = 0.0f; }
-      constexpr float sixth = 1.0f / 6.0f;
-      float c1 = dr - dl;
-      if (c1 * c1 * sixth < c1 * (-(dl + dr) * 0.5f)) dl = -2.0f * dr;
-      c1 = dr - dl;
-      if (c1 * (-(dl + dr) * 0.5f) < -c1 * c1 * sixth) dr = -2.0f * dl;
-      float d0 = -(dl + dr) * 0.25f, c2 = 3.0f * (dl + dr);
-      c1 = dr - dl;
-      if (remap_alg == 2 && (jp < 2 || jp >= NLEV - 2)) {  // PpmFixedParabola
-        d0 = 0.0f;
-        c1 = 0.0f;
-        c2 = 0.0f;
-      }
-      coef[0 * 72 + jp] = d0;
-      coef[1 * 72 + jp] = c1;
-      coef[2 * 72 + jp] = c2;
+  for (int k3 = 0; k3 < RLV; ++k3) {
+    const int jp = l0 + k3;
+    float dl = e[jp] - df[jp], dr = e[jp + 1];
+    if (!(dr * -dl > 0.0f)) { dl = 0.0f; dr = 0.0f; }
+    float c1 = dr - dl;
+    if (c1 * c1 * sixth < c1 * (-(dl + dr) * 0.5f)) dl = -2.0f * dr;
+    c1 = dr - dl;
+    if (c1 * (-(dl + dr) * 0.5f) < -c1 * c1 * sixth) dr = -2.0f * dl;
+    float d0 = -(dl + dr) * 0.25f, c2 = 3.0f * (dl + dr);
+    c1 = dr - dl;
+    if (remap_alg == 2 && (jp < 2 || jp >= NLEV - 2)) {  // PpmFixedParabola
+      d0 = 0.0f;
+      c1 = 0.0f;
+      c2 = 0.0f;
     }
+    coef[jp] = d0;
+    coef[72 + jp] = c1;
+    coef[144 + jp] = c2;
   }
 }
 
-// PPM vertical remap (RemapFunctor + PpmVertRemap, rsplit > 0), one warp per column:
-// lane L owns levels 3L .. 3L+2 (L < 24) for level work and interfaces j = 3L .. 3L+2
-// (L < 25) for the grid quantities; column scans are warp shuffles, phases are
-// separated by __syncwarp only.  Everything runs in double in both forms (R is double
-// at every launch); the remap conserves mass to round-off.  Divisions by the layer
-// thickness and by the constants 3 and 6 are multiplications by reciprocals.
+// PPM vertical remap of v, T (rsplit > 0) and the tracers.  Everything runs in double in
+// the FP64 form; the mixed form reconstructs in FP32 (v and T from their neighbour
+// differences, the tracers from their FP32 cell means) and keeps the cell integrals, the
+// cumulative masses and the grid in FP64, the bottom interface carrying the exact column
+// mass (mass fixer).  Divisions are multiplications by Newton reciprocals.
 template <typename R>
 __global__ void __launch_bounds__(RT) k_remap(RemapArgs a) {
+  using LY = RemapLayout<R>;
+  constexpr bool lo = kF32<R>;
   extern __shared__ double rsm[];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int cidx = blockIdx.x * RCOLS + warp;
-  if (cidx >= a.nelem * 16) return;  // whole warp leaves together; no CTA barriers below
+  const int lane = threadIdx.x, cw = lane >> 3, s = lane & 7;
+  // A launch covers whole elements (16 columns each), so all four columns are live.
+  const int cidx = blockIdx.x * RCOLS + cw;
   const int e = cidx >> 4, p = cidx & 15;
-  double* sm = rsm + warp * r_col<R>();
-  double* D = sm + R_D + 2;
-  double* pio = sm + R_PIO;
-  double* pin = sm + R_PIN;
-  double* z2 = sm + R_Z2;
-  int* kid = reinterpret_cast<int*>(sm + R_KID);
-  double* tgt = sm + R_TGT;
-  double* g = sm + R_G;  // g[c * 74 + j]
-  double* A = sm + R_A + 2;
-  double* mass = sm + R_MASS;
-  double* dma = sm + R_DMA;
-  double* ai = sm + R_AI;
-  double* coef = sm + R_COEF;  // coef[c * 72 + j]
-  double* rD = sm + R_RD;
-  const bool own = lane < 24;
-  const int l0 = 3 * lane;
+  double* sm = rsm + cw * LY::END;
+  double* D = sm + LY::D + 2;
+  double* pio = sm + LY::PIO;
+  double* pin = sm + LY::PIN;
+  double* rD = sm + LY::RDI;
+  double* mass = sm + LY::MASS;
+  double* A = sm + LY::A + 2;
+  R* g = reinterpret_cast<R*>(sm + LY::G);  // g[c * 74 + j]
+  R* dma = reinterpret_cast<R*>(sm + LY::DMA);
+  R* ai = reinterpret_cast<R*>(sm + LY::AI);
+  R* coef = reinterpret_cast<R*>(sm + LY::COEF);  // coef[c * 72 + k]
+  float* dlf = reinterpret_cast<float*>(sm + LY::DLF) + 1;  // df[-1 .. 73]
+  float* rDf = reinterpret_cast<float*>(sm + LY::RDF);
+  float* Af = reinterpret_cast<float*>(sm + LY::A) + 2;  // the tracers' FP32 cell means
+  const int l0 = RLV * s;
   const size_t sb = ((size_t)e * NTL + a.np1) * NLEV * 16 + p;
   const size_t vb = ((size_t)e * NTL + a.np1) * NLEV * 32 + p;
-  // source thickness and surface pressure (compute_ps_v)
-  double s3[3] = {0.0, 0.0, 0.0};
-  if (own) {
+  // ---- source thickness and surface pressure (compute_ps_v) ----
+  double sv[RLV];
 #pragma unroll
-    for (int k = 0; k < 3; ++k) s3[k] = a.dp[sb + (size_t)(l0 + k) * 16];
-  }
-  const double ps = warp_sum(s3[0] + s3[1] + s3[2]) + a.hyai0 * a.ps0;
-  if (lane == 0) a.ps_v[((size_t)e * NTL + a.np1) * 16 + p] = ps;
-  double t3[3] = {0.0, 0.0, 0.0}, rt3[3] = {0.0, 0.0, 0.0};
-  if (own) {
+  for (int k = 0; k < RLV; ++k) sv[k] = a.dp[sb + (size_t)(l0 + k) * 16];
+  double cs = 0.0;
 #pragma unroll
-    for (int k = 0; k < 3; ++k) {
-      const int l = l0 + k;
-      t3[k] = (c_hyai[l + 1] - c_hyai[l]) * a.ps0 + (c_hybi[l + 1] - c_hybi[l]) * ps;
-      tgt[l] = t3[k];
-      float rf;
-      rt3[k] = rcp_newton(t3[k], rf);
-      if (a.rsplit == 0) {  // vertically Eulerian source thickness (RemapFunctor.hpp:42-100)
-        const size_t ie = ((size_t)e * NLEV + l) * 16 + p;
-        const double en = l + 1 < NLEV ? a.eta[ie + 16] : 0.0;
-        s3[k] = t3[k] + a.dt * (en - a.eta[ie]);
-      }
-      D[l] = s3[k];
-      rD[l] = rcp_newton(s3[k], rf);
-      if (isnan(s3[k]) || s3[k] < 0.0) atomicExch(a.invalid, 1);
+  for (int k = 0; k < RLV; ++k) cs += sv[k];
+#pragma unroll
+  for (int off = 1; off < 8; off <<= 1) cs += __shfl_xor_sync(FULL, cs, off, 8);  // same sum in all 8 lanes
+  const double ps = cs + a.hyai0 * a.ps0;
+  if (s == 0) a.ps_v[((size_t)e * NTL + a.np1) * 16 + p] = ps;
+  // ---- target thickness; vertically Eulerian source thickness (RemapFunctor.hpp:42-100) ----
+  double tg[RLV], rt[RLV];
+  bool bad = false;
+#pragma unroll
+  for (int k = 0; k < RLV; ++k) {
+    const int l = l0 + k;
+    tg[k] = c_ai_delta[l] * a.ps0 + c_bi_delta[l] * ps;
+    float rf;
+    rt[k] = rcp_newton(tg[k], rf);
+    if (a.rsplit == 0) {
+      const size_t ie = ((size_t)e * NLEV + l) * 16 + p;
+      const double en = l + 1 < NLEV ? a.eta[ie + 16] : 0.0;
+      sv[k] = tg[k] + a.dt * (en - a.eta[ie]);
     }
+    D[l] = sv[k];
+    rD[l] = rcp_newton(sv[k], rf);
+    if constexpr (lo) rDf[l] = d2f_rn(rD[l]);
+    bad |= bad_thickness(sv[k]);
   }
-  // compute_partitions: pio, pin cumulative thickness
+  if (bad) atomicExch(a.invalid, 1);
+  // ---- compute_partitions: cumulative source (pio) and target (pin) thickness ----
   {
-    double ex = warp_excl_scan(s3[0] + s3[1] + s3[2], lane);
-    double ey = warp_excl_scan(t3[0] + t3[1] + t3[2], lane);
-    if (own) {
+    double ts = 0.0, tt = 0.0;
 #pragma unroll
-      for (int k = 0; k < 3; ++k) {
-        pio[l0 + k] = ex;
-        pin[l0 + k] = ey;
-        ex += s3[k];
-        ey += t3[k];
-      }
+    for (int k = 0; k < RLV; ++k) {
+      ts += sv[k];
+      tt += tg[k];
     }
-    if (lane == 23) {
-      pio[NLEV] = ex;
-      pio[NLEV + 1] = ex + 1.0;
-      pin[NLEV] = ex;  // the column's total mass does not change
+    double xo = seg_excl_prefix(ts, s), xn = seg_excl_prefix(tt, s);
+#pragma unroll
+    for (int k = 0; k < RLV; ++k) {
+      pio[l0 + k] = xo;
+      pin[l0 + k] = xn;
+      xo += sv[k];
+      xn += tg[k];
+    }
+    if (s == 7) {
+      pio[NLEV] = xo;
+      pio[NLEV + 1] = xo + 1.0;
+      pin[NLEV] = xo;  // the column's total mass does not change
     }
   }
   __syncwarp();
-  if (lane == 0) {
+  if (s == 0) {  // ghost cells of the source thickness: mirrored
     D[-1] = D[0];
     D[-2] = D[1];
     D[NLEV] = D[NLEV - 1];
     D[NLEV + 1] = D[NLEV - 2];
   }
   __syncwarp();
-  // compute_integral_bounds
-  if (own) {
+  // ---- compute_integral_bounds: the source cell holding each new interface, and the
+  // partial-cell integral's weights x2 + 1/2, (x2^2 - 1/4) / 2, (x2^3 + 1/8) / 3 of this
+  // lane's target levels (the search compares on the integer pipe) ----
+  int kid[RLV];
+  double wz[RLV][3];
+  float wzf[RLV][3];
 #pragma unroll
-    for (int k3 = 0; k3 < 3; ++k3) {
-      const int k = l0 + k3;
-      int kk = k + 1;
-      while (kk < NLEV + 2 && pio[kk - 1] <= pin[k + 1]) kk++;
-      kk--;
-      if (kk == NLEV + 1) kk = NLEV;
-      if (kk < 1) {  // only reachable with a non-monotone (invalid) source grid
-        kk = 1;
-        atomicExch(a.invalid, 1);
-      }
-      kid[k] = kk - 1;
-      z2[k] = (pin[k + 1] - (pio[kk - 1] + pio[kk]) * 0.5) * rD[kk - 1];
+  for (int k3 = 0; k3 < RLV; ++k3) {
+    const int k = l0 + k3;
+    const double pk = pin[k + 1];
+    const long long key = dkey(pk);
+    int kk = k + 1;
+    while (kk < NLEV + 2 && dkey(pio[kk - 1]) <= key) kk++;
+    kk--;
+    if (kk == NLEV + 1) kk = NLEV;
+    if (kk < 1) {  // only reachable with a non-monotone (invalid) source grid
+      kk = 1;
+      atomicExch(a.invalid, 1);
     }
-  }
-  // Mixed form: the reconstructions run in FP32 from float copies of the grid weights,
-  // z2 and 1/D; the cell integrals and the mass below each interface stay in FP64, and
-  // the bottom interface carries the exact column mass (mass fixer).  v and T are
-  // reconstructed from their neighbour differences (ppm_coefs_delta), so FP32 carries
-  // only differences and parabola offsets, and the cell mean's share of each partial
-  // integral, A[kk] (x2 + 1/2), is added in FP64; the tracers (non-negative, of their own
-  // scale) are reconstructed from their FP32 cell means.  The FP32 arrays occupy the
-  // region of the double weights, which the mixed form never stores (13.8 KB per column
-  // instead of 17.7 KB: four CTAs per SM instead of three).
-  float* gf = reinterpret_cast<float*>(sm + R_G);  // [10][74]
-  float* z2f = gf + 740;
-  float* rDf = z2f + 72;
-  float* dlf = rDf + 72 + 1;  // df[-1 .. 73]
-  float* Af = reinterpret_cast<float*>(sm + R_A) + 2;
-  float* dmaf = reinterpret_cast<float*>(sm + R_DMA);
-  float* aif = reinterpret_cast<float*>(sm + R_AI);
-  float* coeff = reinterpret_cast<float*>(sm + R_COEF);
-  // compute_grids in double; the mixed form keeps only their FP32 images, converted on
-  // the integer pipe (d2f_rn: the FP64 pipe is this kernel's limit)
-  if (lane < 25) {
-#pragma unroll
-    for (int k3 = 0; k3 < 3; ++k3) {
-      const int j = 3 * lane + k3;
-      auto put = [&](int c, double x) {
-        if constexpr (kF32<R>) gf[c * 74 + j] = d2f_rn(x);
-        else g[c * 74 + j] = x;
-      };
-      if (j < NLEV + 2) {
-        const double dm2 = D[j - 2], dm1 = D[j - 1], d0 = D[j];
-        // reciprocals by Newton-Raphson (rcp_newton, within one ulp)
-        float rf;
-        const double r10 = rcp_newton(dm1 + d0, rf);  // shared by g1, g3, g5
-        put(0, dm1 * rcp_newton(dm2 + dm1 + d0, rf));
-        put(1, (2.0 * dm2 + dm1) * r10);
-        put(2, (dm1 + 2.0 * d0) * rcp_newton(dm2 + dm1, rf));
-        if (j < NLEV + 1) {
-          const double dp1 = D[j + 1];
-          const double r6 = rcp_newton(2.0 * dm1 + d0, rf);  // shared by g6, g8
-          const double r7 = rcp_newton(2.0 * d0 + dm1, rf);  // shared by g7, g9
-          put(3, dm1 * r10);
-          put(4, rcp_newton(dm2 + dm1 + d0 + dp1, rf));
-          // row 5 holds g5 (g6 - g7), the only form the edge values use
-          put(5, ((2.0 * dm1 * d0) * r10) * ((dm2 + dm1) * r6 - (dp1 + d0) * r7));
-          put(8, dm1 * (dm2 + dm1) * r6);
-          put(9, d0 * (d0 + dp1) * r7);
-        }
-      }
-    }
-  }
-  __syncwarp();
-  if constexpr (kF32<R>) {
-    {
-      if (own) {
-#pragma unroll
-        for (int k = 0; k < 3; ++k) {
-          z2f[l0 + k] = d2f_rn(z2[l0 + k]);
-          rDf[l0 + k] = d2f_rn(rD[l0 + k]);
-        }
-      }
-      __syncwarp();
-    }
-  }
-  // The partial-cell integral's weights depend on the target level only: this lane's
-  // three levels' x2 + 1/2, (x2^2 - 1/4) / 2, (x2^3 + 1/8) / 3, once for all variables.
-  double wz[3][3];
-  float wzf[3][3];
-#pragma unroll
-  for (int k3 = 0; k3 < 3; ++k3) {
-    const double x2 = own ? z2[l0 + k3] : 0.0;
+    kid[k3] = kk - 1;
+    const double x2 = (pk - (pio[kk - 1] + pio[kk]) * 0.5) * rD[kk - 1];
     wz[k3][0] = x2 + 0.5;
     wz[k3][1] = (x2 * x2 - 0.25) * 0.5;
     wz[k3][2] = (x2 * x2 * x2 + 0.125) * (1.0 / 3.0);
-    if constexpr (kF32<R>) {
-      const float xf = own ? z2f[l0 + k3] : 0.0f;
+    if constexpr (lo) {
+      const float xf = d2f_rn(x2);
       wzf[k3][0] = xf + 0.5f;
       wzf[k3][1] = (xf * xf - 0.25f) * 0.5f;
       wzf[k3][2] = (xf * xf * xf + 0.125f) * (1.0f / 3.0f);
     }
   }
+  // ---- compute_grids (PpmRemap.hpp:367-413, 505-666) at this lane's interfaces, in
+  // double; the weights are stored combined (ppm_interfaces), in R ----
+#pragma unroll
+  for (int i = 0; i < RNI; ++i) {
+    const int j = s + 8 * i;
+    if (j < NLEV + 2) {
+      const double dm2 = D[j - 2], dm1 = D[j - 1], d0 = D[j];
+      float rf;
+      const double r10 = rcp_newton(dm1 + d0, rf);  // shared by g1, g3, g5
+      const double g0 = dm1 * rcp_newton(dm2 + dm1 + d0, rf);
+      g[j] = cvt<R>(g0 * ((dtwice(dm2) + dm1) * r10));                        // k1 = g0 g1
+      g[74 + j] = cvt<R>(g0 * ((dm1 + dtwice(d0)) * rcp_newton(dm2 + dm1, rf)));  // k2 = g0 g2
+      if (j < NLEV + 1) {
+        const double dp1 = D[j + 1];
+        const double r6 = rcp_newton(dtwice(dm1) + d0, rf);  // shared by g5, g8
+        const double r7 = rcp_newton(dtwice(d0) + dm1, rf);  // shared by g5, g9
+        const double g4 = rcp_newton(dm2 + dm1 + d0 + dp1, rf);
+        const double g5 = (dtwice(dm1 * d0) * r10) * ((dm2 + dm1) * r6 - (dp1 + d0) * r7);
+        g[2 * 74 + j] = cvt<R>(dm1 * r10 + g4 * g5);              // h1 = g3 + g4 g5
+        g[3 * 74 + j] = cvt<R>(g4 * (dm1 * (dm2 + dm1) * r6));    // h2 = g4 g8
+        g[4 * 74 + j] = cvt<R>(g4 * (d0 * (d0 + dp1) * r7));      // h3 = g4 g9
+      }
+    }
+  }
+  __syncwarp();
   const int nvar = 3 + a.Q;
 #pragma unroll 1
   for (int var = a.rsplit == 0 ? 3 : 0; var < nvar; ++var) {
-    constexpr bool lo = kF32<R>;
-    // extrinsic values (v dp, T dp for the states; Qdp as is), cell means, masses
-    double x3[3] = {0.0, 0.0, 0.0};
-    if (own) {
+    // extrinsic values (v dp, T dp for the states; Qdp as is) and cell means
+    double x[RLV];
 #pragma unroll
-      for (int k = 0; k < 3; ++k) {
-        const int l = l0 + k;
-        if (var < 2) x3[k] = a.v[vb + (size_t)l * 32 + var * 16] * s3[k];
-        else if (var == 2) x3[k] = a.T[sb + (size_t)l * 16] * s3[k];
-        else x3[k] = a.qdp[((((size_t)e * QTL + a.n0_qdp) * a.Q + (var - 3)) * NLEV + l) * 16 + p];
-        if (!lo || var < 3) A[l] = x3[k] * rD[l];
-        else Af[l] = d2f_rn(x3[k]) * rDf[l];
-      }
+    for (int k = 0; k < RLV; ++k) {
+      const int l = l0 + k;
+      if (var < 2) x[k] = a.v[vb + (size_t)l * 32 + var * 16] * sv[k];
+      else if (var == 2) x[k] = a.T[sb + (size_t)l * 16] * sv[k];
+      else x[k] = a.qdp[((((size_t)e * QTL + a.n0_qdp) * a.Q + (var - 3)) * NLEV + l) * 16 + p];
+      if (!lo || var < 3) A[l] = x[k] * rD[l];
+      else Af[l] = d2f_rn(x[k]) * rDf[l];
     }
+    // mass[i + 1] = sum of x below cell i (mass[0] = mass[1] = 0, mass[73] = column total)
     {
-      double ex = warp_excl_scan(x3[0] + x3[1] + x3[2], lane);
-      if (own) {
+      double tx = 0.0;
 #pragma unroll
-        for (int k = 0; k < 3; ++k) {
-          mass[l0 + k + 1] = ex;
-          ex += x3[k];
-        }
+      for (int k = 0; k < RLV; ++k) tx += x[k];
+      double ex = seg_excl_prefix(tx, s);
+#pragma unroll
+      for (int k = 0; k < RLV; ++k) {
+        mass[l0 + k + 1] = ex;
+        ex += x[k];
       }
-      if (lane == 23) mass[NLEV + 1] = ex;  // mass[NLEV] + x[NLEV-1]
-      if (lane == 0) mass[0] = 0.0;
+      if (s == 7) mass[NLEV + 1] = ex;
+      if (s == 0) mass[0] = 0.0;
     }
     __syncwarp();
-    const bool dlt = lo && var < 3;  // mixed form, v and T: reconstruction from differences
-    if (dlt) {
-      // df[j] = A[j] - A[j-1]; ghosts: mirrored (remap_alg 1, 2) or constant (3) cells
-      if (own) {
+    if constexpr (lo) {
+      if (var < 3) {  // df[j] = A[j] - A[j-1]; ghosts: mirrored (remap_alg 1, 2) or constant (3) cells
 #pragma unroll
-        for (int k = 0; k < 3; ++k) {
+        for (int k = 0; k < RLV; ++k) {
           const int j = l0 + k;
           if (j >= 1) dlf[j] = d2f_rn(A[j] - A[j - 1]);
         }
-      }
-      __syncwarp();
-      if (lane == 0) {
-        dlf[0] = 0.0f;
-        dlf[-1] = a.remap_alg == 3 ? 0.0f : -dlf[1];
-        dlf[NLEV] = 0.0f;
-        dlf[NLEV + 1] = a.remap_alg == 3 ? 0.0f : -dlf[NLEV - 1];
-      }
-    } else if (lane == 0) {  // ghost cells: mirrored (remap_alg 1, 2) or constant (3)
-      if (lo) {
-        Af[-1] = Af[0];
-        Af[-2] = a.remap_alg == 3 ? Af[0] : Af[1];
-        Af[NLEV] = Af[NLEV - 1];
-        Af[NLEV + 1] = a.remap_alg == 3 ? Af[NLEV - 1] : Af[NLEV - 2];
+        __syncwarp();
+        if (s == 0) {
+          dlf[0] = 0.0f;
+          dlf[-1] = a.remap_alg == 3 ? 0.0f : -dlf[1];
+          dlf[NLEV] = 0.0f;
+          dlf[NLEV + 1] = a.remap_alg == 3 ? 0.0f : -dlf[NLEV - 1];
+        }
+        __syncwarp();
+        ppm_interfaces_delta(s, dlf, g, dma, ai);
+        __syncwarp();
+        ppm_cells_delta(l0, a.remap_alg, dlf, ai, coef);
       } else {
+        if (s == 0) {
+          Af[-1] = Af[0];
+          Af[-2] = a.remap_alg == 3 ? Af[0] : Af[1];
+          Af[NLEV] = Af[NLEV - 1];
+          Af[NLEV + 1] = a.remap_alg == 3 ? Af[NLEV - 1] : Af[NLEV - 2];
+        }
+        __syncwarp();
+        ppm_interfaces<float>(s, Af, g, dma, ai);
+        __syncwarp();
+        ppm_cells<float>(l0, a.remap_alg, Af, ai, coef);
+      }
+    } else {
+      if (s == 0) {
         A[-1] = A[0];
         A[-2] = a.remap_alg == 3 ? A[0] : A[1];
         A[NLEV] = A[NLEV - 1];
         A[NLEV + 1] = a.remap_alg == 3 ? A[NLEV - 1] : A[NLEV - 2];
       }
+      __syncwarp();
+      ppm_interfaces<double>(s, A, g, dma, ai);
+      __syncwarp();
+      ppm_cells<double>(l0, a.remap_alg, A, ai, coef);
     }
-    __syncwarp();
-    if (dlt) ppm_coefs_delta(lane, own, l0, a.remap_alg, dlf, gf, dmaf, aif, coeff);
-    else if (lo) ppm_coefs<float>(lane, own, l0, a.remap_alg, Af, gf, dmaf, aif, coeff);
-    else ppm_coefs<double>(lane, own, l0, a.remap_alg, A, g, dma, ai, coef);
     __syncwarp();
     // compute_remap: mass below each new interface, in double; new cell masses are
-    // differences of consecutive interface masses (the lower one from the next lane).
-    double m2[3] = {0.0, 0.0, 0.0};
-    if (own) {
+    // differences of consecutive interface masses (the lowest from the lane below)
+    double m2[RLV];
 #pragma unroll
-      for (int k3 = 0; k3 < 3; ++k3) {
-        const int k = l0 + k3;
-        const int kk = kid[k];
-        if (lo) {
-          const float in = (coeff[kk] * wzf[k3][0] + coeff[72 + kk] * wzf[k3][1]) + coeff[144 + kk] * wzf[k3][2];
-          // v and T: the coefficients are offsets from the cell mean A[kk]
-          const double ind = dlt ? fma(A[kk], wz[k3][0], dbl(in)) : dbl(in);
-          m2[k3] = k == NLEV - 1 ? mass[NLEV + 1] : mass[kk + 1] + ind * D[kk];
-        } else {
-          const double in = (coef[kk] * wz[k3][0] + coef[72 + kk] * wz[k3][1]) + coef[144 + kk] * wz[k3][2];
-          m2[k3] = mass[kk + 1] + in * D[kk];
-        }
+    for (int k3 = 0; k3 < RLV; ++k3) {
+      const int k = l0 + k3, kk = kid[k3];
+      if constexpr (lo) {
+        const float in = (coef[kk] * wzf[k3][0] + coef[72 + kk] * wzf[k3][1]) + coef[144 + kk] * wzf[k3][2];
+        // v and T: the coefficients are offsets from the cell mean A[kk]
+        const double ind = var < 3 ? fma(A[kk], wz[k3][0], dbl(in)) : dbl(in);
+        m2[k3] = k == NLEV - 1 ? mass[NLEV + 1] : mass[kk + 1] + ind * D[kk];
+      } else {
+        const double in = (coef[kk] * wz[k3][0] + coef[72 + kk] * wz[k3][1]) + coef[144 + kk] * wz[k3][2];
+        m2[k3] = mass[kk + 1] + in * D[kk];
       }
     }
-    double below = __shfl_up_sync(FULL, m2[2], 1);
-    if (lane == 0) below = 0.0;
-    if (own) {
+    double below = __shfl_up_sync(FULL, m2[RLV - 1], 1, 8);
+    if (s == 0) below = 0.0;
 #pragma unroll
-      for (int k3 = 0; k3 < 3; ++k3) {
-        const int k = l0 + k3;
-        const double m1 = k3 == 0 ? below : m2[k3 - 1];
-        const double out = m2[k3] - m1;
-        if (var < 2) a.v[vb + (size_t)k * 32 + var * 16] = out * rt3[k3];
-        else if (var == 2) a.T[sb + (size_t)k * 16] = out * rt3[k3];
-        else a.qdp[((((size_t)e * QTL + a.n0_qdp) * a.Q + (var - 3)) * NLEV + k) * 16 + p] = out;
-      }
+    for (int k3 = 0; k3 < RLV; ++k3) {
+      const int k = l0 + k3;
+      const double out = m2[k3] - (k3 == 0 ? below : m2[k3 - 1]);
+      if (var < 2) a.v[vb + (size_t)k * 32 + var * 16] = out * rt[k3];
+      else if (var == 2) a.T[sb + (size_t)k * 16] = out * rt[k3];
+      else a.qdp[((((size_t)e * QTL + a.n0_qdp) * a.Q + (var - 3)) * NLEV + k) * 16 + p] = out;
     }
-    __syncwarp();
+    __syncwarp();  // the next variable overwrites A, mass and coef
   }
 }
 
@@ -1754,7 +1761,7 @@ void launch_euler_step(EulerArgs<R>& a, int E, int time_avg, cudaStream_t s) {
 
 template <typename R>
 size_t remap_smem() {
-  const size_t smem = (size_t)RCOLS * r_col<R>() * sizeof(double);
+  const size_t smem = (size_t)RCOLS * RemapLayout<R>::END * sizeof(double);
   static bool init = false;
   if (!init) {
     cudaFuncSetAttribute(k_remap<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -1767,7 +1774,7 @@ template <typename R>
 void launch_remap(const RemapArgs& a, cudaStream_t s) {
   const size_t smem = remap_smem<R>();
   KScope k("ppm_remap", s);
-  k_remap<R><<<(a.nelem * 16 + RCOLS - 1) / RCOLS, RT, smem, s>>>(a);
+  k_remap<R><<<a.nelem * 16 / RCOLS, RT, smem, s>>>(a);
 }
 
 template <typename R>

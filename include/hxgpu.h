@@ -193,13 +193,22 @@ int hx_synchronize(void);
  * second one, waits for it and returns the elapsed device time in *ms. */
 int hx_timer_start(void);
 int hx_timer_stop(double* ms);
+/* No counterpart in the reference.  Measured FP64 throughput of the current device in
+ * TFLOP/s (2 per fused multiply-add): a kernel of independent FMA chains at full
+ * occupancy, timed with CUDA events after a warm-up launch (~0.1 s).  The roof of the
+ * FP64 form's kernels, which the FP64 pipe bounds rather than HBM.  Returns 0 or
+ * HX_ERR_CUDA; needs no session. */
+int hx_fp64_peak(double* tflops);
 /* No counterpart in the reference.  DSS of one caller-owned device field
  * [nelem][nlev][np*np] (in and out may alias) without allocating device memory, for
  * callers that cannot call cudaMalloc when they need it (a host model that reserves
  * its GPU memory budget up front, code where allocation is forbidden).  Scratch is a
  * fixed 4 MiB __device__ array (at most 455 elements of 72 levels); larger fields are
- * rejected with code 13.  The first call on a device looks the array up and must come
- * before any stream capture on that device.  Calls share the array, so calls that
+ * rejected with code 13.  The array is made resident on the session's device during
+ * init_boundary_exchanges_c (its address is looked up there, which loads it under
+ * CUDA's lazy module loading), so the call itself loads and allocates nothing; it
+ * holds those 4 MiB until the process exits.  It must be made with the session's
+ * device current (HX_ERR_STATE otherwise).  Calls share the array, so calls that
  * overlap on the GPU race; the array keeps the last call's contents and needs no
  * clearing because every call overwrites what it reads.  Enqueued on the session's
  * stream; returns 0, 13 or HX_ERR_STATE/HX_ERR_CUDA. */
@@ -280,8 +289,11 @@ int hx_cube_mesh(int ne, double hypervis_scaling, double* dvv, double* D, double
  * z ^= z >> 31 (Steele, Lea and Flood, OOPSLA 2014).
  * hx_write_restart writes the session's state and time levels; hx_read_restart
  * replaces them (phis included).  Both stream the records through host buffers of at
- * most 256 MiB, so device memory use does not grow.  Errors: HX_ERR_IO (open, read,
- * write, bad magic or version, size mismatch, checksum), HX_ERR_STATE (no session). */
+ * most 256 MiB, so device memory use does not grow.  hx_read_restart reads the file
+ * twice: it verifies the checksum on the host first, so a failed read (damaged,
+ * truncated or mismatched file) leaves the session's state and time levels unchanged.
+ * Errors: HX_ERR_IO (open, read, write, bad magic or version, size mismatch,
+ * checksum), HX_ERR_STATE (no session). */
 #define HX_ERR_IO 202
 #define HX_RESTART_MAGIC "HXRESTRT"
 #define HX_RESTART_VERSION 1
@@ -303,12 +315,11 @@ int hx_read_restart(const char* path);
  * traffic runs on the host link (about 210 GB/s in, 190 GB/s out on a GB300), so the
  * state copied in and out every interval costs as much as a third of a mixed-form
  * interval unless it overlaps the step's kernels.
- * hx_set_async_copies(1): init_elements_states_c returns once time level n0 of v, T and
- * dp3d, and ps_v, are on the device; levels nm1 and np1 and then Qdp keep streaming in
- * on a copy stream, and the first kernel that writes or reads each of them waits for it
- * (levels nm1 and np1 are first written by the DSS of a Caar stage).  The caller must
- * leave the v, T, dp3d and Qdp host arrays unchanged until the next prim_run_subcycle_c
- * (or any other call of this library) returns.  Default 0.
+ * hx_set_async_copies(1): init_elements_states_c returns once v, T, dp3d and ps_v are on
+ * the device (one contiguous copy each); Qdp keeps streaming in on a copy stream and the
+ * first kernel that reads it (the first tracer step) waits for it.  The caller must
+ * leave the Qdp host array unchanged until the next prim_run_subcycle_c (or any other
+ * call of this library) returns.  Default 0.
  * hx_stream_results(v, T, dp3d, Qdp, Q, ps_v, omega_p): host destinations in the
  * layouts of cxx_push_results_to_f90 (all seven, or all NULL to stop).  Every following
  * prim_run_subcycle_c copies its results there before it returns, each piece as soon as

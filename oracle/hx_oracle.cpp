@@ -2005,10 +2005,10 @@ int hx_read_restart(const char* path) {
     if (t < 1 || t > NTL) return err("bad time level in restart header");
   unsigned long long sum = 0;
   for (int e = 0; e < c.E; ++e) sum += restart_sum(&all[(size_t)e * rw], rw, (unsigned long long)e * rw);
+  if (sum != h.checksum) return err("checksum mismatch");
   for (int e = 0; e < c.E; ++e) unpack_record(e, &all[(size_t)e * rw]);
   c.tl.nm1 = h.nm1 - 1; c.tl.n0 = h.n0 - 1; c.tl.np1 = h.np1 - 1;
   c.tl.nstep = h.nstep; c.tl.nstep0 = h.nstep0;
-  if (sum != h.checksum) return err("checksum mismatch");
   return 0;
 }
 

@@ -96,8 +96,19 @@ def test_restart_errors_gpu(gpu_path, tmp_path):
     raw[128 + 99991] ^= 0x01
     bad = tmp_path / "bad.bin"
     bad.write_bytes(bytes(raw))
+    # the checksum is verified before anything is uploaded: a failed read leaves the
+    # session's state as it was
+    L.run_subcycle(DT)
+    before = L.push_results()
     assert L.lib.hx_read_restart(str(bad).encode()) == HX_ERR_IO
     assert "checksum" in L.last_error()[1]
+    short = tmp_path / "short.bin"
+    short.write_bytes(f.read_bytes()[: len(raw) - 4096])
+    assert L.lib.hx_read_restart(str(short).encode()) == HX_ERR_IO
+    assert "short read" in L.last_error()[1]
+    after = L.push_results()
+    for k in before:
+        assert np.array_equal(before[k], after[k]), k
     assert L.lib.hx_read_restart(str(tmp_path / "none.bin").encode()) == HX_ERR_IO
     L2 = H.setup(gpu_path, 4, 3, rsplit=3)
     assert L2.lib.hx_read_restart(str(f).encode()) == HX_ERR_IO

@@ -7,6 +7,10 @@ This file is collected last, so a run that stops at the first failure has alread
 every other test.
 """
 import ctypes
+import os
+import subprocess
+import sys
+import textwrap
 
 import numpy as np
 import pytest
@@ -59,3 +63,42 @@ def test_noalloc_rejects_sizes(gpu_path):
     big = torch.zeros((L.nelem, 72, 16), dtype=torch.float64, device="cuda")
     assert L.lib.hx_dss_noalloc(ctypes.c_void_p(big.data_ptr()), ctypes.c_void_p(big.data_ptr()),
                                 L.nelem, 1) == 13
+
+
+_FRESH = textwrap.dedent("""
+    import ctypes, sys
+    import numpy as np
+    import torch
+    sys.path.insert(0, sys.argv[1])
+    import hxtest as H
+    L = H.setup(sys.argv[2], 4, 2)
+    E = L.nelem
+    f = np.random.default_rng(7).standard_normal((E, 72, 4, 4))
+    L.set("T", 0, f)
+    L.call("hx_run_dss", b"T", 0, 1)
+    ref = L.get("T", 0)
+    d_in = torch.tensor(f, dtype=torch.float64, device="cuda")
+    d_out = torch.empty_like(d_in)
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    for _ in range(2):
+        assert L.lib.hx_dss_noalloc(ctypes.c_void_p(d_in.data_ptr()), ctypes.c_void_p(d_out.data_ptr()), E, 1) == 0
+        assert L.lib.hx_synchronize() == 0
+    free1 = torch.cuda.mem_get_info()[0]
+    assert np.array_equal(d_out.cpu().numpy(), ref)
+    print("FREE", free0, free1)
+""")
+
+
+def test_noalloc_allocates_nothing_in_a_fresh_process(gpu_path):
+    """The property the entry point exists for: in a new process, after session set-up
+    and before the first call, free device memory is recorded; two calls and a
+    synchronisation later it is unchanged (the fixed scratch became resident during
+    init_boundary_exchanges_c, not at the first call)."""
+    pytest.importorskip("torch")
+    here = os.path.dirname(os.path.abspath(__file__))
+    r = subprocess.run([sys.executable, "-c", _FRESH, here, gpu_path], capture_output=True, text=True,
+                       timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
+    line = [x for x in r.stdout.splitlines() if x.startswith("FREE")][-1].split()
+    assert int(line[1]) == int(line[2]), line
