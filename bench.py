@@ -59,34 +59,68 @@ FALLBACK_HBM_GBS = 6800.0
 
 
 # Per launch, measured by ncu at ne16 L72 q10 (1536 elements) over the launches of one
-# remap interval (profiles/launches_and_fp64_ne16.md gives the command): DRAM bytes read +
-# written (dram__bytes_read.sum + dram__bytes_write.sum) and FP64 floating-point
-# operations, DADD + DMUL + 2 DFMA thread instructions
-# (smsp__sass_thread_inst_executed_op_{dadd,dmul,dfma}_pred_on.sum), each averaged over
-# the kernel's launches in that interval.  Both are scaled to the run's size by the
-# element count (levels and tracers fixed).  A kernel that changes invalidates its row:
-# the table is re-captured with the kernels it describes.
+# remap interval (profiles/kernel_counts_ne16_fp64_mixed.md gives the command and the
+# build): DRAM bytes read + written (dram__bytes_read.sum + dram__bytes_write.sum), FP64
+# floating-point operations DADD + DMUL + 2 DFMA and FP64 instructions DADD + DMUL + DFMA
+# (smsp__sass_thread_inst_executed_op_{dadd,dmul,dfma}_pred_on.sum), each averaged over the
+# kernel's launches in that interval and scaled to the run's size by the element count
+# (levels and tracers fixed).  A kernel that changes invalidates its row: the table is
+# re-captured with the kernels it describes.
 NCU_NE16 = {
-    "fp64": {"euler_aal_tracer": (473.5e6, None), "caar_stage": (153.3e6, None),
-             "hv_laplace2": (162.0e6, None), "ppm_remap": (328.5e6, None),
-             "euler_bih_post": (282.0e6, None), "hv_laplace1": (77.4e6, None),
-             "euler_bih_pre": (260.5e6, None), "euler_dss_qdp": (399.9e6, None),
-             "euler_qminmax": (283.2e6, None)},
-    "mixed": {"euler_aal_tracer": (472.6e6, None), "caar_stage": (151.5e6, None),
-              "hv_laplace2": (151.6e6, None), "ppm_remap": (328.5e6, None),
-              "euler_dss_qdp": (399.9e6, None), "euler_qminmax": (276.9e6, None),
-              "euler_bih_post": (274.1e6, None)},
+    "fp64": {
+        "ppm_remap": (328.5e6, 1110.6e6, 844.1e6),
+        "euler_bih_post": (282.5e6, 668.9e6, 376.0e6),
+        "euler_bih_pre": (260.9e6, 583.9e6, 300.8e6),
+        "euler_aal_tracer": (368.5e6, 482.0e6, 301.5e6),
+        "hv_laplace2": (162.0e6, 352.9e6, 210.4e6),
+        "caar_stage": (191.6e6, 320.1e6, 198.6e6),
+        "hv_laplace1": (77.6e6, 292.9e6, 164.6e6),
+        "update_q": (239.4e6, 107.9e6, 63.7e6),
+        "euler_dss_qdp": (298.0e6, 57.5e6, 51.6e6),
+        "precompute_divdp": (29.3e6, 41.9e6, 25.0e6),
+        "euler_aal_setup": (104.6e6, 41.9e6, 25.8e6),
+        "euler_qminmax": (216.7e6, 39.1e6, 28.5e6),
+        "hv_dss_update": (117.6e6, 35.4e6, 30.1e6),
+        "dss_caar": (102.9e6, 15.9e6, 15.9e6),
+        "dp3d_from_ps": (0.2e6, 5.3e6, 3.5e6),
+        "euler_dss_fvar": (14.8e6, 4.0e6, 4.0e6),
+        "euler_bih_weight": (14.2e6, 1.8e6, 1.8e6),
+        "euler_minmax_nbr": (17.8e6, 0.0e6, 0.0e6),
+        "prim_step_init": (53.3e6, 0.0e6, 0.0e6),
+    },
+    "mixed": {
+        "ppm_remap": (327.5e6, 351.4e6, 258.5e6),
+        "update_q": (239.2e6, 107.9e6, 63.7e6),
+        "caar_stage": (188.3e6, 57.7e6, 50.8e6),
+        "euler_dss_qdp": (297.9e6, 57.5e6, 51.6e6),
+        "euler_aal_tracer": (363.2e6, 53.1e6, 53.1e6),
+        "euler_bih_post": (274.5e6, 43.7e6, 43.7e6),
+        "hv_laplace2": (151.8e6, 28.0e6, 23.1e6),
+        "dss_caar": (102.9e6, 15.9e6, 15.9e6),
+        "hv_dss_update": (115.7e6, 15.9e6, 15.9e6),
+        "dp3d_from_ps": (0.2e6, 5.3e6, 3.5e6),
+        "euler_aal_setup": (104.0e6, 4.6e6, 4.6e6),
+        "euler_dss_fvar": (14.9e6, 4.0e6, 4.0e6),
+        "hv_laplace1": (70.3e6, 3.5e6, 3.5e6),
+        "euler_bih_weight": (14.2e6, 1.8e6, 1.8e6),
+        "euler_qminmax": (214.6e6, 0.1e6, 0.1e6),
+        "euler_minmax_nbr": (17.8e6, 0.0e6, 0.0e6),
+        "euler_bih_pre": (257.4e6, 0.0e6, 0.0e6),
+        "prim_step_init": (53.3e6, 0.0e6, 0.0e6),
+        "precompute_divdp": (28.8e6, 0.0e6, 0.0e6),
+    },
 }
 NCU_NE16_ELEMENTS = 1536
 
 
 def ncu_row(form: str, kernel: str, E: int, Q: int):
-    """(DRAM bytes, FP64 FLOPs) per launch scaled to E elements, or (None, None)."""
+    """(DRAM bytes, FP64 FLOPs, FP64 instructions) per launch scaled to E elements, or
+    Nones."""
     v = NCU_NE16.get(form, {}).get(kernel)
     if v is None or Q != 10:
-        return None, None
+        return None, None, None
     sc = E / NCU_NE16_ELEMENTS
-    return (v[0] * sc if v[0] is not None else None), (v[1] * sc if v[1] is not None else None)
+    return tuple(x * sc for x in v)
 
 
 def measure_link(nbytes: int = 1 << 30, reps: int = 3):
@@ -555,14 +589,18 @@ def roofline(stats, E, Q, rsize, steps, form="fp64", hbm_peak=None, fp64_peak_tf
         per_launch = nb[1] / nb[0] if nb else None
         t_launch = ms / launches * 1e-3 if launches else None
         gbs = per_launch / t_launch / 1e9 if (per_launch and t_launch) else None
-        traffic, flops = ncu_row(form, name, E, Q)
+        traffic, flops, inst = ncu_row(form, name, E, Q)
         tf = flops / t_launch / 1e12 if (flops and t_launch) else None
+        ti = inst / t_launch / 1e12 if (inst and t_launch) else None
         rows.append(dict(kernel=name, launches=launches, total_ms=ms, share=ms / total,
                          bytes_per_launch=per_launch, gbs=gbs,
                          hbm_frac=gbs / hbm_peak if (gbs and hbm_peak) else None,
                          dram_bytes_per_launch_ncu=traffic,
                          fp64_flops_per_launch=flops, fp64_tflops=tf,
-                         fp64_frac=tf / fp64_peak_tflops if (tf and fp64_peak_tflops) else None))
+                         fp64_frac=tf / fp64_peak_tflops if (tf and fp64_peak_tflops) else None,
+                         # FP64 instructions against the pipe's instruction rate (half the
+                         # FMA FLOP peak): DADD and DMUL take a full slot for one FLOP
+                         fp64_inst_frac=ti / (fp64_peak_tflops / 2) if (ti and fp64_peak_tflops) else None))
     rows.sort(key=lambda r: -r["total_ms"])
     return rows
 
@@ -699,7 +737,7 @@ def main():
     # larger, else HBM.
     if top["fp64_frac"] is not None and top["fp64_frac"] > (top["hbm_frac"] or 0.0):
         roof = {"bound": "fp64", "kernel": top["kernel"], "achieved": top["fp64_tflops"], "peak": f64peak,
-                "unit": "TFLOP/s", "frac": top["fp64_frac"],
+                "unit": "TFLOP/s", "frac": top["fp64_frac"], "fp64_inst_frac": top["fp64_inst_frac"],
                 "peak_source": "measured in this run (hx_fp64_peak: independent DFMA chains, full occupancy)",
                 "hbm": {"achieved": top["gbs"], "peak": peak, "unit": "GB/s", "frac": top["hbm_frac"],
                         "peak_source": peak_kind}}

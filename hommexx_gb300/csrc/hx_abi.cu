@@ -295,8 +295,10 @@ struct BackendT : Backend {
     qlim = dalloc<double>((size_t)E * Q * 2 * NLEV); qlim_tmp = dalloc<double>((size_t)E * Q * 2 * NLEV);
     dp0 = dalloc<double>(NLEV);
     gen_scr = dalloc<double>(n3 * 2);  // generic DSS of v / T / dp3d / omega_p (Qdp uses qscr)
-    invalid = dalloc<int>(2);  // [0] invalid layer thickness, [1] an asynchronous-copy wait gave up
-    ck(cudaMallocHost(&h_invalid, 2 * sizeof(int)), "cudaMallocHost");
+    // [0] invalid layer thickness, [1] an asynchronous-copy wait gave up, [2] the first
+    // index-check violation of the HX_BOUNDS_CHECK build
+    invalid = dalloc<int>(3);
+    ck(cudaMallocHost(&h_invalid, 3 * sizeof(int)), "cudaMallocHost");
     ck(cudaEventCreateWithFlags(&ev_qdp_in, cudaEventDisableTiming), "cudaEventCreate");
     ck(cudaEventCreateWithFlags(&ev_mark, cudaEventDisableTiming), "cudaEventCreate");
     ck(cudaEventCreateWithFlags(&ev_dyn_in, cudaEventDisableTiming), "cudaEventCreate");
@@ -446,7 +448,7 @@ struct BackendT : Backend {
     m.spheremp_d = sp_d; m.rspheremp_d = rsp_d; m.lapm = lapm;
     return m;
   }
-  DssTable table() const { return DssTable{tab_cnt, tab_src}; }
+  DssTable table() const { return DssTable{tab_cnt, tab_src, E * 16, invalid + 2}; }
   bool dss_view(const int** c, const int** sr, const double** r) const {
     *c = tab_cnt;
     *sr = tab_src;
@@ -585,8 +587,13 @@ struct BackendT : Backend {
     post("remap");
   }
   int remap_status() {
-    ck(cudaMemcpyAsync(h_invalid, invalid, 2 * sizeof(int), cudaMemcpyDeviceToHost, g_stream), "flag");
+    ck(cudaMemcpyAsync(h_invalid, invalid, 3 * sizeof(int), cudaMemcpyDeviceToHost, g_stream), "flag");
     ck(cudaStreamSynchronize(g_stream), "remap sync");
+    if (h_invalid[2]) {
+      const int code = h_invalid[2];
+      ck(cudaMemsetAsync(invalid + 2, 0, sizeof(int), g_stream), "memset");
+      fail(HX_ERR_CUDA, "device index check failed (code " + std::to_string(code) + ")");
+    }
     if (h_invalid[1]) {
       ck(cudaMemsetAsync(invalid + 1, 0, sizeof(int), g_stream), "memset");
       fail(HX_ERR_CUDA, "tracer advection: a shared-memory bulk copy did not complete");
@@ -1114,7 +1121,8 @@ struct BackendT : Backend {
 
   // One dry step on the work levels; the state enters and leaves at level tj.cur.  When
   // keep is non-null it receives the stage inputs: 0-4 the RK stage inputs, 5 .. 4+hsub
-  // the hyperviscosity subcycle inputs, 5+hsub the remap input.
+  // the hyperviscosity subcycle inputs, 5+hsub the last subcycle's output (the remap
+  // input on remap steps), so that every subcycle's output is checkpointed for its VJP.
   void traj_step(double dt, bool remap, size_t keep) {
     const int n0 = tj.cur, nm1 = (n0 + 2) % 3, np1 = (n0 + 1) % 3;
     const bool k = keep != (size_t)-1;
@@ -1136,8 +1144,8 @@ struct BackendT : Backend {
       save(5 + i, np1);
       hypervis_cycles(np1, dt, 0.0, 1);
     }
+    save(5 + hsub, np1);
     if (remap) {
-      save(5 + hsub, np1);
       launch_remap(np1, 0, false);
       launch_dp_from_ps(E, tj.dp3, tj.ps, np1, s.ps0, g_stream);
       post("dp3d_from_ps");
@@ -1319,17 +1327,12 @@ struct BackendT : Backend {
       post("remap_vjp");
     }
     for (int i = hsub - 1; i >= 0; --i) {
-      // recompute the subcycle's output on a work level
-      const int w = (tj.cur + 1) % 3;
-      launch_copy_dyn(E, level3(w), st(5 + i), g_stream);
-      {
-        WorkScope ws(*this);
-        hypervis_cycles(w, dt, 0.0, 1);
-      }
+      // the subcycle's output is the next checkpoint (the next subcycle's input, or the
+      // last subcycle's output for i = hsub - 1)
       HvVjpArgs<R> h;
       h.m = metric();
       h.dss = table();
-      h.x = st(5 + i); h.xo = level3(w); h.a = A; h.xb = P;
+      h.x = st(5 + i); h.xo = st(6 + i); h.a = A; h.xb = P;
       h.pre = bufA; h.mid = bufB;
       h.dt = dt / hsub; h.nu = s.prm.nu; h.nu_s = s.prm.nu_s; h.nu_p = s.prm.nu_p;
       h.nu_top = s.prm.nu_top; h.nu_ratio1 = s.prm.nu_ratio1; h.nu_ratio2 = s.prm.nu_ratio2;
@@ -1738,6 +1741,14 @@ int hx_run_dss(const char* name, int tl, int rsmp) {
   int rc = 0;
   int st = run([&] { rc = B().dss_field(name, tl, rsmp != 0); });
   return st ? st : rc;
+}
+
+int hx_build_flags(void) {
+#ifdef HX_BOUNDS_CHECK
+  return 1;
+#else
+  return 0;
+#endif
 }
 
 int hx_num_elems(void) { return S().E; }

@@ -79,10 +79,13 @@ __device__ __forceinline__ void vlaplace_contra_T(const Pt<R>& t, const PM<R>& m
 __device__ __forceinline__ double dss_gather_w(const double* base, long long es, int ls, int e, int l,
                                                int p, const DssTable& tab, const double* w) {
   const int ep = e * 16 + p;
+  if (!in_bounds(ep >= 0 && ep < tab.npts, tab.flag, kBoundsDssPoint)) return 0.0;
   double acc = w[ep] * base[(size_t)e * es + (size_t)l * ls + p];
-  const int n = tab.cnt[ep];
+  int n = tab.cnt[ep];
+  if (!in_bounds(n >= 0 && n <= MAXSRC, tab.flag, kBoundsDssCount)) n = 0;
   for (int k = 0; k < n; ++k) {
     const int s = tab.src[ep * MAXSRC + k];
+    if (!in_bounds(s >= 0 && s < tab.npts, tab.flag, kBoundsDssSource)) continue;
     acc += w[s] * base[(size_t)(s >> 4) * es + (size_t)l * ls + (s & 15)];
   }
   return acc;

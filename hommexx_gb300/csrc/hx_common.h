@@ -45,10 +45,23 @@ struct MetricP {
 };
 
 // DSS gather table: for (e, p) the ordered sources src[(e*16+p)*3 + k] = se*16 + sp,
-// k < cnt[e*16+p], in the reference accumulation order.
+// k < cnt[e*16+p], in the reference accumulation order.  npts = E*16 and flag (the
+// session's bounds-violation word) serve the index checks of the HX_BOUNDS_CHECK build.
 struct DssTable {
   const int* cnt;
   const int* src;
+  int npts;
+  int* flag;
+};
+
+// Codes of the HX_BOUNDS_CHECK build's index checks, recorded in the flag word (the first
+// violation wins) while the offending access is skipped.
+enum BoundsCode : int {
+  kBoundsDssPoint = 1,    // a gather for a point outside the table
+  kBoundsDssCount = 2,    // more than MAXSRC (or a negative number of) contributions
+  kBoundsDssSource = 3,   // a source index outside the mesh
+  kBoundsRemapCell = 4,   // a remap source cell (kid) outside the column
+  kBoundsTracerSlab = 5,  // a Qdp slab (tracer, time level) outside the array
 };
 
 // A 3-D field view: element e, level l, point p at base[e*es + l*ls + p].

@@ -76,6 +76,23 @@ struct Pt {
     for (int k = 0; k < 4; ++k) a += dy[k] * sh16(s, 4 * k + j);
     return a;
   }
+  // ddx(s0) + ddy(s1) and ddx(s0) - ddy(s1) as one chain of eight multiply-adds
+  __device__ __forceinline__ R dxy(R s0, R s1) const {
+    R a = dx[0] * sh16(s0, 4 * i);
+#pragma unroll
+    for (int k = 1; k < 4; ++k) a += dx[k] * sh16(s0, 4 * i + k);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) a += dy[k] * sh16(s1, 4 * k + j);
+    return a;
+  }
+  __device__ __forceinline__ R dxmy(R s0, R s1) const {
+    R a = dx[0] * sh16(s0, 4 * i);
+#pragma unroll
+    for (int k = 1; k < 4; ++k) a += dx[k] * sh16(s0, 4 * i + k);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) a -= dy[k] * sh16(s1, 4 * k + j);
+    return a;
+  }
   // sum_k w(i,k) dvv[k][j]  — weak-form row contraction
   __device__ __forceinline__ R wrow(R w) const {
     R a = 0;
@@ -99,6 +116,8 @@ struct PM {
   R gr00, gr01, gr10, gr11;  // Dinv * rrearth, for gradient_sphere
   R dm00, dm01, dm10, dm11;  // Dinv * metdet, for divergence_sphere
   R l00, l01, l10, l11;  // spheremp * (Dinv Dinv^T) * rrearth, for laplace_simple
+  R e00, e01, e10, e11;  // D * rrearth, mp / metdet / rrearth and 2 spheremp rrearth^2, for
+  R mpf, f2;             // vlaplace_sphere_wk_contra
   __device__ __forceinline__ void load(const MetricP<R>& m, int e, int p) {
     const R* Di = m.Dinv + (size_t)e * 64;
     const R* D = m.D + (size_t)e * 64;
@@ -119,6 +138,9 @@ struct PM {
     l01 = sp * (di00 * di01 + di10 * di11) * rre<R>();
     l10 = sp * (di01 * di00 + di11 * di10) * rre<R>();
     l11 = sp * (di01 * di01 + di11 * di11) * rre<R>();
+    e00 = d00 * rre<R>(); e01 = d01 * rre<R>(); e10 = d10 * rre<R>(); e11 = d11 * rre<R>();
+    mpf = mp * fdiv;
+    f2 = R(2) * sp * rre<R>() * rre<R>();
   }
 };
 
@@ -136,14 +158,14 @@ template <typename R>
 __device__ __forceinline__ R divergence_sphere(const Pt<R>& t, const PM<R>& m, R v0, R v1) {
   const R gv0 = m.dm00 * v0 + m.dm10 * v1;
   const R gv1 = m.dm01 * v0 + m.dm11 * v1;
-  return (t.ddx(gv0) + t.ddy(gv1)) * m.fdiv;
+  return t.dxy(gv0, gv1) * m.fdiv;
 }
 
 template <typename R>
 __device__ __forceinline__ R vorticity_sphere(const Pt<R>& t, const PM<R>& m, R v0, R v1) {
   const R c0 = m.d00 * v0 + m.d01 * v1;
   const R c1 = m.d10 * v0 + m.d11 * v1;
-  return (t.ddx(c1) - t.ddy(c0)) * m.fdiv;
+  return t.dxmy(c1, c0) * m.fdiv;
 }
 
 // divergence_sphere_wk of the vector (g0, g1)
@@ -201,28 +223,27 @@ __device__ __forceinline__ R laplace_tensor(const Pt<R>& t, const PM<R>& m, cons
   return divergence_sphere_wk(t, m, t0, t1);
 }
 
-// vlaplace_sphere_wk_contra (SphereOperators.hpp:816-862)
+// vlaplace_sphere_wk_contra (SphereOperators.hpp:816-862): grad_sphere_wk_testcov of the
+// divergence (times nu_ratio when it applies) minus curl_sphere_wk_testcov of the
+// vorticity, plus 2 spheremp v / rearth^2.  Factors are folded per point: mp times the
+// divergence and the vorticity take mp / metdet / rearth (m.mpf), and the two weak
+// operators' covariant results are combined before D / rearth (m.e) is applied once.
 template <typename R>
 __device__ __forceinline__ void vlaplace_contra(const Pt<R>& t, const PM<R>& m, R nu_ratio, R v0, R v1,
                                                 R& l0, R& l1) {
-  R div = divergence_sphere(t, m, v0, v1);
-  if (nu_ratio > R(0) && nu_ratio != R(1)) div *= nu_ratio;
-  // grad_sphere_wk_testcov(div)
-  const R w = m.mp * div;
+  const R gv0 = m.dm00 * v0 + m.dm10 * v1;
+  const R gv1 = m.dm01 * v0 + m.dm11 * v1;
+  R w = t.dxy(gv0, gv1) * m.mpf;  // mp div
+  if (nu_ratio > R(0) && nu_ratio != R(1)) w *= nu_ratio;
+  const R c0 = m.d00 * v0 + m.d01 * v1;
+  const R c1 = m.d10 * v0 + m.d11 * v1;
+  const R wv = t.dxmy(c1, c0) * m.mpf;  // mp vort
   const R X = t.wrow(w), Y = t.wcol(w);
-  const R b0 = -(m.a00 * X + m.a01 * Y);
-  const R b1 = -(m.a10 * X + m.a11 * Y);
-  R g0 = (m.d00 * b0 + m.d10 * b1) * rre<R>();
-  R g1 = (m.d01 * b0 + m.d11 * b1) * rre<R>();
-  // curl_sphere_wk_testcov_update(-1, 1, vort, g)
-  const R vort = vorticity_sphere(t, m, v0, v1);
-  const R wv = m.mp * vort;
-  const R sb0 = -t.wcol(wv), sb1 = t.wrow(wv);
-  g0 = g0 - (m.d00 * sb0 + m.d10 * sb1) * rre<R>();
-  g1 = g1 - (m.d01 * sb0 + m.d11 * sb1) * rre<R>();
-  const R f = R(2) * m.sp * rre<R>() * rre<R>();
-  l0 = f * v0 + g0;
-  l1 = f * v1 + g1;
+  // (grad_wk_testcov - curl_wk_testcov) in covariant components
+  const R q0 = t.wcol(wv) - (m.a00 * X + m.a01 * Y);
+  const R q1 = -(m.a10 * X + m.a11 * Y) - t.wrow(wv);
+  l0 = m.f2 * v0 + (m.e00 * q0 + m.e10 * q1);
+  l1 = m.f2 * v1 + (m.e01 * q0 + m.e11 * q1);
 }
 
 // vlaplace_sphere_wk_cartesian (SphereOperators.hpp:750-814); tv = tensorVisc[0..3],
@@ -238,15 +259,37 @@ __device__ __forceinline__ void vlaplace_cartesian(const Pt<R>& t, const PM<R>& 
   l1 = s2c[3] * lc[0] + s2c[4] * lc[1] + s2c[5] * lc[2] + f * v1;
 }
 
+// Index checks of the debug build (compiled with -DHX_BOUNDS_CHECK, the library's
+// stand-in for a memory checker): an index outside its array records `code` in the flag
+// word (the first violation wins) and the caller skips the access; the host reports the
+// code after the interval (HX_ERR_CUDA).  In the regular build the check is the constant
+// true and costs nothing.
+__device__ __forceinline__ bool in_bounds(bool ok, int* flag, int code) {
+#ifdef HX_BOUNDS_CHECK
+  if (!ok) {
+    if (flag) atomicCAS(flag, 0, code);
+    return false;
+  }
+#else
+  (void)ok;
+  (void)flag;
+  (void)code;
+#endif
+  return true;
+}
+
 // DSS gather of one point-level: own value plus the table's sources, in order, in double.
 template <typename T>
 __device__ __forceinline__ double dss_gather(const T* base, long long es, int ls, int e, int l, int p,
                                              const DssTable& tab) {
   const int ep = e * 16 + p;
+  if (!in_bounds(ep >= 0 && ep < tab.npts, tab.flag, kBoundsDssPoint)) return 0.0;
   double acc = (double)base[(size_t)e * es + (size_t)l * ls + p];
-  const int n = tab.cnt[ep];
+  int n = tab.cnt[ep];
+  if (!in_bounds(n >= 0 && n <= MAXSRC, tab.flag, kBoundsDssCount)) n = 0;
   for (int k = 0; k < n; ++k) {
     const int s = tab.src[ep * MAXSRC + k];
+    if (!in_bounds(s >= 0 && s < tab.npts, tab.flag, kBoundsDssSource)) continue;
     acc += (double)base[(size_t)(s >> 4) * es + (size_t)l * ls + (s & 15)];
   }
   return acc;
@@ -339,6 +382,14 @@ template <typename T> __device__ __forceinline__ bool less(T a, T b) { return a 
 template <> __device__ __forceinline__ bool less<double>(double a, double b) {
   return dkey(a) < dkey(b);  // exact for non-NaN except that -0 < +0
 }
+// a < b for non-NaN values, zeros of either sign equal (the IEEE comparison): FP32 as is,
+// FP64 on the integer pipe.
+__device__ __forceinline__ long long dkz(double x) {
+  const long long k = dkey(x);
+  return k == -1 ? 0 : k;  // -0 -> +0
+}
+template <typename T> __device__ __forceinline__ bool lt(T a, T b) { return a < b; }
+template <> __device__ __forceinline__ bool lt<double>(double a, double b) { return dkz(a) < dkz(b); }
 // min(|a|, |b|, |c|) with the sign of s.
 template <typename T> __device__ __forceinline__ T min3abs_signed(T a, T b, T c, T s) {
   return fmin(fmin(fabs(a), fabs(b)), fabs(c)) * copysign(T(1), s);

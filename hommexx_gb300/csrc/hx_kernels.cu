@@ -71,17 +71,20 @@ __global__ void __launch_bounds__(LG * 16) k_caar(CaarArgs<R> a) {
   PM<R> m;
   m.load(a.m, e, p);
   const R eta = R(a.eta_ave_w);
+  const bool accum = a.eta_ave_w != 0.0;
   const size_t vN0 = ((size_t)e * NTL + a.n0) * NLEV * 32;
   const size_t sN0 = ((size_t)e * NTL + a.n0) * NLEV * 16;
   // ---- phase A: v dp, vn0, div(v dp), T_v ----
 #pragma unroll 1
   for (int k = 0; k < NL; ++k) {
     const int l = lg + LG * k;
+    // hardware conversions here: after the global loads the integer-pipe form measured
+    // slower (8.8 vs 8.1 ms per ne30 interval in the mixed form)
     const R u = cvt_hw<R>(a.v[vN0 + l * 32 + p]), w = cvt_hw<R>(a.v[vN0 + l * 32 + 16 + p]);
     const double td = a.T[sN0 + l * 16 + p], dd = a.dp[sN0 + l * 16 + p];
     const R d = cvt_hw<R>(dd);
     const R vd0 = u * d, vd1 = w * d;
-    if (a.eta_ave_w != 0.0) {  // stages 2-4 accumulate nothing (eta_ave_w = 0)
+    if (accum) {  // stages 2-4 accumulate nothing (eta_ave_w = 0)
       const size_t iv = ((size_t)e * NLEV + l) * 32 + p;
       a.vn0[iv] += dbl_hw(eta * vd0);
       a.vn0[iv + 16] += dbl_hw(eta * vd1);
@@ -206,7 +209,7 @@ __global__ void __launch_bounds__(LG * 16) k_caar(CaarArgs<R> a) {
     const R a0 = m.gr00 * u + m.gr10 * w, a1 = m.gr01 * u + m.gr11 * w;
     const R vgp = a0 * p0 + a1 * p1;
     const R omega = (vgp - (cvt<R>(s_om[l * SROW + p]) + R(0.5) * div)) * rp;
-    if (a.eta_ave_w != 0.0) a.omega_p[((size_t)e * NLEV + l) * 16 + p] += dbl_hw(eta * omega);
+    if (accum) a.omega_p[((size_t)e * NLEV + l) * 16 + p] += dbl_hw(eta * omega);
     // time level "nm1" (RK combine of stage 5 fused here), in double
     double tm = a.T[sM + l * 16 + p], dm = a.dp[sM + l * 16 + p];
     double vm0 = a.v[vM + l * 32 + p], vm1 = a.v[vM + l * 32 + 16 + p];
@@ -244,7 +247,7 @@ __global__ void __launch_bounds__(LG * 16) k_caar(CaarArgs<R> a) {
         vva0 += facm * (u - cvt<R>(vc[-32]));
         vva1 += facm * (w - cvt<R>(vc[-16]));
       }
-      if (a.eta_ave_w != 0.0) a.eta_acc[((size_t)e * NLEV + l) * 16 + p] += a.eta_ave_w * el;
+      if (accum) a.eta_acc[((size_t)e * NLEV + l) * 16 + p] += a.eta_ave_w * el;
     }
     // temperature (compute_temperature_np1)
     R tv;
@@ -253,11 +256,9 @@ __global__ void __launch_bounds__(LG * 16) k_caar(CaarArgs<R> a) {
     const R vgt = a0 * T0 + a1 * T1;
     R ttens = R(kKappa) * tv * omega - vgt;
     if (a.rsplit == 0) ttens -= tva;
-    // Conversions on the integer pipe (dbl, and in phase C cvt / rel) relieve the FP64
-    // pipe this kernel is bound by (a hardware double -> float conversion takes that pipe
-    // like an FP64 add).  Phase A keeps the hardware conversions: there they follow the
-    // global loads, and the integer form measured slower (9.2 vs 8.4 ms per ne30
-    // interval), while in phase C it measured faster (8.2 vs 8.4 ms).
+    // Conversions on the integer pipe here (dbl, cvt, rel): a hardware double <-> float
+    // conversion takes the FP64 pipe like an FP64 add, and in phase C the integer form
+    // measured faster.
     const double tnew = spd * (dbl(ttens * dt) + tm);
     // velocity (compute_velocity_np1 with compute_energy_grad): grad(KE + phi) +
     // R T_v / p grad p = (Dinv / rearth) (dE/dx + rr dp/dx) with rr = R T_v / p
@@ -903,43 +904,48 @@ __device__ bool limiter_level(int option, R* x, const R* c, R s1, double& minp_i
   if (s0 > maxp * s1) { maxp = s0 / s1; maxp_io = dbl(maxp); }
   if (!any_outside(x, minp, maxp)) return false;  // no clipping: addmass = 0
   const R mass = s0;
+  // The clip and bound tests below are exact comparisons (lt: on the integer pipe in FP64).
   if (option == 8) {
     const R tol = R(5e-14);
     for (int iter = 0; iter < 15; ++iter) {
       R addmass = 0;
 #pragma unroll
       for (int k = 0; k < 16; ++k) {
-        R delta = 0;
-        if (x[k] > maxp) { delta = x[k] - maxp; x[k] = maxp; }
-        else if (x[k] < minp) { delta = x[k] - minp; x[k] = minp; }
-        addmass += delta * c[k];
+        const bool hi = lt(maxp, x[k]), lo = !hi && lt(x[k], minp);
+        if (hi || lo) {
+          const R b = hi ? maxp : minp;
+          addmass += (x[k] - b) * c[k];
+          x[k] = b;
+        }
       }
       if (fabs(addmass) <= tol * fabs(mass)) break;
       R wsum = 0;
       if (addmass > R(0)) {
 #pragma unroll
-        for (int k = 0; k < 16; ++k) if (x[k] < maxp) wsum += c[k];
+        for (int k = 0; k < 16; ++k) if (lt(x[k], maxp)) wsum += c[k];
         if (wsum == R(0)) break;
         const R adw = addmass / wsum;
 #pragma unroll
-        for (int k = 0; k < 16; ++k) x[k] += (x[k] < maxp) ? adw : R(0);
+        for (int k = 0; k < 16; ++k) if (lt(x[k], maxp)) x[k] += adw;
       } else {
 #pragma unroll
-        for (int k = 0; k < 16; ++k) if (x[k] > minp) wsum += c[k];
+        for (int k = 0; k < 16; ++k) if (lt(minp, x[k])) wsum += c[k];
         if (wsum == R(0)) break;
         const R adw = addmass / wsum;
 #pragma unroll
-        for (int k = 0; k < 16; ++k) x[k] += (x[k] > minp) ? adw : R(0);
+        for (int k = 0; k < 16; ++k) if (lt(minp, x[k])) x[k] += adw;
       }
     }
   } else {
     R addmass = 0;
 #pragma unroll
     for (int k = 0; k < 16; ++k) {
-      R delta = 0;
-      if (x[k] > maxp) { delta = x[k] - maxp; x[k] = maxp; }
-      else if (x[k] < minp) { delta = x[k] - minp; x[k] = minp; }
-      addmass += delta * c[k];
+      const bool hi = lt(maxp, x[k]), lo = !hi && lt(x[k], minp);
+      if (hi || lo) {
+        const R b = hi ? maxp : minp;
+        addmass += (x[k] - b) * c[k];
+        x[k] = b;
+      }
     }
     if (addmass == R(0)) return true;
     R fac = 0;
@@ -991,10 +997,14 @@ __global__ void __launch_bounds__(LG * 16, kF32<R> ? 6 : 3) k_aal_tracer(EulerAr
   const int e = blockIdx.x;
   const int tid = threadIdx.x, p = tid & 15, lg = tid >> 4;
   const double* slab0 = a.qdp + ((size_t)e * QTL + a.n0_qdp) * a.Q * NLEV * 16;
+  // every slab this CTA copies lies in Qdp: tracer level 0 or 1, element inside the grid
+  const bool slabs_ok = in_bounds(a.n0_qdp >= 0 && a.n0_qdp < QTL && e < (int)gridDim.x, a.err + 1,
+                                  kBoundsTracerSlab);
   if (tid == 0) {
     mbar_init(bar, 1);
-    if (a.Q > 0) bulk_load(q_buf, slab0, kSlab, bar);
+    if (a.Q > 0 && slabs_ok) bulk_load(q_buf, slab0, kSlab, bar);
   }
+  if (!slabs_ok) return;
   Pt<R> t;
   t.init(p);
   PM<R> m;
@@ -1044,7 +1054,7 @@ __global__ void __launch_bounds__(LG * 16, kF32<R> ? 6 : 3) k_aal_tracer(EulerAr
       const int l = lg + LG * k;
       const double qdd = q_buf[l * 16 + p];
       const R qd = cvt<R>(qdd);
-      const R dvs = t.ddx(w0[k] * qd) + t.ddy(w1[k] * qd);  // div(vstar Qdp) / fdiv
+      const R dvs = t.dxy(w0[k] * qd, w1[k] * qd);  // div(vstar Qdp) / fdiv
       const double q0 = add_hv ? a.qtens[qb + l * 16 + p] : 0.0;
       if constexpr (kF32<R>) s_q[l * SROW + p] = qdd + dbl(mdf * dvs) + q0;
       else s_q[l * SROW + p] = (qdd + mdf * dvs + q0);
@@ -1087,20 +1097,65 @@ template <typename R> constexpr size_t aal_smem() {
   return aal_buf_offset<R>() + NLEV * 16 * sizeof(double) + 16;  // + the Qdp slab and its barrier
 }
 
+// The nine levels lo, lo + 8, ... of one point with N contributions from other elements
+// at offsets so[] from the point's own value; N is uniform within a warp (warps grouped by
+// point class), so each case is a branch, not a set of predicated adds.
+template <int N, bool AVG>
+__device__ __forceinline__ void dss_levels(const double* own, const long long* so, double* dst,
+                                           const double* s0, double f, int lo) {
+#pragma unroll 3
+  for (int l = lo; l < NLEV; l += 8) {
+    double acc = own[l * 16];
+#pragma unroll
+    for (int k = 0; k < N; ++k) acc += own[so[k] + l * 16];
+    if constexpr (AVG) dst[l * 16] = fma(acc, f, s0[l * 16] * (1.0 / 3.0));
+    else dst[l * 16] = acc * f;
+  }
+}
+
 // DSS(rspheremp) of the tracer scratch into Qdp(np1); with time_avg the last RK2 stage
-// also applies qdp_time_avg: Qdp(np1) = (Qdp(n0) + 2 Qdp(np1)) / 3.
+// also applies qdp_time_avg: Qdp(np1) = (Qdp(n0) + 2 Qdp(np1)) / 3, formed as
+// Qdp(n0) / 3 + gather (2/3 rspheremp).  Grid E*Q, 128 threads: warps by point class
+// over a group of 8 levels, each thread its point on the 9 levels lo, lo + 8, ..., so the
+// point's table entries and factors are read once.
 template <typename R>
 __global__ void __launch_bounds__(EQ_THREADS) k_dss_tracers(EulerArgs<R> a, int time_avg) {
-  int e, q, l, p;
-  eq_index_dss(a.Q, e, q, l, p);
-  const double rs = a.m.rspheremp_d[e * 16 + p];
-  const double v = dss_gather(a.qscr + (size_t)q * NLEV * 16, (long long)a.Q * NLEV * 16, 16, e, l, p, a.dss) * rs;
-  const size_t d = ((((size_t)e * QTL + a.np1_qdp) * a.Q + q) * NLEV + l) * 16 + p;
+  const int eq = blockIdx.x, e = eq / a.Q, q = eq - e * a.Q;
+  int lo, p;
+  dss_thread_point(lo, p);
+  const int ep = e * 16 + p;
+  const double rs = a.m.rspheremp_d[ep];
+  const long long es = (long long)a.Q * NLEV * 16;
+  double* dst = a.qdp + (((size_t)e * QTL + a.np1_qdp) * a.Q + q) * NLEV * 16 + p;
+  if (!in_bounds(ep < a.dss.npts, a.dss.flag, kBoundsDssPoint)) return;
+  int n = a.dss.cnt[ep];
+  if (!in_bounds(n >= 0 && n <= MAXSRC, a.dss.flag, kBoundsDssCount)) n = 0;
+  long long so[MAXSRC] = {0, 0, 0};  // offsets of the sources' values from this point's
+#pragma unroll
+  for (int k = 0; k < MAXSRC; ++k) {
+    if (k < n) {
+      int sk = a.dss.src[ep * MAXSRC + k];
+      if (!in_bounds(sk >= 0 && sk < a.dss.npts, a.dss.flag, kBoundsDssSource)) sk = ep;
+      so[k] = ((long long)(sk >> 4) - e) * es + (sk & 15) - p;
+    }
+  }
+  const double* own = a.qscr + (size_t)q * NLEV * 16 + (size_t)e * es + p;
   if (time_avg) {
-    const size_t s0 = ((((size_t)e * QTL + a.avg_n0_qdp) * a.Q + q) * NLEV + l) * 16 + p;
-    a.qdp[d] = (a.qdp[s0] + 2.0 * v) * (1.0 / 3.0);
+    const double f = rs * (2.0 / 3.0);
+    const double* s0 = a.qdp + (((size_t)e * QTL + a.avg_n0_qdp) * a.Q + q) * NLEV * 16 + p;
+    switch (n) {
+      case 0: dss_levels<0, true>(own, so, dst, s0, f, lo); break;
+      case 1: dss_levels<1, true>(own, so, dst, s0, f, lo); break;
+      case 2: dss_levels<2, true>(own, so, dst, s0, f, lo); break;
+      default: dss_levels<3, true>(own, so, dst, s0, f, lo); break;
+    }
   } else {
-    a.qdp[d] = v;
+    switch (n) {
+      case 0: dss_levels<0, false>(own, so, dst, nullptr, rs, lo); break;
+      case 1: dss_levels<1, false>(own, so, dst, nullptr, rs, lo); break;
+      case 2: dss_levels<2, false>(own, so, dst, nullptr, rs, lo); break;
+      default: dss_levels<3, false>(own, so, dst, nullptr, rs, lo); break;
+    }
   }
 }
 
@@ -1168,15 +1223,11 @@ struct RemapLayout {
 
 // (ar - cm) (cm - al) > 0, the parabola's monotonicity test: FP32 as is; FP64 as exact
 // comparisons on the integer pipe (zeros of either sign compare equal).
-__device__ __forceinline__ long long dkey0(double x) {
-  const long long k = dkey(x);
-  return k == -1 ? 0 : k;  // -0 -> +0
-}
 template <typename T> __device__ __forceinline__ bool monotone(T al, T cm, T ar) {
   return (ar - cm) * (cm - al) > T(0);
 }
 template <> __device__ __forceinline__ bool monotone<double>(double al, double cm, double ar) {
-  const long long kl = dkey0(al), kc = dkey0(cm), kr = dkey0(ar);
+  const long long kl = dkz(al), kc = dkz(cm), kr = dkz(ar);
   return (kr > kc && kc > kl) || (kr < kc && kc < kl);
 }
 // The slope limiter min(|da|, |2 y|, |2 x|) with the sign of da: FP32 as is; FP64 on the
@@ -1237,20 +1288,18 @@ __device__ __forceinline__ void ppm_cells(int l0, int remap_alg, const T* A, con
     T al = ai[jp], ar = ai[jp + 1];
     const T cm = A[jp];
     if (!monotone(al, cm, ar)) { al = cm; ar = cm; }
+    // The two overshoot corrections are selected, not branched on: a warp whose lanes
+    // disagree would otherwise run both bodies for all of them.  When the first applies
+    // (al = 3 A - 2 ar) the second test is (ar - al)(A - (al + ar)/2) = 3/2 (ar - A)^2
+    // < -3/2 (ar - A)^2, never true, so it is evaluated on the unmodified edges only.
     T d = ar - al, s2 = al + ar;
-    T q = d * d * sixth, r = d * (cm - s2 * T(0.5));
-    if (less(q, r)) {
-      al = T(3) * cm - T(2) * ar;
-      d = ar - al;
-      s2 = al + ar;
-      q = d * d * sixth;
-      r = d * (cm - s2 * T(0.5));
-    }
-    if (less(r, -q)) {
-      ar = T(3) * cm - T(2) * al;
-      d = ar - al;
-      s2 = al + ar;
-    }
+    const T q = d * d * sixth, r = d * (cm - s2 * T(0.5));
+    const bool fix_l = less(q, r), fix_r = !fix_l && less(r, -q);
+    const T c3 = T(3) * cm;
+    al = fix_l ? c3 - T(2) * ar : al;
+    ar = fix_r ? c3 - T(2) * al : ar;
+    d = ar - al;
+    s2 = al + ar;
     T c0 = T(1.5) * cm - s2 * T(0.25), c1 = d, c2 = T(3) * (s2 - T(2) * cm);
     if (remap_alg == 2 && (jp < 2 || jp >= NLEV - 2)) {  // PpmFixedParabola
       c0 = cm;
@@ -1319,7 +1368,7 @@ __device__ __forceinline__ void ppm_cells_delta(int l0, int remap_alg, const flo
 // cumulative masses and the grid in FP64, the bottom interface carrying the exact column
 // mass (mass fixer).  Divisions are multiplications by Newton reciprocals.
 template <typename R>
-__global__ void __launch_bounds__(RT) k_remap(RemapArgs a) {
+__global__ void __launch_bounds__(RT, 4) k_remap(RemapArgs a) {
   using LY = RemapLayout<R>;
   constexpr bool lo = kF32<R>;
   extern __shared__ double rsm[];
@@ -1424,6 +1473,7 @@ __global__ void __launch_bounds__(RT) k_remap(RemapArgs a) {
       kk = 1;
       atomicExch(a.invalid, 1);
     }
+    if (!in_bounds(kk >= 1 && kk <= NLEV, a.invalid + 2, kBoundsRemapCell)) kk = 1;
     kid[k3] = kk - 1;
     const double x2 = (pk - (pio[kk - 1] + pio[kk]) * 0.5) * rD[kk - 1];
     wz[k3][0] = x2 + 0.5;
@@ -1462,16 +1512,31 @@ __global__ void __launch_bounds__(RT) k_remap(RemapArgs a) {
   }
   __syncwarp();
   const int nvar = 3 + a.Q;
-#pragma unroll 1
-  for (int var = a.rsplit == 0 ? 3 : 0; var < nvar; ++var) {
-    // extrinsic values (v dp, T dp for the states; Qdp as is) and cell means
-    double x[RLV];
+  // The variable's values at this lane's levels: v (two components), T, then the
+  // tracers.  Each variable's loads are issued one variable ahead, so their latency
+  // overlaps the reconstruction of the previous one.
+  auto load = [&](int var, double* y) {
 #pragma unroll
     for (int k = 0; k < RLV; ++k) {
       const int l = l0 + k;
-      if (var < 2) x[k] = a.v[vb + (size_t)l * 32 + var * 16] * sv[k];
-      else if (var == 2) x[k] = a.T[sb + (size_t)l * 16] * sv[k];
-      else x[k] = a.qdp[((((size_t)e * QTL + a.n0_qdp) * a.Q + (var - 3)) * NLEV + l) * 16 + p];
+      if (var < 2) y[k] = a.v[vb + (size_t)l * 32 + var * 16];
+      else if (var == 2) y[k] = a.T[sb + (size_t)l * 16];
+      else y[k] = a.qdp[((((size_t)e * QTL + a.n0_qdp) * a.Q + (var - 3)) * NLEV + l) * 16 + p];
+    }
+  };
+  const int var0 = a.rsplit == 0 ? 3 : 0;
+  double xn[RLV];
+  if (var0 < nvar) load(var0, xn);
+#pragma unroll 1
+  for (int var = var0; var < nvar; ++var) {
+    // extrinsic values (v dp, T dp for the states; Qdp as is) and cell means
+    double x[RLV];
+#pragma unroll
+    for (int k = 0; k < RLV; ++k) x[k] = var < 3 ? xn[k] * sv[k] : xn[k];
+    if (var + 1 < nvar) load(var + 1, xn);
+#pragma unroll
+    for (int k = 0; k < RLV; ++k) {
+      const int l = l0 + k;
       if (!lo || var < 3) A[l] = x[k] * rD[l];
       else Af[l] = d2f_rn(x[k]) * rDf[l];
     }
@@ -1750,7 +1815,7 @@ void launch_euler_step(EulerArgs<R>& a, int E, int time_avg, cudaStream_t s) {
     }
     {
       KScope k("euler_dss_qdp", s);
-      k_dss_tracers<R><<<dim3(E * a.Q, NLEV / EQ_LEVELS), EQ_THREADS, 0, s>>>(a, time_avg);
+      k_dss_tracers<R><<<E * a.Q, EQ_THREADS, 0, s>>>(a, time_avg);
     }
   }
   {

@@ -185,6 +185,11 @@ int hx_qsize(void);
 int hx_enable_timing(int on);
 int hx_kernel_stats(char* names, int name_len, long long* launches, double* total_ms,
                     int max);
+/* No counterpart in the reference.  Bit 0: the library was built with device index
+ * checks (HX_BOUNDS_CHECK=1 at build time: DSS table sources, the remap's source-cell
+ * search and the tracer slabs are checked, a violation is reported as HX_ERR_CUDA by the
+ * interval that met it, and the access is skipped). */
+int hx_build_flags(void);
 /* Number of kernels this library launched since initialisation. */
 long long hx_launch_count(void);
 /* Block the host until all device work of the session has finished. */

@@ -49,9 +49,24 @@ def test_gpu_library_exports_every_declared_function(gpu_lib_cpu):
     assert not missing, missing
 
 
+def test_bounds_checked_build_exports_every_declared_function():
+    """The debug build with device index checks (HX_BOUNDS_CHECK) compiles, loads without
+    a GPU and says so in hx_build_flags."""
+    import sys
+    from hommexx_gb300 import build as B
+    path = B.build(bounds_check=True)
+    # loaded in a process of its own: its kernels carry the regular library's names
+    r = subprocess.run([sys.executable, "-c", f"import ctypes; print(ctypes.CDLL({path!r}).hx_build_flags())"],
+                       capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0 and r.stdout.strip() == "1", r.stdout + r.stderr
+    exp = exported(path)
+    missing = [n for n in declared_functions() if n not in exp]
+    assert not missing, missing
+
+
 def test_oracle_exports_reference_surface(oracle_path):
     exp = exported(oracle_path)
-    device_only = ("hx_dss_noalloc", "hx_cube_mesh", "hx_fp64_peak")
+    device_only = ("hx_dss_noalloc", "hx_cube_mesh", "hx_fp64_peak", "hx_build_flags")
     missing = [n for n in declared_functions() if n not in exp and n not in device_only]
     assert not missing, missing
 
