@@ -312,15 +312,16 @@ __device__ __forceinline__ void dss_thread_point(int& lo, int& p) {
 
 // ---- segmented column scans (128 threads: 16 columns x 8 segments of 9 levels) ------
 // Exclusive prefix of the per-segment totals within an 8-lane group.
-__device__ __forceinline__ double seg_excl_prefix(double tot, int seg) {
-  double incl = tot;
+template <typename T>
+__device__ __forceinline__ T seg_excl_prefix(T tot, int seg) {
+  T incl = tot;
 #pragma unroll
   for (int off = 1; off < 8; off <<= 1) {
-    const double y = __shfl_up_sync(FULL, incl, off, 8);
+    const T y = __shfl_up_sync(FULL, incl, off, 8);
     if (seg >= off) incl += y;
   }
-  double ex = __shfl_up_sync(FULL, incl, 1, 8);
-  return seg == 0 ? 0.0 : ex;
+  T ex = __shfl_up_sync(FULL, incl, 1, 8);
+  return seg == 0 ? T(0) : ex;
 }
 // Exclusive suffix (sum of later segments).
 __device__ __forceinline__ double seg_excl_suffix(double tot, int seg) {

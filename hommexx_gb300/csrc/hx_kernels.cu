@@ -154,24 +154,49 @@ __global__ void __launch_bounds__(LG * 16) k_caar(CaarArgs<R> a) {
       s_dp[(l0 + k) * SROW + col] = ph;  // dp no longer needed: holds phi now
       phig[(l0 + k) * 16 + col] = ph;
     }
-    // omega integral: exclusive prefix of div_vdp (the mixed form's FP32 div(v dp)
-    // widened exactly on the integer pipe)
-    double dv[9];
+    // omega integral: exclusive prefix of div_vdp.  The mixed form sums its FP32
+    // div(v dp) in FP32 (unlike the pressure and geopotential integrals, it feeds only the
+    // omega term of the FP32 tendencies) and widens the partial sums exactly on the
+    // integer pipe; with rsplit = 0 the same sums give eta_dot_dpdn, whose accumulation
+    // sets the tracers' source thickness, and stay in FP64.
+    auto omega_fp64 = [&]() {
+      double dv[9];
 #pragma unroll
-    for (int k = 0; k < 9; ++k) {
-      if constexpr (kF32<R>) dv[k] = dbl(f_div[(l0 + k) * 16 + col]);
-      else dv[k] = s_div[(l0 + k) * SROW + col];
+      for (int k = 0; k < 9; ++k) {
+        if constexpr (kF32<R>) dv[k] = dbl(f_div[(l0 + k) * 16 + col]);
+        else dv[k] = s_div[(l0 + k) * SROW + col];
+      }
+      double dt_ = 0.0;
+#pragma unroll
+      for (int k = 0; k < 9; ++k) dt_ += dv[k];
+      double acc = seg_excl_prefix(dt_, seg);
+#pragma unroll
+      for (int k = 0; k < 9; ++k) {
+        s_om[(l0 + k) * SROW + col] = acc;
+        acc = acc + dv[k];
+      }
+      if (seg == 7) s_tot[col] = acc;
+    };
+    if constexpr (kF32<R>) {
+      if (a.rsplit != 0) {
+        float dvf[9], tf = 0.0f;
+#pragma unroll
+        for (int k = 0; k < 9; ++k) {
+          dvf[k] = f_div[(l0 + k) * 16 + col];
+          tf += dvf[k];
+        }
+        float accf = seg_excl_prefix(tf, seg);
+#pragma unroll
+        for (int k = 0; k < 9; ++k) {
+          s_om[(l0 + k) * SROW + col] = dbl(accf);
+          accf += dvf[k];
+        }
+      } else {
+        omega_fp64();
+      }
+    } else {
+      omega_fp64();
     }
-    double dt_ = 0.0;
-#pragma unroll
-    for (int k = 0; k < 9; ++k) dt_ += dv[k];
-    double acc = seg_excl_prefix(dt_, seg);
-#pragma unroll
-    for (int k = 0; k < 9; ++k) {
-      s_om[(l0 + k) * SROW + col] = acc;
-      acc = acc + dv[k];
-    }
-    if (seg == 7) s_tot[col] = acc;
   }
   __syncthreads();
   // ---- phase C: omega_p, T, v, dp3d at np1 ----
@@ -286,24 +311,57 @@ __global__ void __launch_bounds__(LG * 16) k_caar(CaarArgs<R> a) {
 
 // DSS of the Caar output into the state of time level np1, times rspheremp
 // (BoundaryExchange::exchange(rspheremp) on v, T, dp3d: CaarFunctor.cpp:114).
-// Grid (E, 9), 128 threads: 8 levels per block, warps by point class.
+// Grid E, 128 threads: warps by point class over a group of 8 levels, each thread its
+// point on the 9 levels lo, lo + 8, ...; the number of contributions N is uniform within
+// a warp, so each case is a branch taken once, and every field sums in the table's order.
+template <int N>
+__device__ __forceinline__ void dss_state_levels(const double* own, const long long* so, double* vo, double* To,
+                                                 double* dpo, double r, int lo) {
+#pragma unroll 3
+  for (int l = lo; l < NLEV; l += 8) {
+    double acc[4];
+#pragma unroll
+    for (int f = 0; f < 4; ++f) acc[f] = own[l * 64 + f * 16];
+#pragma unroll
+    for (int k = 0; k < N; ++k)
+#pragma unroll
+      for (int f = 0; f < 4; ++f) acc[f] += own[so[k] + l * 64 + f * 16];
+    vo[l * 32] = acc[0] * r;
+    vo[l * 32 + 16] = acc[1] * r;
+    To[l * 16] = acc[2] * r;
+    dpo[l * 16] = acc[3] * r;
+  }
+}
+
 __global__ void __launch_bounds__(128) k_dss_state(const double* __restrict__ src, double* v, double* T,
                                                    double* dp, int np1, const double* __restrict__ rsmp,
                                                    DssTable tab) {
   int lo, p;
   dss_thread_point(lo, p);
-  const int e = blockIdx.x, l = blockIdx.y * 8 + lo;
-  const double r = rsmp[e * 16 + p];
-  const double a0 = dss_gather(src, NLEV * 64, 64, e, l, p, tab) * r;
-  const double a1 = dss_gather(src + 16, NLEV * 64, 64, e, l, p, tab) * r;
-  const double a2 = dss_gather(src + 32, NLEV * 64, 64, e, l, p, tab) * r;
-  const double a3 = dss_gather(src + 48, NLEV * 64, 64, e, l, p, tab) * r;
-  const size_t vb = (((size_t)e * NTL + np1) * NLEV + l) * 32 + p;
-  const size_t sb = (((size_t)e * NTL + np1) * NLEV + l) * 16 + p;
-  v[vb] = a0;
-  v[vb + 16] = a1;
-  T[sb] = a2;
-  dp[sb] = a3;
+  const int e = blockIdx.x, ep = e * 16 + p;
+  if (!in_bounds(ep < tab.npts, tab.flag, kBoundsDssPoint)) return;
+  const double r = rsmp[ep];
+  int n = tab.cnt[ep];
+  if (!in_bounds(n >= 0 && n <= MAXSRC, tab.flag, kBoundsDssCount)) n = 0;
+  long long so[MAXSRC] = {0, 0, 0};  // offsets of the sources' values from this point's
+#pragma unroll
+  for (int k = 0; k < MAXSRC; ++k) {
+    if (k < n) {
+      int sk = tab.src[ep * MAXSRC + k];
+      if (!in_bounds(sk >= 0 && sk < tab.npts, tab.flag, kBoundsDssSource)) sk = ep;
+      so[k] = ((long long)(sk >> 4) - e) * (NLEV * 64) + (sk & 15) - p;
+    }
+  }
+  const double* own = src + (size_t)e * NLEV * 64 + p;
+  double* vo = v + ((size_t)e * NTL + np1) * NLEV * 32 + p;
+  double* To = T + ((size_t)e * NTL + np1) * NLEV * 16 + p;
+  double* dpo = dp + ((size_t)e * NTL + np1) * NLEV * 16 + p;
+  switch (n) {
+    case 0: dss_state_levels<0>(own, so, vo, To, dpo, r, lo); break;
+    case 1: dss_state_levels<1>(own, so, vo, To, dpo, r, lo); break;
+    case 2: dss_state_levels<2>(own, so, vo, To, dpo, r, lo); break;
+    default: dss_state_levels<3>(own, so, vo, To, dpo, r, lo); break;
+  }
 }
 
 // ======================================================================================
@@ -977,8 +1035,9 @@ __device__ bool limiter_level(int option, R* x, const R* c, R s1, double& minp_i
 // doubles) streams into shared memory by a bulk asynchronous copy while the current
 // one is limited and stored, so the tracer loop does not wait on global loads.
 // Occupancy: 6 CTAs per SM in the mixed form (at most 80 registers; the kernel waits on
-// memory and shared-memory latency more than it issues, so occupancy pays for a 12-byte
-// spill), 3 in the FP64 form (168 registers).
+// memory and shared-memory latency more than it issues, so occupancy pays for a small
+// spill; five CTAs with no spill measured 10 % slower), 3 in the FP64 form (168
+// registers).
 template <typename R> constexpr size_t aal_buf_offset() {  // bytes, 16-byte aligned
   return (NLEV * SROW * sizeof(double) + (3 * NLEV * SROW + NLEV) * sizeof(R) + 15) / 16 * 16;
 }
@@ -1345,10 +1404,12 @@ __device__ __forceinline__ void ppm_cells_delta(int l0, int remap_alg, const flo
     const int jp = l0 + k3;
     float dl = e[jp] - df[jp], dr = e[jp + 1];
     if (!(dr * -dl > 0.0f)) { dl = 0.0f; dr = 0.0f; }
+    // the overshoot corrections selected, not branched on (as in ppm_cells)
     float c1 = dr - dl;
-    if (c1 * c1 * sixth < c1 * (-(dl + dr) * 0.5f)) dl = -2.0f * dr;
-    c1 = dr - dl;
-    if (c1 * (-(dl + dr) * 0.5f) < -c1 * c1 * sixth) dr = -2.0f * dl;
+    const float q = c1 * c1 * sixth, r = c1 * (-(dl + dr) * 0.5f);
+    const bool fix_l = q < r, fix_r = !fix_l && r < -q;
+    dl = fix_l ? -2.0f * dr : dl;
+    dr = fix_r ? -2.0f * dl : dr;
     float d0 = -(dl + dr) * 0.25f, c2 = 3.0f * (dl + dr);
     c1 = dr - dl;
     if (remap_alg == 2 && (jp < 2 || jp >= NLEV - 2)) {  // PpmFixedParabola
@@ -1721,7 +1782,7 @@ void launch_caar(const CaarArgs<R>& a, int E, cudaStream_t s) {
 void launch_dss_state(int E, const double* src, double* v, double* T, double* dp, int np1,
                       const double* rsmp, DssTable t, cudaStream_t s) {
   KScope k("dss_caar", s);
-  k_dss_state<<<dim3(E, NLEV / 8), 128, 0, s>>>(src, v, T, dp, np1, rsmp, t);
+  k_dss_state<<<E, 128, 0, s>>>(src, v, T, dp, np1, rsmp, t);
 }
 
 template <typename R>

@@ -54,8 +54,8 @@ def test_benchmark_config_fp64_parity(gpu_path, oracle_path):
 
 def test_benchmark_config_mixed_close(gpu_path, oracle_path):
     """The mixed form at the same configuration after one remap interval, against the FP64
-    oracle: T, dp3d and ps within the benchmark spec's 1e-5 bar by a wide margin (the 1-day
-    error is test_benchmark_config_one_day_against_oracle's)."""
+    oracle: T, dp3d and ps within the mixed form's 1e-5 relative error target by a wide
+    margin (the 1-day error is test_benchmark_config_one_day_against_oracle's)."""
     _, rg = _run(gpu_path, 1, 1)
     _, ro = _run(oracle_path, 0, 1)
     errs = {k: H.rel_err(rg[k], ro[k]) for k in ("T", "dp3d", "v", "Qdp", "ps_v")}
@@ -66,7 +66,7 @@ def test_benchmark_config_mixed_close(gpu_path, oracle_path):
 
 def test_benchmark_config_one_day_against_oracle(gpu_path, oracle_path):
     """Both GPU forms against the oracle after one simulated day (96 remap intervals, 288
-    dynamics steps) at ne30 q10: the mixed form within the benchmark spec's 1e-5 relative bar
+    dynamics steps) at ne30 q10: the mixed form within its 1e-5 relative error target
     in T and dp3d, the FP64 form far inside it (round-off differences grow over a day of
     nonlinear dynamics, so the per-interval 1e-12 bar does not apply here), and both
     conserving the global dry mass.  With HX_RESULTS_DIR set, the errors are written to
