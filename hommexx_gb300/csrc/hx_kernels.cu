@@ -311,57 +311,24 @@ __global__ void __launch_bounds__(LG * 16) k_caar(CaarArgs<R> a) {
 
 // DSS of the Caar output into the state of time level np1, times rspheremp
 // (BoundaryExchange::exchange(rspheremp) on v, T, dp3d: CaarFunctor.cpp:114).
-// Grid E, 128 threads: warps by point class over a group of 8 levels, each thread its
-// point on the 9 levels lo, lo + 8, ...; the number of contributions N is uniform within
-// a warp, so each case is a branch taken once, and every field sums in the table's order.
-template <int N>
-__device__ __forceinline__ void dss_state_levels(const double* own, const long long* so, double* vo, double* To,
-                                                 double* dpo, double r, int lo) {
-#pragma unroll 3
-  for (int l = lo; l < NLEV; l += 8) {
-    double acc[4];
-#pragma unroll
-    for (int f = 0; f < 4; ++f) acc[f] = own[l * 64 + f * 16];
-#pragma unroll
-    for (int k = 0; k < N; ++k)
-#pragma unroll
-      for (int f = 0; f < 4; ++f) acc[f] += own[so[k] + l * 64 + f * 16];
-    vo[l * 32] = acc[0] * r;
-    vo[l * 32 + 16] = acc[1] * r;
-    To[l * 16] = acc[2] * r;
-    dpo[l * 16] = acc[3] * r;
-  }
-}
-
+// Grid (E, 9), 128 threads: 8 levels per block, warps by point class.
 __global__ void __launch_bounds__(128) k_dss_state(const double* __restrict__ src, double* v, double* T,
                                                    double* dp, int np1, const double* __restrict__ rsmp,
                                                    DssTable tab) {
   int lo, p;
   dss_thread_point(lo, p);
-  const int e = blockIdx.x, ep = e * 16 + p;
-  if (!in_bounds(ep < tab.npts, tab.flag, kBoundsDssPoint)) return;
-  const double r = rsmp[ep];
-  int n = tab.cnt[ep];
-  if (!in_bounds(n >= 0 && n <= MAXSRC, tab.flag, kBoundsDssCount)) n = 0;
-  long long so[MAXSRC] = {0, 0, 0};  // offsets of the sources' values from this point's
-#pragma unroll
-  for (int k = 0; k < MAXSRC; ++k) {
-    if (k < n) {
-      int sk = tab.src[ep * MAXSRC + k];
-      if (!in_bounds(sk >= 0 && sk < tab.npts, tab.flag, kBoundsDssSource)) sk = ep;
-      so[k] = ((long long)(sk >> 4) - e) * (NLEV * 64) + (sk & 15) - p;
-    }
-  }
-  const double* own = src + (size_t)e * NLEV * 64 + p;
-  double* vo = v + ((size_t)e * NTL + np1) * NLEV * 32 + p;
-  double* To = T + ((size_t)e * NTL + np1) * NLEV * 16 + p;
-  double* dpo = dp + ((size_t)e * NTL + np1) * NLEV * 16 + p;
-  switch (n) {
-    case 0: dss_state_levels<0>(own, so, vo, To, dpo, r, lo); break;
-    case 1: dss_state_levels<1>(own, so, vo, To, dpo, r, lo); break;
-    case 2: dss_state_levels<2>(own, so, vo, To, dpo, r, lo); break;
-    default: dss_state_levels<3>(own, so, vo, To, dpo, r, lo); break;
-  }
+  const int e = blockIdx.x, l = blockIdx.y * 8 + lo;
+  const double r = rsmp[e * 16 + p];
+  const double a0 = dss_gather(src, NLEV * 64, 64, e, l, p, tab) * r;
+  const double a1 = dss_gather(src + 16, NLEV * 64, 64, e, l, p, tab) * r;
+  const double a2 = dss_gather(src + 32, NLEV * 64, 64, e, l, p, tab) * r;
+  const double a3 = dss_gather(src + 48, NLEV * 64, 64, e, l, p, tab) * r;
+  const size_t vb = (((size_t)e * NTL + np1) * NLEV + l) * 32 + p;
+  const size_t sb = (((size_t)e * NTL + np1) * NLEV + l) * 16 + p;
+  v[vb] = a0;
+  v[vb + 16] = a1;
+  T[sb] = a2;
+  dp[sb] = a3;
 }
 
 // ======================================================================================
@@ -1782,7 +1749,7 @@ void launch_caar(const CaarArgs<R>& a, int E, cudaStream_t s) {
 void launch_dss_state(int E, const double* src, double* v, double* T, double* dp, int np1,
                       const double* rsmp, DssTable t, cudaStream_t s) {
   KScope k("dss_caar", s);
-  k_dss_state<<<E, 128, 0, s>>>(src, v, T, dp, np1, rsmp, t);
+  k_dss_state<<<dim3(E, NLEV / 8), 128, 0, s>>>(src, v, T, dp, np1, rsmp, t);
 }
 
 template <typename R>
