@@ -196,8 +196,10 @@ def kernel_bytes(E: int, Q: int, rsize: int, rsplit: int = RSPLIT, hsub: int = H
                 if last:
                     add("euler_bih_pre", 1, 2 * Q * F + F)
                     add("euler_bih_post", 1, 2 * Q * F)
-                add("euler_aal_setup", 1, 10 * F + (F if (last and nu_p_positive) else 0))
-                add("euler_aal_tracer", 1, Q * Fd + Q * F + 3 * F + (Q * F if last else 0) + 2 * qlim)
+                # setup phase fused into the tracer kernel: derived_dp, divdp_proj, divdp,
+                # vn0 (2), f_dss in, fscr out (+ dpdiss_bih in the biharmonic stage)
+                add("euler_aal_tracer", 1, Q * Fd + Q * F + 7 * F + (F if (last and nu_p_positive) else 0)
+                    + (Q * F if last else 0) + 2 * qlim)
                 add("euler_dss_qdp", 1, Q * F + Q * Fd + (Q * Fd if last else 0))
                 add("euler_dss_fvar", 1, 2 * F)
     add("dp3d_from_ps", 1, F)

@@ -1036,17 +1036,28 @@ __global__ void __launch_bounds__(LG * 16, kF32<R> ? 6 : 3) k_aal_tracer(EulerAr
   PM<R> m;
   m.load(a.m, e, p);
   const double spd = a.m.spheremp_d[(size_t)e * 16 + p];
-  // tracer-independent part of div(vstar Qdp): the contravariant flux per unit Qdp,
-  // (Dinv-contraction of vstar) * metdet
+  // AALSetupPhase (compute_2d_advection_step), per element here: the layer thickness
+  // dp = derived_dp - rhs_multiplier dt divdp_proj, vstar = vn0 / dp, the limiter's
+  // thickness dpdissk = dp - dt divdp (+ the biharmonic dp term), and f_dss spheremp for
+  // the DSS of f_dss; then the tracer-independent part of div(vstar Qdp), the
+  // contravariant flux per unit Qdp, (Dinv-contraction of vstar) * metdet
+  const R rhsdt = R(a.rhs_multiplier * a.dt);
+  const bool hvdk = a.nu_p > 0 && a.rhs_viss != 0.0;
+  const R hvf = R(-a.rhs_viss * a.dt * a.nu_q);
   R w0[NL], w1[NL];
 #pragma unroll
   for (int k = 0; k < NL; ++k) {
     const int l = lg + LG * k;
+    const size_t i3 = ((size_t)e * NLEV + l) * 16 + p;
     const size_t iv = ((size_t)e * NLEV + l) * 32 + p;
-    const R vs0 = cvt<R>(a.vstar[iv]), vs1 = cvt<R>(a.vstar[iv + 16]);
+    const R dpt = cvt<R>(a.derived_dp[i3]) - rhsdt * cvt<R>(a.divdp_proj[i3]);
+    const R rdpt = R(1) / dpt;
+    const R vs0 = cvt<R>(a.vn0[iv]) * rdpt, vs1 = cvt<R>(a.vn0[iv + 16]) * rdpt;
+    R dm = dpt - R(a.dt) * cvt<R>(a.divdp[i3]);
+    if (hvdk) dm += hvf * cvt<R>(a.dpdiss_bih[i3]) / a.m.spheremp[(size_t)e * 16 + p];
+    a.fscr[i3] = a.f_dss[i3] * spd;
     w0[k] = (m.di00 * vs0 + m.di10 * vs1) * m.md;
     w1[k] = (m.di01 * vs0 + m.di11 * vs1) * m.md;
-    const R dm = cvt<R>(a.dpdissk[((size_t)e * NLEV + l) * 16 + p]);
     s_dm[l * SROW + p] = dm;
     s_rdm[l * SROW + p] = R(1) / dm;
     s_c[l * SROW + p] = m.sp * dm;
@@ -1826,7 +1837,7 @@ void launch_euler_step(EulerArgs<R>& a, int E, int time_avg, cudaStream_t s) {
       k_minmax_nbr<<<nblk((long long)E * a.Q * NLEV, 256), 256, 0, s>>>(E, a.Q, a.qlim_tmp, a.qlim, a.conn);
     }
   }
-  {
+  if (a.Q == 0) {  // with tracers, k_aal_tracer does the setup phase per element itself
     KScope k("euler_aal_setup", s);
     k_aal_setup<R><<<nblk((long long)E * NLEV * 16, 256), 256, 0, s>>>(a, E);
   }
