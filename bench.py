@@ -68,46 +68,44 @@ FALLBACK_HBM_GBS = 6800.0
 # re-captured with the kernels it describes.
 NCU_NE16 = {
     "fp64": {
-        "ppm_remap": (327.7e6, 1258.5e6, 952.8e6),
+        "ppm_remap": (327.4e6, 1258.5e6, 952.8e6),
         "euler_bih_post": (282.3e6, 668.9e6, 376.0e6),
-        "euler_bih_pre": (260.9e6, 583.9e6, 300.8e6),
-        "euler_aal_tracer": (368.5e6, 482.0e6, 301.5e6),
-        "hv_laplace2": (162.0e6, 352.9e6, 210.4e6),
-        "caar_stage": (191.5e6, 320.1e6, 198.6e6),
+        "euler_bih_pre": (260.7e6, 583.9e6, 300.8e6),
+        "euler_aal_tracer": (426.4e6, 522.5e6, 325.6e6),
+        "hv_laplace2": (161.9e6, 352.9e6, 210.4e6),
+        "caar_stage": (200.4e6, 321.6e6, 199.5e6),
         "hv_laplace1": (77.6e6, 292.9e6, 164.6e6),
-        "update_q": (239.1e6, 107.9e6, 63.7e6),
-        "euler_dss_qdp": (330.8e6, 52.2e6, 46.3e6),
-        "euler_aal_setup": (104.7e6, 41.9e6, 25.8e6),
+        "update_q": (239.2e6, 107.9e6, 63.7e6),
+        "euler_dss_qdp": (330.7e6, 52.2e6, 46.3e6),
         "precompute_divdp": (29.3e6, 41.9e6, 25.0e6),
-        "euler_qminmax": (216.8e6, 39.1e6, 28.5e6),
+        "euler_qminmax": (216.6e6, 39.1e6, 28.5e6),
         "hv_dss_update": (117.6e6, 35.4e6, 30.1e6),
-        "dss_caar": (102.9e6, 15.9e6, 15.9e6),
+        "dss_caar": (102.1e6, 15.9e6, 15.9e6),
         "dp3d_from_ps": (0.2e6, 5.3e6, 3.5e6),
         "euler_dss_fvar": (14.8e6, 4.0e6, 4.0e6),
         "euler_bih_weight": (14.2e6, 1.8e6, 1.8e6),
         "euler_minmax_nbr": (17.8e6, 0.0e6, 0.0e6),
-        "prim_step_init": (53.1e6, 0.0e6, 0.0e6),
+        "prim_step_init": (52.9e6, 0.0e6, 0.0e6),
     },
     "mixed": {
         "ppm_remap": (327.4e6, 351.4e6, 258.5e6),
-        "update_q": (239.4e6, 107.9e6, 63.7e6),
-        "caar_stage": (188.3e6, 53.6e6, 46.6e6),
-        "euler_aal_tracer": (363.2e6, 53.1e6, 53.1e6),
-        "euler_dss_qdp": (331.0e6, 52.2e6, 46.3e6),
-        "euler_bih_post": (274.4e6, 43.7e6, 43.7e6),
-        "hv_laplace2": (152.0e6, 28.0e6, 23.1e6),
-        "hv_dss_update": (116.1e6, 15.9e6, 15.9e6),
-        "dss_caar": (102.9e6, 15.9e6, 15.9e6),
+        "update_q": (239.1e6, 107.9e6, 63.7e6),
+        "euler_aal_tracer": (425.2e6, 55.4e6, 55.4e6),
+        "caar_stage": (188.2e6, 53.6e6, 46.6e6),
+        "euler_dss_qdp": (330.8e6, 52.2e6, 46.3e6),
+        "euler_bih_post": (274.3e6, 43.7e6, 43.7e6),
+        "hv_laplace2": (152.2e6, 28.0e6, 23.1e6),
+        "dss_caar": (101.9e6, 15.9e6, 15.9e6),
+        "hv_dss_update": (116.3e6, 15.9e6, 15.9e6),
         "dp3d_from_ps": (0.2e6, 5.3e6, 3.5e6),
-        "euler_aal_setup": (104.0e6, 4.6e6, 4.6e6),
         "euler_dss_fvar": (14.8e6, 4.0e6, 4.0e6),
-        "hv_laplace1": (70.3e6, 3.5e6, 3.5e6),
+        "hv_laplace1": (70.2e6, 3.5e6, 3.5e6),
         "euler_bih_weight": (14.2e6, 1.8e6, 1.8e6),
-        "euler_qminmax": (214.6e6, 0.1e6, 0.1e6),
-        "euler_minmax_nbr": (17.8e6, 0.0e6, 0.0e6),
-        "euler_bih_pre": (257.3e6, 0.0e6, 0.0e6),
-        "prim_step_init": (53.3e6, 0.0e6, 0.0e6),
+        "euler_qminmax": (214.5e6, 0.1e6, 0.1e6),
         "precompute_divdp": (28.8e6, 0.0e6, 0.0e6),
+        "euler_minmax_nbr": (17.8e6, 0.0e6, 0.0e6),
+        "euler_bih_pre": (257.2e6, 0.0e6, 0.0e6),
+        "prim_step_init": (53.2e6, 0.0e6, 0.0e6),
     },
 }
 NCU_NE16_ELEMENTS = 1536
