@@ -85,6 +85,23 @@ struct Pt {
     for (int k = 0; k < 4; ++k) a += dy[k] * sh16(s1, 4 * k + j);
     return a;
   }
+  // acc + ddx(s0) + ddy(s1), the same chain started from acc
+  __device__ __forceinline__ R dxy_acc(R s0, R s1, R acc) const {
+    R a = acc;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) a += dx[k] * sh16(s0, 4 * i + k);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) a += dy[k] * sh16(s1, 4 * k + j);
+    return a;
+  }
+  // the derivative weights times a per-point factor (folds a scale of the result)
+  __device__ __forceinline__ void scale(R f) {
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      dx[k] *= f;
+      dy[k] *= f;
+    }
+  }
   __device__ __forceinline__ R dxmy(R s0, R s1) const {
     R a = dx[0] * sh16(s0, 4 * i);
 #pragma unroll
@@ -495,6 +512,17 @@ __device__ __forceinline__ double rcp_newton1(double x, float& rf) {
   rf = __fdividef(1.0f, d2f_seed(x));
   const double r = f2d(rf);
   return fma(r, fma(-x, r, 1.0), r);
+}
+
+// 1 / x in R: the FP32 quotient in FP32; in FP64 rcp_newton (four FMAs instead of the
+// IEEE division's longer sequence; within one ulp, for |x| in 2^-125 .. 2^125).
+template <typename R> __device__ __forceinline__ R recip(R x) {
+  if constexpr (kF32<R>) {
+    return R(1) / x;
+  } else {
+    float rf;
+    return rcp_newton(x, rf);
+  }
 }
 
 // a / b from r = rcp_newton(b): the product a r corrected once by its residual,

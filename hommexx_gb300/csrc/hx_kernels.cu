@@ -729,7 +729,7 @@ __global__ void __launch_bounds__(96) k_qminmax(EulerArgs<R> a, double* qlim_out
     const size_t i3 = ((size_t)e * NLEV + lv + 24 * r) * 16 + 4 * c;
 #pragma unroll
     for (int j = 0; j < 4; ++j)
-      rdp[r][j] = R(1) / (cvt<R>(a.derived_dp[i3 + j]) - rhsdt * cvt<R>(a.divdp_proj[i3 + j]));
+      rdp[r][j] = recip(cvt<R>(a.derived_dp[i3 + j]) - rhsdt * cvt<R>(a.divdp_proj[i3 + j]));
   }
 #pragma unroll 1
   for (int q = 0; q < a.Q; ++q) {
@@ -1043,7 +1043,7 @@ __global__ void __launch_bounds__(LG * 16, kF32<R> ? 6 : 3) k_aal_tracer(EulerAr
   // contravariant flux per unit Qdp, (Dinv-contraction of vstar) * metdet
   const R rhsdt = R(a.rhs_multiplier * a.dt);
   const bool hvdk = a.nu_p > 0 && a.rhs_viss != 0.0;
-  const R hvf = R(-a.rhs_viss * a.dt * a.nu_q);
+  const R hvf = R(-a.rhs_viss * a.dt * a.nu_q) * recip(m.sp);  // over this element's spheremp
   R w0[NL], w1[NL];
 #pragma unroll
   for (int k = 0; k < NL; ++k) {
@@ -1051,17 +1051,20 @@ __global__ void __launch_bounds__(LG * 16, kF32<R> ? 6 : 3) k_aal_tracer(EulerAr
     const size_t i3 = ((size_t)e * NLEV + l) * 16 + p;
     const size_t iv = ((size_t)e * NLEV + l) * 32 + p;
     const R dpt = cvt<R>(a.derived_dp[i3]) - rhsdt * cvt<R>(a.divdp_proj[i3]);
-    const R rdpt = R(1) / dpt;
+    const R rdpt = recip(dpt);
     const R vs0 = cvt<R>(a.vn0[iv]) * rdpt, vs1 = cvt<R>(a.vn0[iv + 16]) * rdpt;
     R dm = dpt - R(a.dt) * cvt<R>(a.divdp[i3]);
-    if (hvdk) dm += hvf * cvt<R>(a.dpdiss_bih[i3]) / a.m.spheremp[(size_t)e * 16 + p];
+    if (hvdk) dm += hvf * cvt<R>(a.dpdiss_bih[i3]);
     a.fscr[i3] = a.f_dss[i3] * spd;
-    w0[k] = (m.di00 * vs0 + m.di10 * vs1) * m.md;
-    w1[k] = (m.di01 * vs0 + m.di11 * vs1) * m.md;
+    w0[k] = m.dm00 * vs0 + m.dm10 * vs1;  // metdet folded into Dinv
+    w1[k] = m.dm01 * vs0 + m.dm11 * vs1;
     s_dm[l * SROW + p] = dm;
-    s_rdm[l * SROW + p] = R(1) / dm;
+    s_rdm[l * SROW + p] = recip(dm);
     s_c[l * SROW + p] = m.sp * dm;
   }
+  // -dt times divergence_sphere's scale, folded into the derivative weights: the
+  // advection below forms Qdp + q0 - dt div(vstar Qdp) as one multiply-add chain
+  t.scale(R(-a.dt) * m.fdiv);
   __syncthreads();
   for (int l = tid; l < NLEV; l += blockDim.x) {
     R s1 = 0;
@@ -1070,7 +1073,6 @@ __global__ void __launch_bounds__(LG * 16, kF32<R> ? 6 : 3) k_aal_tracer(EulerAr
     s_c1[l] = s1;
   }
   const bool add_hv = a.rhs_viss != 0.0;
-  const R mdf = R(-a.dt) * m.fdiv;  // -dt times divergence_sphere's scale
   unsigned parity = 0;
 #pragma unroll 1
   for (int q = 0; q < a.Q; ++q) {
@@ -1091,10 +1093,13 @@ __global__ void __launch_bounds__(LG * 16, kF32<R> ? 6 : 3) k_aal_tracer(EulerAr
       const int l = lg + LG * k;
       const double qdd = q_buf[l * 16 + p];
       const R qd = cvt<R>(qdd);
-      const R dvs = t.dxy(w0[k] * qd, w1[k] * qd);  // div(vstar Qdp) / fdiv
       const double q0 = add_hv ? a.qtens[qb + l * 16 + p] : 0.0;
-      if constexpr (kF32<R>) s_q[l * SROW + p] = qdd + dbl(mdf * dvs) + q0;
-      else s_q[l * SROW + p] = (qdd + mdf * dvs + q0);
+      if constexpr (kF32<R>) {
+        s_q[l * SROW + p] = qdd + dbl(t.dxy(w0[k] * qd, w1[k] * qd)) + q0;  // -dt div(vstar Qdp)
+      } else {
+        const double acc = add_hv ? qdd + q0 : qdd;
+        s_q[l * SROW + p] = t.dxy_acc(w0[k] * qd, w1[k] * qd, acc);
+      }
     }
     __syncthreads();
     if (tid == 0 && q + 1 < a.Q) {  // the buffer is free: fetch the next tracer's slab
