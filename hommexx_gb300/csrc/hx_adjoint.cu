@@ -18,6 +18,8 @@
 // The forward these reverse restates src/share/cxx/CaarFunctorImpl.hpp:97-889,
 // SphereOperators.hpp:291-862, HyperviscosityFunctorImpl.{hpp:72-257,cpp:56-84},
 // RemapFunctor.hpp:225-463 and PpmRemap.hpp:174-689.
+#include <type_traits>
+
 #include "hx_device.cuh"
 
 namespace hx {
@@ -94,19 +96,26 @@ __device__ __forceinline__ double dss_gather_w(const double* base, long long es,
 // ======================================================================================
 // caar stage reversed, one CTA per element.  Forward: out = R S (spheremp (xm + dt F(x))).
 // ======================================================================================
+// Shared memory of k_caar_vjp: four [72][17] double arrays and three in S (the FP64
+// form: double; the mixed form: float, the operators' own type), 68.5 or 53.9 KB: three
+// or four CTAs per SM.
+template <typename R> using CaarVjpS = typename std::conditional<kF32<R>, float, double>::type;
+template <typename R> constexpr size_t caar_vjp_smem() {
+  return (4 * sizeof(double) + 3 * sizeof(CaarVjpS<R>)) * NLEV * SROW;
+}
 template <typename R, int LG>
 __global__ void __launch_bounds__(LG * 16) k_caar_vjp(CaarVjpArgs<R> a) {
   constexpr int NL = NLEV / LG;
+  using S = CaarVjpS<R>;
   extern __shared__ double sm[];
-  // (T and dp3d are read from the stage input, which stays in L1: seven arrays of shared
-  // memory keep three CTAs per SM)
-  double* s_div = sm;                     // div(v dp); then the omega-integral cotangent
-  double* s_p = sm + 1 * NLEV * SROW;     // pressure
-  double* s_rp = sm + 2 * NLEV * SROW;    // 1 / pressure
-  double* s_I = sm + 3 * NLEV * SROW;     // sum_{j<l} div_vdp_j
-  double* s_phib = sm + 4 * NLEV * SROW;  // cotangent of phi; then the scans' T cotangent
-  double* s_pb = sm + 5 * NLEV * SROW;    // cotangent of p; then the scans' dp3d cotangent
-  double* s_dvb = sm + 6 * NLEV * SROW;   // cotangent of div(v dp)
+  // (T and dp3d are read from the stage input, which stays in L1)
+  double* s_p = sm;                       // pressure
+  double* s_phib = sm + 1 * NLEV * SROW;  // cotangent of phi; then the scans' T cotangent
+  double* s_pb = sm + 2 * NLEV * SROW;    // cotangent of p; then the scans' dp3d cotangent
+  double* s_dvb = sm + 3 * NLEV * SROW;   // cotangent of div(v dp)
+  S* s_div = reinterpret_cast<S*>(sm + 4 * NLEV * SROW);  // div(v dp); then the omega-integral cotangent
+  S* s_rp = s_div + NLEV * SROW;          // 1 / pressure
+  S* s_I = s_rp + NLEV * SROW;            // sum_{j<l} div_vdp_j
   const int e = blockIdx.x, tid = threadIdx.x, p = tid & 15, lg = tid >> 4;
   Pt<R> t;
   t.init(p);
@@ -123,7 +132,7 @@ __global__ void __launch_bounds__(LG * 16) k_caar_vjp(CaarVjpArgs<R> a) {
     const double dd = xd[l * 16 + p];
     const R d = (R)dd;
     const R div = divergence_sphere(t, m, u * d, w * d);
-    s_div[l * SROW + p] = (double)div;
+    s_div[l * SROW + p] = (S)div;
   }
   __syncthreads();
   // ---- phase B: pressure, 1/p, omega integral (as the forward, in double) ----
@@ -145,16 +154,17 @@ __global__ void __launch_bounds__(LG * 16) k_caar_vjp(CaarVjpArgs<R> a) {
       pr = pr + 0.5 * (prev + d);
       prev = d;
       s_p[(l0 + k) * SROW + col] = pr;
-      s_rp[(l0 + k) * SROW + col] = 1.0 / pr;
+      float rf;
+      s_rp[(l0 + k) * SROW + col] = (S)rcp_newton(pr, rf);
     }
     double dt_ = 0.0;
 #pragma unroll
-    for (int k = 0; k < 9; ++k) dt_ += s_div[(l0 + k) * SROW + col];
+    for (int k = 0; k < 9; ++k) dt_ += (double)s_div[(l0 + k) * SROW + col];
     double acc = seg_excl_prefix(dt_, seg);
 #pragma unroll
     for (int k = 0; k < 9; ++k) {
-      s_I[(l0 + k) * SROW + col] = acc;
-      acc = acc + s_div[(l0 + k) * SROW + col];
+      s_I[(l0 + k) * SROW + col] = (S)acc;
+      acc = acc + (double)s_div[(l0 + k) * SROW + col];
     }
   }
   __syncthreads();
@@ -227,7 +237,7 @@ __global__ void __launch_bounds__(LG * 16) k_caar_vjp(CaarVjpArgs<R> a) {
     pb += gradient_sphere_T(t, m, gpb0, gpb1);
     s_phib[l * SROW + p] = (double)ephib;
     s_pb[l * SROW + p] = (double)pb;
-    s_div[l * SROW + p] = (double)(-o);
+    s_div[l * SROW + p] = (S)(-o);
     s_dvb[l * SROW + p] = (double)(-gdp - R(0.5) * o);
     ov[l * 32 + p] += (double)vb0;
     ov[l * 32 + 16 + p] += (double)vb1;
@@ -249,7 +259,15 @@ __global__ void __launch_bounds__(LG * 16) k_caar_vjp(CaarVjpArgs<R> a) {
       const double phb = s_phib[i];
       const double rb = phb + 2.0 * acc;
       acc += phb;
-      const double rp = s_rp[i], T = xT[(l0 + k) * 16 + col], dp = xd[(l0 + k) * 16 + col];
+      // 1 / p in double (the mixed form keeps only its FP32 image in shared memory)
+      double rp;
+      if constexpr (kF32<R>) {
+        float rf;
+        rp = rcp_newton(s_p[i], rf);
+      } else {
+        rp = s_rp[i];
+      }
+      const double T = xT[(l0 + k) * 16 + col], dp = xd[(l0 + k) * 16 + col];
       const double hr = dp * 0.5 * rp;  // r = Rgas T dp / (2 p)
       Tb2[k] = kRgas * hr * rb;
       dpb2[k] = kRgas * T * 0.5 * rp * rb;
@@ -274,7 +292,7 @@ __global__ void __launch_bounds__(LG * 16) k_caar_vjp(CaarVjpArgs<R> a) {
 #pragma unroll
     for (int k = 8; k >= 0; --k) {
       const int i = (l0 + k) * SROW + col;
-      const double ib = s_div[i];
+      const double ib = (double)s_div[i];
       s_dvb[i] += acc;
       acc += ib;
     }
@@ -458,7 +476,7 @@ __global__ void k_copy_dyn(int E, DynV d, DynV s) {
 // branch and index search matches it); contributions that a lane makes to another
 // lane's index go through per-offset shared arrays that the owner sums afterwards.
 // ======================================================================================
-constexpr int VC = 4;  // columns (warps) per CTA
+constexpr int VC = 1;  // columns (warps) per CTA: the shared memory (21.8 KB a column) sets the occupancy, and one-warp CTAs fill an SM best
 // shared-memory slots of one column (doubles)
 constexpr int V_D = 0;              // D[-2 .. 73]
 constexpr int V_RD = V_D + 76;      // 1 / D[0 .. 71]
@@ -1108,7 +1126,7 @@ void upload_adjoint_constants(const double* dvv16, const double* hyai, const dou
 template <typename R>
 void launch_caar_vjp(const CaarVjpArgs<R>& a, int E, cudaStream_t s) {
   constexpr int LG = LG_ADJ<R>();
-  const size_t smem = 7 * NLEV * SROW * sizeof(double);
+  const size_t smem = caar_vjp_smem<R>();
   static bool init = false;
   if (!init) {
     cudaFuncSetAttribute(k_caar_vjp<R, LG>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);

@@ -422,11 +422,16 @@ template <> __device__ __forceinline__ double min3abs_signed<double>(double a, d
 }
 
 // ---- double <-> float conversions on the integer pipe --------------------------------
-// F2F conversions also issue to the FP64 pipe; the mixed form converts at every load
-// and store of a double field.  These restate the IEEE 754 binary64 <-> binary32
-// conversions (round to nearest, ties to even) as integer field manipulation; zeros are
-// handled inline and the rare subnormal, overflowing, infinite and NaN cases fall back to
-// the hardware conversion, so the results equal the hardware's for every input.
+// F2F conversions issue to the FP64 pipe at the cost of an FP64 multiply-add; the mixed
+// form converts at every load and store of a double field.  These restate the IEEE 754
+// binary64 <-> binary32 conversions (round to nearest, ties to even) as integer field
+// manipulation; zeros are handled inline and the rare subnormal, overflowing, infinite and
+// NaN cases fall back to the hardware conversion, so the results equal the hardware's for
+// every input.  The inlined fallback compiles to a predicated conversion that each warp
+// still issues; an out-of-line fallback (a branch around a call) removes that, and pays
+// off in d2f_seed and dtwice below (FP64 kernels), but here it measured slower in the
+// mixed form's tracer advection (more FP64-pipe instructions, 6.9 vs 6.2 ms per ne30
+// interval), so these two keep the inline form.
 __device__ __forceinline__ float d2f_rn(double x) {
   const unsigned hi = (unsigned)__double2hiint(x);
   const unsigned lo = (unsigned)__double2loint(x);
@@ -451,6 +456,10 @@ __device__ __forceinline__ double f2d(float x) {
   return __hiloint2double((int)((u & 0x80000000u) | ((e + 896u) << 20) | ((u & 0x7FFFFFu) >> 3)),
                           (int)(u << 29));
 }
+// The out-of-line rare cases of d2f_seed and dtwice: a uniform branch around a call
+// instead of a predicated FP64-pipe instruction in every warp.
+__device__ __noinline__ float d2f_slow(double x) { return __double2float_rn(x); }
+__device__ __noinline__ double dtwice_slow(double x) { return x * 2.0; }
 // double -> R and R -> double (identities in the FP64 form)
 template <typename R> __device__ __forceinline__ R cvt(double x);
 template <> __device__ __forceinline__ double cvt<double>(double x) { return x; }
@@ -479,18 +488,20 @@ template <typename R> __device__ __forceinline__ R rel_hw(double x) {
 __device__ __forceinline__ float d2f_seed(double x) {
   const unsigned hi = (unsigned)__double2hiint(x);
   const int e = (int)((hi >> 20) & 0x7FFu) - 896;
-  if (e <= 0 || e >= 255) return __double2float_rn(x);
+  if (e <= 0 || e >= 255) return d2f_slow(x);
   const unsigned lo = (unsigned)__double2loint(x);
   return __uint_as_float((hi & 0x80000000u) | ((unsigned)e << 23) | ((hi & 0xFFFFFu) << 3) | (lo >> 29));
 }
 
 // 2 x, exact, on the integer pipe (the exponent field incremented) for normal x below
-// 2^1022 in magnitude; zeros, subnormals and larger values take the FP64 product.
+// 2^1022 in magnitude and for zeros; subnormals and larger values take the FP64 product
+// (out of line, as the conversions' rare cases).
 __device__ __forceinline__ double dtwice(double x) {
   const long long b = __double_as_longlong(x);
   const int e = (int)((b >> 52) & 0x7FF);
-  if (e == 0 || e >= 0x7FE) return x * 2.0;
-  return __longlong_as_double(b + (1LL << 52));
+  const bool zero = (b << 1) == 0;
+  if ((e == 0 || e >= 0x7FE) && !zero) return dtwice_slow(x);
+  return zero ? x : __longlong_as_double(b + (1LL << 52));
 }
 
 // 1/x in FP64 from the approximate FP32 reciprocal of x (__fdividef of the truncated
