@@ -68,43 +68,43 @@ FALLBACK_HBM_GBS = 6800.0
 # re-captured with the kernels it describes.
 NCU_NE16 = {
     "fp64": {
-        "ppm_remap": (327.4e6, 1258.5e6, 952.8e6),
+        "ppm_remap": (327.6e6, 1245.0e6, 939.2e6),
         "euler_bih_post": (282.3e6, 668.9e6, 376.0e6),
         "euler_bih_pre": (260.7e6, 583.9e6, 300.8e6),
-        "euler_aal_tracer": (426.4e6, 522.5e6, 325.6e6),
-        "hv_laplace2": (161.9e6, 352.9e6, 210.4e6),
-        "caar_stage": (200.4e6, 321.6e6, 199.5e6),
-        "hv_laplace1": (77.6e6, 292.9e6, 164.6e6),
-        "update_q": (239.2e6, 107.9e6, 63.7e6),
+        "euler_aal_tracer": (426.3e6, 489.6e6, 299.0e6),
+        "hv_laplace2": (162.0e6, 352.9e6, 210.4e6),
+        "caar_stage": (200.4e6, 320.0e6, 197.9e6),
+        "hv_laplace1": (77.7e6, 292.9e6, 164.6e6),
+        "update_q": (239.3e6, 107.9e6, 63.7e6),
         "euler_dss_qdp": (330.7e6, 52.2e6, 46.3e6),
         "precompute_divdp": (29.3e6, 41.9e6, 25.0e6),
-        "euler_qminmax": (216.6e6, 39.1e6, 28.5e6),
+        "euler_qminmax": (214.4e6, 35.5e6, 26.7e6),
         "hv_dss_update": (117.6e6, 35.4e6, 30.1e6),
-        "dss_caar": (102.1e6, 15.9e6, 15.9e6),
+        "dss_caar": (102.3e6, 15.9e6, 15.9e6),
         "dp3d_from_ps": (0.2e6, 5.3e6, 3.5e6),
         "euler_dss_fvar": (14.8e6, 4.0e6, 4.0e6),
         "euler_bih_weight": (14.2e6, 1.8e6, 1.8e6),
         "euler_minmax_nbr": (17.8e6, 0.0e6, 0.0e6),
-        "prim_step_init": (52.9e6, 0.0e6, 0.0e6),
+        "prim_step_init": (53.0e6, 0.0e6, 0.0e6),
     },
     "mixed": {
-        "ppm_remap": (327.4e6, 351.4e6, 258.5e6),
-        "update_q": (239.1e6, 107.9e6, 63.7e6),
-        "euler_aal_tracer": (425.2e6, 55.4e6, 55.4e6),
-        "caar_stage": (188.2e6, 53.6e6, 46.6e6),
+        "ppm_remap": (327.4e6, 345.9e6, 253.1e6),
+        "update_q": (239.2e6, 107.9e6, 63.7e6),
+        "euler_aal_tracer": (424.4e6, 55.4e6, 55.4e6),
         "euler_dss_qdp": (330.8e6, 52.2e6, 46.3e6),
-        "euler_bih_post": (274.3e6, 43.7e6, 43.7e6),
+        "caar_stage": (188.2e6, 52.0e6, 45.1e6),
+        "euler_bih_post": (274.2e6, 43.7e6, 43.7e6),
         "hv_laplace2": (152.2e6, 28.0e6, 23.1e6),
-        "dss_caar": (101.9e6, 15.9e6, 15.9e6),
+        "dss_caar": (102.1e6, 15.9e6, 15.9e6),
         "hv_dss_update": (116.3e6, 15.9e6, 15.9e6),
         "dp3d_from_ps": (0.2e6, 5.3e6, 3.5e6),
-        "euler_dss_fvar": (14.8e6, 4.0e6, 4.0e6),
+        "euler_dss_fvar": (14.9e6, 4.0e6, 4.0e6),
         "hv_laplace1": (70.2e6, 3.5e6, 3.5e6),
         "euler_bih_weight": (14.2e6, 1.8e6, 1.8e6),
-        "euler_qminmax": (214.5e6, 0.1e6, 0.1e6),
+        "euler_qminmax": (214.6e6, 0.1e6, 0.1e6),
         "precompute_divdp": (28.8e6, 0.0e6, 0.0e6),
         "euler_minmax_nbr": (17.8e6, 0.0e6, 0.0e6),
-        "euler_bih_pre": (257.2e6, 0.0e6, 0.0e6),
+        "euler_bih_pre": (257.3e6, 0.0e6, 0.0e6),
         "prim_step_init": (53.2e6, 0.0e6, 0.0e6),
     },
 }
@@ -348,6 +348,7 @@ def run_gpu(args, rank, world):
         te = _max_over_ranks(te, world)
         L.stream_results(None)
         L.set_async_copies(False)
+        link_after = measure_link()  # the same test right after the loop
         calls = {"init_elements_states_c_ms": 1e3 * tp[0] / args.steps,
                  "prim_run_subcycle_c_ms": 1e3 * tp[1] / args.steps,
                  "cxx_push_results_to_f90_ms": 1e3 * tp[2] / args.steps}
@@ -361,7 +362,7 @@ def run_gpu(args, rank, world):
               + f"; link h2d {link['h2d_gbs']:.1f} GB/s, d2h {link['d2h_gbs']:.1f} GB/s", file=sys.stderr)
         del keep
         out[tag] = dict(t=t, te=te, launches=launches, stats=stats, clocks=cs.summary(),
-                        h2d=h2d, d2h=d2h, link=link, calls=calls)
+                        h2d=h2d, d2h=d2h, link=link, link_after=link_after, calls=calls)
         if tag == "fp64":
             out["fp64_state_after"] = None
         L.finalize()
@@ -766,7 +767,7 @@ def main():
         "e2e": {"value": sypd(args.steps, f["te"]) * world, "unit": "SYPD",
                 "h2d_bytes_per_step": f["h2d"], "d2h_bytes_per_step": f["d2h"],
                 "ms_per_step": ms_e2e, "exposed_ms_per_step": ms_e2e - ms_dev,
-                "link": f["link"], "calls": f["calls"],
+                "link": f["link"], "link_after_loop": f["link_after"], "calls": f["calls"],
                 "copies": "init_elements_states_c / prim_run_subcycle_c / cxx_push_results_to_f90 "
                           "from host memory page-locked at allocation; time levels nm1/np1 and Qdp in "
                           "and the results out overlap the step (hx_set_async_copies, "
