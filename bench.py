@@ -732,7 +732,7 @@ def main():
         m = out["mixed"]
         print(json.dumps({"metric": "ne30L72 SYPD (mixed preqx step)", "value": sypd(args.steps, m["t"]),
                           "unit": "SYPD", "ms_per_step": m["t"] / args.steps * 1e3,
-                          "kernels": roofline(m["stats"], E, QSIZE, 8, args.steps)}))
+                          "kernels": roofline(m["stats"], E, QSIZE, 8, args.steps, "mixed")}))
         return
     f = out["fp64"]
     peak, peak_kind = _peaks()

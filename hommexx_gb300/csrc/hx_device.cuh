@@ -569,6 +569,20 @@ __device__ __forceinline__ void bulk_load(void* dst, const void* src, unsigned b
                "l"(src), "r"(bytes), "r"(smem_addr(bar))
                : "memory");
 }
+// Two copies completing one phase of the barrier (one arrival expecting both sizes).
+__device__ __forceinline__ void bulk_load2(void* dst1, const void* src1, unsigned bytes1, void* dst2,
+                                           const void* src2, unsigned bytes2, unsigned long long* bar) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes1 + bytes2)
+               : "memory");
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_addr(dst1)),
+               "l"(src1), "r"(bytes1), "r"(smem_addr(bar))
+               : "memory");
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_addr(dst2)),
+               "l"(src2), "r"(bytes2), "r"(smem_addr(bar))
+               : "memory");
+}
 // Waits for the completion of phase `parity` of the barrier; false after `tries` polls
 // (each poll may suspend the thread for a short, hardware-chosen time).
 __device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned parity, int tries) {

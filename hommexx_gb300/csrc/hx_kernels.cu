@@ -1012,6 +1012,7 @@ template <typename R, int LG>
 __global__ void __launch_bounds__(LG * 16, kF32<R> ? 6 : 3) k_aal_tracer(EulerArgs<R> a) {
   constexpr int NL = NLEV / LG;
   constexpr unsigned kSlab = NLEV * 16 * sizeof(double);
+  constexpr unsigned kLim = 2 * NLEV * sizeof(double);
   extern __shared__ __align__(16) double tsm[];
   double* s_q = tsm;                                            // [72][17] double
   R* s_dm = reinterpret_cast<R*>(tsm + NLEV * SROW);            // dpdissk
@@ -1019,16 +1020,18 @@ __global__ void __launch_bounds__(LG * 16, kF32<R> ? 6 : 3) k_aal_tracer(EulerAr
   R* s_c = s_rdm + NLEV * SROW;                                 // spheremp * dpdissk
   R* s_c1 = s_c + NLEV * SROW;                                  // sum of c per level [72]
   double* q_buf = reinterpret_cast<double*>(reinterpret_cast<char*>(tsm) + aal_buf_offset<R>());  // [72][16]
-  unsigned long long* bar = reinterpret_cast<unsigned long long*>(q_buf + NLEV * 16);
+  double* q_lim = q_buf + NLEV * 16;  // [2][2][72]: the tracer's qlim (min, max), by tracer parity
+  unsigned long long* bar = reinterpret_cast<unsigned long long*>(q_lim + 4 * NLEV);
   const int e = blockIdx.x;
   const int tid = threadIdx.x, p = tid & 15, lg = tid >> 4;
   const double* slab0 = a.qdp + ((size_t)e * QTL + a.n0_qdp) * a.Q * NLEV * 16;
   // every slab this CTA copies lies in Qdp: tracer level 0 or 1, element inside the grid
   const bool slabs_ok = in_bounds(a.n0_qdp >= 0 && a.n0_qdp < QTL && e < (int)gridDim.x, a.err + 1,
                                   kBoundsTracerSlab);
+  const double* lim0 = a.qlim + (size_t)e * a.Q * 2 * NLEV;
   if (tid == 0) {
     mbar_init(bar, 1);
-    if (a.Q > 0 && slabs_ok) bulk_load(q_buf, slab0, kSlab, bar);
+    if (a.Q > 0 && slabs_ok) bulk_load2(q_buf, slab0, kSlab, q_lim, lim0, kLim, bar);
   }
   if (!slabs_ok) return;
   Pt<R> t;
@@ -1102,9 +1105,10 @@ __global__ void __launch_bounds__(LG * 16, kF32<R> ? 6 : 3) k_aal_tracer(EulerAr
       }
     }
     __syncthreads();
-    if (tid == 0 && q + 1 < a.Q) {  // the buffer is free: fetch the next tracer's slab
+    if (tid == 0 && q + 1 < a.Q) {  // the buffer is free: fetch the next tracer's slab and bounds
       fence_proxy_async_smem();
-      bulk_load(q_buf, slab0 + (size_t)(q + 1) * NLEV * 16, kSlab, bar);
+      bulk_load2(q_buf, slab0 + (size_t)(q + 1) * NLEV * 16, kSlab, q_lim + ((q + 1) & 1) * 2 * NLEV,
+                 lim0 + (size_t)(q + 1) * 2 * NLEV, kLim, bar);
     }
     for (int l = tid; l < NLEV; l += blockDim.x) {
       if (s_c1[l] > R(0)) {
@@ -1115,7 +1119,8 @@ __global__ void __launch_bounds__(LG * 16, kF32<R> ? 6 : 3) k_aal_tracer(EulerAr
           x[k] = cvt<R>(s_q[l * SROW + k]) * s_rdm[l * SROW + k];
         }
         double* ql = a.qlim + ((size_t)e * a.Q + q) * 2 * NLEV;
-        double mn = ql[l], mx = ql[NLEV + l];
+        const double* qls = q_lim + (q & 1) * 2 * NLEV;  // the same bounds, prefetched
+        double mn = qls[l], mx = qls[NLEV + l];
         const bool lim = limiter_level<R>(a.limiter_option, x, c, s_c1[l], mn, mx);
         ql[l] = mn;
         ql[NLEV + l] = mx;
@@ -1136,7 +1141,8 @@ __global__ void __launch_bounds__(LG * 16, kF32<R> ? 6 : 3) k_aal_tracer(EulerAr
 }
 
 template <typename R> constexpr size_t aal_smem() {
-  return aal_buf_offset<R>() + NLEV * 16 * sizeof(double) + 16;  // + the Qdp slab and its barrier
+  // + the Qdp slab, two tracers' bounds and the barrier
+  return aal_buf_offset<R>() + (NLEV * 16 + 4 * NLEV) * sizeof(double) + 16;
 }
 
 // The nine levels lo, lo + 8, ... of one point with N contributions from other elements
