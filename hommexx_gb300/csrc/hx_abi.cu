@@ -12,6 +12,7 @@
 // There is no MPI: every connection is local, and DSS is a gather over a table built
 // once from the add_connection calls (src/share/cxx/mpi/Connectivity.cpp:77-170).
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <algorithm>
 #include <cmath>
@@ -105,7 +106,17 @@ void flush_timing() {
   g_tim.used = 0;
 }
 
+// NVTX ranges: one per kernel launch (its timing name) and one per phase, named as the
+// reference's GPTL timers (prim_driver.cpp:33,116, prim_advance_exp.cpp:99,116,
+// prim_advec_tracers_remap.cpp:34), so an nsys or ncu timeline shows the phases.  The
+// NVTX v3 calls are no-ops unless a tool is attached.
+struct Nvtx {
+  explicit Nvtx(const char* name) { nvtxRangePushA(name); }
+  ~Nvtx() { nvtxRangePop(); }
+};
+
 void hook_before(const char* name, cudaStream_t s) {
+  nvtxRangePushA(name);
   ++g_tim.launches;
   if (!g_tim.on) return;
   if (g_tim.used + 2 > g_tim.pool.size()) flush_timing();
@@ -115,6 +126,7 @@ void hook_before(const char* name, cudaStream_t s) {
 }
 void hook_after(const char*, cudaStream_t s) {
   if (g_tim.on) cudaEventRecord(g_tim.pool[g_tim.used - 1], s);
+  nvtxRangePop();
 }
 
 // ---- the resident model -----------------------------------------------------------------
@@ -503,6 +515,7 @@ struct BackendT : Backend {
   }
 
   void rk5(int nm1, int n0, int np1, int n0_qdp, double dt, double w) override {
+    Nvtx r("tl-ae U3-5stage_timestep");
     caar_stage(n0, n0, nm1, dt / 5.0, w / 4.0, n0_qdp, 0, n0);
     caar_stage(n0, nm1, np1, dt / 5.0, 0.0, n0_qdp, 0, n0);
     caar_stage(n0, np1, np1, dt / 3.0, 0.0, n0_qdp, 0, n0);
@@ -512,6 +525,7 @@ struct BackendT : Backend {
   }
 
   void hypervis(int np1, double dt, double w) override {
+    Nvtx r("tl-ae advance_hypervis_dp");
     hypervis_cycles(np1, dt, w, s.prm.hypervis_subcycle);
   }
 
@@ -563,6 +577,7 @@ struct BackendT : Backend {
   }
 
   void tracers_rk2(double dt) override {
+    Nvtx r("tl-at prim_advec_tracers_remap_RK2");
     s.tl.update_tracers_levels(s.prm.qsplit);
     precompute_divdp();
     euler_step(s.tl.np1_qdp, s.tl.n0_qdp, dt / 2.0, 0.0, 2, -1);
@@ -606,6 +621,7 @@ struct BackendT : Backend {
   }
 
   void prim_step(double dt) override {
+    Nvtx r("tl-sc prim_step-loop");
     const Params& p = s.prm;
     launch_prim_step_init(E, eta, vn0, omega_p, dpdiss_ave, dpdiss_bih, derived_dp, dp, s.tl.n0,
                              p.nu_p > 0 ? 1 : 0, g_stream);
@@ -730,6 +746,7 @@ struct BackendT : Backend {
   }
 
   void run_subcycle(double dt, int last_time_step) override {
+    Nvtx r("tl-sc prim_run_subcycle_c");
     const Params& p = s.prm;
     const double dt_remap = p.rsplit > 0 ? dt * p.qsplit * p.rsplit : dt * p.qsplit;
     // prim_driver.cpp:37-58; the arrays of init_diagnostics_c must be set
