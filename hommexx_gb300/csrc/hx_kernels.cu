@@ -1233,7 +1233,7 @@ template <typename R> constexpr size_t aal_smem() {
 template <int N, bool AVG>
 __device__ __forceinline__ void dss_levels(const double* own, const long long* so, double* dst,
                                            const double* s0, double f, int lo) {
-#pragma unroll 3
+#pragma unroll
   for (int l = lo; l < NLEV; l += 8) {
     double acc = own[l * 16];
 #pragma unroll
