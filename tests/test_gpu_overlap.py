@@ -102,3 +102,46 @@ def test_async_state_visible_to_other_calls(gpu_path):
         L.set_async_copies(False)
     finally:
         _pin(L, list(host_in.values()), on=False)
+
+
+@pytest.mark.parametrize("kw", [dict(rsplit=3), dict(ne=8, rsplit=3, precision=1)],
+                         ids=lambda kw: "-".join(f"{k}{v}" for k, v in kw.items()))
+def test_overlapped_copies_in_place(gpu_path, kw):
+    """The coupled driver's pattern: the same state arrays are the source of
+    init_elements_states_c and the destination of cxx_push_results_to_f90, so each
+    interval starts from the previous one's result while the copies overlap the step.
+    Three intervals match the plain sequence run the same way, bit for bit."""
+    kw = dict(kw)
+    ne, Q, prec = kw.pop("ne", 4), kw.pop("Q", 4), kw.pop("precision", 0)
+    keys = ("v", "T", "dp3d", "Qdp", "ps_v")
+    st = H.state(ne, Q)
+    # plain sequence, in place
+    L = H.setup(gpu_path, ne, Q, precision=prec, **kw)
+    host = {k: np.ascontiguousarray(st[k]).copy() for k in keys}
+    want = []
+    for _ in range(3):
+        L.set_state(host)
+        L.run_subcycle(DT)
+        r = L.push_results()
+        for k in keys:
+            host[k][...] = r[k]
+        want.append({k: v.copy() for k, v in r.items()})
+    # overlapped sequence, in place, page-locked
+    L = H.setup(gpu_path, ne, Q, precision=prec, **kw)
+    host = {k: np.ascontiguousarray(st[k]).copy() for k in keys}
+    r0 = L.push_results()
+    res = {k: host[k] if k in host else np.full_like(v, np.nan) for k, v in r0.items()}
+    _pin(L, list(res.values()))
+    try:
+        L.set_async_copies(True)
+        L.stream_results(res)
+        for i in range(3):
+            L.set_state(host)
+            L.run_subcycle(DT)
+            got = L.push_results(res)
+            for k in want[i]:
+                assert np.array_equal(got[k], want[i][k]), (i, k)
+        L.stream_results(None)
+        L.set_async_copies(False)
+    finally:
+        _pin(L, list(res.values()), on=False)
