@@ -1332,23 +1332,26 @@ constexpr int RLV = 9;    // levels per lane
 constexpr int RNI = 10;   // interface slots per lane (j = s + 8 i)
 // Shared memory of one column, in doubles.  The reconstruction arrays hold R (double in
 // the FP64 form, float in the mixed form, two to a double); the mixed form adds the FP32
-// neighbour differences of v and T and FP32 reciprocals of the source thickness.
+// neighbour differences of v and T.  The arrays of the grid phase are reused once it is
+// done: the cumulative thicknesses pio and pin hold the slopes and edge values, and the
+// source reciprocals 1/D, which only the source-cell search reads (the lanes keep their
+// own levels' in registers), the grid weights.  With that, 960 doubles a column in FP64
+// (7.5 KB: seven CTAs of four columns per SM instead of six) and 705 in the mixed form.
 template <typename R>
 struct RemapLayout {
   static constexpr int RW = kF32<R> ? 2 : 1;
   static constexpr int D = 0;                           // D[-2 .. 73], source thickness with ghosts
-  static constexpr int PIO = D + 76;                    // pio[0 .. 73]
-  static constexpr int PIN = PIO + 74;                  // pin[0 .. 72]
-  static constexpr int RDI = PIN + 74;                  // 1 / D[0 .. 71]
-  static constexpr int MASS = RDI + 72;                 // mass[0 .. 73]
+  static constexpr int PIO = D + 76;                    // pio[0 .. 73]; then dma[0 .. 73], R
+  static constexpr int PIN = PIO + 74;                  // pin[0 .. 72]; then ai[0 .. 72], R
+  static constexpr int RDI = PIN + 74;                  // 1 / D[0 .. 71] in the grid phase; then G
+  static constexpr int G = RDI;                         // combined grid weights [5][74], R
+  static constexpr int MASS = G + (5 * 74 / RW > 72 ? 5 * 74 / RW : 72);  // mass[0 .. 73]
   static constexpr int A = MASS + 74;                   // cell means A[-2 .. 73], double
-  static constexpr int G = A + 76;                      // combined grid weights [5][74], R
-  static constexpr int DMA = G + 5 * 74 / RW;           // slopes dma[0 .. 73], R
-  static constexpr int AI = DMA + 74 / RW;              // edge values ai[0 .. 72], R
-  static constexpr int COEF = AI + 74 / RW;             // parabola coefficients [3][72], R
+  static constexpr int DMA = PIO;
+  static constexpr int AI = PIN;
+  static constexpr int COEF = A + 76;                   // parabola coefficients [3][72], R
   static constexpr int DLF = COEF + 216 / RW;           // mixed: df[-1 .. 73], float
-  static constexpr int RDF = DLF + (kF32<R> ? 38 : 0);  // mixed: 1 / D[0 .. 71], float
-  static constexpr int END = RDF + (kF32<R> ? 36 : 0);
+  static constexpr int END = DLF + (kF32<R> ? 38 : 0);
 };
 
 // (ar - cm) (cm - al) > 0, the parabola's monotonicity test: FP32 as is; FP64 as exact
@@ -1520,7 +1523,6 @@ __global__ void __launch_bounds__(RT, 4) k_remap(RemapArgs a) {
   R* ai = reinterpret_cast<R*>(sm + LY::AI);
   R* coef = reinterpret_cast<R*>(sm + LY::COEF);  // coef[c * 72 + k]
   float* dlf = reinterpret_cast<float*>(sm + LY::DLF) + 1;  // df[-1 .. 73]
-  float* rDf = reinterpret_cast<float*>(sm + LY::RDF);
   float* Af = reinterpret_cast<float*>(sm + LY::A) + 2;  // the tracers' FP32 cell means
   const int l0 = RLV * s;
   const size_t sb = ((size_t)e * NTL + a.np1) * NLEV * 16 + p;
@@ -1537,7 +1539,8 @@ __global__ void __launch_bounds__(RT, 4) k_remap(RemapArgs a) {
   const double ps = cs + a.hyai0 * a.ps0;
   if (s == 0) a.ps_v[((size_t)e * NTL + a.np1) * 16 + p] = ps;
   // ---- target thickness; vertically Eulerian source thickness (RemapFunctor.hpp:42-100) ----
-  double tg[RLV], rt[RLV];
+  double tg[RLV], rt[RLV], rdl[RLV];  // target thickness, its reciprocal, 1 / source thickness
+  float rdf[RLV];
   bool bad = false;
 #pragma unroll
   for (int k = 0; k < RLV; ++k) {
@@ -1551,8 +1554,9 @@ __global__ void __launch_bounds__(RT, 4) k_remap(RemapArgs a) {
       sv[k] = tg[k] + a.dt * (en - a.eta[ie]);
     }
     D[l] = sv[k];
-    rD[l] = rcp_newton(sv[k], rf);
-    if constexpr (lo) rDf[l] = d2f_rn(rD[l]);
+    rdl[k] = rcp_newton(sv[k], rf);
+    rD[l] = rdl[k];
+    if constexpr (lo) rdf[k] = d2f_rn(rdl[k]);
     bad |= bad_thickness(sv[k]);
   }
   if (bad) atomicExch(a.invalid, 1);
@@ -1618,6 +1622,7 @@ __global__ void __launch_bounds__(RT, 4) k_remap(RemapArgs a) {
       wzf[k3][2] = (xf * xf * xf + 0.125f) * (1.0f / 3.0f);
     }
   }
+  __syncwarp();  // every lane's search is done: 1/D's space takes the grid weights
   // ---- compute_grids (PpmRemap.hpp:367-413, 505-666) at this lane's interfaces, in
   // double; the weights are stored combined (ppm_interfaces), in R ----
 #pragma unroll
@@ -1669,8 +1674,8 @@ __global__ void __launch_bounds__(RT, 4) k_remap(RemapArgs a) {
 #pragma unroll
     for (int k = 0; k < RLV; ++k) {
       const int l = l0 + k;
-      if (!lo || var < 3) A[l] = x[k] * rD[l];
-      else Af[l] = d2f_rn(x[k]) * rDf[l];
+      if (!lo || var < 3) A[l] = x[k] * rdl[k];
+      else Af[l] = d2f_rn(x[k]) * rdf[k];
     }
     // mass[i + 1] = sum of x below cell i (mass[0] = mass[1] = 0, mass[73] = column total)
     {
