@@ -70,42 +70,42 @@ NCU_NE16 = {
     "fp64": {
         "ppm_remap": (327.6e6, 1245.0e6, 939.2e6),
         "euler_bih_post": (282.3e6, 668.9e6, 376.0e6),
-        "euler_bih_pre": (260.7e6, 583.9e6, 300.8e6),
+        "euler_bih_pre": (260.8e6, 583.9e6, 300.8e6),
         "euler_aal_tracer": (426.3e6, 489.6e6, 299.0e6),
         "hv_laplace2": (162.0e6, 352.9e6, 210.4e6),
         "caar_stage": (200.4e6, 320.0e6, 197.9e6),
-        "hv_laplace1": (77.7e6, 292.9e6, 164.6e6),
-        "update_q": (239.3e6, 107.9e6, 63.7e6),
-        "euler_dss_qdp": (330.7e6, 52.2e6, 46.3e6),
+        "hv_laplace1": (77.6e6, 292.9e6, 164.6e6),
+        "update_q": (239.2e6, 107.9e6, 63.7e6),
+        "euler_dss_qdp": (326.0e6, 52.2e6, 46.3e6),
         "precompute_divdp": (29.3e6, 41.9e6, 25.0e6),
-        "euler_qminmax": (214.4e6, 35.5e6, 26.7e6),
-        "hv_dss_update": (117.6e6, 35.4e6, 30.1e6),
-        "dss_caar": (102.3e6, 15.9e6, 15.9e6),
+        "euler_qminmax": (214.5e6, 35.5e6, 26.7e6),
+        "hv_dss_update": (117.7e6, 35.4e6, 30.1e6),
+        "dss_caar": (79.1e6, 15.9e6, 15.9e6),
         "dp3d_from_ps": (0.2e6, 5.3e6, 3.5e6),
         "euler_dss_fvar": (14.8e6, 4.0e6, 4.0e6),
         "euler_bih_weight": (14.2e6, 1.8e6, 1.8e6),
         "euler_minmax_nbr": (17.8e6, 0.0e6, 0.0e6),
-        "prim_step_init": (53.0e6, 0.0e6, 0.0e6),
+        "prim_step_init": (53.1e6, 0.0e6, 0.0e6),
     },
     "mixed": {
         "ppm_remap": (327.4e6, 345.9e6, 253.1e6),
-        "update_q": (239.2e6, 107.9e6, 63.7e6),
-        "euler_aal_tracer": (424.4e6, 55.4e6, 55.4e6),
-        "euler_dss_qdp": (330.8e6, 52.2e6, 46.3e6),
+        "update_q": (239.1e6, 107.9e6, 63.7e6),
+        "euler_aal_tracer": (424.5e6, 55.4e6, 55.4e6),
+        "euler_dss_qdp": (326.2e6, 52.2e6, 46.3e6),
         "caar_stage": (188.2e6, 52.0e6, 45.1e6),
-        "euler_bih_post": (274.2e6, 43.7e6, 43.7e6),
-        "hv_laplace2": (152.2e6, 28.0e6, 23.1e6),
-        "dss_caar": (102.1e6, 15.9e6, 15.9e6),
-        "hv_dss_update": (116.3e6, 15.9e6, 15.9e6),
+        "euler_bih_post": (274.3e6, 43.7e6, 43.7e6),
+        "hv_laplace2": (150.3e6, 28.0e6, 23.1e6),
+        "dss_caar": (79.3e6, 15.9e6, 15.9e6),
+        "hv_dss_update": (116.5e6, 15.9e6, 15.9e6),
         "dp3d_from_ps": (0.2e6, 5.3e6, 3.5e6),
-        "euler_dss_fvar": (14.9e6, 4.0e6, 4.0e6),
+        "euler_dss_fvar": (14.8e6, 4.0e6, 4.0e6),
         "hv_laplace1": (70.2e6, 3.5e6, 3.5e6),
         "euler_bih_weight": (14.2e6, 1.8e6, 1.8e6),
         "euler_qminmax": (214.6e6, 0.1e6, 0.1e6),
         "precompute_divdp": (28.8e6, 0.0e6, 0.0e6),
         "euler_minmax_nbr": (17.8e6, 0.0e6, 0.0e6),
         "euler_bih_pre": (257.3e6, 0.0e6, 0.0e6),
-        "prim_step_init": (53.2e6, 0.0e6, 0.0e6),
+        "prim_step_init": (53.3e6, 0.0e6, 0.0e6),
     },
 }
 NCU_NE16_ELEMENTS = 1536
