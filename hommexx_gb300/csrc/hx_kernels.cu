@@ -401,7 +401,10 @@ __device__ __forceinline__ void dss_gather_to_smem(const double* own, int n, con
     case 1: dss_gather_levels<1, NF>(own, so, ls, s_in, rs, lo, pg); break;
     case 2: dss_gather_levels<2, NF>(own, so, ls, s_in, rs, lo, pg); break;
     case 3: dss_gather_levels<3, NF>(own, so, ls, s_in, rs, lo, pg); break;
-    default: break;  // a point outside the table (index-check build): nothing gathered
+    default:  // a point outside the table (index-check build, flagged): zeros, as dss_gather
+      for (int l = lo; l < NLEV; l += 8)
+        for (int f = 0; f < NF; ++f) s_in[(f * NLEV + l) * 16 + pg] = R(0);
+      break;
   }
 }
 
