@@ -1221,7 +1221,8 @@ __global__ void __launch_bounds__(LG * 16, kF32<R> ? 6 : 3) k_aal_tracer(EulerAr
       const int l = lg + LG * k;
       a.qscr[qb + l * 16 + p] = spd * s_q[l * SROW + p];
     }
-    __syncthreads();
+    // (no barrier here: the next tracer's slab vote is one, and every thread reaches it
+    // only after its stores of this tracer)
   }
 }
 
