@@ -1,5 +1,5 @@
 """bench.py's output contract on the CPU: the reference arm (the oracle, timed on the host
-cores) prints one JSON line with the keys the benchmark driver reads, and the roofline
+cores) prints one JSON line with the keys of the benchmark line's contract, and the roofline
 table covers the same kernels in both forms.  The reference arm runs here at ne4, the same
 code path as its ne30 default."""
 import json
