@@ -389,6 +389,11 @@ template <typename T> __device__ __forceinline__ bool pos(T x) { return x > T(0)
 template <> __device__ __forceinline__ bool pos<double>(double x) {
   return __double_as_longlong(x) > 0;  // > +0 (non-NaN)
 }
+// x == 0 (either sign): FP32 as is; FP64 on the integer pipe.
+template <typename T> __device__ __forceinline__ bool is_zero(T x) { return x == T(0); }
+template <> __device__ __forceinline__ bool is_zero<double>(double x) {
+  return (__double_as_longlong(x) << 1) == 0;
+}
 // a b > 0 for non-NaN a, b: FP32 as is; FP64 on the integer pipe as "the same sign and
 // neither zero" (differs from the product's test only where a b would underflow to 0).
 template <typename T> __device__ __forceinline__ bool pos_prod(T a, T b) { return a * b > T(0); }

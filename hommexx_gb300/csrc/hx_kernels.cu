@@ -852,8 +852,14 @@ __global__ void __launch_bounds__(96) k_qminmax(EulerArgs<R> a, double* qlim_out
       }
       if (c == 0) {
         if (a.rhs_multiplier == 1.0) {
-          dmn = fmin(qo[l], dmn);
-          dmx = fmax(qo[NLEV + l], dmx);
+          if constexpr (kF32<R>) {
+            dmn = fmin(qo[l], dmn);
+            dmx = fmax(qo[NLEV + l], dmx);
+          } else {  // exact, on the integer pipe (one lane of four: an FP64-pipe fmin here
+                    // costs a full warp instruction; 2.21 -> 2.09 ms per interval)
+            dmn = dkey_value(kmin(dkey(qo[l]), dkey(dmn)));
+            dmx = dkey_value(kmax(dkey(qo[NLEV + l]), dkey(dmx)));
+          }
         }
         ql[l] = dmn;
         ql[NLEV + l] = dmx;
@@ -1007,14 +1013,15 @@ __device__ bool limiter_level(int option, R* x, const R* c, R s1, double& minp_i
   R s0 = 0;
 #pragma unroll
   for (int k = 0; k < 16; ++k) s0 += x[k] * c[k];
-  if (s1 <= R(0)) return false;
+  // The tests here and below are exact comparisons (pos, lt: on the integer pipe in FP64,
+  // where a comparison on the FP64 pipe would cost a warp instruction like a multiply-add).
+  if (!pos(s1)) return false;
   R minp = cvt<R>(minp_io), maxp = cvt<R>(maxp_io);
-  if (minp < R(0)) { minp = R(0); minp_io = 0.0; }
-  if (s0 < minp * s1) { minp = s0 / s1; minp_io = dbl(minp); }
-  if (s0 > maxp * s1) { maxp = s0 / s1; maxp_io = dbl(maxp); }
+  if (lt(minp, R(0))) { minp = R(0); minp_io = 0.0; }
+  if (lt(s0, minp * s1)) { minp = s0 / s1; minp_io = dbl(minp); }
+  if (lt(maxp * s1, s0)) { maxp = s0 / s1; maxp_io = dbl(maxp); }
   if (!any_outside(x, minp, maxp)) return false;  // no clipping: addmass = 0
   const R mass = s0;
-  // The clip and bound tests below are exact comparisons (lt: on the integer pipe in FP64).
   if (option == 8) {
     const R tol = R(5e-14);
     for (int iter = 0; iter < 15; ++iter) {
@@ -1028,19 +1035,19 @@ __device__ bool limiter_level(int option, R* x, const R* c, R s1, double& minp_i
           x[k] = b;
         }
       }
-      if (fabs(addmass) <= tol * fabs(mass)) break;
+      if (!lt(tol * fabs(mass), fabs(addmass))) break;  // |addmass| <= tol |mass|
       R wsum = 0;
-      if (addmass > R(0)) {
+      if (pos(addmass)) {
 #pragma unroll
         for (int k = 0; k < 16; ++k) if (lt(x[k], maxp)) wsum += c[k];
-        if (wsum == R(0)) break;
+        if (!pos(wsum)) break;  // a sum of non-negative weights: zero
         const R adw = addmass / wsum;
 #pragma unroll
         for (int k = 0; k < 16; ++k) if (lt(x[k], maxp)) x[k] += adw;
       } else {
 #pragma unroll
         for (int k = 0; k < 16; ++k) if (lt(minp, x[k])) wsum += c[k];
-        if (wsum == R(0)) break;
+        if (!pos(wsum)) break;
         const R adw = addmass / wsum;
 #pragma unroll
         for (int k = 0; k < 16; ++k) if (lt(minp, x[k])) x[k] += adw;
@@ -1057,12 +1064,12 @@ __device__ bool limiter_level(int option, R* x, const R* c, R s1, double& minp_i
         x[k] = b;
       }
     }
-    if (addmass == R(0)) return true;
+    if (is_zero(addmass)) return true;
     R fac = 0;
-    if (addmass > R(0)) {
+    if (pos(addmass)) {
 #pragma unroll
       for (int k = 0; k < 16; ++k) fac += c[k] * (maxp - x[k]);
-      if (fac > R(0)) {
+      if (pos(fac)) {
         fac = addmass / fac;
 #pragma unroll
         for (int k = 0; k < 16; ++k) x[k] += fac * (maxp - x[k]);
@@ -1070,7 +1077,7 @@ __device__ bool limiter_level(int option, R* x, const R* c, R s1, double& minp_i
     } else {
 #pragma unroll
       for (int k = 0; k < 16; ++k) fac += c[k] * (x[k] - minp);
-      if (fac > R(0)) {
+      if (pos(fac)) {
         fac = addmass / fac;
 #pragma unroll
         for (int k = 0; k < 16; ++k) x[k] += fac * (x[k] - minp);
