@@ -1040,14 +1040,14 @@ __device__ bool limiter_level(int option, R* x, const R* c, R s1, double& minp_i
       if (pos(addmass)) {
 #pragma unroll
         for (int k = 0; k < 16; ++k) if (lt(x[k], maxp)) wsum += c[k];
-        if (!pos(wsum)) break;  // a sum of non-negative weights: zero
+        if (is_zero(wsum)) break;
         const R adw = addmass / wsum;
 #pragma unroll
         for (int k = 0; k < 16; ++k) if (lt(x[k], maxp)) x[k] += adw;
       } else {
 #pragma unroll
         for (int k = 0; k < 16; ++k) if (lt(minp, x[k])) wsum += c[k];
-        if (!pos(wsum)) break;
+        if (is_zero(wsum)) break;
         const R adw = addmass / wsum;
 #pragma unroll
         for (int k = 0; k < 16; ++k) if (lt(minp, x[k])) x[k] += adw;
